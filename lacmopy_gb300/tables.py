@@ -1,0 +1,154 @@
+"""Collision-efficiency tables E_col(R1, R2) on a logarithmic radius grid.
+
+Host-side, one-time set-up of the collision kernel input (not on the per-step
+path).  The generators restate the reference's table construction with the
+same floating-point operations, so the tables equal the ones the reference ships
+in ``Ecol_grid_data/`` bit for bit:
+
+* ``generate_E_col_grid_R_Long_Bott_np`` follows collision/kernel.py:512-569
+  with the efficiency of collision/kernel.py:350-373 (Long kernel, Bott 1998);
+* ``generate_E_col_grid_R_Hall_Bott_np`` follows collision/kernel.py:581-696,
+  bilinear interpolation of the Hall (1980) table as corrected by Bott (1998).
+  The 15 x 21 raw table ships as ``data/hall_bott_1998_raw.npz``.
+
+``load_kernel_data_Ecol`` mirrors file_handling.py:764-804: it returns the table
+and the binning parameters (low-radius log, log bin factor, bin count).
+"""
+import math
+import os
+from functools import lru_cache
+
+import numpy as np
+
+_DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+
+
+def _radius_grid(R_low, R_high, no_bins_10):
+    bin_factor = 10 ** (1.0 / no_bins_10)
+    no_bins = int(math.ceil(no_bins_10 * math.log10(R_high / R_low))) + 1
+    radius_grid = np.zeros(no_bins, dtype=np.float64)
+    r = float(R_low)
+    radius_grid[0] = r
+    for n in range(1, no_bins):
+        r = r * bin_factor
+        radius_grid[n] = r
+    return radius_grid
+
+
+def compute_E_col_Long_Bott(R_i, R_j):
+    """Long (1974) collection efficiency as modified by Bott (1998)."""
+    if R_j >= R_i:
+        R_max, R_min = R_j, R_i
+    else:
+        R_max, R_min = R_i, R_j
+    if R_max <= 50:
+        return 4.5E-4 * R_max * R_max * (1.0 - 3.0 / (max(3.0, R_min) + 1.0E-2))
+    return 1.0
+
+
+def generate_E_col_grid_R_Long_Bott_np(R_low, R_high, no_bins_10,
+                                       radius_grid_in=None):
+    if radius_grid_in is None:
+        radius_grid = _radius_grid(R_low, R_high, no_bins_10)
+    else:
+        radius_grid = np.asarray(radius_grid_in, dtype=np.float64)
+    nb = radius_grid.shape[0]
+    rg = [float(v) for v in radius_grid]
+    E = np.zeros((nb, nb), dtype=np.float64)
+    for j in range(nb):
+        R_j = rg[j]
+        for i in range(j + 1):
+            E[j, i] = compute_E_col_Long_Bott(rg[i], R_j)
+            E[i, j] = E[j, i]
+    return E, radius_grid
+
+
+def _hall_bott_raw():
+    d = np.load(os.path.join(_DATA, "hall_bott_1998_raw.npz"))
+    return d["E_col"], d["R_col"], d["R_ratio"]
+
+
+def generate_E_col_grid_R_Hall_Bott_np(R_low, R_high, no_bins_10,
+                                       radius_grid_in=None):
+    E_raw, R_raw, q_raw = _hall_bott_raw()
+    E_raw = [[float(v) for v in row] for row in E_raw]
+    R_raw = [float(v) for v in R_raw]
+    q_raw = [float(v) for v in q_raw]
+    n_R, n_q = len(R_raw), len(q_raw)
+    if radius_grid_in is None:
+        radius_grid = _radius_grid(R_low, R_high, no_bins_10)
+    else:
+        radius_grid = np.asarray(radius_grid_in, dtype=np.float64)
+    rg = [float(v) for v in radius_grid]
+    nb = len(rg)
+    E = np.zeros((nb, nb), dtype=np.float64)
+    for iR, R_col in enumerate(rg):
+        if R_col <= R_raw[0]:
+            iRt = -1
+        elif R_col > R_raw[-1]:
+            iRt = n_R - 1
+        else:
+            for k in range(n_R - 1):
+                if R_raw[k] < R_col <= R_raw[k + 1]:
+                    iRt = k
+                    break
+        for ir in range(iR + 1):
+            ratio = rg[ir] / R_col
+            if ratio >= 1.0:
+                iq = n_q - 2
+            else:
+                for k in range(n_q - 1):
+                    if q_raw[k] <= ratio < q_raw[k + 1]:
+                        iq = k
+                        break
+            if iRt == n_R - 1:
+                q = (ratio - q_raw[iq]) / (q_raw[iq + 1] - q_raw[iq])
+                e = (1. - q) * E_raw[iRt][iq] + q * E_raw[iRt][iq + 1]
+                E[iR, ir] = e if e <= 1.0 else 1.0
+            elif iRt == -1:
+                q = (ratio - q_raw[iq]) / (q_raw[iq + 1] - q_raw[iq])
+                E[iR, ir] = (1. - q) * E_raw[0][iq] + q * E_raw[0][iq + 1]
+            else:
+                p = (R_col - R_raw[iRt]) / (R_raw[iRt + 1] - R_raw[iRt])
+                q = (ratio - q_raw[iq]) / (q_raw[iq + 1] - q_raw[iq])
+                f = E_raw
+                E[iR, ir] = ((1. - p) * (1. - q) * f[iRt][iq]
+                             + (1. - p) * q * f[iRt][iq + 1]
+                             + p * (1. - q) * f[iRt + 1][iq]
+                             + p * q * f[iRt + 1][iq + 1])
+            E[ir, iR] = E[iR, ir]
+    return E, radius_grid
+
+
+# The reference's shipped tables were made with these arguments.
+TABLE_ARGS = {"Long_Bott": (0.01, 51., 100), "Hall_Bott": (0.01, 301., 100)}
+
+
+@lru_cache(maxsize=4)
+def _cached(kernel_type):
+    R_low, R_high, n10 = TABLE_ARGS[kernel_type]
+    if kernel_type == "Long_Bott":
+        E, rg = generate_E_col_grid_R_Long_Bott_np(R_low, R_high, n10)
+    elif kernel_type == "Hall_Bott":
+        E, rg = generate_E_col_grid_R_Hall_Bott_np(R_low, R_high, n10)
+    else:
+        raise ValueError(kernel_type)
+    E.setflags(write=False)
+    rg.setflags(write=False)
+    return E, rg
+
+
+def load_kernel_data_Ecol(kernel_type, E_col_const=0.5):
+    """Return ``(E_col_grid, radius_grid, R_low, bin_factor, R_low_log,
+    bin_factor_log, no_kernel_bins)`` like file_handling.py:764-804.
+
+    ``kernel_type`` is 'Long_Bott', 'Hall_Bott' (kernel method 'Ecol_grid_R')
+    or 'Hydro_E_const' (kernel method 'Ecol_const', constant efficiency).
+    """
+    if kernel_type == "Hydro_E_const":
+        return float(E_col_const), None, None, None, None, None, None
+    E, rg = _cached(kernel_type)
+    R_low = rg[0]
+    bin_factor = rg[1] / rg[0]
+    return (E, rg, R_low, bin_factor, np.log(R_low), np.log(bin_factor),
+            len(rg))
