@@ -1,0 +1,236 @@
+/*
+ * lacmo_gb300 — C ABI of the GB300 (sm_103a) super-droplet (SIP) hot path.
+ *
+ * Drop-in boundary for LacmoPy's per-timestep step functions.  Every entry
+ * point takes raw DEVICE pointers, sizes and a CUDA stream (as void*), never
+ * synchronises unless stated, and returns an int status (LACMO_OK = 0).  The
+ * caller owns all memory; scratch ("workspace") memory is also passed in by
+ * the caller, sized by lacmo_workspace_bytes().  Arrays keep the reference's
+ * layout (row-major NumPy): particle arrays are indexed by SIP ID, pos/vel/
+ * rel_pos are [2][n], grid fields are [fields][nx][nz], staggered velocity
+ * and mass flux are [2][nx+1][nz+1].  The one internal format is the cell
+ * index: int32 cell[n] = i*nz + j for active SIPs and -1-i for SIPs removed at
+ * the ground (the reference keeps cells[2][n] int64 plus active_ids[n];
+ * lacmo_cells_import/export convert).
+ *
+ * Reference file:line citations are relative to the LacmoPy source tree.
+ */
+#ifndef LACMO_GB300_H
+#define LACMO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LACMO_ABI_VERSION 1
+
+/* status codes (negative: error, nothing or part of the work done) */
+#define LACMO_OK 0
+#define LACMO_ERR_ARG (-1)          /* bad size, null pointer, bad option    */
+#define LACMO_ERR_CUDA (-2)         /* a CUDA runtime call failed            */
+#define LACMO_ERR_DRAWS (-3)        /* injected draw buffer too short        */
+#define LACMO_ERR_WORKSPACE (-4)    /* workspace too small                   */
+#define LACMO_ERR_CAPACITY (-5)     /* size above a fixed capacity           */
+/* device-side condition flags, read with lacmo_read_flags() */
+#define LACMO_FLAG_DRAWS_SHORT 0x1u     /* a collision step skipped: draws   */
+#define LACMO_FLAG_CELL_CLAMPED 0x2u    /* x == x_max after the periodic wrap */
+#define LACMO_FLAG_NONFINITE 0x4u       /* NaN/inf met in a SIP mass         */
+
+#define LACMO_SOLUTE_AS 0
+#define LACMO_SOLUTE_NACL 1
+
+/* SIP state, device pointers; arrays indexed by SIP ID 0..n-1. */
+typedef struct {
+  int64_t n;
+  double* pos;            /* [2][n] x, z (m)                                 */
+  double* vel;            /* [2][n] u, w (m/s)                               */
+  double* rel_pos;        /* [2][n] relative cell position                   */
+  double* m_w;            /* [n] water mass (1e-18 kg)                       */
+  double* m_s;            /* [n] solute mass (1e-18 kg)                      */
+  double* xi;             /* [n] multiplicity                                */
+  double* T_p;            /* [n] particle temperature (K)                    */
+  int32_t* cell;          /* [n] see header comment                          */
+  double* water_removed;  /* [1] water mass removed at the ground            */
+  int64_t* no_cols;       /* [2] collision counters (single, multiple)       */
+} lacmo_sips_t;
+
+/* Grid state, device pointers. */
+typedef struct {
+  int64_t nx, nz;
+  double* scalar_fields;          /* [10][nx][nz] T,p,Theta,rho_d,r_v,r_l,S,e_s,1/m_d,1/rho_d */
+  double* mat_prop;               /* [7][nx][nz]  K,D_v,L_v,sigma_w,c_p,mu,rho_f              */
+  const double* velocity;         /* [2][nx+1][nz+1]                                          */
+  const double* mass_flux_air_dry;/* [2][nx+1][nz+1]                                          */
+  double* delta_m_l;              /* [nx][nz] condensed mass of the last sub-step (kg)        */
+  double x_min, x_max, z_min, z_max, dx, dz;
+  double volume_cell, p_ref, p_ref_inv;
+} lacmo_grid_t;
+
+/* Step parameters (integration.py:1298-1313 argument list). */
+typedef struct {
+  double dt, dt_sub, dt_sub_half, dt_col_over_dV, g_set;
+  int32_t scale_dt_cond, no_col_per_adv, act_collisions, act_relaxation;
+  int32_t no_iter_impl_mass, solute;
+  const double* init_profile_r_v;         /* [nz] or NULL                    */
+  const double* init_profile_Theta;       /* [nz] or NULL                    */
+  const double* relaxation_time_profile;  /* [nz] or NULL                    */
+  const double* E_col_grid;               /* [nb][nb], NULL: constant E      */
+  double E_col_const;
+  int64_t no_kernel_bins;
+  double R_kernel_low_log, bin_factor_R_log;
+} lacmo_params_t;
+
+/* Uniform draws for the all-or-nothing collisions.  With draws != NULL the
+ * steps consume the buffer in the reference's order (cells x-outer, z-inner;
+ * pairs i<j lexicographic, SIPs by ascending ID) from a device-side cursor
+ * that starts at 0 when the workspace is reset; this reproduces the
+ * reference's np.random.rand stream when the buffer holds it.  With
+ * draws == NULL each pair draws from Philox4x32-10 keyed by seed and
+ * counted by (collision step, cell, pair rank). */
+typedef struct {
+  const double* draws;
+  int64_t n_draws;
+  uint64_t seed;
+} lacmo_draws_t;
+
+/* ---- library, workspace, status ------------------------------------------ */
+int lacmo_abi_version(void);
+const char* lacmo_error_string(int status);
+/* Bytes of device scratch the entry points below need for n SIPs and an
+ * nx x nz grid (no allocation happens inside the library). */
+size_t lacmo_workspace_bytes(int64_t n, int64_t nx, int64_t nz);
+/* Zero the workspace: draw cursor, collision-step counter, flags. */
+int lacmo_workspace_reset(void* ws, size_t ws_bytes, int64_t n, int64_t nx, int64_t nz,
+                          void* stream);
+/* Copy the device-side flags to *flags (synchronises the stream). */
+int lacmo_read_flags(const void* ws, int64_t n, int64_t nx, int64_t nz, uint32_t* flags,
+                     void* stream);
+
+/* ---- layout conversion ------------------------------------------------------ */
+/* cells[2][n] int64 + active_ids[n] (uint8) -> cell[n] (file_handling.py
+ * state layout; integration.py:509-550 cell convention). */
+int lacmo_cells_import(const int64_t* cells, const uint8_t* active_ids, int32_t* cell,
+                       int64_t n, int64_t nx, int64_t nz, void* stream);
+/* cell[n] -> cells[2][n] int64 + active_ids[n]; fills rel_pos of active SIPs
+ * from pos (integration.py:509-550) so the reference's rel_pos is complete. */
+int lacmo_cells_export(const int32_t* cell, const double* pos, double* rel_pos,
+                       int64_t* cells, uint8_t* active_ids, int64_t n, int64_t nx, int64_t nz,
+                       double x_min, double z_min, double dx, double dz, void* stream);
+
+/* ---- time integration --------------------------------------------------------- */
+/* Prepare derived per-cell data and the cell binning from the current state.
+ * Call after importing a state or changing it outside these entry points. */
+int lacmo_prepare(const lacmo_sips_t* sips, const lacmo_grid_t* grid, const lacmo_params_t* prm,
+                  void* ws, size_t ws_bytes, void* stream);
+/* One advection step dt: replaces integration.py:1298 integrate_adv_step_np
+ * (with integrate_subloop_n_steps_np :1095, propagate_particles_subloop_step
+ * :944, propagate_grid_subloop_step :402, compute_divergence_upwind :150,
+ * compute_relaxation_term :325 and the all-cells collision step
+ * collision/all_or_nothing.py:754).  Requires lacmo_prepare() once before. */
+int lacmo_integrate_adv_step(const lacmo_sips_t* sips, const lacmo_grid_t* grid,
+                             const lacmo_params_t* prm, const lacmo_draws_t* draws, void* ws,
+                             size_t ws_bytes, void* stream);
+/* Phases of lacmo_integrate_adv_step, for callers that run the collision
+ * steps themselves (e.g. to draw each step's uniforms from a host generator
+ * exactly as the reference does):
+ * _begin: x_{n+1/2}, re-index and the first-half advective + relaxation
+ *   increments kept in the workspace (integration.py:1474-1508);
+ * _second_half: the second-half increments (integration.py:1536-1561);
+ * _substep: one particle + grid sub-step with those increments; positions
+ *   move by dt_sub_pos, T_p is written when write_T_p != 0
+ *   (integration.py:1265-1281, 1593-1610). */
+int lacmo_adv_step_begin(const lacmo_sips_t* sips, const lacmo_grid_t* grid,
+                         const lacmo_params_t* prm, void* ws, size_t ws_bytes, void* stream);
+int lacmo_adv_step_second_half(const lacmo_sips_t* sips, const lacmo_grid_t* grid,
+                               const lacmo_params_t* prm, void* ws, size_t ws_bytes,
+                               void* stream);
+int lacmo_adv_substep(const lacmo_sips_t* sips, const lacmo_grid_t* grid,
+                      const lacmo_params_t* prm, double dt_sub_pos, int write_T_p, void* ws,
+                      size_t ws_bytes, void* stream);
+/* One particle sub-step: replaces integration.py:944
+ * propagate_particles_subloop_step_np (T_p, Newton condensation with the
+ * per-cell delta_m_l, drag, position, ground removal, cell re-index). */
+int lacmo_propagate_particles_subloop_step(const lacmo_sips_t* sips, const lacmo_grid_t* grid,
+                                           const lacmo_params_t* prm, double dt_sub,
+                                           double dt_sub_pos, void* ws, size_t ws_bytes,
+                                           void* stream);
+/* One grid sub-step: replaces integration.py:402 propagate_grid_subloop_step_np
+ * (and update_material_properties :359). */
+int lacmo_propagate_grid_subloop_step(const lacmo_grid_t* grid, const double* delta_Theta_ad,
+                                      const double* delta_r_v_ad, const double* delta_m_l,
+                                      void* stream);
+/* Replaces integration.py:150 compute_divergence_upwind_np; bc 0 periodic,
+ * 1 solid.  out[nx][nz]. */
+int lacmo_divergence_upwind(const double* field, const double* flux, int64_t nx, int64_t nz,
+                            double dx, double dz, int bc_x, int bc_z, double* out, void* stream);
+/* Replaces integration.py:325 compute_relaxation_term. out[nz]. */
+int lacmo_relaxation_term(const double* field, int64_t nx, int64_t nz, const double* profile0,
+                          const double* t_relax, double dt, double* out, void* stream);
+/* Replaces grid.py:370 update_grid_r_l_np (uses the current cell binning). */
+int lacmo_update_grid_r_l(const lacmo_sips_t* sips, const lacmo_grid_t* grid, void* ws,
+                          size_t ws_bytes, void* stream);
+
+/* ---- collisions ------------------------------------------------------------------ */
+/* All cells of the 2-D grid: replaces collision/all_or_nothing.py:754
+ * collision_step_Ecol_grid_R_all_cells_2D_multicomp_np (and :498 / :637 per
+ * cell).  Uses the binning of the last lacmo_prepare / sub-step.  Injected
+ * draws are read from the start of the buffer (it must hold the count from
+ * lacmo_collision_pair_count). */
+int lacmo_collision_step_cells(const lacmo_sips_t* sips, const lacmo_grid_t* grid,
+                               const lacmo_params_t* prm, const lacmo_draws_t* draws, void* ws,
+                               size_t ws_bytes, void* stream);
+/* Number of pair draws the next all-cells collision step consumes
+ * (synchronises the stream; used to size an injected draw buffer). */
+int lacmo_collision_pair_count(const void* ws, int64_t n, int64_t nx, int64_t nz,
+                               int64_t* pairs, void* stream);
+/* Box model, Golovin kernel: replaces collision/all_or_nothing.py:109
+ * collision_step_Golovin_np.  rnd: n(n-1)/2 draws or NULL for Philox
+ * (seed, step).  n <= LACMO_BOX_MAX_SIPS. */
+#define LACMO_BOX_MAX_SIPS 8192
+#define LACMO_ECOL_BOX_MAX_SIPS 4096
+int lacmo_collision_step_golovin(double* xis, double* masses, int64_t n, double dt_over_dV,
+                                 int64_t* no_cols, const double* rnd, uint64_t seed,
+                                 uint64_t step, void* stream);
+/* Box model, E_col(R1, R2) table and 1-D velocities: replaces
+ * collision/all_or_nothing.py:269 collision_step_Ecol_grid_R_np. */
+int lacmo_collision_step_ecol_grid_r_box(double* xis, double* masses, double* radii,
+                                         const double* vel, const double* mass_densities,
+                                         int64_t n, double dt_over_dV, const double* E_col_grid,
+                                         int64_t no_kernel_bins, double R_kernel_low_log,
+                                         double bin_factor_R_log, int64_t* no_cols,
+                                         const double* rnd, uint64_t seed, uint64_t step,
+                                         void* stream);
+/* Beard terminal velocity: replaces collision/kernel.py:193 update_velocity_Beard. */
+int lacmo_update_velocity_beard(double* vel, const double* R, int64_t n, void* stream);
+
+/* ---- elementwise microphysics (unit-level parity) ------------------------------------ */
+/* microphysics.py:1359 / :1239 compute_mass_rate_and_derivative_{AS,NaCl}_np */
+int lacmo_mass_rate_and_derivative(int solute, int64_t n, const double* m_w, const double* m_s,
+                                   const double* w_s, const double* R_p, const double* T_p,
+                                   const double* rho_p, const double* T_amb, const double* p_amb,
+                                   const double* S_amb, const double* e_s_amb, const double* L_v,
+                                   const double* K, const double* D_v, const double* sigma_p,
+                                   double* gamma, double* dgamma_dm, void* stream);
+/* integration.py:728 compute_dml_and_gamma_impl_Newton_full_np */
+int lacmo_newton_full(int solute, int64_t n, double dt_sub, int no_iter, const double* m_w,
+                      const double* m_s, const double* w_s, const double* R_p, const double* T_p,
+                      const double* rho_p, const double* T_amb, const double* p_amb,
+                      const double* S_amb, const double* e_s_amb, const double* L_v,
+                      const double* K, const double* D_v, const double* sigma_p, double* dm,
+                      double* gamma0, void* stream);
+/* grid.py:257 interpolate_velocity_from_cell_bilinear (cells as cell[n]) */
+int lacmo_interpolate_velocity(const int32_t* cell, const double* rel_pos, const double* grid_vel,
+                               int64_t n, int64_t nx, int64_t nz, double* out, void* stream);
+/* Correctly-rounded radius and kernel bin of the collision path
+ * (microphysics.py:83-100, collision/all_or_nothing.py:35-67). */
+int lacmo_radius_and_bin(const double* m, const double* rho, int64_t n, double R_kernel_low_log,
+                         double bin_factor_R_log, int64_t no_kernel_bins, double* R,
+                         int64_t* bin, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LACMO_GB300_H */

@@ -1,0 +1,12 @@
+"""lacmopy_gb300: GB300 (sm_103a) CUDA implementation of LacmoPy's per-timestep
+super-droplet hot path (advection + re-index, Newton condensation with grid
+feedback, all-or-nothing collisions), behind a C ABI (include/lacmo_gb300.h).
+
+Modules mirror the reference's step functions by name and argument list:
+``integration`` (integration.py / grid.py / microphysics.py helpers) and
+``collision`` (collision/all_or_nothing.py, collision/box_model.py driver).
+``DeviceState`` keeps a state resident on the GPU between steps.
+"""
+from .device import DeviceState  # noqa: F401
+
+__all__ = ["DeviceState"]

@@ -1,0 +1,122 @@
+"""ctypes binding of liblacmo_gb300.so (the C ABI in include/lacmo_gb300.h).
+
+Loading fails loudly: there is no CPU fallback for any entry point.  The
+structs mirror the header; every pointer is a device address.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblacmo_gb300.so")
+
+OK = 0
+ERRORS = {-1: "invalid argument", -2: "CUDA runtime error", -3: "injected draw buffer too short",
+          -4: "workspace missing or too small", -5: "size above the fixed capacity"}
+FLAG_DRAWS_SHORT = 0x1
+FLAG_CELL_CLAMPED = 0x2
+FLAG_NONFINITE = 0x4
+BOX_MAX_SIPS = 8192
+ECOL_BOX_MAX_SIPS = 4096
+
+vp = ctypes.c_void_p
+i64 = ctypes.c_int64
+i32 = ctypes.c_int32
+dbl = ctypes.c_double
+u64 = ctypes.c_uint64
+sz = ctypes.c_size_t
+
+
+class Sips(ctypes.Structure):
+    _fields_ = [("n", i64), ("pos", vp), ("vel", vp), ("rel_pos", vp), ("m_w", vp), ("m_s", vp),
+                ("xi", vp), ("T_p", vp), ("cell", vp), ("water_removed", vp), ("no_cols", vp)]
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("nx", i64), ("nz", i64), ("scalar_fields", vp), ("mat_prop", vp),
+                ("velocity", vp), ("mass_flux_air_dry", vp), ("delta_m_l", vp),
+                ("x_min", dbl), ("x_max", dbl), ("z_min", dbl), ("z_max", dbl), ("dx", dbl),
+                ("dz", dbl), ("volume_cell", dbl), ("p_ref", dbl), ("p_ref_inv", dbl)]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("dt", dbl), ("dt_sub", dbl), ("dt_sub_half", dbl), ("dt_col_over_dV", dbl),
+                ("g_set", dbl), ("scale_dt_cond", i32), ("no_col_per_adv", i32),
+                ("act_collisions", i32), ("act_relaxation", i32), ("no_iter_impl_mass", i32),
+                ("solute", i32), ("init_profile_r_v", vp), ("init_profile_Theta", vp),
+                ("relaxation_time_profile", vp), ("E_col_grid", vp), ("E_col_const", dbl),
+                ("no_kernel_bins", i64), ("R_kernel_low_log", dbl), ("bin_factor_R_log", dbl)]
+
+
+class Draws(ctypes.Structure):
+    _fields_ = [("draws", vp), ("n_draws", i64), ("seed", u64)]
+
+
+P = ctypes.POINTER
+# name -> (restype, argtypes)
+PROTOTYPES = {
+    "lacmo_abi_version": (ctypes.c_int, []),
+    "lacmo_error_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "lacmo_workspace_bytes": (sz, [i64, i64, i64]),
+    "lacmo_workspace_reset": (ctypes.c_int, [vp, sz, i64, i64, i64, vp]),
+    "lacmo_read_flags": (ctypes.c_int, [vp, i64, i64, i64, P(ctypes.c_uint32), vp]),
+    "lacmo_cells_import": (ctypes.c_int, [vp, vp, vp, i64, i64, i64, vp]),
+    "lacmo_cells_export": (ctypes.c_int, [vp, vp, vp, vp, vp, i64, i64, i64, dbl, dbl, dbl, dbl,
+                                          vp]),
+    "lacmo_prepare": (ctypes.c_int, [P(Sips), P(Grid), P(Params), vp, sz, vp]),
+    "lacmo_integrate_adv_step": (ctypes.c_int, [P(Sips), P(Grid), P(Params), P(Draws), vp, sz,
+                                                vp]),
+    "lacmo_adv_step_begin": (ctypes.c_int, [P(Sips), P(Grid), P(Params), vp, sz, vp]),
+    "lacmo_adv_step_second_half": (ctypes.c_int, [P(Sips), P(Grid), P(Params), vp, sz, vp]),
+    "lacmo_adv_substep": (ctypes.c_int, [P(Sips), P(Grid), P(Params), dbl, ctypes.c_int, vp, sz,
+                                         vp]),
+    "lacmo_propagate_particles_subloop_step": (ctypes.c_int, [P(Sips), P(Grid), P(Params), dbl,
+                                                              dbl, vp, sz, vp]),
+    "lacmo_propagate_grid_subloop_step": (ctypes.c_int, [P(Grid), vp, vp, vp, vp]),
+    "lacmo_divergence_upwind": (ctypes.c_int, [vp, vp, i64, i64, dbl, dbl, ctypes.c_int,
+                                               ctypes.c_int, vp, vp]),
+    "lacmo_relaxation_term": (ctypes.c_int, [vp, i64, i64, vp, vp, dbl, vp, vp]),
+    "lacmo_update_grid_r_l": (ctypes.c_int, [P(Sips), P(Grid), vp, sz, vp]),
+    "lacmo_collision_step_cells": (ctypes.c_int, [P(Sips), P(Grid), P(Params), P(Draws), vp, sz,
+                                                  vp]),
+    "lacmo_collision_pair_count": (ctypes.c_int, [vp, i64, i64, i64, P(i64), vp]),
+    "lacmo_collision_step_golovin": (ctypes.c_int, [vp, vp, i64, dbl, vp, vp, u64, u64, vp]),
+    "lacmo_collision_step_ecol_grid_r_box": (ctypes.c_int, [vp, vp, vp, vp, vp, i64, dbl, vp, i64,
+                                                            dbl, dbl, vp, vp, u64, u64, vp]),
+    "lacmo_update_velocity_beard": (ctypes.c_int, [vp, vp, i64, vp]),
+    "lacmo_mass_rate_and_derivative": (ctypes.c_int, [ctypes.c_int, i64] + [vp] * 16 + [vp]),
+    "lacmo_newton_full": (ctypes.c_int, [ctypes.c_int, i64, dbl, ctypes.c_int] + [vp] * 16 + [vp]),
+    "lacmo_interpolate_velocity": (ctypes.c_int, [vp, vp, vp, i64, i64, i64, vp, vp]),
+    "lacmo_radius_and_bin": (ctypes.c_int, [vp, vp, i64, dbl, dbl, i64, vp, vp, vp]),
+}
+
+_lib = None
+
+
+class LacmoError(RuntimeError):
+    pass
+
+
+def load():
+    """Load the CUDA library (raises if it is missing: no fallback exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise LacmoError(
+            f"{LIB_PATH} is missing; build it with `python -m lacmopy_gb300.build` "
+            "(nvcc, sm_103a). The SIP hot path has no CPU fallback.")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in PROTOTYPES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if lib.lacmo_abi_version() != 1:
+        raise LacmoError("liblacmo_gb300.so ABI version mismatch")
+    _lib = lib
+    return lib
+
+
+def check(status, what=""):
+    if status != OK:
+        raise LacmoError(f"{what}: {ERRORS.get(status, status)} (status {status})")
+    return status

@@ -1,0 +1,395 @@
+// extern "C" entry points: argument checks, workspace carving and the
+// launch sequence of one advection step (integration.py:1298-1611).
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include "lacmo_internal.cuh"
+
+namespace lacmo {
+
+static inline size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct WsPlan {
+  size_t off[32];
+  size_t total;
+};
+
+static WsPlan ws_plan(int64_t n, int64_t nx, int64_t nz) {
+  const size_t C = (size_t)(nx * nz), N = (size_t)(n > 0 ? n : 1);
+  const size_t sizes[] = {
+      4 * C,           // counts
+      4 * (C + 1),     // start
+      8 * (C + 1),     // draw_off
+      4 * N,           // perm
+      4 * N,           // rank
+      8 * N,           // dmxi
+      4 * N,           // rm_id
+      8 * N,           // rm_val
+      8 * 6 * C,       // aux
+      8 * C,           // dTh
+      8 * C,           // drv
+      8 * C,           // div
+      8 * 2 * (size_t)nz,  // relax
+      8 * N,           // colR
+      8 * N,           // colrho
+      4 * N,           // colk
+      64,              // scalars
+  };
+  WsPlan p;
+  size_t o = 0;
+  for (size_t k = 0; k < sizeof(sizes) / sizeof(sizes[0]); ++k) {
+    p.off[k] = o;
+    o += al(sizes[k]);
+  }
+  p.total = o;
+  return p;
+}
+
+size_t ws_bytes(int64_t n, int64_t nx, int64_t nz) { return ws_plan(n, nx, nz).total; }
+
+bool ws_carve(void* base, size_t bytes, int64_t n, int64_t nx, int64_t nz, Ws* w) {
+  WsPlan p = ws_plan(n, nx, nz);
+  if (!base || bytes < p.total) return false;
+  char* b = (char*)base;
+  w->counts = (int32_t*)(b + p.off[0]);
+  w->start = (int32_t*)(b + p.off[1]);
+  w->draw_off = (int64_t*)(b + p.off[2]);
+  w->perm = (int32_t*)(b + p.off[3]);
+  w->rank = (int32_t*)(b + p.off[4]);
+  w->dmxi = (double*)(b + p.off[5]);
+  w->rm_id = (int32_t*)(b + p.off[6]);
+  w->rm_val = (double*)(b + p.off[7]);
+  w->aux = (double*)(b + p.off[8]);
+  w->dTh = (double*)(b + p.off[9]);
+  w->drv = (double*)(b + p.off[10]);
+  w->div = (double*)(b + p.off[11]);
+  w->relax = (double*)(b + p.off[12]);
+  w->colR = (double*)(b + p.off[13]);
+  w->colrho = (double*)(b + p.off[14]);
+  w->colk = (int32_t*)(b + p.off[15]);
+  char* sc = b + p.off[16];
+  w->flags = (uint32_t*)sc;
+  w->rm_count = (int32_t*)(sc + 4);
+  w->cursor = (int64_t*)(sc + 8);
+  w->col_step = (int64_t*)(sc + 16);
+  w->total_pairs = (int64_t*)(sc + 24);
+  return true;
+}
+
+static bool sips_ok(const lacmo_sips_t* s) {
+  return s && s->n > 0 && s->n < (int64_t)0x7fffffff && s->pos && s->vel && s->rel_pos && s->m_w &&
+         s->m_s && s->xi && s->T_p && s->cell && s->water_removed && s->no_cols;
+}
+static bool grid_ok(const lacmo_grid_t* g) {
+  return g && g->nx > 0 && g->nz > 0 && g->nx * g->nz < (int64_t)0x7fffffff && g->scalar_fields &&
+         g->mat_prop && g->velocity && g->mass_flux_air_dry && g->delta_m_l && g->dx > 0 &&
+         g->dz > 0;
+}
+static bool prm_ok(const lacmo_params_t* p) {
+  return p && p->no_iter_impl_mass >= 1 && (p->solute == 0 || p->solute == 1) &&
+         p->scale_dt_cond >= 1 && p->no_col_per_adv >= 1 &&
+         (p->E_col_grid == nullptr || p->no_kernel_bins > 0);
+}
+
+#define LCHK(x)                                   \
+  do {                                            \
+    if ((x) != cudaSuccess) return LACMO_ERR_CUDA; \
+  } while (0)
+
+// integration.py:1095-1294
+static int subloop(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
+                   const lacmo_draws_t& d, const Ws& w, int no_cond, int no_col, cudaStream_t s) {
+  const int64_t C = g.nx * g.nz;
+  const bool col = p.act_collisions != 0;
+  if (col && no_col == 1) LCHK(launch_collide_cells(sp, g, p, d, w, s));
+  for (int k = 0; k < no_cond; ++k) {
+    if (col && no_col > 1) LCHK(launch_collide_cells(sp, g, p, d, w, s));
+    LCHK(launch_particles(sp, g, p, p.dt_sub, p.dt_sub, false, w, s));
+    LCHK(launch_cell_update(sp, g, w, w.dTh, w.drv, true, s));
+    LCHK(launch_bin(sp, C, w, s));
+  }
+  if (col && no_col > no_cond) LCHK(launch_collide_cells(sp, g, p, d, w, s));
+  return LACMO_OK;
+}
+
+static int adv_step(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
+                    const lacmo_draws_t& d, const Ws& w, cudaStream_t s) {
+  const int64_t C = g.nx * g.nz;
+  // b) x_{n+1/2} (integration.py:1474-1481)
+  LCHK(launch_move(sp, g, p.dt_sub_half, w, s));
+  LCHK(launch_bin(sp, C, w, s));
+  // c) advective increments (+ relaxation)
+  LCHK(launch_advection(g, p, w, 1.0, false, s));
+  int no_col = p.no_col_per_adv == 1 ? 0 : (p.no_col_per_adv == 2 ? 1 : p.scale_dt_cond);
+  int rc = subloop(sp, g, p, d, w, p.scale_dt_cond, no_col, s);
+  if (rc) return rc;
+  // e) second-half increments
+  LCHK(launch_advection(g, p, w, 2.0, true, s));
+  no_col = (p.no_col_per_adv == 1 || p.no_col_per_adv == 2) ? 1 : p.scale_dt_cond;
+  rc = subloop(sp, g, p, d, w, p.scale_dt_cond - 1, no_col, s);
+  if (rc) return rc;
+  // last sub-step: positions move by dt_sub/2 (integration.py:1593-1610)
+  LCHK(launch_particles(sp, g, p, p.dt_sub, p.dt_sub_half, true, w, s));
+  LCHK(launch_cell_update(sp, g, w, w.dTh, w.drv, true, s));
+  LCHK(launch_bin(sp, C, w, s));
+  return LACMO_OK;
+}
+
+}  // namespace lacmo
+
+using namespace lacmo;
+
+extern "C" {
+
+int lacmo_abi_version(void) { return LACMO_ABI_VERSION; }
+
+const char* lacmo_error_string(int status) {
+  switch (status) {
+    case LACMO_OK: return "ok";
+    case LACMO_ERR_ARG: return "invalid argument";
+    case LACMO_ERR_CUDA: return "CUDA runtime error";
+    case LACMO_ERR_DRAWS: return "injected draw buffer too short";
+    case LACMO_ERR_WORKSPACE: return "workspace missing or too small";
+    case LACMO_ERR_CAPACITY: return "size above the fixed capacity";
+    default: return "unknown status";
+  }
+}
+
+size_t lacmo_workspace_bytes(int64_t n, int64_t nx, int64_t nz) {
+  if (n < 0 || nx <= 0 || nz <= 0) return 0;
+  return ws_bytes(n, nx, nz);
+}
+
+int lacmo_workspace_reset(void* ws, size_t bytes, int64_t n, int64_t nx, int64_t nz, void* stream) {
+  Ws w;
+  if (!ws_carve(ws, bytes, n, nx, nz, &w)) return LACMO_ERR_WORKSPACE;
+  LCHK(cudaMemsetAsync(ws, 0, ws_bytes(n, nx, nz), (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_read_flags(const void* ws, int64_t n, int64_t nx, int64_t nz, uint32_t* flags,
+                     void* stream) {
+  Ws w;
+  if (!flags || !ws_carve((void*)ws, ws_bytes(n, nx, nz), n, nx, nz, &w)) return LACMO_ERR_ARG;
+  LCHK(cudaMemcpyAsync(flags, w.flags, 4, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  LCHK(cudaStreamSynchronize((cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_cells_import(const int64_t* cells, const uint8_t* act, int32_t* cell, int64_t n,
+                       int64_t nx, int64_t nz, void* stream) {
+  if (!cells || !act || !cell || n <= 0 || nx <= 0 || nz <= 0) return LACMO_ERR_ARG;
+  LCHK(launch_cells_import(cells, act, cell, n, nx, nz, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_cells_export(const int32_t* cell, const double* pos, double* rel_pos, int64_t* cells,
+                       uint8_t* act, int64_t n, int64_t nx, int64_t nz, double x_min, double z_min,
+                       double dx, double dz, void* stream) {
+  if (!cell || !pos || !rel_pos || !cells || !act || n <= 0 || nx <= 0 || nz <= 0)
+    return LACMO_ERR_ARG;
+  LCHK(launch_cells_export(cell, pos, rel_pos, cells, act, n, nx, nz, x_min, z_min, dx, dz,
+                           (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_prepare(const lacmo_sips_t* sp, const lacmo_grid_t* g, const lacmo_params_t* p, void* ws,
+                  size_t bytes, void* stream) {
+  if (!sips_ok(sp) || !grid_ok(g) || !prm_ok(p)) return LACMO_ERR_ARG;
+  Ws w;
+  if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  LCHK(launch_cell_aux(*g, w, s));
+  LCHK(launch_histogram(sp->cell, sp->n, w, s));
+  LCHK(launch_bin(*sp, g->nx * g->nz, w, s));
+  return LACMO_OK;
+}
+
+int lacmo_integrate_adv_step(const lacmo_sips_t* sp, const lacmo_grid_t* g,
+                             const lacmo_params_t* p, const lacmo_draws_t* d, void* ws,
+                             size_t bytes, void* stream) {
+  if (!sips_ok(sp) || !grid_ok(g) || !prm_ok(p) || !d) return LACMO_ERR_ARG;
+  if (d->draws && d->n_draws < 0) return LACMO_ERR_ARG;
+  Ws w;
+  if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
+  return adv_step(*sp, *g, *p, *d, w, (cudaStream_t)stream);
+}
+
+int lacmo_adv_step_begin(const lacmo_sips_t* sp, const lacmo_grid_t* g, const lacmo_params_t* p,
+                         void* ws, size_t bytes, void* stream) {
+  if (!sips_ok(sp) || !grid_ok(g) || !prm_ok(p)) return LACMO_ERR_ARG;
+  Ws w;
+  if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  LCHK(launch_move(*sp, *g, p->dt_sub_half, w, s));
+  LCHK(launch_bin(*sp, g->nx * g->nz, w, s));
+  LCHK(launch_advection(*g, *p, w, 1.0, false, s));
+  return LACMO_OK;
+}
+
+int lacmo_adv_step_second_half(const lacmo_sips_t* sp, const lacmo_grid_t* g,
+                               const lacmo_params_t* p, void* ws, size_t bytes, void* stream) {
+  if (!sips_ok(sp) || !grid_ok(g) || !prm_ok(p)) return LACMO_ERR_ARG;
+  Ws w;
+  if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
+  LCHK(launch_advection(*g, *p, w, 2.0, true, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_adv_substep(const lacmo_sips_t* sp, const lacmo_grid_t* g, const lacmo_params_t* p,
+                      double dt_sub_pos, int write_T_p, void* ws, size_t bytes, void* stream) {
+  if (!sips_ok(sp) || !grid_ok(g) || !prm_ok(p)) return LACMO_ERR_ARG;
+  Ws w;
+  if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  LCHK(launch_particles(*sp, *g, *p, p->dt_sub, dt_sub_pos, write_T_p != 0, w, s));
+  LCHK(launch_cell_update(*sp, *g, w, w.dTh, w.drv, true, s));
+  LCHK(launch_bin(*sp, g->nx * g->nz, w, s));
+  return LACMO_OK;
+}
+
+int lacmo_propagate_particles_subloop_step(const lacmo_sips_t* sp, const lacmo_grid_t* g,
+                                           const lacmo_params_t* p, double dt_sub,
+                                           double dt_sub_pos, void* ws, size_t bytes,
+                                           void* stream) {
+  if (!sips_ok(sp) || !grid_ok(g) || !prm_ok(p)) return LACMO_ERR_ARG;
+  Ws w;
+  if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  LCHK(launch_cell_aux(*g, w, s));
+  LCHK(launch_particles(*sp, *g, *p, dt_sub, dt_sub_pos, true, w, s));
+  LCHK(launch_cell_update(*sp, *g, w, nullptr, nullptr, false, s));
+  LCHK(launch_bin(*sp, g->nx * g->nz, w, s));
+  return LACMO_OK;
+}
+
+int lacmo_propagate_grid_subloop_step(const lacmo_grid_t* g, const double* dTh, const double* drv,
+                                      const double* dml, void* stream) {
+  if (!grid_ok(g) || !dTh || !drv || !dml) return LACMO_ERR_ARG;
+  LCHK(launch_grid_only(*g, dTh, drv, dml, nullptr, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_divergence_upwind(const double* f, const double* flux, int64_t nx, int64_t nz, double dx,
+                            double dz, int bcx, int bcz, double* out, void* stream) {
+  if (!f || !flux || !out || nx <= 0 || nz <= 0 || (bcx != 0 && bcx != 1) ||
+      (bcz != 0 && bcz != 1))
+    return LACMO_ERR_ARG;
+  LCHK(launch_divergence(f, flux, nx, nz, dx, dz, bcx, bcz, out, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_relaxation_term(const double* f, int64_t nx, int64_t nz, const double* prof,
+                          const double* trel, double dt, double* out, void* stream) {
+  if (!f || !prof || !trel || !out || nx <= 0 || nz <= 0) return LACMO_ERR_ARG;
+  LCHK(launch_relaxation(f, nx, nz, prof, trel, dt, out, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_update_grid_r_l(const lacmo_sips_t* sp, const lacmo_grid_t* g, void* ws, size_t bytes,
+                          void* stream) {
+  if (!sips_ok(sp) || !grid_ok(g)) return LACMO_ERR_ARG;
+  Ws w;
+  if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
+  LCHK(launch_r_l_binned(*sp, *g, w, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_collision_step_cells(const lacmo_sips_t* sp, const lacmo_grid_t* g,
+                               const lacmo_params_t* p, const lacmo_draws_t* d, void* ws,
+                               size_t bytes, void* stream) {
+  if (!sips_ok(sp) || !grid_ok(g) || !prm_ok(p) || !d) return LACMO_ERR_ARG;
+  Ws w;
+  if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
+  if (d->draws) LCHK(cudaMemsetAsync(w.cursor, 0, 8, (cudaStream_t)stream));
+  LCHK(launch_collide_cells(*sp, *g, *p, *d, w, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_collision_pair_count(const void* ws, int64_t n, int64_t nx, int64_t nz, int64_t* pairs,
+                               void* stream) {
+  Ws w;
+  if (!pairs || !ws_carve((void*)ws, ws_bytes(n, nx, nz), n, nx, nz, &w)) return LACMO_ERR_ARG;
+  LCHK(cudaMemcpyAsync(pairs, w.total_pairs, 8, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  LCHK(cudaStreamSynchronize((cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_collision_step_golovin(double* xis, double* masses, int64_t n, double dtdv,
+                                 int64_t* no_cols, const double* rnd, uint64_t seed, uint64_t step,
+                                 void* stream) {
+  if (!xis || !masses || !no_cols || n < 0) return LACMO_ERR_ARG;
+  if (n > LACMO_BOX_MAX_SIPS) return LACMO_ERR_CAPACITY;
+  if (n < 2) return LACMO_OK;
+  LCHK(launch_golovin(xis, masses, n, dtdv, no_cols, rnd, seed, step, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_collision_step_ecol_grid_r_box(double* xis, double* masses, double* radii,
+                                         const double* vel, const double* rho, int64_t n,
+                                         double dtdv, const double* E, int64_t nb, double lo,
+                                         double bl, int64_t* no_cols, const double* rnd,
+                                         uint64_t seed, uint64_t step, void* stream) {
+  if (!xis || !masses || !radii || !vel || !rho || !E || nb <= 0 || !no_cols || n < 0)
+    return LACMO_ERR_ARG;
+  if (n > LACMO_ECOL_BOX_MAX_SIPS) return LACMO_ERR_CAPACITY;
+  if (n < 1) return LACMO_OK;
+  LCHK(launch_ecol_box(xis, masses, radii, vel, rho, n, dtdv, E, nb, lo, bl, no_cols, rnd, seed,
+                       step, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_update_velocity_beard(double* vel, const double* R, int64_t n, void* stream) {
+  if (!vel || !R || n < 0) return LACMO_ERR_ARG;
+  if (n == 0) return LACMO_OK;
+  LCHK(launch_beard(vel, R, n, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_mass_rate_and_derivative(int sol, int64_t n, const double* m_w, const double* m_s,
+                                   const double* w_s, const double* R_p, const double* T_p,
+                                   const double* rho_p, const double* T_amb, const double* p_amb,
+                                   const double* S_amb, const double* e_s_amb, const double* L_v,
+                                   const double* K, const double* D_v, const double* sigma_p,
+                                   double* gamma, double* dgamma, void* stream) {
+  InPtrs in = {{m_w, m_s, w_s, R_p, T_p, rho_p, T_amb, p_amb, S_amb, e_s_amb, L_v, K, D_v, sigma_p}};
+  for (int k = 0; k < 14; ++k)
+    if (!in.p[k]) return LACMO_ERR_ARG;
+  if (!gamma || !dgamma || n < 0 || (sol != 0 && sol != 1)) return LACMO_ERR_ARG;
+  if (n == 0) return LACMO_OK;
+  LCHK(launch_mass_rate(sol, n, in, gamma, dgamma, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_newton_full(int sol, int64_t n, double dt_sub, int no_iter, const double* m_w,
+                      const double* m_s, const double* w_s, const double* R_p, const double* T_p,
+                      const double* rho_p, const double* T_amb, const double* p_amb,
+                      const double* S_amb, const double* e_s_amb, const double* L_v,
+                      const double* K, const double* D_v, const double* sigma_p, double* dm,
+                      double* gamma0, void* stream) {
+  InPtrs in = {{m_w, m_s, w_s, R_p, T_p, rho_p, T_amb, p_amb, S_amb, e_s_amb, L_v, K, D_v, sigma_p}};
+  for (int k = 0; k < 14; ++k)
+    if (!in.p[k]) return LACMO_ERR_ARG;
+  if (!dm || !gamma0 || n < 0 || no_iter < 1 || (sol != 0 && sol != 1)) return LACMO_ERR_ARG;
+  if (n == 0) return LACMO_OK;
+  LCHK(launch_newton(sol, n, dt_sub, no_iter, in, dm, gamma0, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_interpolate_velocity(const int32_t* cell, const double* rel, const double* gv, int64_t n,
+                               int64_t nx, int64_t nz, double* out, void* stream) {
+  if (!cell || !rel || !gv || !out || n < 0 || nx <= 0 || nz <= 0) return LACMO_ERR_ARG;
+  if (n == 0) return LACMO_OK;
+  LCHK(launch_interp(cell, rel, gv, n, nx, nz, out, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_radius_and_bin(const double* m, const double* rho, int64_t n, double lo, double bl,
+                         int64_t nb, double* R, int64_t* bin, void* stream) {
+  if (!m || !rho || !R || n < 0 || (bin && nb <= 0)) return LACMO_ERR_ARG;
+  if (n == 0) return LACMO_OK;
+  LCHK(launch_radius_bin(m, rho, n, lo, bl, nb, R, bin, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+}  // extern "C"

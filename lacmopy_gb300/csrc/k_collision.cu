@@ -1,0 +1,467 @@
+// All-or-nothing (AON) collision kernels, bit-exact with the reference.
+//
+// The reference visits the pairs (i, j), i < j, of a cell in lexicographic
+// order and each pair may update SIPs i and j (collision/all_or_nothing.py:
+// 553-633).  Two pairs that share no SIP commute exactly, and every pair that
+// shares a SIP with (i, j) and comes earlier lexicographically has a smaller
+// index sum i + j, every later one a larger sum.  So processing the
+// anti-diagonals s = i + j = 1 .. 2n-3 in order, the pairs of one diagonal in
+// parallel, gives the sequential result bit for bit: 2n-3 barrier steps of at
+// most n/2 independent pairs.  The collision counters are integer sums.
+//
+// Bit-exactness also needs the reference's floating-point operation order
+// (this file is compiled with -fmad=false, so no a*b+c is fused) and the same
+// pow/log values: the radius (3/(4 pi) m/rho)^(1/3) and the kernel bin
+// int((log R - a)/b + 0.5) use the correctly-rounded routines of
+// lacmo_crmath.h.  Draws come either from an injected buffer in the
+// reference's consumption order or from Philox4x32-10.
+#include <cuda_runtime.h>
+
+#include "lacmo_crmath.h"
+#include "lacmo_internal.cuh"
+#include "lacmo_physics.cuh"
+
+namespace lacmo {
+
+__device__ __forceinline__ double col_radius(double m, double rho) {
+  return lacmo_cr_pow(LC_FOUR_PI_OVER_THREE_INV * m / rho, LC_ONE_THIRD);
+}
+// collision/all_or_nothing.py:35-67; float -> int as x86-64 compiled code
+// does it (NaN / out of range -> INT64_MIN -> bin 0)
+__device__ __forceinline__ int32_t col_bin(double R, double lo, double bl, int64_t nb) {
+  const double v = (lacmo_cr_log(R) - lo) / bl + 0.5;
+  int64_t ind = (v > -9.2233720368547758e18 && v < 9.2233720368547758e18) ? (int64_t)v : INT64_MIN;
+  if (ind < 0) ind = 0;
+  else if (ind > nb - 1) ind = nb - 1;
+  return (int32_t)ind;
+}
+__device__ __forceinline__ int64_t pair_rank(int64_t i, int64_t j, int64_t n) {
+  return i * n - i * (i + 1) / 2 + (j - i - 1);
+}
+
+// ---------------------------------------------------------------------------
+// 2-D cells: one warp per cell (collision/all_or_nothing.py:498-635, 637-751,
+// 754-846).  SIP state of cells with up to CELL_SMEM SIPs lives in shared
+// memory; larger cells use per-SIP global scratch.
+constexpr int CELL_SMEM = 256;
+constexpr int CELL_WARPS = 4;
+
+struct CellArgs {
+  double *xi, *m_w, *m_s;
+  const double* vel;
+  const double* T;
+  const int32_t *start, *perm;
+  const int64_t* draw_off;
+  int64_t n, C;
+  double dtdv;
+  const double* E;
+  double E_const;
+  int64_t nb;
+  double lo, bl;
+  int sol;
+  const double* draws;
+  int64_t n_draws;
+  uint64_t seed;
+  const int64_t *cursor, *col_step, *total_pairs;
+  int64_t* no_cols;
+  uint32_t* flags;
+  double *gR, *grho;
+  int32_t* gk;
+};
+
+__global__ void __launch_bounds__(CELL_WARPS * 32) k_collide_cells(CellArgs a) {
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double* base = smem + (size_t)wid * CELL_SMEM * 7;
+  int32_t* kbase = (int32_t*)(smem + (size_t)CELL_WARPS * CELL_SMEM * 7) + wid * CELL_SMEM;
+  const int64_t cursor = a.draws ? *a.cursor : 0;
+  if (a.draws && cursor + *a.total_pairs > a.n_draws) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.flags, LACMO_FLAG_DRAWS_SHORT);
+    return;
+  }
+  const uint64_t cstep = (uint64_t)*a.col_step;
+  const bool use_E = a.E != nullptr;
+  int64_t c0 = 0, c1 = 0;
+  for (int64_t c = blockIdx.x * (int64_t)CELL_WARPS + wid; c < a.C;
+       c += (int64_t)gridDim.x * CELL_WARPS) {
+    const int32_t b = a.start[c];
+    const int n = a.start[c + 1] - b;
+    if (n < 2) continue;
+    const bool in_smem = n <= CELL_SMEM;
+    const double Tc = a.T[c];
+    const double* rnd = a.draws ? a.draws + cursor + a.draw_off[c] : nullptr;
+    // state: shared memory (local index) or global scratch (by SIP ID)
+    double *sxi = base, *smw = base + CELL_SMEM, *sms = base + 2 * CELL_SMEM,
+           *sR = base + 3 * CELL_SMEM, *srho = base + 4 * CELL_SMEM, *su = base + 5 * CELL_SMEM,
+           *sw = base + 6 * CELL_SMEM;
+    int32_t* sk = kbase;
+    const int32_t* ids = a.perm + b;
+    // load, radius and bin at the cell temperature (all_or_nothing.py:812-826)
+    for (int q = lane; q < n; q += 32) {
+      const int32_t id = ids[q];
+      const double x = a.xi[id], mw = a.m_w[id], ms = a.m_s[id];
+      const double m_p = mw + ms;
+      const double w_s = ms / m_p;
+      const double rho = (a.sol == SOL_AS) ? density_water(Tc) * poly_rho_AS(w_s)
+                                           : density_NaCl_solution(w_s, Tc);
+      const double R = col_radius(m_p, rho);
+      const int32_t kb = use_E ? col_bin(R, a.lo, a.bl, a.nb) : 0;
+      if (in_smem) {
+        sxi[q] = x; smw[q] = mw; sms[q] = ms; sR[q] = R; srho[q] = rho;
+        su[q] = a.vel[id]; sw[q] = a.vel[a.n + id]; sk[q] = kb;
+      } else {
+        a.gR[id] = R; a.grho[id] = rho; a.gk[id] = kb;
+      }
+    }
+    __syncwarp();
+    for (int s = 1; s <= 2 * n - 3; ++s) {
+      const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
+      const int ihi = (s - 1) >> 1;
+      for (int i = ilo + lane; i <= ihi; i += 32) {
+        const int j = s - i;
+        // indices into the state arrays
+        int ii = i, jj = j;
+        double *XI = sxi, *MW = smw, *MS = sms, *RR = sR, *RHO = srho;
+        const double *U = su, *W = sw;
+        int32_t* KK = sk;
+        if (!in_smem) {
+          ii = ids[i]; jj = ids[j];
+          XI = a.xi; MW = a.m_w; MS = a.m_s; RR = a.gR; RHO = a.grho;
+          U = a.vel; W = a.vel + a.n; KK = a.gk;
+        }
+        int imin, imax;
+        if (XI[ii] <= XI[jj]) { imin = ii; imax = jj; } else { imin = jj; imax = ii; }
+        const double xi_min = XI[imin], xi_max = XI[imax];
+        const double m_w_min = MW[imin], m_w_max = MW[imax];
+        const double m_s_min = MS[imin], m_s_max = MS[imax];
+        const double Rs = RR[ii] + RR[jj];
+        const double e = use_E ? __ldg(a.E + (int64_t)KK[ii] * a.nb + KK[jj]) : a.E_const;
+        const double du = U[ii] - U[jj], dw = W[ii] - W[jj];
+        const double dv = sqrt(du * du + dw * dw);
+        const double p_crit = xi_max * a.dtdv * (LC_PI * Rs * Rs * e * dv * 1.0E-12);
+        if (p_crit > 1.0) {
+          const double xi_col = p_crit * xi_min;
+          MW[imin] = m_w_min + p_crit * m_w_max;
+          MS[imin] = m_s_min + p_crit * m_s_max;
+          RR[imin] = col_radius((MW[imin] + MS[imin]), RHO[imin]);
+          XI[imax] -= xi_col;
+          if (use_E) KK[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
+          c1 += 1;
+        } else {
+          const int64_t rk = pair_rank(i, j, n);
+          const double r = rnd ? rnd[rk]
+                               : philox_uniform(a.seed, (uint64_t)rk,
+                                                (cstep << 32) | (uint64_t)c);
+          if (p_crit > r) {
+            c0 += 1;
+            const double xi_rel_dev = (xi_max - xi_min) / xi_max;
+            if (xi_rel_dev < 1.0E-5) {
+              const double xi_ges = xi_min + xi_max;
+              MW[imin] = 2.0 * (xi_min * m_w_min + xi_max * m_w_max) / xi_ges;
+              MS[imin] = 2.0 * (xi_min * m_s_min + xi_max * m_s_max) / xi_ges;
+              MW[imax] = MW[imin];
+              MS[imax] = MS[imin];
+              RR[imin] = col_radius((MW[imin] + MS[imin]), RHO[imin]);
+              RR[imax] = RR[imin];
+              XI[imax] = 0.5 * 0.7 * xi_ges;
+              XI[imin] = 0.5 * xi_ges - XI[imax];
+              if (use_E) { KK[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb); KK[imax] = KK[imin]; }
+            } else {
+              MW[imin] += m_w_max;
+              MS[imin] += m_s_max;
+              RR[imin] = col_radius((MW[imin] + MS[imin]), RHO[imin]);
+              XI[imax] -= xi_min;
+              if (use_E) KK[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
+            }
+          }
+        }
+      }
+      if (!in_smem) __threadfence_block();
+      __syncwarp();
+    }
+    if (in_smem) {
+      for (int q = lane; q < n; q += 32) {
+        const int32_t id = ids[q];
+        a.xi[id] = sxi[q]; a.m_w[id] = smw[q]; a.m_s[id] = sms[q];
+      }
+    }
+    __syncwarp();
+  }
+  // counters (integer sums commute)
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    c0 += __shfl_down_sync(0xffffffffu, c0, off);
+    c1 += __shfl_down_sync(0xffffffffu, c1, off);
+  }
+  if (lane == 0 && (c0 | c1)) {
+    atomicAdd((unsigned long long*)a.no_cols, (unsigned long long)c0);
+    atomicAdd((unsigned long long*)(a.no_cols + 1), (unsigned long long)c1);
+  }
+}
+
+__global__ void k_col_advance(int64_t* cursor, int64_t* col_step, const int64_t* total,
+                              const uint32_t* flags, int draws) {
+  if (draws && !(*flags & LACMO_FLAG_DRAWS_SHORT)) *cursor += *total;
+  *col_step += 1;
+}
+
+// ---------------------------------------------------------------------------
+// Box models: one CTA runs the whole single-cell step, SIP state in shared
+// memory, one __syncthreads per anti-diagonal.
+constexpr int BOX_THREADS = 1024;
+
+// collision/all_or_nothing.py:109-185 (Golovin kernel, kernel.py:461-480)
+__global__ void __launch_bounds__(BOX_THREADS) k_golovin(double* xis, double* masses, int n,
+                                                         double dtdv, int64_t* no_cols,
+                                                         const double* rnd, uint64_t seed,
+                                                         uint64_t step) {
+  extern __shared__ double sm[];
+  double* X = sm;
+  double* M = sm + n;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) { X[q] = xis[q]; M[q] = masses[q]; }
+  __syncthreads();
+  int64_t c0 = 0, c1 = 0;
+  for (int s = 1; s <= 2 * n - 3; ++s) {
+    const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
+    const int ihi = (s - 1) >> 1;
+    for (int i = ilo + threadIdx.x; i <= ihi; i += blockDim.x) {
+      const int j = s - i;
+      int imin, imax;
+      if (X[i] <= X[j]) { imin = i; imax = j; } else { imin = j; imax = i; }
+      const double xi_min = X[imin], xi_max = X[imax];
+      const double m_min = M[imin], m_max = M[imax];
+      const double p_crit = xi_max * ((m_min + m_max) * 1.5E-18) * dtdv;
+      if (p_crit > 1.0) {
+        c1 += 1;
+        const double xi_col = p_crit * xi_min;
+        M[imin] = (xi_min * m_min + xi_col * m_max) / xi_min;
+        X[imax] -= xi_col;
+      } else {
+        const int64_t rk = pair_rank(i, j, n);
+        const double r = rnd ? rnd[rk] : philox_uniform(seed, (uint64_t)rk, step);
+        if (p_crit > r) {
+          c0 += 1;
+          const double xi_rel_dev = (xi_max - xi_min) / xi_max;
+          if (xi_rel_dev < 1.0E-5) {
+            const double xi_ges = xi_min + xi_max;
+            M[imin] = 2.0 * (xi_min * m_min + xi_max * m_max) / xi_ges;
+            M[imax] = M[imin];
+            X[imax] = 0.5 * 0.7 * xi_ges;
+            X[imin] = 0.5 * xi_ges - X[imax];
+          } else {
+            M[imin] += m_max;
+            X[imax] -= xi_min;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < n; q += blockDim.x) { xis[q] = X[q]; masses[q] = M[q]; }
+  for (int off = 16; off > 0; off >>= 1) {
+    c0 += __shfl_down_sync(0xffffffffu, c0, off);
+    c1 += __shfl_down_sync(0xffffffffu, c1, off);
+  }
+  if ((threadIdx.x & 31) == 0 && (c0 | c1)) {
+    atomicAdd((unsigned long long*)no_cols, (unsigned long long)c0);
+    atomicAdd((unsigned long long*)(no_cols + 1), (unsigned long long)c1);
+  }
+}
+
+// collision/all_or_nothing.py:269-390 (E_col(R1, R2) table, 1-D velocities)
+__global__ void __launch_bounds__(BOX_THREADS) k_ecol_box(double* xis, double* masses,
+                                                          double* radii, const double* vel,
+                                                          const double* rho, int n, double dtdv,
+                                                          const double* E, int64_t nb, double lo,
+                                                          double bl, int64_t* no_cols,
+                                                          const double* rnd, uint64_t seed,
+                                                          uint64_t step) {
+  extern __shared__ double sm[];
+  double* X = sm;
+  double* M = sm + n;
+  double* R = sm + 2 * n;
+  double* Vv = sm + 3 * n;
+  double* Rh = sm + 4 * n;
+  int32_t* K = (int32_t*)(sm + 5 * n);
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    X[q] = xis[q]; M[q] = masses[q]; R[q] = radii[q]; Vv[q] = vel[q]; Rh[q] = rho[q];
+    K[q] = col_bin(R[q], lo, bl, nb);
+  }
+  __syncthreads();
+  int64_t c0 = 0, c1 = 0;
+  for (int s = 1; s <= 2 * n - 3; ++s) {
+    const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
+    const int ihi = (s - 1) >> 1;
+    for (int i = ilo + threadIdx.x; i <= ihi; i += blockDim.x) {
+      const int j = s - i;
+      int imin, imax;
+      if (X[i] <= X[j]) { imin = i; imax = j; } else { imin = j; imax = i; }
+      const double xi_min = X[imin], xi_max = X[imax];
+      const double m_min = M[imin], m_max = M[imax];
+      const double Rs = R[i] + R[j];
+      const double p_crit = xi_max * dtdv *
+                            (LC_PI * Rs * Rs * __ldg(E + (int64_t)K[i] * nb + K[j]) *
+                             fabs(Vv[i] - Vv[j]) * 1.0E-12);
+      if (p_crit > 1.0) {
+        const double xi_col = p_crit * xi_min;
+        M[imin] = (xi_min * m_min + xi_col * m_max) / xi_min;
+        R[imin] = col_radius(M[imin], Rh[imin]);
+        X[imax] -= xi_col;
+        K[imin] = col_bin(R[imin], lo, bl, nb);
+        c1 += 1;
+      } else {
+        const int64_t rk = pair_rank(i, j, n);
+        const double r = rnd ? rnd[rk] : philox_uniform(seed, (uint64_t)rk, step);
+        if (p_crit > r) {
+          c0 += 1;
+          const double xi_rel_dev = (xi_max - xi_min) / xi_max;
+          if (xi_rel_dev < 1.0E-5) {
+            const double xi_ges = xi_min + xi_max;
+            M[imin] = 2.0 * (xi_min * m_min + xi_max * m_max) / xi_ges;
+            M[imax] = M[imin];
+            R[imin] = col_radius(M[imin], Rh[imin]);
+            R[imax] = R[imin];
+            X[imax] = 0.5 * 0.7 * xi_ges;
+            X[imin] = 0.5 * xi_ges - X[imax];
+            K[imin] = col_bin(R[imin], lo, bl, nb);
+            K[imax] = K[imin];
+          } else {
+            M[imin] += m_max;
+            R[imin] = col_radius(M[imin], Rh[imin]);
+            X[imax] -= xi_min;
+            K[imin] = col_bin(R[imin], lo, bl, nb);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < n; q += blockDim.x) { xis[q] = X[q]; masses[q] = M[q]; radii[q] = R[q]; }
+  for (int off = 16; off > 0; off >>= 1) {
+    c0 += __shfl_down_sync(0xffffffffu, c0, off);
+    c1 += __shfl_down_sync(0xffffffffu, c1, off);
+  }
+  if ((threadIdx.x & 31) == 0 && (c0 | c1)) {
+    atomicAdd((unsigned long long*)no_cols, (unsigned long long)c0);
+    atomicAdd((unsigned long long*)(no_cols + 1), (unsigned long long)c1);
+  }
+}
+
+// collision/kernel.py:107-167 Beard (1976) terminal velocity (R in um)
+__device__ double beard_velocity(double R) {
+  const double rho_w = 1.0E3, rho_a = 1.225, visc = 1.818E-5, sigma = 73.0E-3;
+  const double g = 9.80665, drho = rho_w - rho_a;
+  if (R < 10.0) {
+    const double l0 = 6.62E-2;
+    const double C1 = drho * g / (4.5 * visc);
+    const double C_sc = 1.0 + 1.257 * l0 / R;
+    return C1 * C_sc * R * R * 1.0E-12;
+  } else if (R < 535.0) {
+    const double N_Da = 32.0E-18 * R * R * R * rho_a * drho * g / (3.0 * visc * visc);
+    double Y = log(N_Da);
+    const double p1[7] = {-0.327815e-5, 0.855176e-4, -0.578878e-3, -0.987059e-3,
+                          -0.153193e-2, 0.992696, -0.318657e1};
+    double r = p1[0] * Y + p1[1];
+    for (int k = 2; k < 7; ++k) r = r * Y + p1[k];
+    const double l0 = 6.62E-2;
+    const double C_sc = 1.0 + 1.257 * l0 / R;
+    return visc * C_sc * exp(r) / (rho_a * R * 2.0E-6);
+  } else if (R < 3500.0) {
+    const double N_Bo = 16.0E-12 * R * R * drho * g / (3.0 * sigma);
+    const double v4 = (visc * visc) * (visc * visc);
+    const double N_P16 = pow(sigma * sigma * sigma * rho_a * rho_a / (v4 * drho * g), 1.0 / 6.0);
+    const double Y = log(N_Bo * N_P16);
+    const double p2[6] = {0.238449e-2, -0.542819e-1, 0.475294, -0.204914e1, 0.523778e1,
+                          -0.500015e1};
+    double r = p2[0] * Y + p2[1];
+    for (int k = 2; k < 6; ++k) r = r * Y + p2[k];
+    return visc * N_P16 * exp(r) / (rho_a * R * 2.0E-6);
+  }
+  return 9.04929248;
+}
+__global__ void k_beard(double* vel, const double* R, int64_t n) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    vel[k] = beard_velocity(R[k]);
+}
+__global__ void k_radius_bin(const double* m, const double* rho, int64_t n, double lo, double bl,
+                             int64_t nb, double* R, int64_t* k) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const double r = col_radius(m[q], rho[q]);
+    R[q] = r;
+    if (k) k[q] = col_bin(r, lo, bl, nb);
+  }
+}
+
+// ---------------------------------------------------------------------------
+static inline int nblk(int64_t n, int t) {
+  int64_t b = (n + t - 1) / t;
+  if (b < 1) b = 1;
+  return (int)(b < 152 * 32 ? b : 152 * 32);
+}
+static const size_t CELL_SMEM_BYTES = (size_t)CELL_WARPS * CELL_SMEM * (7 * 8 + 4);
+
+cudaError_t launch_collide_cells(const lacmo_sips_t& sp, const lacmo_grid_t& g,
+                                 const lacmo_params_t& p, const lacmo_draws_t& d, const Ws& w,
+                                 cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_collide_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)CELL_SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  CellArgs a;
+  a.xi = sp.xi; a.m_w = sp.m_w; a.m_s = sp.m_s; a.vel = sp.vel; a.T = g.scalar_fields;
+  a.start = w.start; a.perm = w.perm; a.draw_off = w.draw_off;
+  a.n = sp.n; a.C = g.nx * g.nz; a.dtdv = p.dt_col_over_dV;
+  a.E = p.E_col_grid; a.E_const = p.E_col_const; a.nb = p.no_kernel_bins;
+  a.lo = p.R_kernel_low_log; a.bl = p.bin_factor_R_log; a.sol = p.solute;
+  a.draws = d.draws; a.n_draws = d.n_draws; a.seed = d.seed;
+  a.cursor = w.cursor; a.col_step = w.col_step; a.total_pairs = w.total_pairs;
+  a.no_cols = sp.no_cols; a.flags = w.flags;
+  a.gR = w.colR; a.grho = w.colrho; a.gk = w.colk;
+  int blocks = nblk((a.C + CELL_WARPS - 1) / CELL_WARPS, 1);
+  k_collide_cells<<<blocks, CELL_WARPS * 32, CELL_SMEM_BYTES, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_col_advance<<<1, 1, 0, s>>>(w.cursor, w.col_step, w.total_pairs, w.flags, d.draws ? 1 : 0);
+  return cudaGetLastError();
+}
+cudaError_t launch_col_advance(const Ws& w, cudaStream_t s) {
+  k_col_advance<<<1, 1, 0, s>>>(w.cursor, w.col_step, w.total_pairs, w.flags, 0);
+  return cudaGetLastError();
+}
+cudaError_t launch_golovin(double* xis, double* m, int64_t n, double dtdv, int64_t* no_cols,
+                           const double* rnd, uint64_t seed, uint64_t step, cudaStream_t s) {
+  size_t sh = (size_t)n * 16;
+  cudaError_t e = cudaFuncSetAttribute(k_golovin, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(LACMO_BOX_MAX_SIPS * 16));
+  if (e != cudaSuccess) return e;
+  k_golovin<<<1, BOX_THREADS, sh, s>>>(xis, m, (int)n, dtdv, no_cols, rnd, seed, step);
+  return cudaGetLastError();
+}
+cudaError_t launch_ecol_box(double* xis, double* m, double* R, const double* vel,
+                            const double* rho, int64_t n, double dtdv, const double* E, int64_t nb,
+                            double lo, double bl, int64_t* no_cols, const double* rnd,
+                            uint64_t seed, uint64_t step, cudaStream_t s) {
+  size_t sh = (size_t)n * 44;
+  cudaError_t e = cudaFuncSetAttribute(k_ecol_box, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(LACMO_ECOL_BOX_MAX_SIPS * 44));
+  if (e != cudaSuccess) return e;
+  k_ecol_box<<<1, BOX_THREADS, sh, s>>>(xis, m, R, vel, rho, (int)n, dtdv, E, nb, lo, bl, no_cols,
+                                        rnd, seed, step);
+  return cudaGetLastError();
+}
+cudaError_t launch_beard(double* vel, const double* R, int64_t n, cudaStream_t s) {
+  k_beard<<<nblk(n, 128), 128, 0, s>>>(vel, R, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_radius_bin(const double* m, const double* rho, int64_t n, double lo, double bl,
+                              int64_t nb, double* R, int64_t* k, cudaStream_t s) {
+  k_radius_bin<<<nblk(n, 128), 128, 0, s>>>(m, rho, n, lo, bl, nb, R, k);
+  return cudaGetLastError();
+}
+
+}  // namespace lacmo

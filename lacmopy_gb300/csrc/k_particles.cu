@@ -1,0 +1,694 @@
+// Particle, grid and cell-binning kernels of the SIP hot path (FP64).
+//
+// k_particles fuses one whole particle sub-step of the reference
+// (integration.py:944-1091): T_p from the cell, radius / mass fraction /
+// density, the implicit Newton condensation (integration.py:728-940), the
+// implicit drag update with the staggered bilinear wind interpolation
+// (integration.py:632-719, grid.py:257-323), the Euler position update with
+// periodic x, capped z and ground removal (integration.py:552-630) and the
+// cell re-index (integration.py:509-550).  It reads each SIP attribute once
+// and writes it once; grid data come from small L2-resident arrays.
+//
+// Order-dependent sums the reference accumulates in ascending SIP ID (the
+// per-cell condensed mass delta_m_l, integration.py:916-936, and
+// water_removed, integration.py:620-628) are formed here in the same order:
+// k_cell_update folds each cell's dm*xi over the cell's SIPs sorted by ID, and
+// the removal list is sorted by ID before it is folded.  Results are therefore
+// deterministic and, given identical per-SIP values, equal to the reference's.
+#include <cuda_runtime.h>
+
+#include "lacmo_internal.cuh"
+#include "lacmo_physics.cuh"
+
+namespace lacmo {
+
+static inline int nblocks(int64_t n, int t, int cap = 152 * 32) {
+  int64_t b = (n + t - 1) / t;
+  if (b < 1) b = 1;
+  return (int)(b < cap ? b : cap);
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_cells_import(const int64_t* __restrict__ cells, const uint8_t* __restrict__ act,
+                               int32_t* __restrict__ cell, int64_t n, int64_t nz) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = cells[k], j = cells[n + k];
+    cell[k] = act[k] ? (int32_t)(i * nz + j) : (int32_t)(-1 - i);
+  }
+}
+
+__global__ void k_cells_export(const int32_t* __restrict__ cell, const double* __restrict__ pos,
+                               double* __restrict__ rel, int64_t* __restrict__ cells,
+                               uint8_t* __restrict__ act, int64_t n, int64_t nz, double x_min,
+                               double z_min, double dx, double dz) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    int32_t c = cell[k];
+    if (c >= 0) {
+      int64_t i = c / nz, j = c - (c / nz) * nz;
+      cells[k] = i; cells[n + k] = j; act[k] = 1;
+      rel[k] = (pos[k] - x_min) / dx - (double)i;
+      rel[n + k] = (pos[n + k] - z_min) / dz - (double)j;
+    } else {
+      cells[k] = -1 - (int64_t)c; cells[n + k] = -1; act[k] = 0;
+    }
+  }
+}
+
+// per-cell terms of the mass rate for the next sub-step
+__device__ __forceinline__ void write_aux(const double* gsf, const double* gmp, double* aux,
+                                          int64_t c, int64_t C) {
+  CellAmb a = make_cell_amb(gsf[c], gsf[C + c], gsf[6 * C + c], gsf[7 * C + c], gmp[2 * C + c],
+                            gmp[c], gmp[C + c]);
+  aux[c] = a.sigw; aux[C + c] = a.rhow; aux[2 * C + c] = a.lap0; aux[3 * C + c] = a.lbp0;
+  aux[4 * C + c] = a.c1; aux[5 * C + c] = a.c2;
+}
+
+__global__ void k_cell_aux(const double* gsf, const double* gmp, double* aux, int64_t C) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
+       c += (int64_t)gridDim.x * blockDim.x)
+    write_aux(gsf, gmp, aux, c, C);
+}
+
+// ---------------------------------------------------------------------------
+// binning: histogram (arrival rank) -> scan -> scatter -> order by ID
+__global__ void k_histogram(const int32_t* __restrict__ cell, int64_t n, int32_t* counts,
+                            int32_t* rank) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    int32_t c = cell[k];
+    if (c >= 0) rank[k] = atomicAdd(counts + c, 1);
+  }
+}
+
+// Single block: folds the sorted ground-removal list into water_removed, then
+// the exclusive scans of the SIP counts (slots) and pair counts (draws).
+__global__ void __launch_bounds__(1024) k_scan(int32_t* counts, int32_t* start, int64_t* draw_off,
+                                               int64_t* total_pairs, int64_t C, int32_t* rm_count,
+                                               int32_t* rm_id, double* rm_val,
+                                               double* water_removed) {
+  __shared__ int64_t s_slot[1024];
+  __shared__ int64_t s_pair[1024];
+  __shared__ int32_t s_id[2048];
+  __shared__ double s_val[2048];
+  const int t = threadIdx.x;
+  // ---- ground removals, ascending ID (integration.py:620-628) ----
+  int nrm = *rm_count;
+  if (nrm > 0 && nrm <= 2048) {
+    int P = 1;
+    while (P < nrm) P <<= 1;
+    for (int q = t; q < P; q += blockDim.x) {
+      s_id[q] = q < nrm ? rm_id[q] : 0x7fffffff;
+      s_val[q] = q < nrm ? rm_val[q] : 0.0;
+    }
+    __syncthreads();
+    for (int kk = 2; kk <= P; kk <<= 1) {
+      for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+        for (int q = t; q < P; q += blockDim.x) {
+          int p2 = q ^ jj;
+          if (p2 > q) {
+            bool up = ((q & kk) == 0);
+            int a = s_id[q], b = s_id[p2];
+            if ((a > b) == up) {
+              s_id[q] = b; s_id[p2] = a;
+              double v = s_val[q]; s_val[q] = s_val[p2]; s_val[p2] = v;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    if (t == 0) {
+      double wr = water_removed[0];
+      for (int q = 0; q < nrm; ++q) wr += s_val[q];
+      water_removed[0] = wr;
+    }
+    __syncthreads();
+  } else if (nrm > 2048) {
+    // rare: repeated extraction of the smallest remaining ID
+    if (t == 0) {
+      double wr = water_removed[0];
+      int32_t last = -1;
+      for (int r = 0; r < nrm; ++r) {
+        int32_t best = 0x7fffffff; int bq = -1;
+        for (int q = 0; q < nrm; ++q)
+          if (rm_id[q] > last && rm_id[q] < best) { best = rm_id[q]; bq = q; }
+        wr += rm_val[bq];
+        last = best;
+      }
+      water_removed[0] = wr;
+    }
+    __syncthreads();
+  }
+  if (t == 0) *rm_count = 0;
+  // ---- scans ----
+  int64_t chunk = (C + blockDim.x - 1) / blockDim.x;
+  int64_t b0 = t * chunk, b1 = b0 + chunk < C ? b0 + chunk : C;
+  int64_t ss = 0, sp = 0;
+  for (int64_t c = b0; c < b1; ++c) {
+    int64_t m = counts[c];
+    ss += m; sp += m * (m - 1) / 2;
+  }
+  s_slot[t] = ss; s_pair[t] = sp;
+  __syncthreads();
+  for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+    int64_t a = t >= off ? s_slot[t - off] : 0, b = t >= off ? s_pair[t - off] : 0;
+    __syncthreads();
+    s_slot[t] += a; s_pair[t] += b;
+    __syncthreads();
+  }
+  int64_t os = s_slot[t] - ss, op = s_pair[t] - sp;
+  for (int64_t c = b0; c < b1; ++c) {
+    int64_t m = counts[c];
+    start[c] = (int32_t)os; draw_off[c] = op;
+    os += m; op += m * (m - 1) / 2;
+    counts[c] = 0;
+  }
+  if (t == blockDim.x - 1) { start[C] = (int32_t)os; draw_off[C] = op; *total_pairs = op; }
+}
+
+__global__ void k_scatter(const int32_t* __restrict__ cell, const int32_t* __restrict__ rank,
+                          const int32_t* __restrict__ start, int32_t* perm, int64_t n) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    int32_t c = cell[k];
+    if (c >= 0) perm[start[c] + rank[k]] = (int32_t)k;
+  }
+}
+
+// one warp per cell: order the cell's slots by ascending SIP ID
+constexpr int ORDER_SMEM = 256;
+__global__ void __launch_bounds__(256) k_order(const int32_t* __restrict__ start, int32_t* perm,
+                                               int32_t* scratch, int64_t C) {
+  __shared__ int32_t s_ids[8][ORDER_SMEM];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int64_t c = blockIdx.x * 8LL + wid; c < C; c += (int64_t)gridDim.x * 8) {
+    const int32_t b = start[c], L = start[c + 1] - b;
+    if (L <= 1) continue;
+    if (L <= ORDER_SMEM) {
+      for (int q = lane; q < L; q += 32) s_ids[wid][q] = perm[b + q];
+      __syncwarp();
+      int32_t mine[ORDER_SMEM / 32];
+      int32_t r[ORDER_SMEM / 32];
+#pragma unroll
+      for (int u = 0; u < ORDER_SMEM / 32; ++u) { mine[u] = 0; r[u] = 0; }
+#pragma unroll
+      for (int u = 0; u < ORDER_SMEM / 32; ++u)
+        if (lane + 32 * u < L) mine[u] = s_ids[wid][lane + 32 * u];
+      for (int q = 0; q < L; ++q) {
+        int32_t v = s_ids[wid][q];
+#pragma unroll
+        for (int u = 0; u < ORDER_SMEM / 32; ++u) r[u] += (v < mine[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < ORDER_SMEM / 32; ++u)
+        if (lane + 32 * u < L) perm[b + r[u]] = mine[u];
+      __syncwarp();
+    } else {
+      for (int q = lane; q < L; q += 32) scratch[b + q] = perm[b + q];
+      __syncwarp();
+      for (int q = lane; q < L; q += 32) {
+        int32_t v = scratch[b + q];
+        int32_t r = 0;
+        for (int p = 0; p < L; ++p) r += (scratch[b + p] < v);
+        perm[b + r] = v;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+struct PArgs {
+  double *pos, *vel, *m_w, *rel, *T_p;
+  const double *m_s, *xi;
+  int32_t* cell;
+  const double *gsf, *gmp, *aux, *gv;
+  int64_t n, nx, nz;
+  double x_min, x_max, z_min, z_cap, dx, dz;
+  double dt_sub, dt_pos, g_set;
+  int no_iter, sol, write_Tp;
+  double* dmxi;
+  int32_t *counts, *rank, *rm_count, *rm_id;
+  double* rm_val;
+  uint32_t* flags;
+};
+
+template <bool PHYS>
+__global__ void __launch_bounds__(128) k_particles(PArgs a) {
+  const int64_t C = a.nx * a.nz;
+  const GridVel gv{a.gv, a.nx, a.nz};
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c = a.cell[k];
+    const bool active = c >= 0;
+    const int64_t i = active ? (int64_t)c / a.nz : (int64_t)(-1 - c);
+    const int64_t j = active ? (int64_t)c - i * a.nz : -1;
+    double x = a.pos[k], z = a.pos[a.n + k];
+    double u = a.vel[k], w = a.vel[a.n + k];
+    double mw = a.m_w[k];
+    double xik = 0.0;
+    double rel_x = 0.0, rel_z = 0.0;
+    if (PHYS) {
+      const double T_p = __ldg(a.gsf + i * a.nz + (active ? j : a.nz - 1));
+      if (a.write_Tp) a.T_p[k] = T_p;
+      if (active) {
+        CellAmb amb;
+        amb.T = T_p; amb.p = __ldg(a.gsf + C + c); amb.S = __ldg(a.gsf + 6 * C + c);
+        amb.e_s = __ldg(a.gsf + 7 * C + c); amb.K = __ldg(a.gmp + c); amb.D_v = __ldg(a.gmp + C + c);
+        amb.L_v = __ldg(a.gmp + 2 * C + c);
+        amb.sigw = __ldg(a.aux + c); amb.rhow = __ldg(a.aux + C + c);
+        amb.lap0 = __ldg(a.aux + 2 * C + c); amb.lbp0 = __ldg(a.aux + 3 * C + c);
+        amb.c1 = __ldg(a.aux + 4 * C + c); amb.c2 = __ldg(a.aux + 5 * C + c);
+        const double ms = a.m_s[k];
+        xik = a.xi[k];
+        // integration.py:1044 compute_R_p_w_s_rho_p, :916-936 Newton
+        double m_p = mw + ms;
+        double w_s = ms / m_p;
+        double rho = (a.sol == SOL_AS) ? density_AS_solution_rw(w_s, amb.rhow)
+                                       : density_NaCl_solution(w_s, T_p);
+        double R = radius_from_mass(m_p, rho);
+        double sig = (a.sol == SOL_AS) ? surface_tension_AS_sw(w_s, amb.sigw)
+                                       : surface_tension_NaCl_sw(w_s, amb.sigw);
+        double dm = newton_full(a.sol, a.dt_sub, a.no_iter, mw, ms, w_s, R, T_p, rho, sig, amb,
+                                nullptr);
+        mw += dm;
+        a.dmxi[k] = dm * xik;
+        // integration.py:1075 radius of ammonium sulfate whatever the solute
+        m_p = mw + ms;
+        w_s = ms / m_p;
+        rho = density_AS_solution_rw(w_s, amb.rhow);
+        R = radius_from_mass(m_p, rho);
+        // integration.py:699-718
+        rel_x = (x - a.x_min) / a.dx - (double)i;
+        rel_z = (z - a.z_min) / a.dz - (double)j;
+        double uf, wf;
+        gv.interp(i, j, rel_x, rel_z, uf, wf);
+        const double mu_f = __ldg(a.gmp + 5 * C + c), rho_f = __ldg(a.gmp + 6 * C + c);
+        const double d0 = uf - u, d1 = wf - w;
+        const double vel_dev = sqrt(d0 * d0 + d1 * d1);
+        const double Re_p = 2.0E-6 * rho_f * R * vel_dev / mu_f;
+        double k_dt = 4.5E12 * a.dt_sub * mu_f / (rho * R * R);
+        if (Re_p > 0.5) {
+          if (Re_p < 1000.0) k_dt *= (1 + 0.15 * pow(Re_p, 0.687));
+          else k_dt *= 0.0183333333333 * Re_p;
+        }
+        u = (u + k_dt * uf) / (1.0 + k_dt);
+        w = (w + k_dt * wf - a.dt_sub * a.g_set) / (1.0 + k_dt);
+      }
+    } else if (active) {
+      xik = a.xi[k];
+      rel_x = (x - a.x_min) / a.dx - (double)i;
+      rel_z = (z - a.z_min) / a.dz - (double)j;
+    }
+    // integration.py:552-630
+    x += a.dt_pos * u;
+    z += a.dt_pos * w;
+    x = py_mod(x, a.x_max);
+    z = np_min(z, a.z_cap);
+    int32_t newc = c;
+    if (active) {
+      if (z <= a.z_min) {
+        z = a.z_min - 0.01 * a.dz;
+        u = 0.0; w = 0.0;
+        const int slot = atomicAdd(a.rm_count, 1);
+        a.rm_id[slot] = (int32_t)k;
+        a.rm_val[slot] = xik * mw;
+        // the re-index of this call leaves the old relative position divided
+        // by the cell size (integration.py:548-549)
+        a.rel[k] = rel_x / a.dx - (double)i;
+        a.rel[a.n + k] = rel_z / a.dz - (-1.0);
+        newc = (int32_t)(-1 - i);
+      } else {
+        int64_t ci = (int64_t)floor(x / a.dx), cj = (int64_t)floor(z / a.dz);
+        if (ci >= a.nx || ci < 0 || cj >= a.nz || cj < 0) {
+          atomicOr(a.flags, LACMO_FLAG_CELL_CLAMPED);
+          ci = ci < 0 ? 0 : (ci >= a.nx ? a.nx - 1 : ci);
+          cj = cj < 0 ? 0 : (cj >= a.nz ? a.nz - 1 : cj);
+        }
+        newc = (int32_t)(ci * a.nz + cj);
+        a.rank[k] = atomicAdd(a.counts + newc, 1);
+      }
+    } else {
+      a.rel[k] = a.rel[k] / a.dx - (double)i;
+      a.rel[a.n + k] = a.rel[a.n + k] / a.dz - (-1.0);
+    }
+    a.pos[k] = x; a.pos[a.n + k] = z;
+    a.vel[k] = u; a.vel[a.n + k] = w;
+    if (PHYS && active) a.m_w[k] = mw;
+    a.cell[k] = newc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// integration.py:402-484 for one cell (and update_material_properties :359)
+__device__ __forceinline__ void grid_cell_update(double* gsf, double* gmp, int64_t c, int64_t C,
+                                                 double p_ref, double p_ref_inv, double dTh,
+                                                 double drv, double dml, double V) {
+  double Th = gsf[2 * C + c];
+  const double rho_d = gsf[3 * C + c];
+  double r_v = gsf[4 * C + c];
+  const double mdi = gsf[8 * C + c];
+  const double L_v = gmp[2 * C + c];
+  Th += dTh;
+  r_v += drv - dml * mdi;
+  const double ToT = pow(p_ref_inv * LC_R_D * rho_d * Th, LC_KAPPA_FACTOR2);
+  Th += ToT * (L_v * dml) / (LC_C_PD * rho_d * V * (1.0 + r_v * LC_HEAT_FACTOR_R_V));
+  const double pdr = pow(rho_d * Th * LC_R_D * p_ref_inv, LC_KAPPA_FACTOR);
+  const double T = Th * pow(pdr, LC_KAPPA_AIR_DRY);
+  const double p = pdr * p_ref * (1 + r_v / LC_EPSILON_GC);
+  const double e_s = 2.53E11 * exp(-5420.0 / T);
+  const double S = rho_d * r_v * T * LC_R_V / e_s;
+  gsf[c] = T; gsf[C + c] = p; gsf[2 * C + c] = Th; gsf[4 * C + c] = r_v;
+  gsf[6 * C + c] = S; gsf[7 * C + c] = e_s;
+  gmp[c] = 4.1868E-3 * (5.69 + 0.017 * (T - 273.15));
+  gmp[C + c] = 4.01218E-5 * pow(T, 1.94) / p;
+  gmp[2 * C + c] = 1.0E3 * (2500.82 - 2.358 * (T - 273.0));
+  gmp[3 * C + c] = surface_tension_water(T);
+  gmp[4 * C + c] = LC_C_PD * (1 + 0.897 * r_v);
+  gmp[5 * C + c] = 1.458E-6 * pow(T, 1.5) / (T + 110.4);
+  gmp[6 * C + c] = rho_d * (1.0 + r_v);
+}
+
+// one warp per cell: delta_m_l as the ascending-ID fold of dm*xi over the
+// cell's SIPs, then the grid update of the cell and its mass-rate terms
+__global__ void __launch_bounds__(256) k_cell_update(const int32_t* __restrict__ start,
+                                                     const int32_t* __restrict__ perm,
+                                                     const double* __restrict__ dmxi,
+                                                     double* delta_m_l, double* gsf, double* gmp,
+                                                     double* aux, const double* dTh,
+                                                     const double* drv, int64_t C, double p_ref,
+                                                     double p_ref_inv, double V, int grid_update) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; c < C;
+       c += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int32_t b = start[c], e = start[c + 1];
+    double acc = 0.0;
+    for (int32_t base = b; base < e; base += 32) {
+      const int32_t idx = base + lane;
+      const double v = idx < e ? dmxi[perm[idx]] : 0.0;
+      const int m = (e - base) < 32 ? (e - base) : 32;
+      for (int q = 0; q < m; ++q) acc += __shfl_sync(0xffffffffu, v, q);
+    }
+    if (lane == 0) {
+      const double dml = acc * 1.0E-18;
+      delta_m_l[c] = dml;
+      if (grid_update) {
+        grid_cell_update(gsf, gmp, c, C, p_ref, p_ref_inv, dTh[c], drv[c], dml, V);
+        write_aux(gsf, gmp, aux, c, C);
+      }
+    }
+  }
+}
+
+__global__ void k_grid_only(double* gsf, double* gmp, double* aux, const double* dTh,
+                            const double* drv, const double* dml, int64_t C, double p_ref,
+                            double p_ref_inv, double V) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    grid_cell_update(gsf, gmp, c, C, p_ref, p_ref_inv, dTh[c], drv[c], dml[c], V);
+    if (aux) write_aux(gsf, gmp, aux, c, C);
+  }
+}
+
+// grid.py:370-412 (ascending-ID fold per cell)
+__global__ void __launch_bounds__(256) k_r_l(const int32_t* __restrict__ start,
+                                             const int32_t* __restrict__ perm,
+                                             const double* __restrict__ m_w,
+                                             const double* __restrict__ xi, double* gsf, int64_t C) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; c < C;
+       c += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int32_t b = start[c], e = start[c + 1];
+    double acc = 0.0;
+    for (int32_t base = b; base < e; base += 32) {
+      const int32_t idx = base + lane;
+      double v = 0.0;
+      if (idx < e) { int32_t id = perm[idx]; v = m_w[id] * xi[id]; }
+      const int m = (e - base) < 32 ? (e - base) : 32;
+      for (int q = 0; q < m; ++q) acc += __shfl_sync(0xffffffffu, v, q);
+    }
+    if (lane == 0) gsf[5 * C + c] = acc * (1.0E-18 * gsf[8 * C + c]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// integration.py:80-148 limiter and face flux (Hundsdorfer et al. 1995)
+__device__ __forceinline__ double limiter_arg(double a0, double a1, double a2) {
+  const double r = (fabs(a1 - a2) > 1.0E-8 * fabs(a0 - a1)) ? (a0 - a1) / (a1 - a2)
+                                                             : (a0 - a1) * 1.0E8 * np_sign(a1 - a2);
+  const double K = (1.0 + 2.0 * r) * LC_ONE_THIRD;
+  return np_max(0.0, fmin(2.0 * r, fmin(K, 2.0)));
+}
+__device__ __forceinline__ double face_flux(double u, double am2, double am1, double a0,
+                                            double ap1) {
+  const double lp = limiter_arg(a0, am1, am2);
+  const double f_pos = am1 + 0.5 * lp * (am1 - am2);
+  const double ln = limiter_arg(am1, a0, ap1);
+  const double f_neg = a0 + 0.5 * ln * (a0 - ap1);
+  return (u >= 0.0) ? u * f_pos : u * f_neg;
+}
+__device__ __forceinline__ int64_t bc_idx(int64_t i, int64_t N, int bc) {
+  if (bc == 0) { i %= N; return i < 0 ? i + N : i; }
+  return i < 0 ? 0 : (i > N - 1 ? N - 1 : i);
+}
+// integration.py:150-287, divergence of field * flux in cell (i, j)
+__device__ double divergence_cell(const double* f, const double* flux, int64_t nx, int64_t nz,
+                                  int64_t i, int64_t j, double dx, double dz, int bcx, int bcz) {
+  double Fx[2], Fz[2];
+  for (int s = 0; s < 2; ++s) {
+    const int64_t fi = i + s;  // face index
+    double u = flux[fi * (nz + 1) + j];
+    Fx[s] = face_flux(u, f[bc_idx(fi - 2, nx, bcx) * nz + j], f[bc_idx(fi - 1, nx, bcx) * nz + j],
+                      f[bc_idx(fi, nx, bcx) * nz + j], f[bc_idx(fi + 1, nx, bcx) * nz + j]);
+    if (bcx == 1 && (fi == 0 || fi == nx)) Fx[s] = 0.0;
+    const int64_t fj = j + s;
+    double w = flux[(nx + 1) * (nz + 1) + i * (nz + 1) + fj];
+    Fz[s] = face_flux(w, f[i * nz + bc_idx(fj - 2, nz, bcz)], f[i * nz + bc_idx(fj - 1, nz, bcz)],
+                      f[i * nz + bc_idx(fj, nz, bcz)], f[i * nz + bc_idx(fj + 1, nz, bcz)]);
+    if (bcz == 1 && (fj == 0 || fj == nz)) Fz[s] = 0.0;
+  }
+  return (Fx[1] - Fx[0]) / dx + (Fz[1] - Fz[0]) / dz;
+}
+
+__global__ void k_divergence(const double* f, const double* flux, int64_t nx, int64_t nz, double dx,
+                             double dz, int bcx, int bcz, double* out) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nx * nz;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = c / nz, j = c - i * nz;
+    out[c] = divergence_cell(f, flux, nx, nz, i, j, dx, dz, bcx, bcz);
+  }
+}
+
+// integration.py:325-354; the column sum runs over x in order like NumPy's
+// axis-0 reduction of a C-ordered array
+__global__ void k_relaxation(const double* f, int64_t nx, int64_t nz, const double* prof,
+                             const double* trel, double dt, double* out) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nz;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    double s = f[j];
+    for (int64_t i = 1; i < nx; ++i) s += f[i * nz + j];
+    out[j] = dt * (prof[j] - s / (double)nx) / trel[j];
+  }
+}
+
+// integration.py:1483-1508 (factor 1) and 1536-1561 (factor 2, minus the
+// previous increment): advective + relaxation increments per sub-step
+__global__ void k_advection(const double* gsf, const double* flux, int64_t nx, int64_t nz,
+                            double dx, double dz, double dt_sub, const double* relax, int relax_on,
+                            double* dTh, double* drv, int second) {
+  const int64_t C = nx * nz;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = c / nz, j = c - i * nz;
+    const double rdi = gsf[9 * C + c];
+    const double drv_div = divergence_cell(gsf + 4 * C, flux, nx, nz, i, j, dx, dz, 0, 1);
+    const double dth_div = divergence_cell(gsf + 2 * C, flux, nx, nz, i, j, dx, dz, 0, 1);
+    double a, b;
+    if (!second) {
+      a = -dt_sub * drv_div * rdi;
+      b = -dt_sub * dth_div * rdi;
+      if (relax_on) { a += relax[j]; b += relax[nz + j]; }
+    } else {
+      a = -2.0 * dt_sub * drv_div * rdi - drv[c];
+      b = -2.0 * dt_sub * dth_div * rdi - dTh[c];
+      if (relax_on) { a += 2. * relax[j]; b += 2. * relax[nz + j]; }
+    }
+    drv[c] = a; dTh[c] = b;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// elementwise microphysics (unit parity entry points)
+__global__ void k_mass_rate(int sol, int64_t n, InPtrs in, double* g, double* dg) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    CellAmb a = make_cell_amb(in.p[6][k], in.p[7][k], in.p[8][k], in.p[9][k], in.p[10][k], in.p[11][k], in.p[12][k]);
+    a.sigw = surface_tension_water(in.p[4][k]);
+    a.rhow = density_water(in.p[4][k]);
+    mass_rate_and_derivative(sol, in.p[0][k], in.p[1][k], in.p[2][k], in.p[3][k], in.p[4][k], in.p[5][k],
+                             in.p[13][k], a, g[k], dg[k]);
+  }
+}
+__global__ void k_newton(int sol, int64_t n, double dt_sub, int no_iter, InPtrs in, double* dm,
+                         double* g0) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    CellAmb a = make_cell_amb(in.p[6][k], in.p[7][k], in.p[8][k], in.p[9][k], in.p[10][k], in.p[11][k], in.p[12][k]);
+    a.sigw = surface_tension_water(in.p[4][k]);
+    a.rhow = density_water(in.p[4][k]);
+    dm[k] = newton_full(sol, dt_sub, no_iter, in.p[0][k], in.p[1][k], in.p[2][k], in.p[3][k], in.p[4][k],
+                        in.p[5][k], in.p[13][k], a, g0 + k);
+  }
+}
+__global__ void k_interp(const int32_t* cell, const double* rel, const double* gvp, int64_t n,
+                         int64_t nx, int64_t nz, double* out) {
+  const GridVel gv{gvp, nx, nz};
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    int32_t c = cell[k];
+    double u = 0.0, v = 0.0;
+    if (c >= 0) {
+      int64_t i = c / nz, j = c - (c / nz) * nz;
+      gv.interp(i, j, rel[k], rel[n + k], u, v);
+    }
+    out[k] = u; out[n + k] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+cudaError_t launch_cells_import(const int64_t* cells, const uint8_t* act, int32_t* cell, int64_t n,
+                                int64_t nx, int64_t nz, cudaStream_t s) {
+  (void)nx;
+  k_cells_import<<<nblocks(n, 256), 256, 0, s>>>(cells, act, cell, n, nz);
+  return cudaGetLastError();
+}
+cudaError_t launch_cells_export(const int32_t* cell, const double* pos, double* rel, int64_t* cells,
+                                uint8_t* act, int64_t n, int64_t nx, int64_t nz, double x_min,
+                                double z_min, double dx, double dz, cudaStream_t s) {
+  (void)nx;
+  k_cells_export<<<nblocks(n, 256), 256, 0, s>>>(cell, pos, rel, cells, act, n, nz, x_min, z_min,
+                                                 dx, dz);
+  return cudaGetLastError();
+}
+cudaError_t launch_cell_aux(const lacmo_grid_t& g, const Ws& w, cudaStream_t s) {
+  int64_t C = g.nx * g.nz;
+  k_cell_aux<<<nblocks(C, 128), 128, 0, s>>>(g.scalar_fields, g.mat_prop, w.aux, C);
+  return cudaGetLastError();
+}
+cudaError_t launch_histogram(const int32_t* cell, int64_t n, const Ws& w, cudaStream_t s) {
+  k_histogram<<<nblocks(n, 256), 256, 0, s>>>(cell, n, w.counts, w.rank);
+  return cudaGetLastError();
+}
+cudaError_t launch_bin(const lacmo_sips_t& sp, int64_t C, const Ws& w, cudaStream_t s) {
+  k_scan<<<1, 1024, 0, s>>>(w.counts, w.start, w.draw_off, w.total_pairs, C, w.rm_count, w.rm_id,
+                            w.rm_val, sp.water_removed);
+  k_scatter<<<nblocks(sp.n, 256), 256, 0, s>>>(sp.cell, w.rank, w.start, w.perm, sp.n);
+  k_order<<<nblocks(C, 256, 152 * 16), 256, 0, s>>>(w.start, w.perm, w.rank, C);
+  return cudaGetLastError();
+}
+cudaError_t launch_particles(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
+                             double dt_sub, double dt_sub_pos, bool write_Tp, const Ws& w,
+                             cudaStream_t s) {
+  PArgs a;
+  a.pos = sp.pos; a.vel = sp.vel; a.m_w = sp.m_w; a.rel = sp.rel_pos; a.T_p = sp.T_p;
+  a.m_s = sp.m_s; a.xi = sp.xi; a.cell = sp.cell;
+  a.gsf = g.scalar_fields; a.gmp = g.mat_prop; a.aux = w.aux; a.gv = g.velocity;
+  a.n = sp.n; a.nx = g.nx; a.nz = g.nz;
+  a.x_min = g.x_min; a.x_max = g.x_max; a.z_min = g.z_min; a.z_cap = g.z_max * 0.999999;
+  a.dx = g.dx; a.dz = g.dz;
+  a.dt_sub = dt_sub; a.dt_pos = dt_sub_pos; a.g_set = p.g_set;
+  a.no_iter = p.no_iter_impl_mass; a.sol = p.solute; a.write_Tp = write_Tp ? 1 : 0;
+  a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
+  a.rm_id = w.rm_id; a.rm_val = w.rm_val; a.flags = w.flags;
+  k_particles<true><<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_move(const lacmo_sips_t& sp, const lacmo_grid_t& g, double dt_pos, const Ws& w,
+                        cudaStream_t s) {
+  PArgs a;
+  a.pos = sp.pos; a.vel = sp.vel; a.m_w = sp.m_w; a.rel = sp.rel_pos; a.T_p = sp.T_p;
+  a.m_s = sp.m_s; a.xi = sp.xi; a.cell = sp.cell;
+  a.gsf = g.scalar_fields; a.gmp = g.mat_prop; a.aux = w.aux; a.gv = g.velocity;
+  a.n = sp.n; a.nx = g.nx; a.nz = g.nz;
+  a.x_min = g.x_min; a.x_max = g.x_max; a.z_min = g.z_min; a.z_cap = g.z_max * 0.999999;
+  a.dx = g.dx; a.dz = g.dz;
+  a.dt_sub = 0.0; a.dt_pos = dt_pos; a.g_set = 0.0;
+  a.no_iter = 0; a.sol = 0; a.write_Tp = 0;
+  a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
+  a.rm_id = w.rm_id; a.rm_val = w.rm_val; a.flags = w.flags;
+  k_particles<false><<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_cell_update(const lacmo_sips_t& sp, const lacmo_grid_t& g, const Ws& w,
+                               const double* dTh, const double* drv, bool grid_update,
+                               cudaStream_t s) {
+  (void)sp;
+  int64_t C = g.nx * g.nz;
+  k_cell_update<<<nblocks(C * 32, 256, 152 * 16), 256, 0, s>>>(
+      w.start, w.perm, w.dmxi, g.delta_m_l, g.scalar_fields, g.mat_prop, w.aux, dTh, drv, C,
+      g.p_ref, g.p_ref_inv, g.volume_cell, grid_update ? 1 : 0);
+  return cudaGetLastError();
+}
+cudaError_t launch_grid_only(const lacmo_grid_t& g, const double* dTh, const double* drv,
+                             const double* dml, double* aux, cudaStream_t s) {
+  int64_t C = g.nx * g.nz;
+  k_grid_only<<<nblocks(C, 128), 128, 0, s>>>(g.scalar_fields, g.mat_prop, aux, dTh, drv, dml, C,
+                                              g.p_ref, g.p_ref_inv, g.volume_cell);
+  return cudaGetLastError();
+}
+cudaError_t launch_advection(const lacmo_grid_t& g, const lacmo_params_t& p, const Ws& w,
+                             double factor, bool second, cudaStream_t s) {
+  (void)factor;
+  int64_t C = g.nx * g.nz;
+  const bool relax_on = p.act_relaxation && p.init_profile_r_v && p.init_profile_Theta &&
+                        p.relaxation_time_profile;
+  if (relax_on) {
+    k_relaxation<<<nblocks(g.nz, 128), 128, 0, s>>>(g.scalar_fields + 4 * C, g.nx, g.nz,
+                                                     p.init_profile_r_v, p.relaxation_time_profile,
+                                                     p.dt_sub, w.relax);
+    k_relaxation<<<nblocks(g.nz, 128), 128, 0, s>>>(g.scalar_fields + 2 * C, g.nx, g.nz,
+                                                     p.init_profile_Theta,
+                                                     p.relaxation_time_profile, p.dt_sub,
+                                                     w.relax + g.nz);
+  }
+  k_advection<<<nblocks(C, 128), 128, 0, s>>>(g.scalar_fields, g.mass_flux_air_dry, g.nx, g.nz,
+                                              g.dx, g.dz, p.dt_sub, w.relax, relax_on ? 1 : 0,
+                                              w.dTh, w.drv, second ? 1 : 0);
+  return cudaGetLastError();
+}
+cudaError_t launch_divergence(const double* f, const double* flux, int64_t nx, int64_t nz,
+                              double dx, double dz, int bcx, int bcz, double* out, cudaStream_t s) {
+  k_divergence<<<nblocks(nx * nz, 128), 128, 0, s>>>(f, flux, nx, nz, dx, dz, bcx, bcz, out);
+  return cudaGetLastError();
+}
+cudaError_t launch_relaxation(const double* f, int64_t nx, int64_t nz, const double* prof,
+                              const double* trel, double dt, double* out, cudaStream_t s) {
+  k_relaxation<<<nblocks(nz, 128), 128, 0, s>>>(f, nx, nz, prof, trel, dt, out);
+  return cudaGetLastError();
+}
+cudaError_t launch_r_l_binned(const lacmo_sips_t& sp, const lacmo_grid_t& g, const Ws& w,
+                              cudaStream_t s) {
+  int64_t C = g.nx * g.nz;
+  k_r_l<<<nblocks(C * 32, 256, 152 * 16), 256, 0, s>>>(w.start, w.perm, sp.m_w, sp.xi,
+                                                       g.scalar_fields, C);
+  return cudaGetLastError();
+}
+cudaError_t launch_mass_rate(int sol, int64_t n, const InPtrs& in, double* g, double* dg,
+                             cudaStream_t s) {
+  k_mass_rate<<<nblocks(n, 128), 128, 0, s>>>(sol, n, in, g, dg);
+  return cudaGetLastError();
+}
+cudaError_t launch_newton(int sol, int64_t n, double dt_sub, int no_iter, const InPtrs& in,
+                          double* dm, double* g0, cudaStream_t s) {
+  k_newton<<<nblocks(n, 128), 128, 0, s>>>(sol, n, dt_sub, no_iter, in, dm, g0);
+  return cudaGetLastError();
+}
+cudaError_t launch_interp(const int32_t* cell, const double* rel, const double* gv, int64_t n,
+                          int64_t nx, int64_t nz, double* out, cudaStream_t s) {
+  k_interp<<<nblocks(n, 128), 128, 0, s>>>(cell, rel, gv, n, nx, nz, out);
+  return cudaGetLastError();
+}
+
+}  // namespace lacmo

@@ -1,0 +1,269 @@
+"""Device-resident SIP/grid state and the calls that advance it on the GPU.
+
+``DeviceState`` holds one model state in GPU memory (PyTorch tensors used as
+plain device buffers) in the reference's array layout, plus the caller-owned
+workspace the C ABI needs.  It is built from the same arrays and scalars the
+reference's ``integrate_adv_step_np`` takes (integration.py:1298-1313), runs
+advection steps with ``adv_step`` and copies the state back into NumPy arrays
+with ``export_to``.
+
+Draw sources for the all-or-nothing collisions:
+* ``"philox"``: counter-based Philox4x32-10 on the device (performance mode);
+* ``"numpy"``: each collision step draws ``np.random.rand(pairs)`` from NumPy's
+  global generator on the host, exactly the count and order the reference
+  consumes, and copies it to the device (parity mode);
+* a 1-D float64 array or CUDA tensor: injected draws consumed in order.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .constants import solute_code
+
+F64 = torch.float64
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def to_device(a, dtype=F64, device="cuda"):
+    """NumPy array / scalar / tensor -> contiguous CUDA tensor of ``dtype``."""
+    if isinstance(a, torch.Tensor):
+        t = a.to(device=device, dtype=dtype)
+        return t.contiguous()
+    arr = np.ascontiguousarray(np.asarray(a))
+    t = torch.from_numpy(arr)
+    if t.dtype != dtype:
+        t = t.to(dtype)
+    return t.to(device, non_blocking=False).contiguous()
+
+
+class DeviceState:
+    GRID_KEYS = ("grid_scalar_fields", "grid_mat_prop", "grid_velocity",
+                 "grid_mass_flux_air_dry")
+
+    def __init__(self, st, device="cuda", draws="philox", seed=1001):
+        self.lib = _lib.load()
+        self.device = device
+        g = st["grid_no_cells"]
+        self.nx, self.nz = int(g[0]), int(g[1])
+        pos = np.asarray(st["pos"]) if not isinstance(st["pos"], torch.Tensor) else st["pos"]
+        self.n = int(pos.shape[1])
+        dev = device
+        self.pos = to_device(st["pos"], device=dev)
+        self.vel = to_device(st["vel"], device=dev)
+        self.rel_pos = to_device(st["rel_pos"], device=dev)
+        self.m_w = to_device(st["m_w"], device=dev)
+        self.m_s = to_device(st["m_s"], device=dev)
+        self.xi = to_device(st["xi"], device=dev)
+        self.T_p = to_device(st["T_p"], device=dev)
+        self.water_removed = to_device(st["water_removed"], device=dev)
+        self.no_cols = to_device(st.get("no_cols", np.zeros(2, np.int64)), torch.int64, dev)
+        self.cell = torch.empty(self.n, dtype=torch.int32, device=dev)
+        cells = to_device(st["cells"], torch.int64, dev)
+        act = to_device(np.asarray(st["active_ids"]).astype(np.uint8)
+                        if not isinstance(st["active_ids"], torch.Tensor) else st["active_ids"],
+                        torch.uint8, dev)
+        s = _stream()
+        _lib.check(self.lib.lacmo_cells_import(_ptr(cells), _ptr(act), _ptr(self.cell), self.n,
+                                               self.nx, self.nz, s), "cells_import")
+        self.gsf = to_device(st["grid_scalar_fields"], device=dev)
+        self.gmp = to_device(st["grid_mat_prop"], device=dev)
+        self.gvel = to_device(st["grid_velocity"], device=dev)
+        self.flux = to_device(st["grid_mass_flux_air_dry"], device=dev)
+        self.delta_m_l = to_device(st["delta_m_l"], device=dev)
+        ranges = np.asarray(st["grid_ranges"], dtype=np.float64)
+        steps = np.asarray(st["grid_steps"], dtype=np.float64)
+        self.grid = _lib.Grid(self.nx, self.nz, self.gsf.data_ptr(), self.gmp.data_ptr(),
+                              self.gvel.data_ptr(), self.flux.data_ptr(),
+                              self.delta_m_l.data_ptr(), ranges[0, 0], ranges[0, 1], ranges[1, 0],
+                              ranges[1, 1], steps[0], steps[1], float(st["grid_volume_cell"]),
+                              float(st["p_ref"]), float(st["p_ref_inv"]))
+        self.sips = _lib.Sips(self.n, self.pos.data_ptr(), self.vel.data_ptr(),
+                              self.rel_pos.data_ptr(), self.m_w.data_ptr(), self.m_s.data_ptr(),
+                              self.xi.data_ptr(), self.T_p.data_ptr(), self.cell.data_ptr(),
+                              self.water_removed.data_ptr(), self.no_cols.data_ptr())
+        self.set_params(st)
+        self.ws_bytes = int(self.lib.lacmo_workspace_bytes(self.n, self.nx, self.nz))
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
+        _lib.check(self.lib.lacmo_workspace_reset(_ptr(self.ws), self.ws_bytes, self.n, self.nx,
+                                                  self.nz, s), "workspace_reset")
+        self.draw_mode = draws
+        self.seed = int(seed)
+        self.draw_buf = None
+        if not isinstance(draws, str):
+            self.draw_buf = to_device(draws, device=dev)
+        self.prepare()
+
+    # -- parameters -------------------------------------------------------------
+    def set_params(self, st):
+        dev = self.device
+        nz = self.nz
+        prof = lambda k: (to_device(st[k], device=dev) if st.get(k) is not None
+                          else torch.zeros(nz, dtype=F64, device=dev))
+        self.prof_rv = prof("init_profile_r_v")
+        self.prof_th = prof("init_profile_Theta")
+        self.t_relax = prof("relaxation_time_profile")
+        E = st["E_col_grid"]
+        if isinstance(E, (float, np.floating)) or np.ndim(E) == 0:
+            self.E = None
+            E_const = float(E)
+            nb, lo, bl = 0, 0.0, 1.0
+        else:
+            self.E = to_device(E, device=dev)
+            E_const = 0.0
+            nb, lo, bl = (int(st["no_kernel_bins"]), float(st["R_kernel_low_log"]),
+                          float(st["bin_factor_R_log"]))
+        has_relax = st.get("init_profile_r_v") is not None
+        self.params = _lib.Params(
+            float(st["dt"]), float(st["dt_sub"]), float(st["dt_sub_half"]),
+            float(st["dt_col_over_dV"]), float(st["g_set"]), int(st["scale_dt_cond"]),
+            int(st["no_col_per_adv"]), int(bool(st["act_collisions"])),
+            int(bool(st["act_relaxation"]) and has_relax), int(st["no_iter_impl_mass"]),
+            solute_code(st["solute_type"]), self.prof_rv.data_ptr(), self.prof_th.data_ptr(),
+            self.t_relax.data_ptr(), self.E.data_ptr() if self.E is not None else None, E_const,
+            nb, lo, bl)
+
+    def prepare(self):
+        _lib.check(self.lib.lacmo_prepare(ctypes.byref(self.sips), ctypes.byref(self.grid),
+                                          ctypes.byref(self.params), _ptr(self.ws), self.ws_bytes,
+                                          _stream()), "prepare")
+
+    # -- stepping ---------------------------------------------------------------
+    def _draws_struct(self):
+        if self.draw_buf is not None:
+            return _lib.Draws(self.draw_buf.data_ptr(), self.draw_buf.numel(), self.seed)
+        return _lib.Draws(None, 0, self.seed)
+
+    def adv_step(self, n_steps=1):
+        """``n_steps`` advection steps (integration.py:1298-1611)."""
+        if self.draw_mode == "numpy":
+            for _ in range(n_steps):
+                self._adv_step_numpy_draws()
+            return
+        d = self._draws_struct()
+        s = _stream()
+        for _ in range(n_steps):
+            _lib.check(self.lib.lacmo_integrate_adv_step(
+                ctypes.byref(self.sips), ctypes.byref(self.grid), ctypes.byref(self.params),
+                ctypes.byref(d), _ptr(self.ws), self.ws_bytes, s), "integrate_adv_step")
+
+    def pair_count(self):
+        out = ctypes.c_int64(0)
+        _lib.check(self.lib.lacmo_collision_pair_count(_ptr(self.ws), self.n, self.nx, self.nz,
+                                                       ctypes.byref(out), _stream()), "pair_count")
+        return int(out.value)
+
+    def collision_step(self, draws=None):
+        """All-cells collision step (collision/all_or_nothing.py:754-846).
+
+        ``draws``: None uses the state's draw mode; an array/tensor injects."""
+        if draws is None and self.draw_mode == "numpy":
+            draws = np.random.rand(self.pair_count())
+        if draws is not None:
+            buf = to_device(draws, device=self.device)
+            if buf.numel() == 0:
+                buf = torch.zeros(1, dtype=F64, device=self.device)
+            d = _lib.Draws(buf.data_ptr(), buf.numel(), self.seed)
+        else:
+            d = _lib.Draws(None, 0, self.seed)
+        _lib.check(self.lib.lacmo_collision_step_cells(
+            ctypes.byref(self.sips), ctypes.byref(self.grid), ctypes.byref(self.params),
+            ctypes.byref(d), _ptr(self.ws), self.ws_bytes, _stream()), "collision_step_cells")
+        torch.cuda.current_stream().synchronize() if draws is not None else None
+
+    def _subloop(self, no_cond, no_col):
+        # integration.py:1095-1294
+        col = bool(self.params.act_collisions)
+        if col and no_col == 1:
+            self.collision_step()
+        for _ in range(no_cond):
+            if col and no_col > 1:
+                self.collision_step()
+            self._substep(self.params.dt_sub, False)
+        if col and no_col > no_cond:
+            self.collision_step()
+
+    def _substep(self, dt_pos, write_Tp):
+        _lib.check(self.lib.lacmo_adv_substep(
+            ctypes.byref(self.sips), ctypes.byref(self.grid), ctypes.byref(self.params),
+            float(dt_pos), int(write_Tp), _ptr(self.ws), self.ws_bytes, _stream()), "adv_substep")
+
+    def _adv_step_numpy_draws(self):
+        p = self.params
+        s = _stream()
+        _lib.check(self.lib.lacmo_adv_step_begin(ctypes.byref(self.sips), ctypes.byref(self.grid),
+                                                 ctypes.byref(p), _ptr(self.ws), self.ws_bytes, s),
+                   "adv_step_begin")
+        ncol = p.no_col_per_adv
+        self._subloop(p.scale_dt_cond, 0 if ncol == 1 else (1 if ncol == 2 else p.scale_dt_cond))
+        _lib.check(self.lib.lacmo_adv_step_second_half(
+            ctypes.byref(self.sips), ctypes.byref(self.grid), ctypes.byref(p), _ptr(self.ws),
+            self.ws_bytes, s), "adv_step_second_half")
+        self._subloop(p.scale_dt_cond - 1, 1 if ncol in (1, 2) else p.scale_dt_cond)
+        self._substep(p.dt_sub_half, True)
+
+    def particles_substep(self, dt_sub, dt_sub_pos):
+        """integration.py:944 propagate_particles_subloop_step_np."""
+        _lib.check(self.lib.lacmo_propagate_particles_subloop_step(
+            ctypes.byref(self.sips), ctypes.byref(self.grid), ctypes.byref(self.params),
+            float(dt_sub), float(dt_sub_pos), _ptr(self.ws), self.ws_bytes, _stream()),
+            "propagate_particles_subloop_step")
+
+    def update_grid_r_l(self):
+        _lib.check(self.lib.lacmo_update_grid_r_l(ctypes.byref(self.sips), ctypes.byref(self.grid),
+                                                  _ptr(self.ws), self.ws_bytes, _stream()),
+                   "update_grid_r_l")
+
+    def flags(self):
+        f = ctypes.c_uint32(0)
+        _lib.check(self.lib.lacmo_read_flags(_ptr(self.ws), self.n, self.nx, self.nz,
+                                             ctypes.byref(f), _stream()), "read_flags")
+        return int(f.value)
+
+    # -- export -----------------------------------------------------------------
+    def cells_and_active(self):
+        cells = torch.empty((2, self.n), dtype=torch.int64, device=self.device)
+        act = torch.empty(self.n, dtype=torch.uint8, device=self.device)
+        g = self.grid
+        _lib.check(self.lib.lacmo_cells_export(_ptr(self.cell), _ptr(self.pos), _ptr(self.rel_pos),
+                                               _ptr(cells), _ptr(act), self.n, self.nx, self.nz,
+                                               g.x_min, g.z_min, g.dx, g.dz, _stream()),
+                   "cells_export")
+        return cells, act
+
+    def export_to(self, st):
+        """Copy the device state into the NumPy arrays of ``st`` in place."""
+        cells, act = self.cells_and_active()
+        torch.cuda.current_stream().synchronize()
+        pairs = [("pos", self.pos), ("vel", self.vel), ("rel_pos", self.rel_pos),
+                 ("m_w", self.m_w), ("m_s", self.m_s), ("xi", self.xi), ("T_p", self.T_p),
+                 ("water_removed", self.water_removed), ("grid_scalar_fields", self.gsf),
+                 ("grid_mat_prop", self.gmp), ("delta_m_l", self.delta_m_l),
+                 ("no_cols", self.no_cols), ("cells", cells)]
+        for k, t in pairs:
+            if k in st and st[k] is not None:
+                np.copyto(st[k], t.cpu().numpy().reshape(np.shape(st[k])))
+        if "active_ids" in st:
+            np.copyto(st["active_ids"], act.cpu().numpy().astype(bool))
+        return st
+
+    def snapshot(self):
+        """The state as a dict of fresh NumPy arrays (reference layout)."""
+        cells, act = self.cells_and_active()
+        torch.cuda.current_stream().synchronize()
+        return {"pos": self.pos.cpu().numpy(), "vel": self.vel.cpu().numpy(),
+                "rel_pos": self.rel_pos.cpu().numpy(), "m_w": self.m_w.cpu().numpy(),
+                "m_s": self.m_s.cpu().numpy(), "xi": self.xi.cpu().numpy(),
+                "T_p": self.T_p.cpu().numpy(), "water_removed": self.water_removed.cpu().numpy(),
+                "grid_scalar_fields": self.gsf.cpu().numpy(),
+                "grid_mat_prop": self.gmp.cpu().numpy(), "delta_m_l": self.delta_m_l.cpu().numpy(),
+                "no_cols": self.no_cols.cpu().numpy(), "cells": cells.cpu().numpy(),
+                "active_ids": act.cpu().numpy().astype(bool)}
