@@ -98,6 +98,8 @@ typedef struct {
 
 /* ---- library, workspace, status ------------------------------------------ */
 int lacmo_abi_version(void);
+/* Number of CUDA kernels this library has launched in this process. */
+uint64_t lacmo_kernel_launches(void);
 const char* lacmo_error_string(int status);
 /* Bytes of device scratch the entry points below need for n SIPs and an
  * nx x nz grid (no allocation happens inside the library). */
@@ -150,6 +152,17 @@ int lacmo_adv_step_second_half(const lacmo_sips_t* sips, const lacmo_grid_t* gri
 int lacmo_adv_substep(const lacmo_sips_t* sips, const lacmo_grid_t* grid,
                       const lacmo_params_t* prm, double dt_sub_pos, int write_T_p, void* ws,
                       size_t ws_bytes, void* stream);
+/* The two halves of a particle sub-step, for callers that time or schedule
+ * them separately: the fused per-SIP kernel (condensation, drag, position,
+ * re-index; it also counts SIPs per new cell), and the cell binning that
+ * folds the ground-removal list into water_removed and sorts the SIPs by
+ * (cell, ID).  lacmo_bin must follow lacmo_particles_only before any other
+ * entry point uses the binning. */
+int lacmo_particles_only(const lacmo_sips_t* sips, const lacmo_grid_t* grid,
+                         const lacmo_params_t* prm, double dt_sub, double dt_sub_pos, void* ws,
+                         size_t ws_bytes, void* stream);
+int lacmo_bin(const lacmo_sips_t* sips, const lacmo_grid_t* grid, void* ws, size_t ws_bytes,
+              void* stream);
 /* One particle sub-step: replaces integration.py:944
  * propagate_particles_subloop_step_np (T_p, Newton condensation with the
  * per-cell delta_m_l, drag, position, ground removal, cell re-index). */

@@ -55,6 +55,9 @@ P = ctypes.POINTER
 # name -> (restype, argtypes)
 PROTOTYPES = {
     "lacmo_abi_version": (ctypes.c_int, []),
+    "lacmo_kernel_launches": (ctypes.c_uint64, []),
+    "lacmo_particles_only": (ctypes.c_int, [P(Sips), P(Grid), P(Params), dbl, dbl, vp, sz, vp]),
+    "lacmo_bin": (ctypes.c_int, [P(Sips), P(Grid), vp, sz, vp]),
     "lacmo_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "lacmo_workspace_bytes": (sz, [i64, i64, i64]),
     "lacmo_workspace_reset": (ctypes.c_int, [vp, sz, i64, i64, i64, vp]),

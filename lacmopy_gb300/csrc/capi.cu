@@ -3,9 +3,14 @@
 #include <cuda_runtime.h>
 #include <string.h>
 
+#include <atomic>
+
 #include "lacmo_internal.cuh"
 
 namespace lacmo {
+
+static std::atomic<uint64_t> g_launches{0};
+void note_launches(int k) { g_launches.fetch_add((uint64_t)k, std::memory_order_relaxed); }
 
 static inline size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -142,6 +147,25 @@ using namespace lacmo;
 extern "C" {
 
 int lacmo_abi_version(void) { return LACMO_ABI_VERSION; }
+
+uint64_t lacmo_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int lacmo_particles_only(const lacmo_sips_t* sp, const lacmo_grid_t* g, const lacmo_params_t* p,
+                         double dt_sub, double dt_sub_pos, void* ws, size_t bytes, void* stream) {
+  if (!sips_ok(sp) || !grid_ok(g) || !prm_ok(p)) return LACMO_ERR_ARG;
+  Ws w;
+  if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
+  LCHK(launch_particles(*sp, *g, *p, dt_sub, dt_sub_pos, true, w, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_bin(const lacmo_sips_t* sp, const lacmo_grid_t* g, void* ws, size_t bytes, void* stream) {
+  if (!sips_ok(sp) || !grid_ok(g)) return LACMO_ERR_ARG;
+  Ws w;
+  if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
+  LCHK(launch_bin(*sp, g->nx * g->nz, w, (cudaStream_t)stream));
+  return LACMO_OK;
+}
 
 const char* lacmo_error_string(int status) {
   switch (status) {

@@ -423,14 +423,14 @@ cudaError_t launch_collide_cells(const lacmo_sips_t& sp, const lacmo_grid_t& g,
   a.no_cols = sp.no_cols; a.flags = w.flags;
   a.gR = w.colR; a.grho = w.colrho; a.gk = w.colk;
   int blocks = nblk((a.C + CELL_WARPS - 1) / CELL_WARPS, 1);
-  k_collide_cells<<<blocks, CELL_WARPS * 32, CELL_SMEM_BYTES, s>>>(a);
+  k_collide_cells<<<blocks, CELL_WARPS * 32, CELL_SMEM_BYTES, s>>>(a); note_launches(1);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_col_advance<<<1, 1, 0, s>>>(w.cursor, w.col_step, w.total_pairs, w.flags, d.draws ? 1 : 0);
+  k_col_advance<<<1, 1, 0, s>>>(w.cursor, w.col_step, w.total_pairs, w.flags, d.draws ? 1 : 0); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_col_advance(const Ws& w, cudaStream_t s) {
-  k_col_advance<<<1, 1, 0, s>>>(w.cursor, w.col_step, w.total_pairs, w.flags, 0);
+  k_col_advance<<<1, 1, 0, s>>>(w.cursor, w.col_step, w.total_pairs, w.flags, 0); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_golovin(double* xis, double* m, int64_t n, double dtdv, int64_t* no_cols,
@@ -439,7 +439,7 @@ cudaError_t launch_golovin(double* xis, double* m, int64_t n, double dtdv, int64
   cudaError_t e = cudaFuncSetAttribute(k_golovin, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(LACMO_BOX_MAX_SIPS * 16));
   if (e != cudaSuccess) return e;
-  k_golovin<<<1, BOX_THREADS, sh, s>>>(xis, m, (int)n, dtdv, no_cols, rnd, seed, step);
+  k_golovin<<<1, BOX_THREADS, sh, s>>>(xis, m, (int)n, dtdv, no_cols, rnd, seed, step); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_ecol_box(double* xis, double* m, double* R, const double* vel,
@@ -451,16 +451,16 @@ cudaError_t launch_ecol_box(double* xis, double* m, double* R, const double* vel
                                        (int)(LACMO_ECOL_BOX_MAX_SIPS * 44));
   if (e != cudaSuccess) return e;
   k_ecol_box<<<1, BOX_THREADS, sh, s>>>(xis, m, R, vel, rho, (int)n, dtdv, E, nb, lo, bl, no_cols,
-                                        rnd, seed, step);
+                                        rnd, seed, step); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_beard(double* vel, const double* R, int64_t n, cudaStream_t s) {
-  k_beard<<<nblk(n, 128), 128, 0, s>>>(vel, R, n);
+  k_beard<<<nblk(n, 128), 128, 0, s>>>(vel, R, n); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_radius_bin(const double* m, const double* rho, int64_t n, double lo, double bl,
                               int64_t nb, double* R, int64_t* k, cudaStream_t s) {
-  k_radius_bin<<<nblk(n, 128), 128, 0, s>>>(m, rho, n, lo, bl, nb, R, k);
+  k_radius_bin<<<nblk(n, 128), 128, 0, s>>>(m, rho, n, lo, bl, nb, R, k); note_launches(1);
   return cudaGetLastError();
 }
 

@@ -561,7 +561,7 @@ __global__ void k_interp(const int32_t* cell, const double* rel, const double* g
 cudaError_t launch_cells_import(const int64_t* cells, const uint8_t* act, int32_t* cell, int64_t n,
                                 int64_t nx, int64_t nz, cudaStream_t s) {
   (void)nx;
-  k_cells_import<<<nblocks(n, 256), 256, 0, s>>>(cells, act, cell, n, nz);
+  k_cells_import<<<nblocks(n, 256), 256, 0, s>>>(cells, act, cell, n, nz); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_cells_export(const int32_t* cell, const double* pos, double* rel, int64_t* cells,
@@ -569,23 +569,23 @@ cudaError_t launch_cells_export(const int32_t* cell, const double* pos, double* 
                                 double z_min, double dx, double dz, cudaStream_t s) {
   (void)nx;
   k_cells_export<<<nblocks(n, 256), 256, 0, s>>>(cell, pos, rel, cells, act, n, nz, x_min, z_min,
-                                                 dx, dz);
+                                                 dx, dz); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_cell_aux(const lacmo_grid_t& g, const Ws& w, cudaStream_t s) {
   int64_t C = g.nx * g.nz;
-  k_cell_aux<<<nblocks(C, 128), 128, 0, s>>>(g.scalar_fields, g.mat_prop, w.aux, C);
+  k_cell_aux<<<nblocks(C, 128), 128, 0, s>>>(g.scalar_fields, g.mat_prop, w.aux, C); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_histogram(const int32_t* cell, int64_t n, const Ws& w, cudaStream_t s) {
-  k_histogram<<<nblocks(n, 256), 256, 0, s>>>(cell, n, w.counts, w.rank);
+  k_histogram<<<nblocks(n, 256), 256, 0, s>>>(cell, n, w.counts, w.rank); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_bin(const lacmo_sips_t& sp, int64_t C, const Ws& w, cudaStream_t s) {
   k_scan<<<1, 1024, 0, s>>>(w.counts, w.start, w.draw_off, w.total_pairs, C, w.rm_count, w.rm_id,
-                            w.rm_val, sp.water_removed);
-  k_scatter<<<nblocks(sp.n, 256), 256, 0, s>>>(sp.cell, w.rank, w.start, w.perm, sp.n);
-  k_order<<<nblocks(C, 256, 152 * 16), 256, 0, s>>>(w.start, w.perm, w.rank, C);
+                            w.rm_val, sp.water_removed); note_launches(1);
+  k_scatter<<<nblocks(sp.n, 256), 256, 0, s>>>(sp.cell, w.rank, w.start, w.perm, sp.n); note_launches(1);
+  k_order<<<nblocks(C, 256, 152 * 16), 256, 0, s>>>(w.start, w.perm, w.rank, C); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_particles(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
@@ -602,7 +602,7 @@ cudaError_t launch_particles(const lacmo_sips_t& sp, const lacmo_grid_t& g, cons
   a.no_iter = p.no_iter_impl_mass; a.sol = p.solute; a.write_Tp = write_Tp ? 1 : 0;
   a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
   a.rm_id = w.rm_id; a.rm_val = w.rm_val; a.flags = w.flags;
-  k_particles<true><<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a);
+  k_particles<true><<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_move(const lacmo_sips_t& sp, const lacmo_grid_t& g, double dt_pos, const Ws& w,
@@ -618,7 +618,7 @@ cudaError_t launch_move(const lacmo_sips_t& sp, const lacmo_grid_t& g, double dt
   a.no_iter = 0; a.sol = 0; a.write_Tp = 0;
   a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
   a.rm_id = w.rm_id; a.rm_val = w.rm_val; a.flags = w.flags;
-  k_particles<false><<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a);
+  k_particles<false><<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_cell_update(const lacmo_sips_t& sp, const lacmo_grid_t& g, const Ws& w,
@@ -628,14 +628,14 @@ cudaError_t launch_cell_update(const lacmo_sips_t& sp, const lacmo_grid_t& g, co
   int64_t C = g.nx * g.nz;
   k_cell_update<<<nblocks(C * 32, 256, 152 * 16), 256, 0, s>>>(
       w.start, w.perm, w.dmxi, g.delta_m_l, g.scalar_fields, g.mat_prop, w.aux, dTh, drv, C,
-      g.p_ref, g.p_ref_inv, g.volume_cell, grid_update ? 1 : 0);
+      g.p_ref, g.p_ref_inv, g.volume_cell, grid_update ? 1 : 0); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_grid_only(const lacmo_grid_t& g, const double* dTh, const double* drv,
                              const double* dml, double* aux, cudaStream_t s) {
   int64_t C = g.nx * g.nz;
   k_grid_only<<<nblocks(C, 128), 128, 0, s>>>(g.scalar_fields, g.mat_prop, aux, dTh, drv, dml, C,
-                                              g.p_ref, g.p_ref_inv, g.volume_cell);
+                                              g.p_ref, g.p_ref_inv, g.volume_cell); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_advection(const lacmo_grid_t& g, const lacmo_params_t& p, const Ws& w,
@@ -647,47 +647,47 @@ cudaError_t launch_advection(const lacmo_grid_t& g, const lacmo_params_t& p, con
   if (relax_on) {
     k_relaxation<<<nblocks(g.nz, 128), 128, 0, s>>>(g.scalar_fields + 4 * C, g.nx, g.nz,
                                                      p.init_profile_r_v, p.relaxation_time_profile,
-                                                     p.dt_sub, w.relax);
+                                                     p.dt_sub, w.relax); note_launches(1);
     k_relaxation<<<nblocks(g.nz, 128), 128, 0, s>>>(g.scalar_fields + 2 * C, g.nx, g.nz,
                                                      p.init_profile_Theta,
                                                      p.relaxation_time_profile, p.dt_sub,
-                                                     w.relax + g.nz);
+                                                     w.relax + g.nz); note_launches(1);
   }
   k_advection<<<nblocks(C, 128), 128, 0, s>>>(g.scalar_fields, g.mass_flux_air_dry, g.nx, g.nz,
                                               g.dx, g.dz, p.dt_sub, w.relax, relax_on ? 1 : 0,
-                                              w.dTh, w.drv, second ? 1 : 0);
+                                              w.dTh, w.drv, second ? 1 : 0); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_divergence(const double* f, const double* flux, int64_t nx, int64_t nz,
                               double dx, double dz, int bcx, int bcz, double* out, cudaStream_t s) {
-  k_divergence<<<nblocks(nx * nz, 128), 128, 0, s>>>(f, flux, nx, nz, dx, dz, bcx, bcz, out);
+  k_divergence<<<nblocks(nx * nz, 128), 128, 0, s>>>(f, flux, nx, nz, dx, dz, bcx, bcz, out); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_relaxation(const double* f, int64_t nx, int64_t nz, const double* prof,
                               const double* trel, double dt, double* out, cudaStream_t s) {
-  k_relaxation<<<nblocks(nz, 128), 128, 0, s>>>(f, nx, nz, prof, trel, dt, out);
+  k_relaxation<<<nblocks(nz, 128), 128, 0, s>>>(f, nx, nz, prof, trel, dt, out); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_r_l_binned(const lacmo_sips_t& sp, const lacmo_grid_t& g, const Ws& w,
                               cudaStream_t s) {
   int64_t C = g.nx * g.nz;
   k_r_l<<<nblocks(C * 32, 256, 152 * 16), 256, 0, s>>>(w.start, w.perm, sp.m_w, sp.xi,
-                                                       g.scalar_fields, C);
+                                                       g.scalar_fields, C); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_mass_rate(int sol, int64_t n, const InPtrs& in, double* g, double* dg,
                              cudaStream_t s) {
-  k_mass_rate<<<nblocks(n, 128), 128, 0, s>>>(sol, n, in, g, dg);
+  k_mass_rate<<<nblocks(n, 128), 128, 0, s>>>(sol, n, in, g, dg); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_newton(int sol, int64_t n, double dt_sub, int no_iter, const InPtrs& in,
                           double* dm, double* g0, cudaStream_t s) {
-  k_newton<<<nblocks(n, 128), 128, 0, s>>>(sol, n, dt_sub, no_iter, in, dm, g0);
+  k_newton<<<nblocks(n, 128), 128, 0, s>>>(sol, n, dt_sub, no_iter, in, dm, g0); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_interp(const int32_t* cell, const double* rel, const double* gv, int64_t n,
                           int64_t nx, int64_t nz, double* out, cudaStream_t s) {
-  k_interp<<<nblocks(n, 128), 128, 0, s>>>(cell, rel, gv, n, nx, nz, out);
+  k_interp<<<nblocks(n, 128), 128, 0, s>>>(cell, rel, gv, n, nx, nz, out); note_launches(1);
   return cudaGetLastError();
 }
 

@@ -36,6 +36,8 @@ struct Ws {
 
 size_t ws_bytes(int64_t n, int64_t nx, int64_t nz);
 bool ws_carve(void* base, size_t bytes, int64_t n, int64_t nx, int64_t nz, Ws* ws);
+// process-wide count of kernels this library has launched (lacmo_kernel_launches)
+void note_launches(int k);
 
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), returns a uniform double
 // in [0, 1) with 53 random bits.

@@ -39,6 +39,8 @@ def to_device(a, dtype=F64, device="cuda"):
         t = a.to(device=device, dtype=dtype)
         return t.contiguous()
     arr = np.ascontiguousarray(np.asarray(a))
+    if not arr.flags.writeable:
+        arr = arr.copy()
     t = torch.from_numpy(arr)
     if t.dtype != dtype:
         t = t.to(dtype)
@@ -95,7 +97,7 @@ class DeviceState:
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
         _lib.check(self.lib.lacmo_workspace_reset(_ptr(self.ws), self.ws_bytes, self.n, self.nx,
                                                   self.nz, s), "workspace_reset")
-        self.draw_mode = draws
+        self.draw_mode = draws if isinstance(draws, str) else "buffer"
         self.seed = int(seed)
         self.draw_buf = None
         if not isinstance(draws, str):

@@ -327,6 +327,28 @@ ORC_EXPORT void orc_update_velocity_Beard(double* vel, const double* R, int64_t 
   for (int64_t i = 0; i < n; ++i) vel[i] = terminal_velocity_Beard(R[i]);
 }
 
+/* Philox4x32-10 (Salmon et al., SC'11) uniform double with 53 random bits;
+   the same generator and counter layout as the GPU kernels use when no draw
+   buffer is given: key = seed, counter = (pair rank, collision step << 32 | cell). */
+static uint32_t mulhi32(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a * b) >> 32); }
+static double philox_uniform(uint64_t key, uint64_t c0, uint64_t c1) {
+  uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
+  uint32_t x0 = (uint32_t)c0, x1 = (uint32_t)(c0 >> 32), x2 = (uint32_t)c1, x3 = (uint32_t)(c1 >> 32);
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0 = mulhi32(0xD2511F53u, x0), lo0 = 0xD2511F53u * x0;
+    uint32_t hi1 = mulhi32(0xCD9E8D57u, x2), lo1 = 0xCD9E8D57u * x2;
+    uint32_t y0 = hi1 ^ x1 ^ k0, y1 = lo1, y2 = hi0 ^ x3 ^ k1, y3 = lo0;
+    x0 = y0; x1 = y1; x2 = y2; x3 = y3;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  uint64_t a = x0 >> 5, b = x1 >> 6;
+  return (double)(a * 67108864ull + b) * (1.0 / 9007199254740992.0);
+}
+ORC_EXPORT void orc_philox_uniform(uint64_t key, const uint64_t* c0, const uint64_t* c1, int64_t n,
+                                   double* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = philox_uniform(key, c0[i], c1[i]);
+}
+
 /* collision/all_or_nothing.py:35-67 */
 static inline int64_t kernel_index(double x, double lo, double bl, int64_t nb) {
   int64_t ind = trunc_i64((COL_LOG(x) - lo) / bl + 0.5);
@@ -432,7 +454,7 @@ static void collide_cell_2d(double* xis, double* m_w, double* m_s, double* radii
                             const double* v0, const double* v1, const double* rho, int64_t n,
                             double dt_over_dV, const double* E, double E_const, int64_t nb,
                             double lo, double bl, int64_t* no_cols, const double* rnd,
-                            int64_t* kbuf) {
+                            int64_t* kbuf, uint64_t seed, uint64_t pc1) {
   if (E) for (int64_t i = 0; i < n; ++i) kbuf[i] = kernel_index(radii[i], lo, bl, nb);
   int64_t cnt = 0;
   for (int64_t i = 0; i < n - 1; ++i) {
@@ -454,7 +476,7 @@ static void collide_cell_2d(double* xis, double* m_w, double* m_s, double* radii
         xis[imax] -= xi_col;
         if (E) kbuf[imin] = kernel_index(radii[imin], lo, bl, nb);
         no_cols[1] += 1;
-      } else if (p_crit > rnd[cnt]) {
+      } else if (p_crit > (rnd ? rnd[cnt] : philox_uniform(seed, (uint64_t)cnt, pc1))) {
         no_cols[0] += 1;
         double xi_rel_dev = (xi_max - xi_min) / xi_max;
         if (xi_rel_dev < 1.0E-5) {
@@ -485,10 +507,11 @@ static void collide_cell_2d(double* xis, double* m_w, double* m_s, double* radii
    a cell in ascending ID; the radius uses the cell temperature and the
    solute's density.  Draws are consumed in that order from rnd[*rnd_pos..].
    Returns 0, or -1 if rnd holds too few draws (nothing is changed then). */
-ORC_EXPORT int orc_collision_step_all_cells_2d(double* xis, double* m_w, double* m_s,
+static int collision_all_cells(double* xis, double* m_w, double* m_s,
     const double* vel, const double* T, const int64_t* cells, int64_t N, int64_t Nx, int64_t Nz,
     double dt_over_dV, const double* E, double E_const, int64_t nb, double lo, double bl,
-    int64_t* no_cols, int sol, const double* rnd, int64_t rnd_len, int64_t* rnd_pos) {
+    int64_t* no_cols, int sol, const double* rnd, int64_t rnd_len, int64_t* rnd_pos,
+    uint64_t seed, int64_t* col_step) {
   int64_t C = Nx * Nz;
   int64_t* start = (int64_t*)calloc(C + 1, sizeof(int64_t));
   int64_t* order = (int64_t*)malloc(sizeof(int64_t) * (N > 0 ? N : 1));
@@ -503,7 +526,8 @@ ORC_EXPORT int orc_collision_step_all_cells_2d(double* xis, double* m_w, double*
     int64_t nc = start[c + 1] - start[c];
     draw0[c + 1] = draw0[c] + nc * (nc - 1) / 2;
   }
-  if (draw0[C] > rnd_len) { free(start); free(order); free(draw0); return -1; }
+  if (rnd && draw0[C] > rnd_len) { free(start); free(order); free(draw0); return -1; }
+  const uint64_t cstep = col_step ? (uint64_t)*col_step : 0;
   {
     int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (C > 0 ? C : 1));
     memcpy(fill, start, sizeof(int64_t) * C);
@@ -543,7 +567,7 @@ ORC_EXPORT int orc_collision_step_all_cells_2d(double* xis, double* m_w, double*
       }
       int64_t cnt[2] = {0, 0};
       collide_cell_2d(xb, wb, sb, Rb, v0, v1, rb, n, dt_over_dV, E, E_const, nb, lo, bl, cnt,
-                      rnd + draw0[c], kb);
+                      rnd ? rnd + draw0[c] : NULL, kb, seed, (cstep << 32) | (uint64_t)c);
       nc0 += cnt[0]; nc1 += cnt[1];
       for (int64_t q = 0; q < n; ++q) {
         int64_t id = ids[q];
@@ -553,9 +577,27 @@ ORC_EXPORT int orc_collision_step_all_cells_2d(double* xis, double* m_w, double*
     free(xb); free(wb); free(sb); free(Rb); free(v0); free(v1); free(rb); free(kb);
   }
   no_cols[0] += nc0; no_cols[1] += nc1;
-  *rnd_pos = draw0[C];
+  if (rnd) *rnd_pos = draw0[C];
+  if (col_step) *col_step += 1;
   free(start); free(order); free(draw0);
   return 0;
+}
+
+ORC_EXPORT int orc_collision_step_all_cells_2d(double* xis, double* m_w, double* m_s,
+    const double* vel, const double* T, const int64_t* cells, int64_t N, int64_t Nx, int64_t Nz,
+    double dt_over_dV, const double* E, double E_const, int64_t nb, double lo, double bl,
+    int64_t* no_cols, int sol, const double* rnd, int64_t rnd_len, int64_t* rnd_pos) {
+  return collision_all_cells(xis, m_w, m_s, vel, T, cells, N, Nx, Nz, dt_over_dV, E, E_const, nb,
+                             lo, bl, no_cols, sol, rnd, rnd_len, rnd_pos, 0, NULL);
+}
+
+/* the same with Philox draws (key seed, collision-step counter *col_step) */
+ORC_EXPORT int orc_collision_step_all_cells_2d_philox(double* xis, double* m_w, double* m_s,
+    const double* vel, const double* T, const int64_t* cells, int64_t N, int64_t Nx, int64_t Nz,
+    double dt_over_dV, const double* E, double E_const, int64_t nb, double lo, double bl,
+    int64_t* no_cols, int sol, uint64_t seed, int64_t* col_step) {
+  return collision_all_cells(xis, m_w, m_s, vel, T, cells, N, Nx, Nz, dt_over_dV, E, E_const, nb,
+                             lo, bl, no_cols, sol, NULL, 0, NULL, seed, col_step);
 }
 
 /* total number of pair draws the next all-cells step consumes */
@@ -865,13 +907,14 @@ typedef struct {
   int64_t rnd_len;
   int64_t* rnd_pos;
   int64_t N;
+  uint64_t seed;
+  int64_t* col_step;
 } orc_adv_t;
 
 static int collide_all(orc_adv_t* a) {
-  return orc_collision_step_all_cells_2d(a->xi, a->m_w, a->m_s, a->vel, a->gsf, a->cells, a->N,
-                                         a->Nx, a->Nz, a->dt_col_over_dV, a->E, a->E_const, a->nb,
-                                         a->lo, a->bl, a->no_cols, a->sol, a->rnd, a->rnd_len,
-                                         a->rnd_pos);
+  return collision_all_cells(a->xi, a->m_w, a->m_s, a->vel, a->gsf, a->cells, a->N, a->Nx, a->Nz,
+                             a->dt_col_over_dV, a->E, a->E_const, a->nb, a->lo, a->bl, a->no_cols,
+                             a->sol, a->rnd, a->rnd_len, a->rnd_pos, a->seed, a->col_step);
 }
 
 /* integration.py:1095-1294 */
@@ -949,12 +992,13 @@ ORC_EXPORT int orc_integrate_adv_step(double* gsf, double* gmp, const double* gv
     double dt_col_over_dV, int scale_dt_cond, int no_col_per_adv, int act_collisions,
     int act_relaxation, const double* prof_r_v, const double* prof_Theta, const double* t_relax,
     int no_iter, double g_set, const double* E, double E_const, int64_t nb, double lo, double bl,
-    int64_t* no_cols, const double* rnd, int64_t rnd_len, int64_t* rnd_pos, int64_t N) {
+    int64_t* no_cols, const double* rnd, int64_t rnd_len, int64_t* rnd_pos, int64_t N,
+    uint64_t seed, int64_t* col_step) {
   orc_adv_t a = {gsf, gmp, gv, flux, p_ref, p_ref_inv, Nx, Nz, ranges, steps, V, pos, vel, cells,
                  rel_pos, m_w, m_s, xi, sol, water_removed, active, T_p, delta_m_l, dt, dt_sub,
                  dt_sub_half, dt_col_over_dV, scale_dt_cond, no_col_per_adv, act_collisions,
                  act_relaxation, prof_r_v, prof_Theta, t_relax, no_iter, g_set, E, E_const, nb, lo,
-                 bl, no_cols, rnd, rnd_len, rnd_pos, N};
+                 bl, no_cols, rnd, rnd_len, rnd_pos, N, seed, col_step};
   return adv_step(&a);
 }
 

@@ -72,7 +72,14 @@ def _lib(variant):
     lib.orc_integrate_adv_step.argtypes = [
         D, D, D, D, dbl, dbl, i64, i64, D, D, dbl, D, D, I64, D, D, D, D, cint, D, U8, D, D,
         dbl, dbl, dbl, dbl, cint, cint, cint, cint, D, D, D, cint, dbl, ctypes.c_void_p, dbl,
-        i64, dbl, dbl, I64, D, i64, I64, i64]
+        i64, dbl, dbl, I64, ctypes.c_void_p, i64, ctypes.c_void_p, i64, ctypes.c_uint64,
+        ctypes.c_void_p]
+    lib.orc_collision_step_all_cells_2d_philox.argtypes = [
+        D, D, D, D, D, I64, i64, i64, i64, dbl, ctypes.c_void_p, dbl, i64, dbl, dbl, I64, cint,
+        ctypes.c_uint64, I64]
+    lib.orc_collision_step_all_cells_2d_philox.restype = cint
+    U64 = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+    lib.orc_philox_uniform.argtypes = [ctypes.c_uint64, U64, U64, i64, D]
     lib.orc_integrate_adv_step.restype = cint
     lib.orc_set_threads.argtypes = [cint]
     lib.orc_get_threads.restype = cint
@@ -256,11 +263,16 @@ class Oracle:
             delta_m_l, dt, dt_sub, dt_sub_half, dt_col_over_dV, scale_dt_cond, no_col_per_adv,
             act_collisions, act_relaxation, init_profile_r_v, init_profile_Theta,
             relaxation_time_profile, no_iter_impl_mass, g_set, E_col_grid, no_kernel_bins,
-            R_kernel_low_log, bin_factor_R_log, no_cols, draws, draw_pos=None):
+            R_kernel_low_log, bin_factor_R_log, no_cols, draws, draw_pos=None, seed=0,
+            col_step=None):
+        """``draws``: uniform buffer consumed from ``draw_pos``, or None for
+        Philox draws keyed by ``seed`` and the counter ``col_step`` (int64[1])."""
         E, Ec = _E(E_col_grid)
         Nz = int(grid_no_cells[1])
         if draw_pos is None:
             draw_pos = np.zeros(1, dtype=np.int64)
+        if draws is None and col_step is None:
+            col_step = np.zeros(1, dtype=np.int64)
         prof = lambda a: (np.zeros(Nz) if a is None else np.ascontiguousarray(a, dtype=np.float64))
         rc = self.lib.orc_integrate_adv_step(
             _c(grid_scalar_fields), _c(grid_mat_prop), _c(grid_velocity),
@@ -274,10 +286,31 @@ class Oracle:
             prof(relaxation_time_profile), int(no_iter_impl_mass), float(g_set),
             None if E is None else E.ctypes.data, Ec, int(no_kernel_bins or 0),
             float(R_kernel_low_log or 0.0), float(bin_factor_R_log or 1.0), _c(no_cols, np.int64),
-            _c(draws), len(draws), draw_pos, len(xi))
+            None if draws is None else _c(draws).ctypes.data, 0 if draws is None else len(draws),
+            draw_pos.ctypes.data, len(xi), int(seed),
+            None if col_step is None else _c(col_step, np.int64).ctypes.data)
         if rc != 0:
             raise ValueError("not enough draws for the advection step")
         return draw_pos
+
+    def collision_step_all_cells_philox(self, xis, m_w, m_s, vel, grid_temperature, cells,
+                                        no_cells, dt_over_dV, E_col_grid, no_kernel_bins,
+                                        R_kernel_low_log, bin_factor_R_log, no_cols, solute_type,
+                                        seed, col_step):
+        E, Ec = _E(E_col_grid)
+        self.lib.orc_collision_step_all_cells_2d_philox(
+            _c(xis), _c(m_w), _c(m_s), _c(vel), np.ascontiguousarray(grid_temperature, dtype=np.float64),
+            _c(cells, np.int64), len(xis), int(no_cells[0]), int(no_cells[1]), float(dt_over_dV),
+            None if E is None else E.ctypes.data, Ec, int(no_kernel_bins or 0),
+            float(R_kernel_low_log or 0.0), float(bin_factor_R_log or 1.0), _c(no_cols, np.int64),
+            _sol(solute_type), int(seed), _c(col_step, np.int64))
+
+    def philox_uniform(self, key, c0, c1):
+        c0 = np.ascontiguousarray(c0, dtype=np.uint64)
+        c1 = np.ascontiguousarray(c1, dtype=np.uint64)
+        out = np.empty(c0.size)
+        self.lib.orc_philox_uniform(int(key), c0, c1, c0.size, out)
+        return out
 
     # -- correctly-rounded routines (variant 'cr') -----------------------------
     def cr_pow(self, x, y):

@@ -47,7 +47,13 @@ def test_mass_rate_newton_vs_golden():
         dm, g0 = I.compute_dml_and_gamma_impl_Newton_full_np(g["dt_sub"], g["no_iter"], g["m_w"],
                                                              g["m_s"], w, R, g["T_p"], rho, *amb,
                                                              sig, sol)
-        np.testing.assert_allclose(dm, g[f"dm_{sol}"], rtol=RTOL, atol=1e-12 * np.abs(g["m_w"]))
+        # dm = m_new - m_w cancels: its error is relative to m_w
+        ref = g[f"dm_{sol}"]
+        bad = np.abs(dm - ref) > RTOL * np.abs(ref) + 1e-13 * np.abs(g["m_w"])
+        if bad.any():
+            k = np.nonzero(bad)[0][:5]
+            raise AssertionError(f"{sol}: {bad.sum()} dm mismatches, e.g. idx {k}: gpu {dm[k]} "
+                                 f"ref {ref[k]} m_w {g['m_w'][k]}")
         np.testing.assert_allclose(g0, g[f"g0_{sol}"], rtol=RTOL, atol=1e-30)
 
 
@@ -175,6 +181,53 @@ def test_cells_full_size_bit_exact_vs_cr_oracle(oracle_cr, oracle_nb, kernel, bo
     assert diff.sum() <= max(5, n // 1000)
 
 
+def test_philox_draws_match_oracle(oracle_cr):
+    """Device Philox (performance mode) == the oracle's Philox: same collision
+    outcomes bit for bit over two consecutive steps (counter advances)."""
+    from lacmopy_gb300 import DeviceState
+    st = _full_state(13, nx=40, nz=40, kernel="Hall_Bott", drizzle_fraction=0.1, r_tot=9.0E-3)
+    ds = DeviceState(st, draws="philox", seed=4242)
+    ds.collision_step()
+    ds.collision_step()
+    out = ds.snapshot()
+    xi, mw, ms = st["xi"].copy(), st["m_w"].copy(), st["m_s"].copy()
+    nc = np.zeros(2, np.int64)
+    cs = np.zeros(1, np.int64)
+    for _ in range(2):
+        oracle_cr.collision_step_all_cells_philox(
+            xi, mw, ms, st["vel"], st["grid_scalar_fields"][0], st["cells"], st["grid_no_cells"],
+            st["dt_col_over_dV"], st["E_col_grid"], st["no_kernel_bins"], st["R_kernel_low_log"],
+            st["bin_factor_R_log"], nc, "AS", 4242, cs)
+    assert nc.sum() > 0
+    assert np.array_equal(out["no_cols"], nc)
+    assert np.array_equal(out["xi"], xi)
+    assert np.array_equal(out["m_w"], mw)
+    assert np.array_equal(out["m_s"], ms)
+
+
+def test_adv_step_philox_vs_oracle(oracle_cr):
+    from lacmopy_gb300 import DeviceState
+    st = _full_state(17, nx=20, nz=20, spcm=(13, 19), r_tot=12.5E-3, drizzle_fraction=0.15)
+    ref = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in st.items()}
+    ds = DeviceState(st, draws="philox", seed=99)
+    ds.adv_step(2)
+    out = ds.snapshot()
+    cs = np.zeros(1, np.int64)
+    for _ in range(2):
+        oracle_cr.integrate_adv_step_np(
+            ref["grid_scalar_fields"], ref["grid_mat_prop"], ref["grid_velocity"],
+            ref["grid_mass_flux_air_dry"], ref["p_ref"], ref["p_ref_inv"], ref["grid_no_cells"],
+            ref["grid_ranges"], ref["grid_steps"], ref["grid_volume_cell"], ref["pos"],
+            ref["vel"], ref["cells"], ref["rel_pos"], ref["m_w"], ref["m_s"], ref["xi"], "AS",
+            ref["water_removed"], None, ref["active_ids"], ref["T_p"], ref["delta_m_l"], 1.0, 0.1,
+            0.05, ref["dt_col_over_dV"], 5, 2, True, True, ref["init_profile_r_v"],
+            ref["init_profile_Theta"], ref["relaxation_time_profile"], 3, ref["g_set"],
+            ref["E_col_grid"], ref["no_kernel_bins"], ref["R_kernel_low_log"],
+            ref["bin_factor_R_log"], ref["no_cols"], None, None, 99, cs)
+    assert ref["no_cols"].sum() > 0
+    _check_adv(out, ref)
+
+
 def test_golovin_5000_bit_exact_vs_cr_oracle(oracle_cr):
     from lacmopy_gb300 import collision as C
     from lacmopy_gb300 import synthetic
@@ -275,13 +328,14 @@ def test_adv_step_vs_golden(case, mode):
 @pytest.mark.parametrize("kernel,nco", [("Long_Bott", 2), ("Hall_Bott", 10)])
 def test_adv_step_30x30_vs_oracle(oracle_nb, kernel, nco):
     from lacmopy_gb300 import DeviceState
-    st = _full_state(21, nx=30, nz=30, kernel=kernel, r_tot=9.0E-3, drizzle_fraction=0.08)
+    st = _full_state(21, nx=30, nz=30, spcm=(13, 19), kernel=kernel, r_tot=12.5E-3,
+                     drizzle_fraction=0.15)
     st["no_col_per_adv"] = nco
     st["dt_col_over_dV"] = (st["dt"] / nco) / st["grid_volume_cell"]
     low = np.nonzero(st["cells"][1] == 0)[0][:40]
     st["pos"][1, low] = 1e-9
     st["vel"][1, low] = -1.0
-    draws = np.random.default_rng(8).random(4 * 10 ** 6)
+    draws = np.random.default_rng(8).random(12 * 10 ** 6)
     ref = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in st.items()}
     ds = DeviceState(st, draws=draws)
     ds.adv_step(2)
