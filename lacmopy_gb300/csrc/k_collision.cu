@@ -69,11 +69,80 @@ struct CellArgs {
   int32_t* gk;
 };
 
+// Exact FP64 evaluation of one pair (collision/all_or_nothing.py:553-633),
+// in the reference's operation order.  Arrays are indexed by ii / jj; r < 0
+// means "draw not fetched yet".  Optional float copies are kept in step.
+struct PairState {
+  double *XI, *MW, *MS, *RR;
+  const double *RHO, *U, *W;
+  int32_t* KK;
+  float *fxi, *fR;  // nullptr when no float copies exist
+};
+
+__device__ __forceinline__ void exact_pair(const PairState& P, int ii, int jj, double r,
+                                           const CellArgs& a, bool use_E, int64_t rk,
+                                           const double* rnd, uint64_t pc1, int64_t& c0,
+                                           int64_t& c1) {
+  double *XI = P.XI, *MW = P.MW, *MS = P.MS, *RR = P.RR;
+  int imin, imax;
+  if (XI[ii] <= XI[jj]) { imin = ii; imax = jj; } else { imin = jj; imax = ii; }
+  const double xi_min = XI[imin], xi_max = XI[imax];
+  const double m_w_min = MW[imin], m_w_max = MW[imax];
+  const double m_s_min = MS[imin], m_s_max = MS[imax];
+  const double Rs = RR[ii] + RR[jj];
+  const double e = use_E ? __ldg(a.E + (int64_t)P.KK[ii] * a.nb + P.KK[jj]) : a.E_const;
+  const double du = P.U[ii] - P.U[jj], dw = P.W[ii] - P.W[jj];
+  const double dv = sqrt(du * du + dw * dw);
+  const double p_crit = xi_max * a.dtdv * (LC_PI * Rs * Rs * e * dv * 1.0E-12);
+  if (p_crit > 1.0) {
+    const double xi_col = p_crit * xi_min;
+    MW[imin] = m_w_min + p_crit * m_w_max;
+    MS[imin] = m_s_min + p_crit * m_s_max;
+    RR[imin] = col_radius((MW[imin] + MS[imin]), P.RHO[imin]);
+    XI[imax] -= xi_col;
+    if (use_E) P.KK[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
+    if (P.fxi) { P.fxi[imax] = (float)XI[imax]; P.fR[imin] = (float)RR[imin]; }
+    c1 += 1;
+    return;
+  }
+  if (r < 0.0) r = rnd ? rnd[rk] : philox_uniform(a.seed, (uint64_t)rk, pc1);
+  if (!(p_crit > r)) return;
+  c0 += 1;
+  const double xi_rel_dev = (xi_max - xi_min) / xi_max;
+  if (xi_rel_dev < 1.0E-5) {
+    const double xi_ges = xi_min + xi_max;
+    MW[imin] = 2.0 * (xi_min * m_w_min + xi_max * m_w_max) / xi_ges;
+    MS[imin] = 2.0 * (xi_min * m_s_min + xi_max * m_s_max) / xi_ges;
+    MW[imax] = MW[imin];
+    MS[imax] = MS[imin];
+    RR[imin] = col_radius((MW[imin] + MS[imin]), P.RHO[imin]);
+    RR[imax] = RR[imin];
+    XI[imax] = 0.5 * 0.7 * xi_ges;
+    XI[imin] = 0.5 * xi_ges - XI[imax];
+    if (use_E) { P.KK[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb); P.KK[imax] = P.KK[imin]; }
+    if (P.fxi) {
+      P.fxi[imin] = (float)XI[imin]; P.fxi[imax] = (float)XI[imax];
+      P.fR[imin] = (float)RR[imin]; P.fR[imax] = (float)RR[imax];
+    }
+  } else {
+    MW[imin] += m_w_max;
+    MS[imin] += m_s_max;
+    RR[imin] = col_radius((MW[imin] + MS[imin]), P.RHO[imin]);
+    XI[imax] -= xi_min;
+    if (use_E) P.KK[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
+    if (P.fxi) { P.fxi[imax] = (float)XI[imax]; P.fR[imin] = (float)RR[imin]; }
+  }
+}
+
+// Shared-memory layout per warp: 7 double arrays, 4 float arrays, 1 int array.
+constexpr size_t CELL_WARP_BYTES = (size_t)CELL_SMEM * (7 * 8 + 4 * 4 + 4);
+
 __global__ void __launch_bounds__(CELL_WARPS * 32) k_collide_cells(CellArgs a) {
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double* base = smem + (size_t)wid * CELL_SMEM * 7;
-  int32_t* kbase = (int32_t*)(smem + (size_t)CELL_WARPS * CELL_SMEM * 7) + wid * CELL_SMEM;
+  double* base = (double*)((char*)smem + (size_t)wid * CELL_WARP_BYTES);
+  float* fbase = (float*)(base + 7 * CELL_SMEM);
+  int32_t* kbase = (int32_t*)(fbase + 4 * CELL_SMEM);
   const int64_t cursor = a.draws ? *a.cursor : 0;
   if (a.draws && cursor + *a.total_pairs > a.n_draws) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.flags, LACMO_FLAG_DRAWS_SHORT);
@@ -81,6 +150,8 @@ __global__ void __launch_bounds__(CELL_WARPS * 32) k_collide_cells(CellArgs a) {
   }
   const uint64_t cstep = (uint64_t)*a.col_step;
   const bool use_E = a.E != nullptr;
+  const float dtdv_f = (float)a.dtdv;
+  const float pi_e12 = (float)(LC_PI * 1.0E-12);
   int64_t c0 = 0, c1 = 0;
   for (int64_t c = blockIdx.x * (int64_t)CELL_WARPS + wid; c < a.C;
        c += (int64_t)gridDim.x * CELL_WARPS) {
@@ -90,10 +161,12 @@ __global__ void __launch_bounds__(CELL_WARPS * 32) k_collide_cells(CellArgs a) {
     const bool in_smem = n <= CELL_SMEM;
     const double Tc = a.T[c];
     const double* rnd = a.draws ? a.draws + cursor + a.draw_off[c] : nullptr;
-    // state: shared memory (local index) or global scratch (by SIP ID)
+    const uint64_t pc1 = (cstep << 32) | (uint64_t)c;
     double *sxi = base, *smw = base + CELL_SMEM, *sms = base + 2 * CELL_SMEM,
            *sR = base + 3 * CELL_SMEM, *srho = base + 4 * CELL_SMEM, *su = base + 5 * CELL_SMEM,
            *sw = base + 6 * CELL_SMEM;
+    float *fxi = fbase, *fR = fbase + CELL_SMEM, *fu = fbase + 2 * CELL_SMEM,
+          *fw = fbase + 3 * CELL_SMEM;
     int32_t* sk = kbase;
     const int32_t* ids = a.perm + b;
     // load, radius and bin at the cell temperature (all_or_nothing.py:812-826)
@@ -107,82 +180,65 @@ __global__ void __launch_bounds__(CELL_WARPS * 32) k_collide_cells(CellArgs a) {
       const double R = col_radius(m_p, rho);
       const int32_t kb = use_E ? col_bin(R, a.lo, a.bl, a.nb) : 0;
       if (in_smem) {
+        const double u = a.vel[id], w = a.vel[a.n + id];
         sxi[q] = x; smw[q] = mw; sms[q] = ms; sR[q] = R; srho[q] = rho;
-        su[q] = a.vel[id]; sw[q] = a.vel[a.n + id]; sk[q] = kb;
+        su[q] = u; sw[q] = w; sk[q] = kb;
+        fxi[q] = (float)x; fR[q] = (float)R; fu[q] = (float)u; fw[q] = (float)w;
       } else {
         a.gR[id] = R; a.grho[id] = rho; a.gk[id] = kb;
       }
     }
     __syncwarp();
-    for (int s = 1; s <= 2 * n - 3; ++s) {
-      const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
-      const int ihi = (s - 1) >> 1;
-      for (int i = ilo + lane; i <= ihi; i += 32) {
-        const int j = s - i;
-        // indices into the state arrays
-        int ii = i, jj = j;
-        double *XI = sxi, *MW = smw, *MS = sms, *RR = sR, *RHO = srho;
-        const double *U = su, *W = sw;
-        int32_t* KK = sk;
-        if (!in_smem) {
-          ii = ids[i]; jj = ids[j];
-          XI = a.xi; MW = a.m_w; MS = a.m_s; RR = a.gR; RHO = a.grho;
-          U = a.vel; W = a.vel + a.n; KK = a.gk;
-        }
-        int imin, imax;
-        if (XI[ii] <= XI[jj]) { imin = ii; imax = jj; } else { imin = jj; imax = ii; }
-        const double xi_min = XI[imin], xi_max = XI[imax];
-        const double m_w_min = MW[imin], m_w_max = MW[imax];
-        const double m_s_min = MS[imin], m_s_max = MS[imax];
-        const double Rs = RR[ii] + RR[jj];
-        const double e = use_E ? __ldg(a.E + (int64_t)KK[ii] * a.nb + KK[jj]) : a.E_const;
-        const double du = U[ii] - U[jj], dw = W[ii] - W[jj];
-        const double dv = sqrt(du * du + dw * dw);
-        const double p_crit = xi_max * a.dtdv * (LC_PI * Rs * Rs * e * dv * 1.0E-12);
-        if (p_crit > 1.0) {
-          const double xi_col = p_crit * xi_min;
-          MW[imin] = m_w_min + p_crit * m_w_max;
-          MS[imin] = m_s_min + p_crit * m_s_max;
-          RR[imin] = col_radius((MW[imin] + MS[imin]), RHO[imin]);
-          XI[imax] -= xi_col;
-          if (use_E) KK[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
-          c1 += 1;
-        } else {
-          const int64_t rk = pair_rank(i, j, n);
-          const double r = rnd ? rnd[rk]
-                               : philox_uniform(a.seed, (uint64_t)rk,
-                                                (cstep << 32) | (uint64_t)c);
-          if (p_crit > r) {
-            c0 += 1;
-            const double xi_rel_dev = (xi_max - xi_min) / xi_max;
-            if (xi_rel_dev < 1.0E-5) {
-              const double xi_ges = xi_min + xi_max;
-              MW[imin] = 2.0 * (xi_min * m_w_min + xi_max * m_w_max) / xi_ges;
-              MS[imin] = 2.0 * (xi_min * m_s_min + xi_max * m_s_max) / xi_ges;
-              MW[imax] = MW[imin];
-              MS[imax] = MS[imin];
-              RR[imin] = col_radius((MW[imin] + MS[imin]), RHO[imin]);
-              RR[imax] = RR[imin];
-              XI[imax] = 0.5 * 0.7 * xi_ges;
-              XI[imin] = 0.5 * xi_ges - XI[imax];
-              if (use_E) { KK[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb); KK[imax] = KK[imin]; }
-            } else {
-              MW[imin] += m_w_max;
-              MS[imin] += m_s_max;
-              RR[imin] = col_radius((MW[imin] + MS[imin]), RHO[imin]);
-              XI[imax] -= xi_min;
-              if (use_E) KK[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
-            }
-          }
-        }
-      }
-      if (!in_smem) __threadfence_block();
-      __syncwarp();
-    }
     if (in_smem) {
+      const PairState P{sxi, smw, sms, sR, srho, su, sw, sk, fxi, fR};
+      for (int s = 1; s <= 2 * n - 3; ++s) {
+        const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
+        const int ihi = (s - 1) >> 1;
+        for (int i = ilo + lane; i <= ihi; i += 32) {
+          const int j = s - i;
+          const int64_t rk = pair_rank(i, j, n);
+          // Certified FP32 upper bound of |p_crit|: every float op and
+          // double->float conversion is within 2^-24 relative, the velocity
+          // difference gets an explicit absolute slack for its cancellation,
+          // and the result is inflated by 2^-16 plus an absolute 1e-36.  Only
+          // if this bound is below both 1 and the draw is the pair certainly
+          // neither a multiple collection nor a collection; otherwise the
+          // exact FP64 evaluation decides.
+          const float ui = fu[i], uj = fu[j], wi = fw[i], wj = fw[j];
+          const float du = ui - uj, dw = wi - wj;
+          const float slack = 0x1p-21f * (fabsf(ui) + fabsf(uj) + fabsf(wi) + fabsf(wj));
+          const float dvu = sqrtf(du * du + dw * dw) + slack;
+          const float rs = fR[i] + fR[j];
+          const float ef = use_E ? (float)__ldg(a.E + (int64_t)sk[i] * a.nb + sk[j])
+                                 : (float)a.E_const;
+          const float xm = fmaxf(fabsf(fxi[i]), fabsf(fxi[j]));
+          const float pub = ((xm * dtdv_f) * pi_e12) * rs * rs * ef * dvu;
+          const float ap = pub * (1.0f + 0x1p-16f) + 1e-36f;
+          double r = -1.0;
+          if (ap < 1.0f && pub >= 1e-28f) {
+            r = rnd ? rnd[rk] : philox_uniform(a.seed, (uint64_t)rk, pc1);
+            if ((double)ap < r) continue;   // certainly no collision
+          }
+          exact_pair(P, i, j, r, a, use_E, rk, rnd, pc1, c0, c1);
+        }
+        __syncwarp();
+      }
       for (int q = lane; q < n; q += 32) {
         const int32_t id = ids[q];
         a.xi[id] = sxi[q]; a.m_w[id] = smw[q]; a.m_s[id] = sms[q];
+      }
+    } else {
+      const PairState P{a.xi, a.m_w, a.m_s, a.gR, a.grho, a.vel, a.vel + a.n, a.gk, nullptr,
+                        nullptr};
+      for (int s = 1; s <= 2 * n - 3; ++s) {
+        const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
+        const int ihi = (s - 1) >> 1;
+        for (int i = ilo + lane; i <= ihi; i += 32) {
+          const int j = s - i;
+          exact_pair(P, ids[i], ids[j], -1.0, a, use_E, pair_rank(i, j, n), rnd, pc1, c0, c1);
+        }
+        __threadfence_block();
+        __syncwarp();
       }
     }
     __syncwarp();
@@ -400,7 +456,7 @@ static inline int nblk(int64_t n, int t) {
   if (b < 1) b = 1;
   return (int)(b < 152 * 32 ? b : 152 * 32);
 }
-static const size_t CELL_SMEM_BYTES = (size_t)CELL_WARPS * CELL_SMEM * (7 * 8 + 4);
+static const size_t CELL_SMEM_BYTES = (size_t)CELL_WARPS * CELL_WARP_BYTES;
 
 cudaError_t launch_collide_cells(const lacmo_sips_t& sp, const lacmo_grid_t& g,
                                  const lacmo_params_t& p, const lacmo_draws_t& d, const Ws& w,

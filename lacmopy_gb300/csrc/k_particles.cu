@@ -371,33 +371,27 @@ __device__ __forceinline__ void grid_cell_update(double* gsf, double* gmp, int64
   gmp[6 * C + c] = rho_d * (1.0 + r_v);
 }
 
-// one warp per cell: delta_m_l as the ascending-ID fold of dm*xi over the
-// cell's SIPs, then the grid update of the cell and its mass-rate terms
-__global__ void __launch_bounds__(256) k_cell_update(const int32_t* __restrict__ start,
+// one thread per cell: delta_m_l as the ascending-ID fold of dm*xi over the
+// cell's SIPs (integration.py:916-936), then the grid update of the cell and
+// its mass-rate terms for the next sub-step; all lanes carry FP64 work
+__global__ void __launch_bounds__(128) k_cell_update(const int32_t* __restrict__ start,
                                                      const int32_t* __restrict__ perm,
                                                      const double* __restrict__ dmxi,
                                                      double* delta_m_l, double* gsf, double* gmp,
                                                      double* aux, const double* dTh,
                                                      const double* drv, int64_t C, double p_ref,
                                                      double p_ref_inv, double V, int grid_update) {
-  const int lane = threadIdx.x & 31;
-  for (int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; c < C;
-       c += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
+       c += (int64_t)gridDim.x * blockDim.x) {
     const int32_t b = start[c], e = start[c + 1];
     double acc = 0.0;
-    for (int32_t base = b; base < e; base += 32) {
-      const int32_t idx = base + lane;
-      const double v = idx < e ? dmxi[perm[idx]] : 0.0;
-      const int m = (e - base) < 32 ? (e - base) : 32;
-      for (int q = 0; q < m; ++q) acc += __shfl_sync(0xffffffffu, v, q);
-    }
-    if (lane == 0) {
-      const double dml = acc * 1.0E-18;
-      delta_m_l[c] = dml;
-      if (grid_update) {
-        grid_cell_update(gsf, gmp, c, C, p_ref, p_ref_inv, dTh[c], drv[c], dml, V);
-        write_aux(gsf, gmp, aux, c, C);
-      }
+#pragma unroll 8
+    for (int32_t k = b; k < e; ++k) acc += __ldg(dmxi + __ldg(perm + k));
+    const double dml = acc * 1.0E-18;
+    delta_m_l[c] = dml;
+    if (grid_update) {
+      grid_cell_update(gsf, gmp, c, C, p_ref, p_ref_inv, dTh[c], drv[c], dml, V);
+      write_aux(gsf, gmp, aux, c, C);
     }
   }
 }
@@ -585,7 +579,7 @@ cudaError_t launch_bin(const lacmo_sips_t& sp, int64_t C, const Ws& w, cudaStrea
   k_scan<<<1, 1024, 0, s>>>(w.counts, w.start, w.draw_off, w.total_pairs, C, w.rm_count, w.rm_id,
                             w.rm_val, sp.water_removed); note_launches(1);
   k_scatter<<<nblocks(sp.n, 256), 256, 0, s>>>(sp.cell, w.rank, w.start, w.perm, sp.n); note_launches(1);
-  k_order<<<nblocks(C, 256, 152 * 16), 256, 0, s>>>(w.start, w.perm, w.rank, C); note_launches(1);
+  k_order<<<nblocks(C * 32, 256, 152 * 16), 256, 0, s>>>(w.start, w.perm, w.rank, C); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_particles(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
@@ -626,7 +620,7 @@ cudaError_t launch_cell_update(const lacmo_sips_t& sp, const lacmo_grid_t& g, co
                                cudaStream_t s) {
   (void)sp;
   int64_t C = g.nx * g.nz;
-  k_cell_update<<<nblocks(C * 32, 256, 152 * 16), 256, 0, s>>>(
+  k_cell_update<<<nblocks(C, 128), 128, 0, s>>>(
       w.start, w.perm, w.dmxi, g.delta_m_l, g.scalar_fields, g.mat_prop, w.aux, dTh, drv, C,
       g.p_ref, g.p_ref_inv, g.volume_cell, grid_update ? 1 : 0); note_launches(1);
   return cudaGetLastError();

@@ -521,7 +521,7 @@ static int collision_all_cells(double* xis, double* m_w, double* m_s,
     if (i >= 0 && i < Nx && j >= 0 && j < Nz) start[i * Nz + j + 1] += 1;
   }
   for (int64_t c = 0; c < C; ++c) start[c + 1] += start[c];
-  draw0[0] = *rnd_pos;
+  draw0[0] = rnd_pos ? *rnd_pos : 0;
   for (int64_t c = 0; c < C; ++c) {
     int64_t nc = start[c + 1] - start[c];
     draw0[c + 1] = draw0[c] + nc * (nc - 1) / 2;
