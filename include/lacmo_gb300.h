@@ -195,6 +195,31 @@ int lacmo_update_grid_r_l(const lacmo_sips_t* sips, const lacmo_grid_t* grid, vo
 int lacmo_collision_step_cells(const lacmo_sips_t* sips, const lacmo_grid_t* grid,
                                const lacmo_params_t* prm, const lacmo_draws_t* draws, void* ws,
                                size_t ws_bytes, void* stream);
+/* All-cells collision step that allocates nothing.  This entry point has no
+ * counterpart in the reference; it exists for callers that cannot allocate
+ * device memory at the time they collide (code inside another framework's
+ * memory pool or under a fixed memory budget, plugin hosts that forbid
+ * cudaMalloc after start-up).  It does the work of lacmo_collision_step_cells
+ * from the SIP cell indices alone (binning included), with its scratch in a
+ * fixed array inside the library (about 15 MB of device memory, held by every
+ * GPU that loads the library until the process exits) instead of a
+ * workspace.  The caller still passes all inputs and outputs: xi, m_w, m_s
+ * are updated in place, vel is [2][n], grid_T is the [nx][nz] temperature,
+ * cell is the int32 cell index of lacmo_cells_import.  Limits:
+ * n <= LACMO_NOALLOC_MAX_SIPS and nx*nz <= LACMO_NOALLOC_MAX_CELLS, else
+ * LACMO_ERR_CAPACITY.  Injected draws are read from the start of the buffer;
+ * Philox draws use `step` as the collision-step counter.  The first call on a
+ * device looks up the array's device address (once per device, with that
+ * device current), so make that first call before any stream capture.  All
+ * calls share the one array and each call clears what must start at zero:
+ * calls whose work overlaps on the GPU race and must be serialised. */
+#define LACMO_NOALLOC_MAX_SIPS 524288
+#define LACMO_NOALLOC_MAX_CELLS 16384
+int lacmo_collision_step_cells_noalloc(double* xi, double* m_w, double* m_s, const double* vel,
+                                       const double* grid_T, const int32_t* cell, int64_t n,
+                                       int64_t nx, int64_t nz, const lacmo_params_t* prm,
+                                       const lacmo_draws_t* draws, uint64_t step,
+                                       int64_t* no_cols, void* stream);
 /* Number of pair draws the next all-cells collision step consumes
  * (synchronises the stream; used to size an injected draw buffer). */
 int lacmo_collision_pair_count(const void* ws, int64_t n, int64_t nx, int64_t nz,

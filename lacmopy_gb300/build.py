@@ -23,6 +23,7 @@ UNITS = {
     "capi.cu": [],
     "k_particles.cu": [],
     "k_collision.cu": ["-fmad=false"],
+    "k_static.cu": [],
 }
 
 
