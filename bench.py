@@ -50,12 +50,18 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="arithmetic of the headline line; the other mode is reported beside it")
+    ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one")
+    ap.add_argument("--only", action="store_true", help="skip the second precision mode")
     return ap.parse_args()
 
 
 def workload_config(args, n_sips):
-    return {"workload": f"icmw2012_case1_{args.nx}x{args.nz}_{sum(args.spcm)}spc_fp64_plain",
-            "precision_mode": "fp64_plain", "nx": args.nx, "nz": args.nz,
+    mode = "fp64_plain" if args.precision == "fp64" else "mixed"
+    return {"workload": f"icmw2012_case1_{args.nx}x{args.nz}_{sum(args.spcm)}spc_{mode}",
+            "precision_mode": mode, "nx": args.nx, "nz": args.nz,
+            "cuda_graph": not getattr(args, "no_graph", False),
             "sips_per_cell": sum(args.spcm), "n_sips": int(n_sips), "kernel": args.kernel,
             "dt_s": 1.0, "cond_substeps": 10, "collision_steps": 2, "newton_iterations": 3,
             "draws": "philox4x32-10 (device)",
@@ -211,40 +217,62 @@ def run_ours(args):
     st = make_state(args, rank)
     n = int(st["xi"].size)
     st0 = copy.deepcopy(st)
-    ds = DeviceState(copy.deepcopy(st), draws="philox", seed=1001 + rank)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
-    for _ in range(args.warmup):
-        ds.adv_step(1)
-    torch.cuda.synchronize()
-    n_active = []
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
-    sampler = ClockSampler(local)
-    sampler.start()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    launches0 = lib.lacmo_kernel_launches()
-    for k in range(args.steps):
-        flush.zero_()
-        n_active.append(ds.cell.ge(0).sum())
-        ev[k][0].record()
-        ds.adv_step(1)
-        ev[k][1].record()
-    torch.cuda.synchronize()
-    launches = lib.lacmo_kernel_launches() - launches0
-    clocks = sampler.stop()
-    if dist:
-        dist.barrier()
-    ms = sum(a.elapsed_time(b) for a, b in ev)
-    ups = float(sum(int(x) for x in n_active))
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        u = torch.tensor([ups], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.all_reduce(u, op=dist.ReduceOp.SUM)
-        ms, ups = float(t.item()), float(u.item())
+    graph = not args.no_graph
+
+    def timed(precision, sample_clocks):
+        ds = DeviceState(copy.deepcopy(st), draws="philox", seed=1001 + rank,
+                         precision=precision)
+        for _ in range(args.warmup):
+            ds.adv_step(1, graph=graph)
+        torch.cuda.synchronize()
+        n_active = []
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        sampler = ClockSampler(local) if sample_clocks else None
+        if sampler:
+            sampler.start()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        launches0 = lib.lacmo_kernel_launches()
+        for k in range(args.steps):
+            flush.zero_()
+            n_active.append(ds.cell.ge(0).sum())
+            ev[k][0].record()
+            ds.adv_step(1, graph=graph)
+            ev[k][1].record()
+        torch.cuda.synchronize()
+        launches = lib.lacmo_kernel_launches() - launches0
+        if graph:
+            # kernels replayed from the captured graph: count them per step
+            per_step = ds.graph_kernel_count()
+            launches = per_step * args.steps
+        clocks = sampler.stop() if sampler else None
+        if dist:
+            dist.barrier()
+        ms = sum(a.elapsed_time(b) for a, b in ev)
+        ups = float(sum(int(x) for x in n_active))
+        if dist:
+            t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+            u = torch.tensor([ups], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dist.all_reduce(u, op=dist.ReduceOp.SUM)
+            ms, ups = float(t.item()), float(u.item())
+        return ds, ms, ups, launches, clocks
+
+    ds, ms, ups, launches, clocks = timed(args.precision, True)
     value = ups / (ms / 1000.0)
+    modes = {("fp64_plain" if args.precision == "fp64" else "mixed"):
+             {"value": value, "ms_per_step": ms / args.steps}}
+    if not args.only:
+        other = "mixed" if args.precision == "fp64" else "fp64"
+        ds2, ms2, ups2, _, _ = timed(other, False)
+        modes["mixed" if other == "mixed" else "fp64_plain"] = {
+            "value": ups2 / (ms2 / 1000.0), "ms_per_step": ms2 / args.steps}
+        del ds2
+    if "mixed" in modes and "fp64_plain" in modes:
+        modes["mixed_over_fp64"] = modes["mixed"]["value"] / modes["fp64_plain"]["value"]
 
     # roofline of the dominant kernel: the fused particle sub-step
     sp, g, p = ds.sips, ds.grid, ds.params
@@ -315,7 +343,7 @@ def run_ours(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic", "config": workload_config(args, n), "roofline": roofline,
                 "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-                "gpu_launches": int(launches),
+                "gpu_launches": int(launches), "modes": modes,
                 "hbm_frac_whole_step": value * BYTES_PER_SIP_UPDATE / 1e9 / peak}
         print(json.dumps(line), flush=True)
     if dist:

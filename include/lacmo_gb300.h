@@ -81,7 +81,17 @@ typedef struct {
   double E_col_const;
   int64_t no_kernel_bins;
   double R_kernel_low_log, bin_factor_R_log;
+  int32_t precision;     /* LACMO_PRECISION_FP64 or LACMO_PRECISION_MIXED     */
 } lacmo_params_t;
+
+/* Arithmetic of lacmo_integrate_adv_step.  FP64: the reference's FP64 path
+ * (per-cell sums in SIP-ID order).  MIXED: the Newton condensation and the
+ * drag update in FP32, with the Newton repeated in FP64 for SIPs near the
+ * critical radius of activation; state, positions, per-cell condensed-mass
+ * sums (into Theta / r_v), multiplicities and the collision step stay FP64;
+ * per-cell sums are formed with atomics (any order). */
+#define LACMO_PRECISION_FP64 0
+#define LACMO_PRECISION_MIXED 1
 
 /* Uniform draws for the all-or-nothing collisions.  With draws != NULL the
  * steps consume the buffer in the reference's order (cells x-outer, z-inner;
@@ -107,6 +117,10 @@ size_t lacmo_workspace_bytes(int64_t n, int64_t nx, int64_t nz);
 /* Zero the workspace: draw cursor, collision-step counter, flags. */
 int lacmo_workspace_reset(void* ws, size_t ws_bytes, int64_t n, int64_t nx, int64_t nz,
                           void* stream);
+/* Number of SIP sub-steps whose Newton ran in FP64 in mixed precision
+ * (near-critical SIPs) since the workspace was reset (synchronises). */
+int lacmo_read_fallbacks(const void* ws, int64_t n, int64_t nx, int64_t nz, uint64_t* count,
+                         void* stream);
 /* Copy the device-side flags to *flags (synchronises the stream). */
 int lacmo_read_flags(const void* ws, int64_t n, int64_t nx, int64_t nz, uint32_t* flags,
                      void* stream);
@@ -135,6 +149,19 @@ int lacmo_prepare(const lacmo_sips_t* sips, const lacmo_grid_t* grid, const lacm
 int lacmo_integrate_adv_step(const lacmo_sips_t* sips, const lacmo_grid_t* grid,
                              const lacmo_params_t* prm, const lacmo_draws_t* draws, void* ws,
                              size_t ws_bytes, void* stream);
+/* A CUDA graph of n_steps consecutive lacmo_integrate_adv_step calls with
+ * fixed arguments, captured on `stream` (not the legacy default stream);
+ * lacmo_plan_launch replays it.  All step-to-step state (SIPs, grid, draw
+ * cursor, Philox step counter) lives in device memory, so replays continue
+ * the time integration.  Not for host-side draw generation. */
+typedef struct lacmo_plan lacmo_plan;
+int lacmo_plan_create(const lacmo_sips_t* sips, const lacmo_grid_t* grid, const lacmo_params_t* prm,
+                      const lacmo_draws_t* draws, void* ws, size_t ws_bytes, int n_steps,
+                      void* stream, lacmo_plan** plan);
+int lacmo_plan_launch(lacmo_plan* plan, void* stream);
+int lacmo_plan_destroy(lacmo_plan* plan);
+/* Kernel launches one replay of the plan performs (-1 on error). */
+int64_t lacmo_plan_kernel_nodes(const lacmo_plan* plan);
 /* Phases of lacmo_integrate_adv_step, for callers that run the collision
  * steps themselves (e.g. to draw each step's uniforms from a host generator
  * exactly as the reference does):

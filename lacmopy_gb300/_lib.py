@@ -44,7 +44,12 @@ class Params(ctypes.Structure):
                 ("act_collisions", i32), ("act_relaxation", i32), ("no_iter_impl_mass", i32),
                 ("solute", i32), ("init_profile_r_v", vp), ("init_profile_Theta", vp),
                 ("relaxation_time_profile", vp), ("E_col_grid", vp), ("E_col_const", dbl),
-                ("no_kernel_bins", i64), ("R_kernel_low_log", dbl), ("bin_factor_R_log", dbl)]
+                ("no_kernel_bins", i64), ("R_kernel_low_log", dbl), ("bin_factor_R_log", dbl),
+                ("precision", i32)]
+
+
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
 
 
 class Draws(ctypes.Structure):
@@ -62,12 +67,18 @@ PROTOTYPES = {
     "lacmo_workspace_bytes": (sz, [i64, i64, i64]),
     "lacmo_workspace_reset": (ctypes.c_int, [vp, sz, i64, i64, i64, vp]),
     "lacmo_read_flags": (ctypes.c_int, [vp, i64, i64, i64, P(ctypes.c_uint32), vp]),
+    "lacmo_read_fallbacks": (ctypes.c_int, [vp, i64, i64, i64, P(ctypes.c_uint64), vp]),
     "lacmo_cells_import": (ctypes.c_int, [vp, vp, vp, i64, i64, i64, vp]),
     "lacmo_cells_export": (ctypes.c_int, [vp, vp, vp, vp, vp, i64, i64, i64, dbl, dbl, dbl, dbl,
                                           vp]),
     "lacmo_prepare": (ctypes.c_int, [P(Sips), P(Grid), P(Params), vp, sz, vp]),
     "lacmo_integrate_adv_step": (ctypes.c_int, [P(Sips), P(Grid), P(Params), P(Draws), vp, sz,
                                                 vp]),
+    "lacmo_plan_create": (ctypes.c_int, [P(Sips), P(Grid), P(Params), P(Draws), vp, sz,
+                                         ctypes.c_int, vp, P(vp)]),
+    "lacmo_plan_launch": (ctypes.c_int, [vp, vp]),
+    "lacmo_plan_destroy": (ctypes.c_int, [vp]),
+    "lacmo_plan_kernel_nodes": (i64, [vp]),
     "lacmo_adv_step_begin": (ctypes.c_int, [P(Sips), P(Grid), P(Params), vp, sz, vp]),
     "lacmo_adv_step_second_half": (ctypes.c_int, [P(Sips), P(Grid), P(Params), vp, sz, vp]),
     "lacmo_adv_substep": (ctypes.c_int, [P(Sips), P(Grid), P(Params), dbl, ctypes.c_int, vp, sz,

@@ -30,7 +30,7 @@ static WsPlan ws_plan(int64_t n, int64_t nx, int64_t nz) {
       8 * N,           // dmxi
       4 * N,           // rm_id
       8 * N,           // rm_val
-      8 * 6 * C,       // aux
+      8 * 6 * C + 4 * 10 * C,  // aux: 6 doubles + 10 floats per cell
       8 * C,           // dTh
       8 * C,           // drv
       8 * C,           // div
@@ -39,6 +39,7 @@ static WsPlan ws_plan(int64_t n, int64_t nx, int64_t nz) {
       8 * N,           // colrho
       4 * N,           // colk
       64,              // scalars
+      4 * 2 * (size_t)((nx + 1) * (nz + 1)),  // gvf
   };
   WsPlan p;
   size_t o = 0;
@@ -78,6 +79,8 @@ bool ws_carve(void* base, size_t bytes, int64_t n, int64_t nx, int64_t nz, Ws* w
   w->cursor = (int64_t*)(sc + 8);
   w->col_step = (int64_t*)(sc + 16);
   w->total_pairs = (int64_t*)(sc + 24);
+  w->nfb = (unsigned long long*)(sc + 32);
+  w->gvf = (float*)(b + p.off[17]);
   return true;
 }
 
@@ -92,6 +95,7 @@ static bool grid_ok(const lacmo_grid_t* g) {
 }
 static bool prm_ok(const lacmo_params_t* p) {
   return p && p->no_iter_impl_mass >= 1 && (p->solute == 0 || p->solute == 1) &&
+         (p->precision == LACMO_PRECISION_FP64 || p->precision == LACMO_PRECISION_MIXED) &&
          p->scale_dt_cond >= 1 && p->no_col_per_adv >= 1 &&
          (p->E_col_grid == nullptr || p->no_kernel_bins > 0);
 }
@@ -117,8 +121,50 @@ static int subloop(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_pa
   return LACMO_OK;
 }
 
+// Mixed precision sub-loop: the particle sub-steps skip the cell binning
+// unless a collision step follows before the next position update.
+static int subloop_mixed(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
+                         const lacmo_draws_t& d, const Ws& w, int no_cond, int no_col,
+                         bool bin_at_end, cudaStream_t s) {
+  const int64_t C = g.nx * g.nz;
+  const bool col = p.act_collisions != 0;
+  if (col && no_col == 1) LCHK(launch_collide_cells(sp, g, p, d, w, s));
+  for (int k = 0; k < no_cond; ++k) {
+    if (col && no_col > 1) LCHK(launch_collide_cells(sp, g, p, d, w, s));
+    const bool bin = (col && no_col > 1) || (k == no_cond - 1 && bin_at_end);
+    LCHK(launch_particles_mixed(sp, g, p, p.dt_sub, p.dt_sub, false, bin, w, s));
+    LCHK(launch_grid_acc(g, w, s));
+    if (bin) LCHK(launch_bin(sp, C, w, s));
+  }
+  if (col && no_col > no_cond) LCHK(launch_collide_cells(sp, g, p, d, w, s));
+  return LACMO_OK;
+}
+
+static int adv_step_mixed(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
+                          const lacmo_draws_t& d, const Ws& w, cudaStream_t s) {
+  const int64_t C = g.nx * g.nz;
+  LCHK(launch_wind_float(g, w, s));
+  LCHK(launch_move(sp, g, p.dt_sub_half, w, s));
+  LCHK(launch_bin(sp, C, w, s));
+  LCHK(launch_advection(g, p, w, 1.0, false, s));
+  const int nc1 = p.no_col_per_adv == 1 ? 0 : (p.no_col_per_adv == 2 ? 1 : p.scale_dt_cond);
+  const int nc2 = (p.no_col_per_adv == 1 || p.no_col_per_adv == 2) ? 1 : p.scale_dt_cond;
+  int rc = subloop_mixed(sp, g, p, d, w, p.scale_dt_cond, nc1, p.act_collisions && nc2 >= 1, s);
+  if (rc) return rc;
+  LCHK(launch_advection(g, p, w, 2.0, true, s));
+  rc = subloop_mixed(sp, g, p, d, w, p.scale_dt_cond - 1, nc2, false, s);
+  if (rc) return rc;
+  // last sub-step; the binning afterwards keeps it valid for the entry points
+  // that use it between advection steps
+  LCHK(launch_particles_mixed(sp, g, p, p.dt_sub, p.dt_sub_half, true, true, w, s));
+  LCHK(launch_grid_acc(g, w, s));
+  LCHK(launch_bin(sp, C, w, s));
+  return LACMO_OK;
+}
+
 static int adv_step(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
                     const lacmo_draws_t& d, const Ws& w, cudaStream_t s) {
+  if (p.precision == LACMO_PRECISION_MIXED) return adv_step_mixed(sp, g, p, d, w, s);
   const int64_t C = g.nx * g.nz;
   // b) x_{n+1/2} (integration.py:1474-1481)
   LCHK(launch_move(sp, g, p.dt_sub_half, w, s));
@@ -188,6 +234,15 @@ int lacmo_workspace_reset(void* ws, size_t bytes, int64_t n, int64_t nx, int64_t
   Ws w;
   if (!ws_carve(ws, bytes, n, nx, nz, &w)) return LACMO_ERR_WORKSPACE;
   LCHK(cudaMemsetAsync(ws, 0, ws_bytes(n, nx, nz), (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_read_fallbacks(const void* ws, int64_t n, int64_t nx, int64_t nz, uint64_t* count,
+                         void* stream) {
+  Ws w;
+  if (!count || !ws_carve((void*)ws, ws_bytes(n, nx, nz), n, nx, nz, &w)) return LACMO_ERR_ARG;
+  LCHK(cudaMemcpyAsync(count, w.nfb, 8, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  LCHK(cudaStreamSynchronize((cudaStream_t)stream));
   return LACMO_OK;
 }
 
@@ -269,6 +324,74 @@ int lacmo_adv_substep(const lacmo_sips_t* sp, const lacmo_grid_t* g, const lacmo
   LCHK(launch_particles(*sp, *g, *p, p->dt_sub, dt_sub_pos, write_T_p != 0, w, s));
   LCHK(launch_cell_update(*sp, *g, w, w.dTh, w.drv, true, s));
   LCHK(launch_bin(*sp, g->nx * g->nz, w, s));
+  return LACMO_OK;
+}
+
+struct lacmo_plan {
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+};
+
+int lacmo_plan_create(const lacmo_sips_t* sp, const lacmo_grid_t* g, const lacmo_params_t* p,
+                      const lacmo_draws_t* d, void* ws, size_t bytes, int n_steps, void* stream,
+                      lacmo_plan** out) {
+  if (!out || n_steps < 1) return LACMO_ERR_ARG;
+  *out = nullptr;
+  if (!sips_ok(sp) || !grid_ok(g) || !prm_ok(p) || !d) return LACMO_ERR_ARG;
+  if (d->draws && d->n_draws < 0) return LACMO_ERR_ARG;
+  Ws w;
+  if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (s == nullptr) return LACMO_ERR_ARG;  // the legacy default stream cannot be captured
+  LCHK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int rc = LACMO_OK;
+  for (int k = 0; k < n_steps && rc == LACMO_OK; ++k) rc = adv_step(*sp, *g, *p, *d, w, s);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &graph);
+  if (rc != LACMO_OK || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc != LACMO_OK ? rc : LACMO_ERR_CUDA;
+  }
+  cudaGraphExec_t exec = nullptr;
+  if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return LACMO_ERR_CUDA;
+  }
+  lacmo_plan* pl = new lacmo_plan{graph, exec};
+  *out = pl;
+  return LACMO_OK;
+}
+
+int lacmo_plan_launch(lacmo_plan* pl, void* stream) {
+  if (!pl) return LACMO_ERR_ARG;
+  LCHK(cudaGraphLaunch(pl->exec, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int64_t lacmo_plan_kernel_nodes(const lacmo_plan* pl) {
+  if (!pl || !pl->graph) return -1;
+  size_t n = 0;
+  if (cudaGraphGetNodes(pl->graph, nullptr, &n) != cudaSuccess) return -1;
+  if (n == 0) return 0;
+  cudaGraphNode_t* nodes = new cudaGraphNode_t[n];
+  int64_t k = 0;
+  if (cudaGraphGetNodes(pl->graph, nodes, &n) == cudaSuccess) {
+    for (size_t i = 0; i < n; ++i) {
+      cudaGraphNodeType t;
+      if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+    }
+  } else {
+    k = -1;
+  }
+  delete[] nodes;
+  return k;
+}
+
+int lacmo_plan_destroy(lacmo_plan* pl) {
+  if (!pl) return LACMO_OK;
+  if (pl->exec) cudaGraphExecDestroy(pl->exec);
+  if (pl->graph) cudaGraphDestroy(pl->graph);
+  delete pl;
   return LACMO_OK;
 }
 

@@ -23,13 +23,46 @@
 
 namespace lacmo {
 
+// x^(1/3 rounded to double) correctly rounded, fast path.  With c = double(1/3)
+// = 1/3 - d, d = 2^-54/3, the value is cbrt(x) * exp(-d ln x).  y = cbrt(x)
+// (faithful) is refined by one Newton step whose residual x - y^3 is formed in
+// double-double, and exp(-d ln x) = 1 - d L + (d L)^2/2 to far below 2^-100.
+// So z = y + t with t computed to ~2^-100 |y|.  The rounded sum y + t is the
+// correctly-rounded result unless y + t lies within 2^-85 |y| of a rounding
+// midpoint; then (or for non-normal x) the full routine decides.  The margin
+// is wider than the full routine's own uncertainty, so both always agree.
+__device__ __forceinline__ double cr_pow13(double x) {
+  if (!(x >= 0x1p-1000 && x <= 0x1p1000)) return lacmo_cr_pow(x, LC_ONE_THIRD);
+  const double y = cbrt(x);
+  const lacmo_dd y2 = lacmo_two_prod(y, y);
+  const lacmo_dd y3 = lacmo_dd_mul_d(y2, y);
+  const double r = (x - y3.hi) - y3.lo;           // x - y3.hi is exact (Sterbenz)
+  const double corr = r / (3.0 * y2.hi);
+  const double dL = 0x1.5555555555555p-56 * log(x);  // d * ln x, d = 2^-54 / 3
+  const double t = corr - y * dL + y * (0.5 * dL * dL);
+  const double s = y + t;
+  const double e = (y - s) + t;                   // y + t = s + e exactly
+  const uint64_t b = lacmo_as_u64(s);
+  const int64_t ex = (int64_t)((b >> 52) & 0x7ff);
+  double half_ulp = lacmo_as_f64((uint64_t)(ex - 53) << 52);
+  if (e < 0.0 && (b & 0x000fffffffffffffULL) == 0) half_ulp *= 0.5;
+  if (fabs(fabs(e) - half_ulp) <= 0x1p-85 * s) return lacmo_cr_pow(x, LC_ONE_THIRD);
+  return s;
+}
+
 __device__ __forceinline__ double col_radius(double m, double rho) {
-  return lacmo_cr_pow(LC_FOUR_PI_OVER_THREE_INV * m / rho, LC_ONE_THIRD);
+  return cr_pow13(LC_FOUR_PI_OVER_THREE_INV * m / rho);
 }
 // collision/all_or_nothing.py:35-67; float -> int as x86-64 compiled code
-// does it (NaN / out of range -> INT64_MIN -> bin 0)
+// does it (NaN / out of range -> INT64_MIN -> bin 0).  The bin of the
+// correctly-rounded log: with the hardware log the index value is within
+// 1e-12 of it, so unless it lies within 1e-9 of an integer the truncation is
+// the same; near a bin edge the correctly-rounded log decides.
 __device__ __forceinline__ int32_t col_bin(double R, double lo, double bl, int64_t nb) {
-  const double v = (lacmo_cr_log(R) - lo) / bl + 0.5;
+  double v = (log(R) - lo) / bl + 0.5;
+  const double fl = floor(v);
+  if (!(v - fl > 1e-9 && (fl + 1.0) - v > 1e-9 && fabs(v) < 1e15))
+    v = (lacmo_cr_log(R) - lo) / bl + 0.5;
   int64_t ind = (v > -9.2233720368547758e18 && v < 9.2233720368547758e18) ? (int64_t)v : INT64_MIN;
   if (ind < 0) ind = 0;
   else if (ind > nb - 1) ind = nb - 1;

@@ -56,13 +56,20 @@ __global__ void k_cells_export(const int32_t* __restrict__ cell, const double* _
   }
 }
 
-// per-cell terms of the mass rate for the next sub-step
+// per-cell terms of the mass rate for the next sub-step; the FP32 table that
+// follows them in the workspace (10 floats per cell) feeds the mixed-precision
+// kernel without double->float conversions there
 __device__ __forceinline__ void write_aux(const double* gsf, const double* gmp, double* aux,
                                           int64_t c, int64_t C) {
   CellAmb a = make_cell_amb(gsf[c], gsf[C + c], gsf[6 * C + c], gsf[7 * C + c], gmp[2 * C + c],
                             gmp[c], gmp[C + c]);
   aux[c] = a.sigw; aux[C + c] = a.rhow; aux[2 * C + c] = a.lap0; aux[3 * C + c] = a.lbp0;
   aux[4 * C + c] = a.c1; aux[5 * C + c] = a.c2;
+  float* af = (float*)(aux + 6 * C);
+  af[c] = (float)a.T; af[C + c] = (float)(a.S - 1.0); af[2 * C + c] = (float)a.sigw;
+  af[3 * C + c] = (float)a.rhow; af[4 * C + c] = (float)a.lap0; af[5 * C + c] = (float)a.lbp0;
+  af[6 * C + c] = (float)a.c1; af[7 * C + c] = (float)a.c2; af[8 * C + c] = (float)gmp[5 * C + c];
+  af[9 * C + c] = (float)gmp[6 * C + c];
 }
 
 __global__ void k_cell_aux(const double* gsf, const double* gmp, double* aux, int64_t C) {
@@ -233,7 +240,51 @@ struct PArgs {
   int32_t *counts, *rank, *rm_count, *rm_id;
   double* rm_val;
   uint32_t* flags;
+  // mixed precision
+  double* acc;                  // [C] per-cell FP64 sums of dm * xi
+  int hist;                     // count SIPs per new cell for a following binning
+  unsigned long long* nfb;      // SIPs whose Newton fell back to FP64
+  const float* auxf;            // [AUXF][C] FP32 per-cell terms (see write_aux)
+  const float* gvf;             // [2][nx+1][nz+1] FP32 wind field
+  double inv_dx, inv_dz;
+  float inv_dxf, inv_dzf, dt_subf, dtg_f;
 };
+
+// FP32 per-cell table of the mixed-precision path
+enum { AF_T, AF_SM1, AF_SIGW, AF_RHOW, AF_LAP0, AF_LBP0, AF_C1, AF_C2, AF_MU, AF_RHOF, AUXF };
+
+struct GridVelF {
+  const float* gv;
+  int64_t nx, nz;
+  __device__ __forceinline__ float at(int c, int64_t i, int64_t j) const {
+    if (i < 0) i += nx + 1;
+    if (j < 0) j += nz + 1;
+    return __ldg(gv + ((int64_t)c * (nx + 1) + i) * (nz + 1) + j);
+  }
+  __device__ __forceinline__ float bilin(int c, int64_t i, int64_t j, float a, float b) const {
+    return a * (b * at(c, i + 1, j + 1) + (1 - b) * at(c, i + 1, j)) +
+           (1 - a) * (b * at(c, i, j + 1) + (1 - b) * at(c, i, j));
+  }
+  // grid.py:257-323 in FP32
+  __device__ __forceinline__ void interp(int64_t i, int64_t j, float wx, float wy, float& u,
+                                         float& v) const {
+    if ((j == 0 && wy <= 0.5f) || (j == nz - 1 && wy >= 0.5f)) {
+      u = wx * at(0, i + 1, j) + (1 - wx) * at(0, i, j);
+    } else if (wy > 0.5f) {
+      u = bilin(0, i, j, wx, wy - 0.5f);
+    } else {
+      u = bilin(0, i, j - 1, wx, wy + 0.5f);
+    }
+    if (wx > 0.5f) v = bilin(1, i, j, wx - 0.5f, wy);
+    else v = bilin(1, i - 1, j, wx + 0.5f, wy);
+  }
+};
+
+__global__ void k_to_float(const double* in, float* out, int64_t n) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = (float)in[k];
+}
 
 template <bool PHYS>
 __global__ void __launch_bounds__(128) k_particles(PArgs a) {
@@ -393,6 +444,168 @@ __global__ void __launch_bounds__(128) k_cell_update(const int32_t* __restrict__
       grid_cell_update(gsf, gmp, c, C, p_ref, p_ref_inv, dTh[c], drv[c], dml, V);
       write_aux(gsf, gmp, aux, c, C);
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision particle sub-step: the same steps as k_particles with the
+// Newton condensation and the drag update in FP32 (lacmo_physics.cuh), an FP64
+// repeat of the Newton for SIPs near the critical radius, and FP64 state,
+// positions, per-cell condensed-mass sums (warp-aggregated atomics) and
+// water_removed.  The per-cell sums are not formed in ID order, so the grid
+// feedback is reproducible to FP64 rounding, not bit for bit.
+__global__ void __launch_bounds__(128) k_particles_mixed(PArgs a) {
+  const int64_t C = a.nx * a.nz;
+  const GridVelF gvf{a.gvf, a.nx, a.nz};
+  const int lane = threadIdx.x & 31;
+  const int64_t n_round = (a.n + 31) / 32 * 32;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_round;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const bool valid = k < a.n;
+    const int32_t c = valid ? a.cell[k] : -1;
+    const bool active = c >= 0;
+    double dmxi = 0.0;
+    if (valid) {
+      const int64_t i = active ? (int64_t)c / a.nz : (int64_t)(-1 - c);
+      const int64_t j = active ? (int64_t)c - i * a.nz : -1;
+      double x = a.pos[k], z = a.pos[a.n + k];
+      double u = a.vel[k], w = a.vel[a.n + k];
+      double mw = a.m_w[k];
+      double xik = 0.0, rel_x = 0.0, rel_z = 0.0;
+      const double T_p = __ldg(a.gsf + i * a.nz + (active ? j : a.nz - 1));
+      if (a.write_Tp) a.T_p[k] = T_p;
+      const double x0 = x, z0 = z;
+      if (active) {
+        const double ms = a.m_s[k];
+        xik = a.xi[k];
+        CellAmbF af;
+        af.T = __ldg(a.auxf + AF_T * C + c); af.S_m1 = __ldg(a.auxf + AF_SM1 * C + c);
+        af.sigw = __ldg(a.auxf + AF_SIGW * C + c); af.rhow = __ldg(a.auxf + AF_RHOW * C + c);
+        af.lap0 = __ldg(a.auxf + AF_LAP0 * C + c); af.lbp0 = __ldg(a.auxf + AF_LBP0 * C + c);
+        af.c1 = __ldg(a.auxf + AF_C1 * C + c); af.c2 = __ldg(a.auxf + AF_C2 * C + c);
+        const float msf = (float)ms;
+        const float mwf = (float)mw;
+        const float mpf = mwf + msf;
+        const float wsf = msf / mpf;
+        float rho = (a.sol == SOL_AS)
+                        ? af.rhow * ((((float)LC_PAR_RHO_AS_0 * wsf + (float)LC_PAR_RHO_AS_1) * wsf +
+                                      (float)LC_PAR_RHO_AS_2) * wsf + (float)LC_PAR_RHO_AS_3)
+                        : (float)LC_PAR_SOL_DENS_NACL_0 + (float)LC_PAR_SOL_DENS_NACL_1 * wsf +
+                              (float)LC_PAR_SOL_DENS_NACL_2 * af.T +
+                              (float)LC_PAR_SOL_DENS_NACL_3 * wsf * wsf +
+                              (float)LC_PAR_SOL_DENS_NACL_4 * wsf * af.T +
+                              (float)LC_PAR_SOL_DENS_NACL_5 * af.T * af.T;
+        float R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * mpf / rho);
+        const float sig = af.sigw * (1.0f + (float)(a.sol == SOL_AS ? LC_PAR_SIGMA_AS
+                                                                      : LC_PAR_SIGMA_NACL) *
+                                                 wsf / (1.f - wsf));
+        const double m_w_effl = ms * (LC_W_S_MAX_AS_INV - 1.0);
+        double dm;
+        const bool ok = newton_mixed(a.sol, (float)a.dt_sub, a.no_iter, mw, msf, wsf, R, af.T, rho,
+                                     sig, af, m_w_effl, &dm);
+        if (!ok) {
+          // near the critical radius: FP64 residual and step
+          CellAmb amb;
+          amb.T = T_p; amb.p = __ldg(a.gsf + C + c); amb.S = __ldg(a.gsf + 6 * C + c);
+          amb.e_s = __ldg(a.gsf + 7 * C + c); amb.K = __ldg(a.gmp + c);
+          amb.D_v = __ldg(a.gmp + C + c); amb.L_v = __ldg(a.gmp + 2 * C + c);
+          amb.sigw = __ldg(a.aux + c); amb.rhow = __ldg(a.aux + C + c);
+          amb.lap0 = __ldg(a.aux + 2 * C + c); amb.lbp0 = __ldg(a.aux + 3 * C + c);
+          amb.c1 = __ldg(a.aux + 4 * C + c); amb.c2 = __ldg(a.aux + 5 * C + c);
+          const double m_p = mw + ms;
+          const double w_s = ms / m_p;
+          const double rho64 = (a.sol == SOL_AS) ? density_AS_solution_rw(w_s, amb.rhow)
+                                                 : density_NaCl_solution(w_s, T_p);
+          const double R64 = radius_from_mass(m_p, rho64);
+          const double sig64 = (a.sol == SOL_AS) ? surface_tension_AS_sw(w_s, amb.sigw)
+                                                 : surface_tension_NaCl_sw(w_s, amb.sigw);
+          dm = newton_full(a.sol, a.dt_sub, a.no_iter, mw, ms, w_s, R64, T_p, rho64, sig64, amb,
+                           nullptr);
+          atomicAdd(a.nfb, 1ull);
+        }
+        mw += dm;
+        dmxi = dm * xik;
+        // drag (integration.py:699-718) in FP32 with the ammonium-sulfate radius
+        const float mpn = (float)mw + msf;
+        const float wn = msf / mpn;
+        rho = af.rhow * ((((float)LC_PAR_RHO_AS_0 * wn + (float)LC_PAR_RHO_AS_1) * wn +
+                          (float)LC_PAR_RHO_AS_2) * wn + (float)LC_PAR_RHO_AS_3);
+        R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * mpn / rho);
+        const float rxf = (float)(x - a.x_min) * a.inv_dxf - (float)i;
+        const float rzf = (float)(z - a.z_min) * a.inv_dzf - (float)j;
+        float uf, wf;
+        gvf.interp(i, j, rxf, rzf, uf, wf);
+        const float mu_f = __ldg(a.auxf + AF_MU * C + c), rho_f = __ldg(a.auxf + AF_RHOF * C + c);
+        const float uo = (float)u, wo = (float)w;
+        const float d0 = uf - uo, d1 = wf - wo;
+        const float vel_dev = sqrtf(d0 * d0 + d1 * d1);
+        const float Re_p = 2.0E-6f * rho_f * R * vel_dev / mu_f;
+        float k_dt = 4.5E12f * a.dt_subf * mu_f / (rho * R * R);
+        if (Re_p > 0.5f) {
+          if (Re_p < 1000.0f) k_dt *= (1.f + 0.15f * powf(Re_p, 0.687f));
+          else k_dt *= 0.0183333333333f * Re_p;
+        }
+        const float inv = 1.0f / (1.0f + k_dt);
+        u = (double)((uo + k_dt * uf) * inv);
+        w = (double)((wo + k_dt * wf - a.dtg_f) * inv);
+      }
+      x += a.dt_pos * u;
+      z += a.dt_pos * w;
+      x = py_mod(x, a.x_max);
+      z = np_min(z, a.z_cap);
+      int32_t newc = c;
+      if (active) {
+        if (z <= a.z_min) {
+          z = a.z_min - 0.01 * a.dz;
+          u = 0.0; w = 0.0;
+          atomicAdd(a.rm_val, xik * mw);   // water_removed (FP64, any order)
+          rel_x = (x0 - a.x_min) / a.dx - (double)i;
+          rel_z = (z0 - a.z_min) / a.dz - (double)j;
+          a.rel[k] = rel_x / a.dx - (double)i;
+          a.rel[a.n + k] = rel_z / a.dz - (-1.0);
+          newc = (int32_t)(-1 - i);
+        } else {
+          int64_t ci = (int64_t)floor(x * a.inv_dx), cj = (int64_t)floor(z * a.inv_dz);
+          if (ci >= a.nx || ci < 0 || cj >= a.nz || cj < 0) {
+            atomicOr(a.flags, LACMO_FLAG_CELL_CLAMPED);
+            ci = ci < 0 ? 0 : (ci >= a.nx ? a.nx - 1 : ci);
+            cj = cj < 0 ? 0 : (cj >= a.nz ? a.nz - 1 : cj);
+          }
+          newc = (int32_t)(ci * a.nz + cj);
+          if (a.hist) a.rank[k] = atomicAdd(a.counts + newc, 1);
+        }
+      } else {
+        a.rel[k] = a.rel[k] / a.dx - (double)i;
+        a.rel[a.n + k] = a.rel[a.n + k] / a.dz - (-1.0);
+      }
+      a.pos[k] = x; a.pos[a.n + k] = z;
+      a.vel[k] = u; a.vel[a.n + k] = w;
+      if (active) a.m_w[k] = mw;
+      a.cell[k] = newc;
+    }
+    // per-cell FP64 sum of dm * xi, one atomic per run of equal cells in the warp
+    const unsigned peers = __match_any_sync(0xffffffffu, active ? c : -1 - lane);
+    const int leader = __ffs(peers) - 1;
+    double sum = 0.0;
+    for (unsigned m = peers; m; m &= m - 1) {
+      const int src = __ffs(m) - 1;
+      sum += __shfl_sync(peers, dmxi, src);
+    }
+    if (active && lane == leader) atomicAdd(a.acc + c, sum);
+  }
+}
+
+// mixed precision: the grid sub-step from the per-cell FP64 sums (then zeroed)
+__global__ void k_grid_acc(double* acc, double* delta_m_l, double* gsf, double* gmp, double* aux,
+                           const double* dTh, const double* drv, int64_t C, double p_ref,
+                           double p_ref_inv, double V) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const double dml = acc[c] * 1.0E-18;
+    acc[c] = 0.0;
+    delta_m_l[c] = dml;
+    grid_cell_update(gsf, gmp, c, C, p_ref, p_ref_inv, dTh[c], drv[c], dml, V);
+    write_aux(gsf, gmp, aux, c, C);
   }
 }
 
@@ -613,6 +826,40 @@ cudaError_t launch_move(const lacmo_sips_t& sp, const lacmo_grid_t& g, double dt
   a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
   a.rm_id = w.rm_id; a.rm_val = w.rm_val; a.flags = w.flags;
   k_particles<false><<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a); note_launches(1);
+  return cudaGetLastError();
+}
+cudaError_t launch_particles_mixed(const lacmo_sips_t& sp, const lacmo_grid_t& g,
+                                   const lacmo_params_t& p, double dt_sub, double dt_sub_pos,
+                                   bool write_Tp, bool hist, const Ws& w, cudaStream_t s) {
+  PArgs a;
+  a.pos = sp.pos; a.vel = sp.vel; a.m_w = sp.m_w; a.rel = sp.rel_pos; a.T_p = sp.T_p;
+  a.m_s = sp.m_s; a.xi = sp.xi; a.cell = sp.cell;
+  a.gsf = g.scalar_fields; a.gmp = g.mat_prop; a.aux = w.aux; a.gv = g.velocity;
+  a.n = sp.n; a.nx = g.nx; a.nz = g.nz;
+  a.x_min = g.x_min; a.x_max = g.x_max; a.z_min = g.z_min; a.z_cap = g.z_max * 0.999999;
+  a.dx = g.dx; a.dz = g.dz;
+  a.dt_sub = dt_sub; a.dt_pos = dt_sub_pos; a.g_set = p.g_set;
+  a.no_iter = p.no_iter_impl_mass; a.sol = p.solute; a.write_Tp = write_Tp ? 1 : 0;
+  a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
+  a.rm_id = w.rm_id; a.rm_val = sp.water_removed; a.flags = w.flags;
+  a.acc = w.div; a.hist = hist ? 1 : 0; a.nfb = w.nfb;
+  a.auxf = (const float*)(w.aux + 6 * g.nx * g.nz); a.gvf = w.gvf;
+  a.inv_dx = 1.0 / g.dx; a.inv_dz = 1.0 / g.dz;
+  a.inv_dxf = (float)(1.0 / g.dx); a.inv_dzf = (float)(1.0 / g.dz);
+  a.dt_subf = (float)dt_sub; a.dtg_f = (float)(dt_sub * p.g_set);
+  k_particles_mixed<<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a); note_launches(1);
+  return cudaGetLastError();
+}
+cudaError_t launch_wind_float(const lacmo_grid_t& g, const Ws& w, cudaStream_t s) {
+  const int64_t m = 2 * (g.nx + 1) * (g.nz + 1);
+  k_to_float<<<nblocks(m, 256), 256, 0, s>>>(g.velocity, w.gvf, m); note_launches(1);
+  return cudaGetLastError();
+}
+cudaError_t launch_grid_acc(const lacmo_grid_t& g, const Ws& w, cudaStream_t s) {
+  int64_t C = g.nx * g.nz;
+  k_grid_acc<<<nblocks(C, 128), 128, 0, s>>>(w.div, g.delta_m_l, g.scalar_fields, g.mat_prop,
+                                             w.aux, w.dTh, w.drv, C, g.p_ref, g.p_ref_inv,
+                                             g.volume_cell); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_cell_update(const lacmo_sips_t& sp, const lacmo_grid_t& g, const Ws& w,

@@ -32,6 +32,8 @@ struct Ws {
   int64_t* cursor;     // injected-draw cursor
   int64_t* col_step;   // collision-step counter (Philox)
   int64_t* total_pairs;
+  unsigned long long* nfb;   // mixed precision: Newton repeats in FP64
+  float* gvf;                // [2][nx+1][nz+1] FP32 copy of the wind (mixed precision)
 };
 
 size_t ws_bytes(int64_t n, int64_t nx, int64_t nz);
@@ -68,6 +70,11 @@ cudaError_t launch_bin(const lacmo_sips_t& sp, int64_t C, const Ws& w, cudaStrea
 cudaError_t launch_particles(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
                              double dt_sub, double dt_sub_pos, bool write_Tp, const Ws& w,
                              cudaStream_t s);
+cudaError_t launch_particles_mixed(const lacmo_sips_t& sp, const lacmo_grid_t& g,
+                                   const lacmo_params_t& p, double dt_sub, double dt_sub_pos,
+                                   bool write_Tp, bool hist, const Ws& w, cudaStream_t s);
+cudaError_t launch_grid_acc(const lacmo_grid_t& g, const Ws& w, cudaStream_t s);
+cudaError_t launch_wind_float(const lacmo_grid_t& g, const Ws& w, cudaStream_t s);
 cudaError_t launch_cell_update(const lacmo_sips_t& sp, const lacmo_grid_t& g, const Ws& w,
                                const double* dTh, const double* drv, bool grid_update,
                                cudaStream_t s);

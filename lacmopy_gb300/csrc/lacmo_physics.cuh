@@ -33,6 +33,13 @@ LACMO_DEV double np_min(double a, double b) { return (a <= b || isnan(a)) ? a : 
 LACMO_DEV double np_sign(double x) { return isnan(x) ? x : (x > 0 ? 1.0 : (x < 0 ? -1.0 : 0.0)); }
 // Python float modulo (sign of the divisor)
 LACMO_DEV double py_mod(double a, double b) {
+  // one wrap at most, the common case: the same value fmod gives (b > 0;
+  // a - b and a + b are exact or the same single rounding as fmod + b)
+  if (b > 0.0) {
+    if (a > 0.0 && a < b) return a;
+    if (a >= b && a < 2.0 * b) return a - b;
+    if (a < 0.0 && a > -b) return a + b;
+  }
   double m = fmod(a, b);
   if (m != 0.0) { if ((b < 0) != (m < 0)) m += b; }
   else m = copysign(0.0, b);
@@ -166,6 +173,106 @@ LACMO_DEV double newton_full(int sol, double dt_sub, int no_iter, double m_w, do
   }
   if (gamma0_out) *gamma0_out = gamma0;
   return mass_new - m_w;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision: the same Fukuta-Walter mass rate, derivative and implicit
+// Newton in FP32.  The residual f2 = S_amb - S_eq is formed from the two
+// deviations from saturation, S_amb - 1 (exact in FP64, rounded once) and
+// S_eq - 1 = (a_w - 1) + a_w (exp(eps_k) - 1) with a_w - 1 from the water-
+// activity polynomial without its constant term and expm1, so it carries no
+// cancellation; the Newton iterates on the increment dm = m_new - m_w, and the
+// new mass m_w + dm is formed in FP64 by the caller.
+struct CellAmbF {
+  float T, S_m1, sigw, rhow, lap0, lbp0, c1, c2;
+};
+
+LACMO_DEV void mass_rate_and_derivative_f(int sol, float m_w, float m_s, float w_s, float R_p,
+                                          float rho_p, float sigma_p, float T_p, float rhow_p,
+                                          const CellAmbF& a, float& g, float& dg, float& f2o) {
+  const float l_alpha_plus_R_p = 1.0E-6f * (R_p + a.lap0);
+  const float l_beta_plus_R_p = 1.0E-6f * (R_p + a.lbp0);
+  const float m_p_inv_SI = 1.0E18f / (m_w + m_s);
+  const float wfac = w_s / ((1.f - w_s) * (1.f - w_s));
+  float drho_dm_over_rho, aw_m1, da_w_dm, dsigma_dm;
+  if (sol == SOL_AS) {
+    const float pd = ((float)LC_PAR_RHO_DERIV_AS_0 * w_s + (float)LC_PAR_RHO_DERIV_AS_1) * w_s +
+                     (float)LC_PAR_RHO_DERIV_AS_2;
+    drho_dm_over_rho = -rhow_p * m_p_inv_SI / rho_p * w_s * pd;
+    aw_m1 = w_s * ((((float)LC_PAR_WAT_ACT_AS_0 * w_s + (float)LC_PAR_WAT_ACT_AS_1) * w_s +
+                    (float)LC_PAR_WAT_ACT_AS_2) * w_s + (float)LC_PAR_WAT_ACT_AS_3);
+    const float da = (((float)LC_PAR_WAT_ACT_DERIV_AS_0 * w_s + (float)LC_PAR_WAT_ACT_DERIV_AS_1) *
+                          w_s + (float)LC_PAR_WAT_ACT_DERIV_AS_2) * w_s +
+                     (float)LC_PAR_WAT_ACT_DERIV_AS_3;
+    da_w_dm = -m_p_inv_SI * w_s * da;
+    dsigma_dm = -(float)LC_PAR_SIGMA_AS * a.sigw * m_p_inv_SI * wfac;
+  } else {
+    drho_dm_over_rho = -w_s * m_p_inv_SI / rho_p *
+                       ((float)LC_PAR_SOL_DENS_NACL_1 + 2.0f * (float)LC_PAR_SOL_DENS_NACL_3 * w_s +
+                        (float)LC_PAR_SOL_DENS_NACL_4 * T_p);
+    aw_m1 = w_s * ((((float)LC_PAR_WAT_ACT_NACL_0 * w_s + (float)LC_PAR_WAT_ACT_NACL_1) * w_s +
+                    (float)LC_PAR_WAT_ACT_NACL_2) * w_s + (float)LC_PAR_WAT_ACT_NACL_3);
+    const float da = (((float)LC_PAR_WAT_ACT_DERIV_NACL_0 * w_s +
+                       (float)LC_PAR_WAT_ACT_DERIV_NACL_1) * w_s +
+                      (float)LC_PAR_WAT_ACT_DERIV_NACL_2) * w_s +
+                     (float)LC_PAR_WAT_ACT_DERIV_NACL_3;
+    da_w_dm = -m_p_inv_SI * w_s * da;
+    dsigma_dm = -(float)LC_PAR_SIGMA_NACL * a.sigw * m_p_inv_SI * wfac;
+  }
+  const float dR_p_dm_over_R_p = (1.0f / 3.0f) * (m_p_inv_SI - drho_dm_over_rho);
+  const float dR_p_dm = 1.0E-6f * dR_p_dm_over_R_p * R_p;
+  const float eps_k = 2.0E6f * sigma_p / ((float)LC_R_V * T_p * rho_p * R_p);
+  const float em1 = expm1f(eps_k);
+  const float kelvin_term = 1.0f + em1;
+  const float Seq_m1 = aw_m1 + (1.0f + aw_m1) * em1;
+  const float S_eq = 1.0f + Seq_m1;
+  const float dSeq_dm =
+      da_w_dm * kelvin_term + S_eq * eps_k * (dsigma_dm / sigma_p - drho_dm_over_rho - dR_p_dm_over_R_p);
+  const float f3 = 1.0f / (l_alpha_plus_R_p * S_eq * a.c1 + l_beta_plus_R_p * a.c2);
+  const float f1f3 = (float)LC_FOUR_PI * R_p * R_p * f3;
+  const float dg1_dm = (dSeq_dm * l_alpha_plus_R_p + S_eq * dR_p_dm) * a.c1 + dR_p_dm * a.c2;
+  const float f2 = a.S_m1 - Seq_m1;
+  g = 1.0E6f * f1f3 * f2;
+  dg = 1.0E-12f * f1f3 * (f2 * (2.0f * dR_p_dm_over_R_p - f3 * dg1_dm) - dSeq_dm);
+  f2o = f2;
+}
+
+// FP32 implicit Newton on the increment (integration.py:728-836 restated on
+// dm).  Returns false when the SIP is near the critical radius of activation
+// (residual |S_amb - S_eq| < 1e-6 while the step is not stiff, |dt dgamma/dm|
+// < 0.5): the caller then repeats the SIP's Newton in FP64.
+LACMO_DEV bool newton_mixed(int sol, float dt_sub, int no_iter, double m_w, float m_s, float w_s,
+                            float R_p, float T_p, float rho_p, float sigma_p, const CellAmbF& a,
+                            double m_w_effl, double* dm_out) {
+  float g, dg, f2;
+  mass_rate_and_derivative_f(sol, (float)m_w, m_s, w_s, R_p, rho_p, sigma_p, T_p, a.rhow, a, g, dg,
+                             f2);
+  float x = dt_sub * dg;
+  bool near_crit = (fabsf(f2) < 1.0e-6f) && (fabsf(x) < 0.5f);
+  float denom_inv = (x < 0.9f) ? 1.0f / (1.0f - x) : 10.0f;
+  const float d_effl = (float)(m_w_effl - m_w);
+  const float d0 = dt_sub * g * denom_inv;
+  float d = (d0 != d0) ? d0 : fmaxf(d_effl, d0);  // NaN propagates as in np.maximum
+  const float m_w32 = (float)m_w;
+  for (int it = 0; it < no_iter - 1; ++it) {
+    const float mass = m_w32 + d;
+    const float m_p = mass + m_s;
+    const float w = m_s / m_p;
+    const float pr = (((float)LC_PAR_RHO_AS_0 * w + (float)LC_PAR_RHO_AS_1) * w +
+                      (float)LC_PAR_RHO_AS_2) * w + (float)LC_PAR_RHO_AS_3;
+    const float rho = a.rhow * pr;
+    const float R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * m_p / rho);
+    const float sig = a.sigw * (1.0f + (float)LC_PAR_SIGMA_AS * w / (1.f - w));
+    mass_rate_and_derivative_f(sol, mass, m_s, w, R, rho, sig, T_p, a.rhow, a, g, dg, f2);
+    x = dt_sub * dg;
+    near_crit = near_crit || ((fabsf(f2) < 1.0e-6f) && (fabsf(x) < 0.5f));
+    denom_inv = (x < 0.9f) ? 1.0f / (1.0f - x) : 10.0f;
+    d += (dt_sub * g - d) * denom_inv;
+    const float dm2 = fmaxf(d_effl, d);
+    d = (d != d) ? d : dm2;
+  }
+  *dm_out = (double)d;
+  return !near_crit;
 }
 
 // grid.py:195-323: staggered bilinear interpolation; index -1 wraps onto the

@@ -51,7 +51,7 @@ class DeviceState:
     GRID_KEYS = ("grid_scalar_fields", "grid_mat_prop", "grid_velocity",
                  "grid_mass_flux_air_dry")
 
-    def __init__(self, st, device="cuda", draws="philox", seed=1001):
+    def __init__(self, st, device="cuda", draws="philox", seed=1001, precision="fp64"):
         self.lib = _lib.load()
         self.device = device
         g = st["grid_no_cells"]
@@ -92,6 +92,9 @@ class DeviceState:
                               self.rel_pos.data_ptr(), self.m_w.data_ptr(), self.m_s.data_ptr(),
                               self.xi.data_ptr(), self.T_p.data_ptr(), self.cell.data_ptr(),
                               self.water_removed.data_ptr(), self.no_cols.data_ptr())
+        if precision not in ("fp64", "mixed"):
+            raise ValueError(f"precision must be 'fp64' or 'mixed', got {precision!r}")
+        self.precision = precision
         self.set_params(st)
         self.ws_bytes = int(self.lib.lacmo_workspace_bytes(self.n, self.nx, self.nz))
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
@@ -131,7 +134,8 @@ class DeviceState:
             int(bool(st["act_relaxation"]) and has_relax), int(st["no_iter_impl_mass"]),
             solute_code(st["solute_type"]), self.prof_rv.data_ptr(), self.prof_th.data_ptr(),
             self.t_relax.data_ptr(), self.E.data_ptr() if self.E is not None else None, E_const,
-            nb, lo, bl)
+            nb, lo, bl, _lib.PRECISION_MIXED if getattr(self, "precision", "fp64") == "mixed"
+            else _lib.PRECISION_FP64)
 
     def prepare(self):
         _lib.check(self.lib.lacmo_prepare(ctypes.byref(self.sips), ctypes.byref(self.grid),
@@ -144,11 +148,20 @@ class DeviceState:
             return _lib.Draws(self.draw_buf.data_ptr(), self.draw_buf.numel(), self.seed)
         return _lib.Draws(None, 0, self.seed)
 
-    def adv_step(self, n_steps=1):
-        """``n_steps`` advection steps (integration.py:1298-1611)."""
+    def adv_step(self, n_steps=1, graph=False):
+        """``n_steps`` advection steps (integration.py:1298-1611).
+
+        ``graph=True`` replays a CUDA graph of one step (captured on first
+        use on a side stream); not available with host-side numpy draws."""
         if self.draw_mode == "numpy":
             for _ in range(n_steps):
                 self._adv_step_numpy_draws()
+            return
+        if graph:
+            plan = self._plan()
+            s = _stream()
+            for _ in range(n_steps):
+                _lib.check(self.lib.lacmo_plan_launch(plan, s), "plan_launch")
             return
         d = self._draws_struct()
         s = _stream()
@@ -156,6 +169,38 @@ class DeviceState:
             _lib.check(self.lib.lacmo_integrate_adv_step(
                 ctypes.byref(self.sips), ctypes.byref(self.grid), ctypes.byref(self.params),
                 ctypes.byref(d), _ptr(self.ws), self.ws_bytes, s), "integrate_adv_step")
+
+    def _plan(self):
+        if getattr(self, "_plan_handle", None) is not None:
+            return self._plan_handle
+        cur = torch.cuda.current_stream()
+        side = torch.cuda.Stream()
+        side.wait_stream(cur)
+        d = self._draws_struct()
+        handle = ctypes.c_void_p()
+        with torch.cuda.stream(side):
+            _lib.check(self.lib.lacmo_plan_create(
+                ctypes.byref(self.sips), ctypes.byref(self.grid), ctypes.byref(self.params),
+                ctypes.byref(d), _ptr(self.ws), self.ws_bytes, 1,
+                ctypes.c_void_p(side.cuda_stream), ctypes.byref(handle)), "plan_create")
+        cur.wait_stream(side)
+        self._plan_handle = handle
+        self._plan_draws = d
+        return handle
+
+    def graph_kernel_count(self):
+        """Kernel nodes in the captured one-step graph (0 if none)."""
+        if getattr(self, "_plan_handle", None) is None:
+            return 0
+        return int(self.lib.lacmo_plan_kernel_nodes(self._plan_handle))
+
+    def __del__(self):
+        h = getattr(self, "_plan_handle", None)
+        if h is not None:
+            try:
+                self.lib.lacmo_plan_destroy(h)
+            except Exception:
+                pass
 
     def pair_count(self):
         out = ctypes.c_int64(0)
@@ -223,6 +268,13 @@ class DeviceState:
         _lib.check(self.lib.lacmo_update_grid_r_l(ctypes.byref(self.sips), ctypes.byref(self.grid),
                                                   _ptr(self.ws), self.ws_bytes, _stream()),
                    "update_grid_r_l")
+
+    def fallbacks(self):
+        """Mixed precision: SIP sub-steps whose Newton was repeated in FP64."""
+        f = ctypes.c_uint64(0)
+        _lib.check(self.lib.lacmo_read_fallbacks(_ptr(self.ws), self.n, self.nx, self.nz,
+                                                 ctypes.byref(f), _stream()), "read_fallbacks")
+        return int(f.value)
 
     def flags(self):
         f = ctypes.c_uint32(0)
