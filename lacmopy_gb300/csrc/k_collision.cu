@@ -77,7 +77,7 @@ __device__ __forceinline__ int64_t pair_rank(int64_t i, int64_t j, int64_t n) {
 // 754-846).  SIP state of cells with up to CELL_SMEM SIPs lives in shared
 // memory; larger cells use per-SIP global scratch.
 constexpr int CELL_SMEM = 256;
-constexpr int CELL_WARPS = 4;
+constexpr int CELL_WARPS = 8;
 
 struct CellArgs {
   double *xi, *m_w, *m_s;
@@ -98,84 +98,142 @@ struct CellArgs {
   const int64_t *cursor, *col_step, *total_pairs;
   int64_t* no_cols;
   uint32_t* flags;
-  double *gR, *grho;
-  int32_t* gk;
+  double *gR, *grho;   // per SIP: exact radius and density, or the step-start m_p, m_s
+  int32_t* gk;         // per SIP: exact kernel bin, or -1 while gR/grho hold m_p, m_s
 };
 
-// Exact FP64 evaluation of one pair (collision/all_or_nothing.py:553-633),
-// in the reference's operation order.  Arrays are indexed by ii / jj; r < 0
-// means "draw not fetched yet".  Optional float copies are kept in step.
-struct PairState {
-  double *XI, *MW, *MS, *RR;
-  const double *RHO, *U, *W;
-  int32_t* KK;
-  float *fxi, *fR;  // nullptr when no float copies exist
+// integer-unit conversions (GB300 runs FP64 conversions on its narrow FP64
+// pipe): round to nearest even, and truncation toward zero for r >= 0
+__device__ __forceinline__ float d2f_rn(double x) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
+  if (e < 897u || e > 1150u) return (float)x;
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const uint64_t m = b & 0x000fffffffffffffull;
+  const uint32_t fm = (uint32_t)(m >> 29), rem = (uint32_t)m & 0x1fffffffu;
+  uint32_t fb = sign | ((e - 896u) << 23) | fm;
+  fb += (rem > 0x10000000u) || (rem == 0x10000000u && (fm & 1u));
+  return __int_as_float((int)fb);
+}
+__device__ __forceinline__ float d2f_down_pos(double r) {  // r in [0, 1)
+  const uint64_t b = (uint64_t)__double_as_longlong(r);
+  const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
+  if (e < 897u) return 0.0f;
+  return __int_as_float((int)(((e - 896u) << 23) | (uint32_t)((b >> 29) & 0x7fffffu)));
+}
+
+// exact per-SIP collision data (collision/all_or_nothing.py:812-826): the
+// density at the step-start masses and cell temperature, the correctly-rounded
+// radius and its kernel bin; computed on first need, then kept in gR/grho/gk
+__device__ __forceinline__ void ensure_exact(const CellArgs& a, int32_t id, double Tc, bool use_E) {
+  if (a.gk[id] >= 0) return;
+  const double m_p = a.gR[id], ms = a.grho[id];
+  const double w_s = ms / m_p;
+  const double rho = (a.sol == SOL_AS) ? density_water(Tc) * poly_rho_AS(w_s)
+                                       : density_NaCl_solution(w_s, Tc);
+  const double R = col_radius(m_p, rho);
+  a.gR[id] = R;
+  a.grho[id] = rho;
+  a.gk[id] = use_E ? col_bin(R, a.lo, a.bl, a.nb) : 0;
+}
+
+struct CellSmem {
+  float *fxi, *fR, *fu, *fw;
+  int32_t *sk, *sid;
 };
 
-__device__ __forceinline__ void exact_pair(const PairState& P, int ii, int jj, double r,
-                                           const CellArgs& a, bool use_E, int64_t rk,
-                                           const double* rnd, uint64_t pc1, int64_t& c0,
-                                           int64_t& c1) {
-  double *XI = P.XI, *MW = P.MW, *MS = P.MS, *RR = P.RR;
-  int imin, imax;
-  if (XI[ii] <= XI[jj]) { imin = ii; imax = jj; } else { imin = jj; imax = ii; }
+// One ordinary collection (p_crit <= 1 and p_crit > r) of the pair imin/imax
+// (collision/all_or_nothing.py:607-633) on the global arrays; the exact
+// radius of imin (and of imax for equal multiplicities) must be available.
+// S (may be null) receives the FP32 copies at local slots lmin/lmax.
+__device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* S, int32_t imin,
+                                             int32_t imax, int lmin, int lmax, double Tc,
+                                             bool use_E) {
+  double *XI = a.xi, *MW = a.m_w, *MS = a.m_s, *RR = a.gR;
+  const double* RHO = a.grho;
   const double xi_min = XI[imin], xi_max = XI[imax];
   const double m_w_min = MW[imin], m_w_max = MW[imax];
   const double m_s_min = MS[imin], m_s_max = MS[imax];
-  const double Rs = RR[ii] + RR[jj];
-  const double e = use_E ? __ldg(a.E + (int64_t)P.KK[ii] * a.nb + P.KK[jj]) : a.E_const;
-  const double du = P.U[ii] - P.U[jj], dw = P.W[ii] - P.W[jj];
-  const double dv = sqrt(du * du + dw * dw);
-  const double p_crit = xi_max * a.dtdv * (LC_PI * Rs * Rs * e * dv * 1.0E-12);
-  if (p_crit > 1.0) {
-    const double xi_col = p_crit * xi_min;
-    MW[imin] = m_w_min + p_crit * m_w_max;
-    MS[imin] = m_s_min + p_crit * m_s_max;
-    RR[imin] = col_radius((MW[imin] + MS[imin]), P.RHO[imin]);
-    XI[imax] -= xi_col;
-    if (use_E) P.KK[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
-    if (P.fxi) { P.fxi[imax] = (float)XI[imax]; P.fR[imin] = (float)RR[imin]; }
-    c1 += 1;
-    return;
-  }
-  if (r < 0.0) r = rnd ? rnd[rk] : philox_uniform(a.seed, (uint64_t)rk, pc1);
-  if (!(p_crit > r)) return;
-  c0 += 1;
   const double xi_rel_dev = (xi_max - xi_min) / xi_max;
   if (xi_rel_dev < 1.0E-5) {
+    ensure_exact(a, imax, Tc, use_E);
     const double xi_ges = xi_min + xi_max;
     MW[imin] = 2.0 * (xi_min * m_w_min + xi_max * m_w_max) / xi_ges;
     MS[imin] = 2.0 * (xi_min * m_s_min + xi_max * m_s_max) / xi_ges;
     MW[imax] = MW[imin];
     MS[imax] = MS[imin];
-    RR[imin] = col_radius((MW[imin] + MS[imin]), P.RHO[imin]);
+    RR[imin] = col_radius((MW[imin] + MS[imin]), RHO[imin]);
     RR[imax] = RR[imin];
     XI[imax] = 0.5 * 0.7 * xi_ges;
     XI[imin] = 0.5 * xi_ges - XI[imax];
-    if (use_E) { P.KK[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb); P.KK[imax] = P.KK[imin]; }
-    if (P.fxi) {
-      P.fxi[imin] = (float)XI[imin]; P.fxi[imax] = (float)XI[imax];
-      P.fR[imin] = (float)RR[imin]; P.fR[imax] = (float)RR[imax];
+    if (use_E) { a.gk[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb); a.gk[imax] = a.gk[imin]; }
+    if (S) {
+      S->fxi[lmin] = d2f_rn(XI[imin]); S->fxi[lmax] = d2f_rn(XI[imax]);
+      S->fR[lmin] = d2f_rn(RR[imin]); S->fR[lmax] = S->fR[lmin];
+      S->sk[lmin] = a.gk[imin]; S->sk[lmax] = a.gk[imax];
     }
   } else {
     MW[imin] += m_w_max;
     MS[imin] += m_s_max;
-    RR[imin] = col_radius((MW[imin] + MS[imin]), P.RHO[imin]);
+    RR[imin] = col_radius((MW[imin] + MS[imin]), RHO[imin]);
     XI[imax] -= xi_min;
-    if (use_E) P.KK[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
-    if (P.fxi) { P.fxi[imax] = (float)XI[imax]; P.fR[imin] = (float)RR[imin]; }
+    if (use_E) a.gk[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
+    if (S) {
+      S->fxi[lmax] = d2f_rn(XI[imax]); S->fR[lmin] = d2f_rn(RR[imin]);
+      S->sk[lmin] = a.gk[imin];
+    }
   }
 }
 
-// Shared-memory layout per warp: 7 double arrays, 4 float arrays, 1 int array.
-constexpr size_t CELL_WARP_BYTES = (size_t)CELL_SMEM * (7 * 8 + 4 * 4 + 4);
+// Exact FP64 evaluation of the pair ii/jj (collision/all_or_nothing.py:
+// 553-633) in the reference's operation order, on the global arrays.
+__device__ __forceinline__ void exact_pair(const CellArgs& a, const CellSmem* S, int32_t ii,
+                                           int32_t jj, int li, int lj, double Tc, bool use_E,
+                                           double r, int64_t& c0, int64_t& c1) {
+  ensure_exact(a, ii, Tc, use_E);
+  ensure_exact(a, jj, Tc, use_E);
+  double *XI = a.xi, *MW = a.m_w, *MS = a.m_s, *RR = a.gR;
+  const double *U = a.vel, *W = a.vel + a.n;
+  int32_t imin, imax;
+  int lmin, lmax;
+  if (XI[ii] <= XI[jj]) { imin = ii; imax = jj; lmin = li; lmax = lj; }
+  else { imin = jj; imax = ii; lmin = lj; lmax = li; }
+  const double xi_min = XI[imin], xi_max = XI[imax];
+  const double Rs = RR[ii] + RR[jj];
+  const double e = use_E ? __ldg(a.E + (int64_t)a.gk[ii] * a.nb + a.gk[jj]) : a.E_const;
+  const double du = U[ii] - U[jj], dw = W[ii] - W[jj];
+  const double dv = sqrt(du * du + dw * dw);
+  const double p_crit = xi_max * a.dtdv * (LC_PI * Rs * Rs * e * dv * 1.0E-12);
+  if (p_crit > 1.0) {
+    const double xi_col = p_crit * xi_min;
+    MW[imin] = MW[imin] + p_crit * MW[imax];
+    MS[imin] = MS[imin] + p_crit * MS[imax];
+    RR[imin] = col_radius((MW[imin] + MS[imin]), a.grho[imin]);
+    XI[imax] -= xi_col;
+    if (use_E) a.gk[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
+    if (S) {
+      S->fxi[lmax] = d2f_rn(XI[imax]); S->fR[lmin] = d2f_rn(RR[imin]);
+      S->sk[lmin] = a.gk[imin];
+    }
+    c1 += 1;
+    return;
+  }
+  if (!(p_crit > r)) return;
+  c0 += 1;
+  collect_once(a, S, imin, imax, lmin, lmax, Tc, use_E);
+}
 
-__global__ void __launch_bounds__(CELL_WARPS * 32) k_collide_cells(CellArgs a) {
-  extern __shared__ double smem[];
+// One warp per cell.  Shared memory holds FP32 copies of xi, R, u, w and the
+// kernel bin (20 B per SIP), which bound p_crit from both sides; the exact FP64
+// evaluation runs only for pairs the bounds leave undecided.
+constexpr size_t CELL_WARP_BYTES = (size_t)CELL_SMEM * (4 * 4 + 4 + 4);
+
+__global__ void __launch_bounds__(CELL_WARPS * 32, 3) k_collide_cells(CellArgs a) {
+  extern __shared__ float fsm[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double* base = (double*)((char*)smem + (size_t)wid * CELL_WARP_BYTES);
-  float* fbase = (float*)(base + 7 * CELL_SMEM);
-  int32_t* kbase = (int32_t*)(fbase + 4 * CELL_SMEM);
+  float* wbase = (float*)((char*)fsm + (size_t)wid * CELL_WARP_BYTES);
+  CellSmem S{wbase, wbase + CELL_SMEM, wbase + 2 * CELL_SMEM, wbase + 3 * CELL_SMEM,
+             (int32_t*)(wbase + 4 * CELL_SMEM), (int32_t*)(wbase + 5 * CELL_SMEM)};
   const int64_t cursor = a.draws ? *a.cursor : 0;
   if (a.draws && cursor + *a.total_pairs > a.n_draws) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.flags, LACMO_FLAG_DRAWS_SHORT);
@@ -185,94 +243,143 @@ __global__ void __launch_bounds__(CELL_WARPS * 32) k_collide_cells(CellArgs a) {
   const bool use_E = a.E != nullptr;
   const float dtdv_f = (float)a.dtdv;
   const float pi_e12 = (float)(LC_PI * 1.0E-12);
+  const float lo_f = (float)a.lo, inv_bl_f = (float)(1.0 / a.bl);
+  const float c43 = (float)LC_FOUR_PI_OVER_THREE_INV;
+  const float ef_const = (float)a.E_const;
   int64_t c0 = 0, c1 = 0;
   for (int64_t c = blockIdx.x * (int64_t)CELL_WARPS + wid; c < a.C;
        c += (int64_t)gridDim.x * CELL_WARPS) {
     const int32_t b = a.start[c];
     const int n = a.start[c + 1] - b;
     if (n < 2) continue;
-    const bool in_smem = n <= CELL_SMEM;
     const double Tc = a.T[c];
+    const float Tf = d2f_rn(Tc);
+    const float rhow_f = (float)LC_PAR_WATER_DENS_0 +
+                         (float)LC_PAR_WATER_DENS_1 * ((Tf - (float)LC_PAR_WATER_DENS_2) *
+                                                        (Tf - (float)LC_PAR_WATER_DENS_2));
     const double* rnd = a.draws ? a.draws + cursor + a.draw_off[c] : nullptr;
     const uint64_t pc1 = (cstep << 32) | (uint64_t)c;
-    double *sxi = base, *smw = base + CELL_SMEM, *sms = base + 2 * CELL_SMEM,
-           *sR = base + 3 * CELL_SMEM, *srho = base + 4 * CELL_SMEM, *su = base + 5 * CELL_SMEM,
-           *sw = base + 6 * CELL_SMEM;
-    float *fxi = fbase, *fR = fbase + CELL_SMEM, *fu = fbase + 2 * CELL_SMEM,
-          *fw = fbase + 3 * CELL_SMEM;
-    int32_t* sk = kbase;
     const int32_t* ids = a.perm + b;
-    // load, radius and bin at the cell temperature (all_or_nothing.py:812-826)
-    for (int q = lane; q < n; q += 32) {
-      const int32_t id = ids[q];
-      const double x = a.xi[id], mw = a.m_w[id], ms = a.m_s[id];
-      const double m_p = mw + ms;
-      const double w_s = ms / m_p;
-      const double rho = (a.sol == SOL_AS) ? density_water(Tc) * poly_rho_AS(w_s)
-                                           : density_NaCl_solution(w_s, Tc);
-      const double R = col_radius(m_p, rho);
-      const int32_t kb = use_E ? col_bin(R, a.lo, a.bl, a.nb) : 0;
-      if (in_smem) {
-        const double u = a.vel[id], w = a.vel[a.n + id];
-        sxi[q] = x; smw[q] = mw; sms[q] = ms; sR[q] = R; srho[q] = rho;
-        su[q] = u; sw[q] = w; sk[q] = kb;
-        fxi[q] = (float)x; fR[q] = (float)R; fu[q] = (float)u; fw[q] = (float)w;
-      } else {
-        a.gR[id] = R; a.grho[id] = rho; a.gk[id] = kb;
-      }
-    }
-    __syncwarp();
-    if (in_smem) {
-      const PairState P{sxi, smw, sms, sR, srho, su, sw, sk, fxi, fR};
-      for (int s = 1; s <= 2 * n - 3; ++s) {
-        const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
-        const int ihi = (s - 1) >> 1;
-        for (int i = ilo + lane; i <= ihi; i += 32) {
-          const int j = s - i;
-          const int64_t rk = pair_rank(i, j, n);
-          // Certified FP32 upper bound of |p_crit|: every float op and
-          // double->float conversion is within 2^-24 relative, the velocity
-          // difference gets an explicit absolute slack for its cancellation,
-          // and the result is inflated by 2^-16 plus an absolute 1e-36.  Only
-          // if this bound is below both 1 and the draw is the pair certainly
-          // neither a multiple collection nor a collection; otherwise the
-          // exact FP64 evaluation decides.
-          const float ui = fu[i], uj = fu[j], wi = fw[i], wj = fw[j];
-          const float du = ui - uj, dw = wi - wj;
-          const float slack = 0x1p-21f * (fabsf(ui) + fabsf(uj) + fabsf(wi) + fabsf(wj));
-          const float dvu = sqrtf(du * du + dw * dw) + slack;
-          const float rs = fR[i] + fR[j];
-          const float ef = use_E ? (float)__ldg(a.E + (int64_t)sk[i] * a.nb + sk[j])
-                                 : (float)a.E_const;
-          const float xm = fmaxf(fabsf(fxi[i]), fabsf(fxi[j]));
-          const float pub = ((xm * dtdv_f) * pi_e12) * rs * rs * ef * dvu;
-          const float ap = pub * (1.0f + 0x1p-16f) + 1e-36f;
-          double r = -1.0;
-          if (ap < 1.0f && pub >= 1e-28f) {
-            r = rnd ? rnd[rk] : philox_uniform(a.seed, (uint64_t)rk, pc1);
-            if ((double)ap < r) continue;   // certainly no collision
-          }
-          exact_pair(P, i, j, r, a, use_E, rk, rnd, pc1, c0, c1);
-        }
-        __syncwarp();
-      }
+    if (n > CELL_SMEM) {
+      // rare oversized cell: exact evaluation of every pair on global data
       for (int q = lane; q < n; q += 32) {
         const int32_t id = ids[q];
-        a.xi[id] = sxi[q]; a.m_w[id] = smw[q]; a.m_s[id] = sms[q];
+        a.gR[id] = a.m_w[id] + a.m_s[id];
+        a.grho[id] = a.m_s[id];
+        a.gk[id] = -1;
       }
-    } else {
-      const PairState P{a.xi, a.m_w, a.m_s, a.gR, a.grho, a.vel, a.vel + a.n, a.gk, nullptr,
-                        nullptr};
+      __syncwarp();
       for (int s = 1; s <= 2 * n - 3; ++s) {
         const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
         const int ihi = (s - 1) >> 1;
         for (int i = ilo + lane; i <= ihi; i += 32) {
           const int j = s - i;
-          exact_pair(P, ids[i], ids[j], -1.0, a, use_E, pair_rank(i, j, n), rnd, pc1, c0, c1);
+          const int32_t ii = ids[i], jj = ids[j];
+          const int64_t rk = pair_rank(i, j, n);
+          const double r = rnd ? rnd[rk] : philox_uniform(a.seed, (uint64_t)rk, pc1);
+          exact_pair(a, nullptr, ii, jj, i, j, Tc, use_E, r, c0, c1);
         }
         __threadfence_block();
         __syncwarp();
       }
+      continue;
+    }
+    // load: FP32 copies, FP32 radius and bin (exact when near a bin edge)
+    for (int q = lane; q < n; q += 32) {
+      const int32_t id = ids[q];
+      const double xd = a.xi[id], mwd = a.m_w[id], msd = a.m_s[id];
+      const double m_p = mwd + msd;
+      a.gR[id] = m_p;
+      a.grho[id] = msd;
+      a.gk[id] = -1;
+      const float mwf = d2f_rn(mwd), msf = d2f_rn(msd);
+      const float mpf = mwf + msf;
+      const float wsf = msf / mpf;
+      const float rho = (a.sol == SOL_AS)
+                            ? rhow_f * ((((float)LC_PAR_RHO_AS_0 * wsf + (float)LC_PAR_RHO_AS_1) *
+                                             wsf + (float)LC_PAR_RHO_AS_2) * wsf +
+                                        (float)LC_PAR_RHO_AS_3)
+                            : (float)LC_PAR_SOL_DENS_NACL_0 + (float)LC_PAR_SOL_DENS_NACL_1 * wsf +
+                                  (float)LC_PAR_SOL_DENS_NACL_2 * Tf +
+                                  (float)LC_PAR_SOL_DENS_NACL_3 * wsf * wsf +
+                                  (float)LC_PAR_SOL_DENS_NACL_4 * wsf * Tf +
+                                  (float)LC_PAR_SOL_DENS_NACL_5 * Tf * Tf;
+      const float Rf = cbrtf(c43 * mpf / rho);
+      int32_t kb = 0;
+      if (use_E) {
+        const float v = (__logf(Rf) - lo_f) * inv_bl_f + 0.5f;
+        const float fl = floorf(v);
+        if (v - fl > 2e-3f && (fl + 1.0f) - v > 2e-3f && v > -1e6f && v < 1e6f && Rf > 0.f) {
+          kb = (int32_t)fl;
+          kb = kb < 0 ? 0 : (kb > a.nb - 1 ? (int32_t)a.nb - 1 : kb);
+        } else {
+          ensure_exact(a, id, Tc, use_E);
+          kb = a.gk[id];
+        }
+      }
+      S.fxi[q] = d2f_rn(xd);
+      S.fR[q] = Rf;
+      S.fu[q] = d2f_rn(a.vel[id]);
+      S.fw[q] = d2f_rn(a.vel[a.n + id]);
+      S.sk[q] = kb;
+      S.sid[q] = id;
+    }
+    __syncwarp();
+    for (int s = 1; s <= 2 * n - 3; ++s) {
+      const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
+      const int ihi = (s - 1) >> 1;
+      for (int i = ilo + lane; i <= ihi; i += 32) {
+        const int j = s - i;
+        const int64_t rk = pair_rank(i, j, n);
+        // Two-sided FP32 bounds of p_crit.  The FP32 radii are within 1e-6
+        // (relative) of the exact ones, every other FP32 operation and
+        // conversion within 2^-24, the velocity difference carries an
+        // absolute slack for its cancellation; the bounds are widened by
+        // 2^-14 relative (and 1e-36 absolute).  Negative multiplicities (left
+        // by multiple collections) go to the exact path.
+        const float xa = S.fxi[i], xb = S.fxi[j];
+        const float ui = S.fu[i], uj = S.fu[j], wi = S.fw[i], wj = S.fw[j];
+        const float du = ui - uj, dw = wi - wj;
+        const float slack = 0x1p-21f * (fabsf(ui) + fabsf(uj) + fabsf(wi) + fabsf(wj));
+        const float dvm = sqrtf(du * du + dw * dw);
+        const float rs = S.fR[i] + S.fR[j];
+        const float ef = use_E ? d2f_rn(__ldg(a.E + (int64_t)S.sk[i] * a.nb + S.sk[j])) : ef_const;
+        const float core = ((fmaxf(xa, xb) * dtdv_f) * pi_e12) * rs * rs * ef;
+        const float p_hi = core * (dvm + slack) * (1.0f + 0x1p-14f) + 1e-36f;
+        const float p_lo = core * fmaxf(dvm - slack, 0.0f) * (1.0f - 0x1p-14f);
+        // the draw as a float interval [r_lo, r_hi] around the exact double
+        // (an injected draw outside [0, 1) gives an empty screen)
+        float r_lo, r_hi;
+        double r = 0.0;
+        uint64_t k53 = 0;
+        if (rnd) {
+          r = rnd[rk];
+          const uint64_t rb = (uint64_t)__double_as_longlong(r);
+          r_lo = rb < 0x3ff0000000000000ull ? d2f_down_pos(r) : 2.0f;
+          r_hi = rb < 0x3ff0000000000000ull ? r_lo + 0x1p-24f : -1.0f;
+        } else {
+          k53 = philox_bits53(a.seed, (uint64_t)rk, pc1);
+          r_lo = (float)(uint32_t)(k53 >> 29) * 0x1p-24f;
+          r_hi = r_lo + 0x1p-24f;
+        }
+        const bool sane = xa > 0.0f && xb > 0.0f && p_hi == p_hi && p_hi < 1.0f &&
+                          core >= 1e-30f;
+        if (sane && p_hi < r_lo) continue;   // certainly no collision
+        if (sane && p_lo > r_hi) {
+          // certainly an ordinary collection (0 < p_crit <= 1 and p_crit > r)
+          const int32_t ii = S.sid[i], jj = S.sid[j];
+          const bool lo_i = a.xi[ii] <= a.xi[jj];
+          const int32_t imin = lo_i ? ii : jj, imax = lo_i ? jj : ii;
+          ensure_exact(a, imin, Tc, use_E);
+          c0 += 1;
+          collect_once(a, &S, imin, imax, lo_i ? i : j, lo_i ? j : i, Tc, use_E);
+          continue;
+        }
+        if (!rnd) r = (double)k53 * (1.0 / 9007199254740992.0);
+        exact_pair(a, &S, S.sid[i], S.sid[j], i, j, Tc, use_E, r, c0, c1);
+      }
+      __threadfence_block();
+      __syncwarp();
     }
     __syncwarp();
   }

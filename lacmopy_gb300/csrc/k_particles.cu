@@ -247,7 +247,7 @@ struct PArgs {
   const float* auxf;            // [AUXF][C] FP32 per-cell terms (see write_aux)
   const float* gvf;             // [2][nx+1][nz+1] FP32 wind field
   double inv_dx, inv_dz;
-  float inv_dxf, inv_dzf, dt_subf, dtg_f;
+  float inv_dxf, inv_dzf, dt_subf, dtg_f, dt_posf;
 };
 
 // FP32 per-cell table of the mixed-precision path
@@ -448,150 +448,175 @@ __global__ void __launch_bounds__(128) k_cell_update(const int32_t* __restrict__
 }
 
 // ---------------------------------------------------------------------------
-// Mixed precision particle sub-step: the same steps as k_particles with the
-// Newton condensation and the drag update in FP32 (lacmo_physics.cuh), an FP64
-// repeat of the Newton for SIPs near the critical radius, and FP64 state,
-// positions, per-cell condensed-mass sums (warp-aggregated atomics) and
-// water_removed.  The per-cell sums are not formed in ID order, so the grid
-// feedback is reproducible to FP64 rounding, not bit for bit.
+// Mixed precision particle sub-step.  GB300 issues FP64 arithmetic, FP64
+// compares and double<->float conversions on a pipe that is 64x narrower than
+// the FP32 one, so this kernel keeps the FP64 pipe for the three state
+// updates x += dx, z += dz, m_w += dm and does everything else in FP32 or in
+// integer units:
+//  * double -> float rounding (to nearest even) and float -> double are done
+//    on the IEEE bit patterns with integer instructions (d2f_int / f2d_int);
+//  * comparisons of non-negative doubles compare their bit patterns;
+//  * the new cell index comes from the FP32 position with a certified margin
+//    (1e-4 of a cell) around cell edges, inside which FP64 decides;
+//  * the per-cell sums of dm * xi are FP64 atomics, which L2 executes.
+// The Newton condensation and the drag update run in FP32 (lacmo_physics.cuh)
+// with the FP64 Newton for SIPs near the critical radius.  Per-cell sums and
+// water_removed are formed in arbitrary order.
+__device__ __forceinline__ float d2f_int(double x) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
+  if (e < 897u || e > 1150u) return (float)x;   // zero, subnormal, huge, inf, nan
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const uint64_t m = b & 0x000fffffffffffffull;
+  const uint32_t fm = (uint32_t)(m >> 29), rem = (uint32_t)m & 0x1fffffffu;
+  uint32_t fb = sign | ((e - 896u) << 23) | fm;
+  fb += (rem > 0x10000000u) || (rem == 0x10000000u && (fm & 1u));
+  return __int_as_float((int)fb);
+}
+__device__ __forceinline__ double f2d_int(float f) {
+  const uint32_t b = (uint32_t)__float_as_int(f);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e == 0u || e == 255u) return (double)f;   // zero, subnormal, inf, nan
+  const uint64_t r = ((uint64_t)(b & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
+                     ((uint64_t)(b & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)r);
+}
 __global__ void __launch_bounds__(128) k_particles_mixed(PArgs a) {
   const int64_t C = a.nx * a.nz;
   const GridVelF gvf{a.gvf, a.nx, a.nz};
-  const int lane = threadIdx.x & 31;
-  const int64_t n_round = (a.n + 31) / 32 * 32;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_round;
+  const float x_maxf = (float)a.x_max, z_minf = (float)a.z_min, z_capf = (float)a.z_cap;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n;
        k += (int64_t)gridDim.x * blockDim.x) {
-    const bool valid = k < a.n;
-    const int32_t c = valid ? a.cell[k] : -1;
+    const int32_t c = a.cell[k];
     const bool active = c >= 0;
-    double dmxi = 0.0;
-    if (valid) {
-      const int64_t i = active ? (int64_t)c / a.nz : (int64_t)(-1 - c);
-      const int64_t j = active ? (int64_t)c - i * a.nz : -1;
-      double x = a.pos[k], z = a.pos[a.n + k];
-      double u = a.vel[k], w = a.vel[a.n + k];
-      double mw = a.m_w[k];
-      double xik = 0.0, rel_x = 0.0, rel_z = 0.0;
-      const double T_p = __ldg(a.gsf + i * a.nz + (active ? j : a.nz - 1));
-      if (a.write_Tp) a.T_p[k] = T_p;
-      const double x0 = x, z0 = z;
-      if (active) {
-        const double ms = a.m_s[k];
-        xik = a.xi[k];
-        CellAmbF af;
-        af.T = __ldg(a.auxf + AF_T * C + c); af.S_m1 = __ldg(a.auxf + AF_SM1 * C + c);
-        af.sigw = __ldg(a.auxf + AF_SIGW * C + c); af.rhow = __ldg(a.auxf + AF_RHOW * C + c);
-        af.lap0 = __ldg(a.auxf + AF_LAP0 * C + c); af.lbp0 = __ldg(a.auxf + AF_LBP0 * C + c);
-        af.c1 = __ldg(a.auxf + AF_C1 * C + c); af.c2 = __ldg(a.auxf + AF_C2 * C + c);
-        const float msf = (float)ms;
-        const float mwf = (float)mw;
-        const float mpf = mwf + msf;
-        const float wsf = msf / mpf;
-        float rho = (a.sol == SOL_AS)
-                        ? af.rhow * ((((float)LC_PAR_RHO_AS_0 * wsf + (float)LC_PAR_RHO_AS_1) * wsf +
-                                      (float)LC_PAR_RHO_AS_2) * wsf + (float)LC_PAR_RHO_AS_3)
-                        : (float)LC_PAR_SOL_DENS_NACL_0 + (float)LC_PAR_SOL_DENS_NACL_1 * wsf +
-                              (float)LC_PAR_SOL_DENS_NACL_2 * af.T +
-                              (float)LC_PAR_SOL_DENS_NACL_3 * wsf * wsf +
-                              (float)LC_PAR_SOL_DENS_NACL_4 * wsf * af.T +
-                              (float)LC_PAR_SOL_DENS_NACL_5 * af.T * af.T;
-        float R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * mpf / rho);
-        const float sig = af.sigw * (1.0f + (float)(a.sol == SOL_AS ? LC_PAR_SIGMA_AS
-                                                                      : LC_PAR_SIGMA_NACL) *
-                                                 wsf / (1.f - wsf));
-        const double m_w_effl = ms * (LC_W_S_MAX_AS_INV - 1.0);
-        double dm;
-        const bool ok = newton_mixed(a.sol, (float)a.dt_sub, a.no_iter, mw, msf, wsf, R, af.T, rho,
-                                     sig, af, m_w_effl, &dm);
-        if (!ok) {
-          // near the critical radius: FP64 residual and step
-          CellAmb amb;
-          amb.T = T_p; amb.p = __ldg(a.gsf + C + c); amb.S = __ldg(a.gsf + 6 * C + c);
-          amb.e_s = __ldg(a.gsf + 7 * C + c); amb.K = __ldg(a.gmp + c);
-          amb.D_v = __ldg(a.gmp + C + c); amb.L_v = __ldg(a.gmp + 2 * C + c);
-          amb.sigw = __ldg(a.aux + c); amb.rhow = __ldg(a.aux + C + c);
-          amb.lap0 = __ldg(a.aux + 2 * C + c); amb.lbp0 = __ldg(a.aux + 3 * C + c);
-          amb.c1 = __ldg(a.aux + 4 * C + c); amb.c2 = __ldg(a.aux + 5 * C + c);
-          const double m_p = mw + ms;
-          const double w_s = ms / m_p;
-          const double rho64 = (a.sol == SOL_AS) ? density_AS_solution_rw(w_s, amb.rhow)
-                                                 : density_NaCl_solution(w_s, T_p);
-          const double R64 = radius_from_mass(m_p, rho64);
-          const double sig64 = (a.sol == SOL_AS) ? surface_tension_AS_sw(w_s, amb.sigw)
-                                                 : surface_tension_NaCl_sw(w_s, amb.sigw);
-          dm = newton_full(a.sol, a.dt_sub, a.no_iter, mw, ms, w_s, R64, T_p, rho64, sig64, amb,
-                           nullptr);
-          atomicAdd(a.nfb, 1ull);
-        }
-        mw += dm;
-        dmxi = dm * xik;
-        // drag (integration.py:699-718) in FP32 with the ammonium-sulfate radius
-        const float mpn = (float)mw + msf;
-        const float wn = msf / mpn;
-        rho = af.rhow * ((((float)LC_PAR_RHO_AS_0 * wn + (float)LC_PAR_RHO_AS_1) * wn +
-                          (float)LC_PAR_RHO_AS_2) * wn + (float)LC_PAR_RHO_AS_3);
-        R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * mpn / rho);
-        const float rxf = (float)(x - a.x_min) * a.inv_dxf - (float)i;
-        const float rzf = (float)(z - a.z_min) * a.inv_dzf - (float)j;
-        float uf, wf;
-        gvf.interp(i, j, rxf, rzf, uf, wf);
-        const float mu_f = __ldg(a.auxf + AF_MU * C + c), rho_f = __ldg(a.auxf + AF_RHOF * C + c);
-        const float uo = (float)u, wo = (float)w;
-        const float d0 = uf - uo, d1 = wf - wo;
-        const float vel_dev = sqrtf(d0 * d0 + d1 * d1);
-        const float Re_p = 2.0E-6f * rho_f * R * vel_dev / mu_f;
-        float k_dt = 4.5E12f * a.dt_subf * mu_f / (rho * R * R);
-        if (Re_p > 0.5f) {
-          if (Re_p < 1000.0f) k_dt *= (1.f + 0.15f * powf(Re_p, 0.687f));
-          else k_dt *= 0.0183333333333f * Re_p;
-        }
-        const float inv = 1.0f / (1.0f + k_dt);
-        u = (double)((uo + k_dt * uf) * inv);
-        w = (double)((wo + k_dt * wf - a.dtg_f) * inv);
-      }
-      x += a.dt_pos * u;
-      z += a.dt_pos * w;
-      x = py_mod(x, a.x_max);
-      z = np_min(z, a.z_cap);
-      int32_t newc = c;
-      if (active) {
-        if (z <= a.z_min) {
-          z = a.z_min - 0.01 * a.dz;
-          u = 0.0; w = 0.0;
-          atomicAdd(a.rm_val, xik * mw);   // water_removed (FP64, any order)
-          rel_x = (x0 - a.x_min) / a.dx - (double)i;
-          rel_z = (z0 - a.z_min) / a.dz - (double)j;
-          a.rel[k] = rel_x / a.dx - (double)i;
-          a.rel[a.n + k] = rel_z / a.dz - (-1.0);
-          newc = (int32_t)(-1 - i);
-        } else {
-          int64_t ci = (int64_t)floor(x * a.inv_dx), cj = (int64_t)floor(z * a.inv_dz);
-          if (ci >= a.nx || ci < 0 || cj >= a.nz || cj < 0) {
-            atomicOr(a.flags, LACMO_FLAG_CELL_CLAMPED);
-            ci = ci < 0 ? 0 : (ci >= a.nx ? a.nx - 1 : ci);
-            cj = cj < 0 ? 0 : (cj >= a.nz ? a.nz - 1 : cj);
-          }
-          newc = (int32_t)(ci * a.nz + cj);
-          if (a.hist) a.rank[k] = atomicAdd(a.counts + newc, 1);
-        }
-      } else {
-        a.rel[k] = a.rel[k] / a.dx - (double)i;
-        a.rel[a.n + k] = a.rel[a.n + k] / a.dz - (-1.0);
-      }
-      a.pos[k] = x; a.pos[a.n + k] = z;
-      a.vel[k] = u; a.vel[a.n + k] = w;
-      if (active) a.m_w[k] = mw;
-      a.cell[k] = newc;
+    const int64_t i = active ? (int64_t)c / a.nz : (int64_t)(-1 - c);
+    const int64_t j = active ? (int64_t)c - i * a.nz : -1;
+    double x = a.pos[k], z = a.pos[a.n + k];
+    const double T_p = __ldg(a.gsf + i * a.nz + (active ? j : a.nz - 1));
+    if (a.write_Tp) a.T_p[k] = T_p;
+    if (!active) {
+      // removed SIPs: velocity 0, x fixed under the wrap, z below ground;
+      // only the relative position keeps its per-call division
+      a.rel[k] = a.rel[k] / a.dx - (double)i;
+      a.rel[a.n + k] = a.rel[a.n + k] / a.dz - (-1.0);
+      continue;
     }
-    // per-cell FP64 sum of dm * xi, one atomic per run of equal cells in the warp
-    const unsigned peers = __match_any_sync(0xffffffffu, active ? c : -1 - lane);
-    const int leader = __ffs(peers) - 1;
-    double sum = 0.0;
-    for (unsigned m = peers; m; m &= m - 1) {
-      const int src = __ffs(m) - 1;
-      sum += __shfl_sync(peers, dmxi, src);
+    double mw = a.m_w[k];
+    const double ms = a.m_s[k];
+    const double xik = a.xi[k];
+    CellAmbF af;
+    af.T = __ldg(a.auxf + AF_T * C + c); af.S_m1 = __ldg(a.auxf + AF_SM1 * C + c);
+    af.sigw = __ldg(a.auxf + AF_SIGW * C + c); af.rhow = __ldg(a.auxf + AF_RHOW * C + c);
+    af.lap0 = __ldg(a.auxf + AF_LAP0 * C + c); af.lbp0 = __ldg(a.auxf + AF_LBP0 * C + c);
+    af.c1 = __ldg(a.auxf + AF_C1 * C + c); af.c2 = __ldg(a.auxf + AF_C2 * C + c);
+    const float msf = d2f_int(ms), mwf = d2f_int(mw), xif = d2f_int(xik);
+    const float mpf = mwf + msf;
+    const float wsf = msf / mpf;
+    float rho = (a.sol == SOL_AS)
+                    ? af.rhow * ((((float)LC_PAR_RHO_AS_0 * wsf + (float)LC_PAR_RHO_AS_1) * wsf +
+                                  (float)LC_PAR_RHO_AS_2) * wsf + (float)LC_PAR_RHO_AS_3)
+                    : (float)LC_PAR_SOL_DENS_NACL_0 + (float)LC_PAR_SOL_DENS_NACL_1 * wsf +
+                          (float)LC_PAR_SOL_DENS_NACL_2 * af.T +
+                          (float)LC_PAR_SOL_DENS_NACL_3 * wsf * wsf +
+                          (float)LC_PAR_SOL_DENS_NACL_4 * wsf * af.T +
+                          (float)LC_PAR_SOL_DENS_NACL_5 * af.T * af.T;
+    float R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * mpf / rho);
+    const float sig = af.sigw * (1.0f + (float)(a.sol == SOL_AS ? LC_PAR_SIGMA_AS
+                                                                  : LC_PAR_SIGMA_NACL) *
+                                             wsf / (1.f - wsf));
+    // efflorescence floor m_s (1/0.78 - 1) as an increment, in FP32
+    const float d_effl = msf * (float)(LC_W_S_MAX_AS_INV - 1.0) - mwf;
+    float d;
+    bool ok = newton_mixed_f(a.sol, a.dt_subf, a.no_iter, mwf, msf, wsf, R, af.T, rho, sig, af,
+                             d_effl, &d);
+    double dm;
+    if (ok) {
+      dm = f2d_int(d);
+    } else {
+      // near the critical radius: FP64 residual and step
+      CellAmb amb;
+      amb.T = T_p; amb.p = __ldg(a.gsf + C + c); amb.S = __ldg(a.gsf + 6 * C + c);
+      amb.e_s = __ldg(a.gsf + 7 * C + c); amb.K = __ldg(a.gmp + c);
+      amb.D_v = __ldg(a.gmp + C + c); amb.L_v = __ldg(a.gmp + 2 * C + c);
+      amb.sigw = __ldg(a.aux + c); amb.rhow = __ldg(a.aux + C + c);
+      amb.lap0 = __ldg(a.aux + 2 * C + c); amb.lbp0 = __ldg(a.aux + 3 * C + c);
+      amb.c1 = __ldg(a.aux + 4 * C + c); amb.c2 = __ldg(a.aux + 5 * C + c);
+      const double m_p = mw + ms;
+      const double w_s = ms / m_p;
+      const double rho64 = (a.sol == SOL_AS) ? density_AS_solution_rw(w_s, amb.rhow)
+                                             : density_NaCl_solution(w_s, T_p);
+      const double R64 = radius_from_mass(m_p, rho64);
+      const double sig64 = (a.sol == SOL_AS) ? surface_tension_AS_sw(w_s, amb.sigw)
+                                             : surface_tension_NaCl_sw(w_s, amb.sigw);
+      dm = newton_full(a.sol, a.dt_sub, a.no_iter, mw, ms, w_s, R64, T_p, rho64, sig64, amb,
+                       nullptr);
+      d = d2f_int(dm);
+      atomicAdd(a.nfb, 1ull);
     }
-    if (active && lane == leader) atomicAdd(a.acc + c, sum);
+    mw += dm;
+    // per-cell FP64 sum of dm * xi (executed by L2)
+    atomicAdd(a.acc + c, f2d_int(d * xif));
+    // drag (integration.py:699-718) in FP32 with the ammonium-sulfate radius
+    const float mpn = (mwf + d) + msf;
+    const float wn = msf / mpn;
+    rho = af.rhow * ((((float)LC_PAR_RHO_AS_0 * wn + (float)LC_PAR_RHO_AS_1) * wn +
+                      (float)LC_PAR_RHO_AS_2) * wn + (float)LC_PAR_RHO_AS_3);
+    R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * mpn / rho);
+    const float xf = d2f_int(x), zf = d2f_int(z);
+    const float rxf = (xf - (float)a.x_min) * a.inv_dxf - (float)i;
+    const float rzf = (zf - (float)a.z_min) * a.inv_dzf - (float)j;
+    float uf, wf;
+    gvf.interp(i, j, rxf, rzf, uf, wf);
+    const float mu_f = __ldg(a.auxf + AF_MU * C + c), rho_f = __ldg(a.auxf + AF_RHOF * C + c);
+    const float uo = d2f_int(a.vel[k]), wo = d2f_int(a.vel[a.n + k]);
+    const float d0 = uf - uo, d1 = wf - wo;
+    const float vel_dev = sqrtf(d0 * d0 + d1 * d1);
+    const float Re_p = 2.0E-6f * rho_f * R * vel_dev / mu_f;
+    float k_dt = 4.5E12f * a.dt_subf * mu_f / (rho * R * R);
+    if (Re_p > 0.5f) {
+      if (Re_p < 1000.0f) k_dt *= (1.f + 0.15f * powf(Re_p, 0.687f));
+      else k_dt *= 0.0183333333333f * Re_p;
+    }
+    const float inv = 1.0f / (1.0f + k_dt);
+    const float un = (uo + k_dt * uf) * inv;
+    const float wn2 = (wo + k_dt * wf - a.dtg_f) * inv;
+    // position (integration.py:552-630)
+    const double x0 = x, z0 = z;
+    x += f2d_int(a.dt_posf * un);
+    z += f2d_int(a.dt_posf * wn2);
+    const float xnf = xf + a.dt_posf * un, znf = zf + a.dt_posf * wn2;
+    double u = f2d_int(un), w = f2d_int(wn2);
+    // periodic x / capped z: exact FP64 only when near or past a boundary
+    if (!(xnf > 1e-3f && xnf < x_maxf - 1e-3f)) x = py_mod(x, a.x_max);
+    if (!(znf < z_capf - 1e-3f)) z = np_min(z, a.z_cap);
+    int32_t newc;
+    if (!(znf > z_minf + 1e-3f) && z <= a.z_min) {
+      z = a.z_min - 0.01 * a.dz;
+      u = 0.0; w = 0.0;
+      atomicAdd(a.rm_val, xik * mw);   // water_removed (FP64, any order)
+      const double rel_x = (x0 - a.x_min) / a.dx - (double)i;
+      const double rel_z = (z0 - a.z_min) / a.dz - (double)j;
+      a.rel[k] = rel_x / a.dx - (double)i;
+      a.rel[a.n + k] = rel_z / a.dz - (-1.0);
+      newc = (int32_t)(-1 - i);
+    } else {
+      const float qx = d2f_int(x) * a.inv_dxf, qz = d2f_int(z) * a.inv_dzf;
+      int64_t ci = (int64_t)floorf(qx), cj = (int64_t)floorf(qz);
+      const float fx = qx - floorf(qx), fz = qz - floorf(qz);
+      if (!(fx > 1e-4f && fx < 0.9999f)) ci = (int64_t)floor(x / a.dx);
+      if (!(fz > 1e-4f && fz < 0.9999f)) cj = (int64_t)floor(z / a.dz);
+      if (ci >= a.nx || ci < 0 || cj >= a.nz || cj < 0) {
+        atomicOr(a.flags, LACMO_FLAG_CELL_CLAMPED);
+        ci = ci < 0 ? 0 : (ci >= a.nx ? a.nx - 1 : ci);
+        cj = cj < 0 ? 0 : (cj >= a.nz ? a.nz - 1 : cj);
+      }
+      newc = (int32_t)(ci * a.nz + cj);
+      if (a.hist) a.rank[k] = atomicAdd(a.counts + newc, 1);
+    }
+    a.pos[k] = x; a.pos[a.n + k] = z;
+    a.vel[k] = u; a.vel[a.n + k] = w;
+    a.m_w[k] = mw;
+    a.cell[k] = newc;
   }
 }
 
@@ -846,7 +871,7 @@ cudaError_t launch_particles_mixed(const lacmo_sips_t& sp, const lacmo_grid_t& g
   a.auxf = (const float*)(w.aux + 6 * g.nx * g.nz); a.gvf = w.gvf;
   a.inv_dx = 1.0 / g.dx; a.inv_dz = 1.0 / g.dz;
   a.inv_dxf = (float)(1.0 / g.dx); a.inv_dzf = (float)(1.0 / g.dz);
-  a.dt_subf = (float)dt_sub; a.dtg_f = (float)(dt_sub * p.g_set);
+  a.dt_subf = (float)dt_sub; a.dtg_f = (float)(dt_sub * p.g_set); a.dt_posf = (float)dt_sub_pos;
   k_particles_mixed<<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a); note_launches(1);
   return cudaGetLastError();
 }

@@ -58,6 +58,21 @@ __device__ __forceinline__ double philox_uniform(uint64_t key, uint64_t c0, uint
   return (double)(a * 67108864ull + b) * (1.0 / 9007199254740992.0);
 }
 
+// The 53 random bits of the same generator (philox_uniform = bits * 2^-53).
+__device__ __forceinline__ uint64_t philox_bits53(uint64_t key, uint64_t c0, uint64_t c1) {
+  uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
+  uint32_t x0 = (uint32_t)c0, x1 = (uint32_t)(c0 >> 32), x2 = (uint32_t)c1, x3 = (uint32_t)(c1 >> 32);
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0 = __umulhi(0xD2511F53u, x0), lo0 = 0xD2511F53u * x0;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, x2), lo1 = 0xCD9E8D57u * x2;
+    uint32_t y0 = hi1 ^ x1 ^ k0, y1 = lo1, y2 = hi0 ^ x3 ^ k1, y3 = lo0;
+    x0 = y0; x1 = y1; x2 = y2; x3 = y3;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  return (uint64_t)(x0 >> 5) * 67108864ull + (uint64_t)(x1 >> 6);
+}
+
 // ---- launches (k_particles.cu) ----
 cudaError_t launch_cells_import(const int64_t* cells, const uint8_t* act, int32_t* cell, int64_t n,
                                 int64_t nx, int64_t nz, cudaStream_t s);

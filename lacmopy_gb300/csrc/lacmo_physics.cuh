@@ -275,6 +275,37 @@ LACMO_DEV bool newton_mixed(int sol, float dt_sub, int no_iter, double m_w, floa
   return !near_crit;
 }
 
+// The same Newton with the masses in FP32 (increment d, floor d_effl).
+LACMO_DEV bool newton_mixed_f(int sol, float dt_sub, int no_iter, float m_w32, float m_s,
+                              float w_s, float R_p, float T_p, float rho_p, float sigma_p,
+                              const CellAmbF& a, float d_effl, float* d_out) {
+  float g, dg, f2;
+  mass_rate_and_derivative_f(sol, m_w32, m_s, w_s, R_p, rho_p, sigma_p, T_p, a.rhow, a, g, dg, f2);
+  float x = dt_sub * dg;
+  bool near_crit = (fabsf(f2) < 1.0e-6f) && (fabsf(x) < 0.5f);
+  float denom_inv = (x < 0.9f) ? 1.0f / (1.0f - x) : 10.0f;
+  const float d0 = dt_sub * g * denom_inv;
+  float d = (d0 != d0) ? d0 : fmaxf(d_effl, d0);
+  for (int it = 0; it < no_iter - 1; ++it) {
+    const float mass = m_w32 + d;
+    const float m_p = mass + m_s;
+    const float w = m_s / m_p;
+    const float pr = (((float)LC_PAR_RHO_AS_0 * w + (float)LC_PAR_RHO_AS_1) * w +
+                      (float)LC_PAR_RHO_AS_2) * w + (float)LC_PAR_RHO_AS_3;
+    const float rho = a.rhow * pr;
+    const float R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * m_p / rho);
+    const float sig = a.sigw * (1.0f + (float)LC_PAR_SIGMA_AS * w / (1.f - w));
+    mass_rate_and_derivative_f(sol, mass, m_s, w, R, rho, sig, T_p, a.rhow, a, g, dg, f2);
+    x = dt_sub * dg;
+    near_crit = near_crit || ((fabsf(f2) < 1.0e-6f) && (fabsf(x) < 0.5f));
+    denom_inv = (x < 0.9f) ? 1.0f / (1.0f - x) : 10.0f;
+    d += (dt_sub * g - d) * denom_inv;
+    d = (d != d) ? d : fmaxf(d_effl, d);
+  }
+  *d_out = d;
+  return !near_crit;
+}
+
 // grid.py:195-323: staggered bilinear interpolation; index -1 wraps onto the
 // last column of the (nx+1)-wide staggered arrays, as NumPy indexing does.
 struct GridVel {
