@@ -100,15 +100,32 @@ struct CellArgs {
   uint32_t* flags;
   double *gR, *grho;   // per SIP: exact radius and density, or the step-start m_p, m_s
   int32_t* gk;         // per SIP: exact kernel bin, or -1 while gR/grho hold m_p, m_s
+  float dtdv_f, lo_f, inv_bl_f, E_const_f;   // FP32 copies for the screen
 };
 
 // integer-unit conversions (GB300 runs FP64 conversions on its narrow FP64
 // pipe): round to nearest even, and truncation toward zero for r >= 0
+__device__ __noinline__ float d2f_rn_slow(double x) { return (float)x; }
 __device__ __forceinline__ float d2f_rn(double x) {
   const uint64_t b = (uint64_t)__double_as_longlong(x);
   const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
-  if (e < 897u || e > 1150u) return (float)x;
+  if (e - 897u > 253u) return d2f_rn_slow(x);
   const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const uint64_t m = b & 0x000fffffffffffffull;
+  const uint32_t fm = (uint32_t)(m >> 29), rem = (uint32_t)m & 0x1fffffffu;
+  uint32_t fb = sign | ((e - 896u) << 23) | fm;
+  fb += (rem > 0x10000000u) || (rem == 0x10000000u && (fm & 1u));
+  return __int_as_float((int)fb);
+}
+// round to nearest even with zero/subnormal results flushed to zero and
+// overflow (and NaN) to infinity: integer instructions only (screen inputs,
+// where a flushed value makes the pair undecided or stays inside the bounds)
+__device__ __forceinline__ float d2f_flush(double x) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  if (e < 897u) return __int_as_float((int)sign);
+  if (e > 1150u) return __int_as_float((int)(sign | 0x7f800000u));
   const uint64_t m = b & 0x000fffffffffffffull;
   const uint32_t fm = (uint32_t)(m >> 29), rem = (uint32_t)m & 0x1fffffffu;
   uint32_t fb = sign | ((e - 896u) << 23) | fm;
@@ -125,8 +142,7 @@ __device__ __forceinline__ float d2f_down_pos(double r) {  // r in [0, 1)
 // exact per-SIP collision data (collision/all_or_nothing.py:812-826): the
 // density at the step-start masses and cell temperature, the correctly-rounded
 // radius and its kernel bin; computed on first need, then kept in gR/grho/gk
-__device__ __forceinline__ void ensure_exact(const CellArgs& a, int32_t id, double Tc, bool use_E) {
-  if (a.gk[id] >= 0) return;
+__device__ __noinline__ void compute_exact(const CellArgs& a, int32_t id, double Tc, bool use_E) {
   const double m_p = a.gR[id], ms = a.grho[id];
   const double w_s = ms / m_p;
   const double rho = (a.sol == SOL_AS) ? density_water(Tc) * poly_rho_AS(w_s)
@@ -136,10 +152,25 @@ __device__ __forceinline__ void ensure_exact(const CellArgs& a, int32_t id, doub
   a.grho[id] = rho;
   a.gk[id] = use_E ? col_bin(R, a.lo, a.bl, a.nb) : 0;
 }
+// the exact kernel bin of SIP id from its current masses, stored nowhere
+__device__ __noinline__ int32_t exact_bin_of(const CellArgs& a, int32_t id, double Tc) {
+  const double m_p = a.m_w[id] + a.m_s[id];
+  const double w_s = a.m_s[id] / m_p;
+  const double rho = (a.sol == SOL_AS) ? density_water(Tc) * poly_rho_AS(w_s)
+                                       : density_NaCl_solution(w_s, Tc);
+  return col_bin(col_radius(m_p, rho), a.lo, a.bl, a.nb);
+}
+__device__ __forceinline__ void ensure_exact(const CellArgs& a, int32_t id, double Tc, bool use_E) {
+  if (a.gk[id] < 0) compute_exact(a, id, Tc, use_E);
+}
 
+// FP32 shared-memory copies of a cell's SIPs (one warp's slice)
 struct CellSmem {
   float *fxi, *fR, *fu, *fw;
   int32_t *sk, *sid;
+  __device__ __forceinline__ explicit CellSmem(float* w)
+      : fxi(w), fR(w + CELL_SMEM), fu(w + 2 * CELL_SMEM), fw(w + 3 * CELL_SMEM),
+        sk((int32_t*)(w + 4 * CELL_SMEM)), sid((int32_t*)(w + 5 * CELL_SMEM)) {}
 };
 
 // One ordinary collection (p_crit <= 1 and p_crit > r) of the pair imin/imax
@@ -186,10 +217,13 @@ __device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* 
 }
 
 // Exact FP64 evaluation of the pair ii/jj (collision/all_or_nothing.py:
-// 553-633) in the reference's operation order, on the global arrays.
-__device__ __forceinline__ void exact_pair(const CellArgs& a, const CellSmem* S, int32_t ii,
-                                           int32_t jj, int li, int lj, double Tc, bool use_E,
-                                           double r, int64_t& c0, int64_t& c1) {
+// 553-633) in the reference's operation order, on the global arrays.  Returns
+// 0 (no collision), 1 (one collection) or 2 (multiple collection).  wsm is
+// the warp's shared-memory slice, or null (cells above its size).
+__device__ __noinline__ int exact_pair(const CellArgs& a, float* wsm, int32_t ii, int32_t jj,
+                                       int li, int lj, double Tc, bool use_E, double r) {
+  CellSmem Sm(wsm);
+  const CellSmem* S = wsm ? &Sm : nullptr;
   ensure_exact(a, ii, Tc, use_E);
   ensure_exact(a, jj, Tc, use_E);
   double *XI = a.xi, *MW = a.m_w, *MS = a.m_s, *RR = a.gR;
@@ -215,25 +249,90 @@ __device__ __forceinline__ void exact_pair(const CellArgs& a, const CellSmem* S,
       S->fxi[lmax] = d2f_rn(XI[imax]); S->fR[lmin] = d2f_rn(RR[imin]);
       S->sk[lmin] = a.gk[imin];
     }
-    c1 += 1;
-    return;
+    return 2;
   }
-  if (!(p_crit > r)) return;
-  c0 += 1;
+  if (!(p_crit > r)) return 0;
   collect_once(a, S, imin, imax, lmin, lmax, Tc, use_E);
+  return 1;
+}
+
+// A pair the FP32 bounds place certainly in an ordinary collection.
+__device__ __noinline__ void certain_collection(const CellArgs& a, float* wsm, int i, int j,
+                                                double Tc, bool use_E) {
+  CellSmem S(wsm);
+  const int32_t ii = S.sid[i], jj = S.sid[j];
+  const bool lo_i = a.xi[ii] <= a.xi[jj];
+  const int32_t imin = lo_i ? ii : jj, imax = lo_i ? jj : ii;
+  ensure_exact(a, imin, Tc, use_E);
+  collect_once(a, &S, imin, imax, lo_i ? i : j, lo_i ? j : i, Tc, use_E);
+}
+
+__device__ __noinline__ double philox_from_bits(uint64_t k53) {
+  return (double)k53 * (1.0 / 9007199254740992.0);
+}
+
+// FP32 screen of the pair (i, j) at lexicographic rank rk: 0 = certainly no
+// collision, 1 = certainly one ordinary collection (0 < p_crit <= 1 and
+// p_crit > r), 2 = undecided (the exact FP64 evaluation decides).  Two-sided
+// bounds of p_crit: the FP32 radii are within 1e-6 (relative) of the exact
+// ones, every other FP32 operation and conversion within 2^-24, the velocity
+// difference carries an absolute slack for its cancellation, and the bounds
+// are widened by 2^-14 relative (and 1e-36 absolute).  Non-positive
+// multiplicities (left by multiple collections) are undecided.  The draw is
+// bracketed by a float interval [r_lo, r_hi]; *k53 returns the Philox bits.
+struct ScreenCtx {
+  const double* rnd;
+  uint64_t seed, pc1;
+  bool use_E;
+};
+__device__ __forceinline__ int screen_pair(const CellArgs& a, const CellSmem& S,
+                                           const ScreenCtx& x, int i, int j, int64_t rk,
+                                           uint64_t* k53out) {
+  const float xa = S.fxi[i], xb = S.fxi[j];
+  const float ui = S.fu[i], uj = S.fu[j], wi = S.fw[i], wj = S.fw[j];
+  const float du = ui - uj, dw = wi - wj;
+  const float slack = 0x1p-21f * (fabsf(ui) + fabsf(uj) + fabsf(wi) + fabsf(wj));
+  const float dvm = sqrtf(du * du + dw * dw);
+  const float rs = S.fR[i] + S.fR[j];
+  const float ef = x.use_E ? d2f_flush(__ldg(a.E + (int64_t)S.sk[i] * a.nb + S.sk[j])) : a.E_const_f;
+  const float core = ((fmaxf(xa, xb) * a.dtdv_f) * (float)(LC_PI * 1.0E-12)) * rs * rs * ef;
+  const float p_hi = core * (dvm + slack) * (1.0f + 0x1p-14f) + 1e-36f;
+  const float p_lo = core * fmaxf(dvm - slack, 0.0f) * (1.0f - 0x1p-14f);
+  float r_lo, r_hi;
+  if (x.rnd) {
+    // an injected draw outside [0, 1) leaves the pair undecided
+    const uint64_t rb = (uint64_t)__double_as_longlong(x.rnd[rk]);
+    const bool in01 = rb < 0x3ff0000000000000ull;
+    r_lo = in01 ? d2f_down_pos(__longlong_as_double((long long)rb)) : 2.0f;
+    r_hi = in01 ? r_lo + 0x1p-24f : -1.0f;
+  } else {
+    const uint64_t k53 = philox_bits53(x.seed, (uint64_t)rk, x.pc1);
+    *k53out = k53;
+    r_lo = (float)(uint32_t)(k53 >> 29) * 0x1p-24f;
+    r_hi = r_lo + 0x1p-24f;
+  }
+  const bool sane = xa > 0.0f && xb > 0.0f && p_hi < 1.0f && core >= 1e-30f;
+  if (sane && p_hi < r_lo) return 0;
+  if (sane && p_lo > r_hi) return 1;
+  return 2;
 }
 
 // One warp per cell.  Shared memory holds FP32 copies of xi, R, u, w and the
-// kernel bin (20 B per SIP), which bound p_crit from both sides; the exact FP64
-// evaluation runs only for pairs the bounds leave undecided.
+// kernel bin (24 B per SIP with the SIP ID).  A first pass screens every pair
+// of the cell with the step-start state, lanes striding through the pairs in
+// lexicographic order.  Most cells have no pair the screen does not skip and
+// are done.  Otherwise let p* be the first such pair: every pair before p*
+// is skipped in the sequential order too (nothing changed before it), and the
+// anti-diagonal schedule runs the pairs from p* on, with the screen deciding
+// most of them and the exact FP64 evaluation the rest.
 constexpr size_t CELL_WARP_BYTES = (size_t)CELL_SMEM * (4 * 4 + 4 + 4);
 
-__global__ void __launch_bounds__(CELL_WARPS * 32, 3) k_collide_cells(CellArgs a) {
+__global__ void __launch_bounds__(CELL_WARPS * 32, 3)
+    k_collide_cells(const __grid_constant__ CellArgs a) {
   extern __shared__ float fsm[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   float* wbase = (float*)((char*)fsm + (size_t)wid * CELL_WARP_BYTES);
-  CellSmem S{wbase, wbase + CELL_SMEM, wbase + 2 * CELL_SMEM, wbase + 3 * CELL_SMEM,
-             (int32_t*)(wbase + 4 * CELL_SMEM), (int32_t*)(wbase + 5 * CELL_SMEM)};
+  const CellSmem S(wbase);
   const int64_t cursor = a.draws ? *a.cursor : 0;
   if (a.draws && cursor + *a.total_pairs > a.n_draws) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.flags, LACMO_FLAG_DRAWS_SHORT);
@@ -241,11 +340,7 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3) k_collide_cells(CellArgs a
   }
   const uint64_t cstep = (uint64_t)*a.col_step;
   const bool use_E = a.E != nullptr;
-  const float dtdv_f = (float)a.dtdv;
-  const float pi_e12 = (float)(LC_PI * 1.0E-12);
-  const float lo_f = (float)a.lo, inv_bl_f = (float)(1.0 / a.bl);
   const float c43 = (float)LC_FOUR_PI_OVER_THREE_INV;
-  const float ef_const = (float)a.E_const;
   int64_t c0 = 0, c1 = 0;
   for (int64_t c = blockIdx.x * (int64_t)CELL_WARPS + wid; c < a.C;
        c += (int64_t)gridDim.x * CELL_WARPS) {
@@ -253,10 +348,6 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3) k_collide_cells(CellArgs a
     const int n = a.start[c + 1] - b;
     if (n < 2) continue;
     const double Tc = a.T[c];
-    const float Tf = d2f_rn(Tc);
-    const float rhow_f = (float)LC_PAR_WATER_DENS_0 +
-                         (float)LC_PAR_WATER_DENS_1 * ((Tf - (float)LC_PAR_WATER_DENS_2) *
-                                                        (Tf - (float)LC_PAR_WATER_DENS_2));
     const double* rnd = a.draws ? a.draws + cursor + a.draw_off[c] : nullptr;
     const uint64_t pc1 = (cstep << 32) | (uint64_t)c;
     const int32_t* ids = a.perm + b;
@@ -277,22 +368,23 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3) k_collide_cells(CellArgs a
           const int32_t ii = ids[i], jj = ids[j];
           const int64_t rk = pair_rank(i, j, n);
           const double r = rnd ? rnd[rk] : philox_uniform(a.seed, (uint64_t)rk, pc1);
-          exact_pair(a, nullptr, ii, jj, i, j, Tc, use_E, r, c0, c1);
+          const int o = exact_pair(a, nullptr, ii, jj, i, j, Tc, use_E, r);
+          c0 += o == 1;
+          c1 += o == 2;
         }
         __threadfence_block();
         __syncwarp();
       }
       continue;
     }
+    const float Tf = d2f_rn(Tc);
+    const float rhow_f = (float)LC_PAR_WATER_DENS_0 +
+                         (float)LC_PAR_WATER_DENS_1 * ((Tf - (float)LC_PAR_WATER_DENS_2) *
+                                                        (Tf - (float)LC_PAR_WATER_DENS_2));
     // load: FP32 copies, FP32 radius and bin (exact when near a bin edge)
     for (int q = lane; q < n; q += 32) {
       const int32_t id = ids[q];
-      const double xd = a.xi[id], mwd = a.m_w[id], msd = a.m_s[id];
-      const double m_p = mwd + msd;
-      a.gR[id] = m_p;
-      a.grho[id] = msd;
-      a.gk[id] = -1;
-      const float mwf = d2f_rn(mwd), msf = d2f_rn(msd);
+      const float mwf = d2f_rn(a.m_w[id]), msf = d2f_rn(a.m_s[id]);
       const float mpf = mwf + msf;
       const float wsf = msf / mpf;
       const float rho = (a.sol == SOL_AS)
@@ -307,17 +399,16 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3) k_collide_cells(CellArgs a
       const float Rf = cbrtf(c43 * mpf / rho);
       int32_t kb = 0;
       if (use_E) {
-        const float v = (__logf(Rf) - lo_f) * inv_bl_f + 0.5f;
+        const float v = (__logf(Rf) - a.lo_f) * a.inv_bl_f + 0.5f;
         const float fl = floorf(v);
         if (v - fl > 2e-3f && (fl + 1.0f) - v > 2e-3f && v > -1e6f && v < 1e6f && Rf > 0.f) {
-          kb = (int32_t)fl;
+          kb = __float2int_rz(fl);
           kb = kb < 0 ? 0 : (kb > a.nb - 1 ? (int32_t)a.nb - 1 : kb);
         } else {
-          ensure_exact(a, id, Tc, use_E);
-          kb = a.gk[id];
+          kb = exact_bin_of(a, id, Tc);
         }
       }
-      S.fxi[q] = d2f_rn(xd);
+      S.fxi[q] = d2f_rn(a.xi[id]);
       S.fR[q] = Rf;
       S.fu[q] = d2f_rn(a.vel[id]);
       S.fw[q] = d2f_rn(a.vel[a.n + id]);
@@ -325,58 +416,50 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3) k_collide_cells(CellArgs a
       S.sid[q] = id;
     }
     __syncwarp();
+    const ScreenCtx X{rnd, a.seed, pc1, use_E};
+    // pass 1: screen all pairs with the step-start state, lexicographic walk
+    int pstar = 0x7fffffff;
+    {
+      int i = 0, j = 1 + lane, p = lane;
+      for (;;) {
+        while (j > n - 1 && i < n - 2) { j += i + 2 - n; ++i; }
+        if (j > n - 1) break;
+        uint64_t k53;
+        if (screen_pair(a, S, X, i, j, p, &k53) != 0) { pstar = p; break; }
+        j += 32;
+        p += 32;
+      }
+    }
+    pstar = __reduce_min_sync(0xffffffffu, pstar);
+    if (pstar == 0x7fffffff) continue;   // nothing collides in this cell
+    // exact data of the cell's SIPs, computed lazily from the step-start masses
+    for (int q = lane; q < n; q += 32) {
+      const int32_t id = S.sid[q];
+      a.gR[id] = a.m_w[id] + a.m_s[id];
+      a.grho[id] = a.m_s[id];
+      a.gk[id] = -1;
+    }
+    __syncwarp();
+    // pass 2: anti-diagonal schedule of the pairs from p* on
     for (int s = 1; s <= 2 * n - 3; ++s) {
       const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
       const int ihi = (s - 1) >> 1;
       for (int i = ilo + lane; i <= ihi; i += 32) {
         const int j = s - i;
         const int64_t rk = pair_rank(i, j, n);
-        // Two-sided FP32 bounds of p_crit.  The FP32 radii are within 1e-6
-        // (relative) of the exact ones, every other FP32 operation and
-        // conversion within 2^-24, the velocity difference carries an
-        // absolute slack for its cancellation; the bounds are widened by
-        // 2^-14 relative (and 1e-36 absolute).  Negative multiplicities (left
-        // by multiple collections) go to the exact path.
-        const float xa = S.fxi[i], xb = S.fxi[j];
-        const float ui = S.fu[i], uj = S.fu[j], wi = S.fw[i], wj = S.fw[j];
-        const float du = ui - uj, dw = wi - wj;
-        const float slack = 0x1p-21f * (fabsf(ui) + fabsf(uj) + fabsf(wi) + fabsf(wj));
-        const float dvm = sqrtf(du * du + dw * dw);
-        const float rs = S.fR[i] + S.fR[j];
-        const float ef = use_E ? d2f_rn(__ldg(a.E + (int64_t)S.sk[i] * a.nb + S.sk[j])) : ef_const;
-        const float core = ((fmaxf(xa, xb) * dtdv_f) * pi_e12) * rs * rs * ef;
-        const float p_hi = core * (dvm + slack) * (1.0f + 0x1p-14f) + 1e-36f;
-        const float p_lo = core * fmaxf(dvm - slack, 0.0f) * (1.0f - 0x1p-14f);
-        // the draw as a float interval [r_lo, r_hi] around the exact double
-        // (an injected draw outside [0, 1) gives an empty screen)
-        float r_lo, r_hi;
-        double r = 0.0;
+        if (rk < pstar) continue;
         uint64_t k53 = 0;
-        if (rnd) {
-          r = rnd[rk];
-          const uint64_t rb = (uint64_t)__double_as_longlong(r);
-          r_lo = rb < 0x3ff0000000000000ull ? d2f_down_pos(r) : 2.0f;
-          r_hi = rb < 0x3ff0000000000000ull ? r_lo + 0x1p-24f : -1.0f;
-        } else {
-          k53 = philox_bits53(a.seed, (uint64_t)rk, pc1);
-          r_lo = (float)(uint32_t)(k53 >> 29) * 0x1p-24f;
-          r_hi = r_lo + 0x1p-24f;
-        }
-        const bool sane = xa > 0.0f && xb > 0.0f && p_hi == p_hi && p_hi < 1.0f &&
-                          core >= 1e-30f;
-        if (sane && p_hi < r_lo) continue;   // certainly no collision
-        if (sane && p_lo > r_hi) {
-          // certainly an ordinary collection (0 < p_crit <= 1 and p_crit > r)
-          const int32_t ii = S.sid[i], jj = S.sid[j];
-          const bool lo_i = a.xi[ii] <= a.xi[jj];
-          const int32_t imin = lo_i ? ii : jj, imax = lo_i ? jj : ii;
-          ensure_exact(a, imin, Tc, use_E);
+        const int sc = screen_pair(a, S, X, i, j, rk, &k53);
+        if (sc == 0) continue;
+        if (sc == 1) {
+          certain_collection(a, wbase, i, j, Tc, use_E);
           c0 += 1;
-          collect_once(a, &S, imin, imax, lo_i ? i : j, lo_i ? j : i, Tc, use_E);
           continue;
         }
-        if (!rnd) r = (double)k53 * (1.0 / 9007199254740992.0);
-        exact_pair(a, &S, S.sid[i], S.sid[j], i, j, Tc, use_E, r, c0, c1);
+        const int o = exact_pair(a, wbase, S.sid[i], S.sid[j], i, j, Tc, use_E,
+                                 rnd ? rnd[rk] : philox_from_bits(k53));
+        c0 += o == 1;
+        c1 += o == 2;
       }
       __threadfence_block();
       __syncwarp();
@@ -618,6 +701,8 @@ cudaError_t launch_collide_cells(const lacmo_sips_t& sp, const lacmo_grid_t& g,
   a.cursor = w.cursor; a.col_step = w.col_step; a.total_pairs = w.total_pairs;
   a.no_cols = sp.no_cols; a.flags = w.flags;
   a.gR = w.colR; a.grho = w.colrho; a.gk = w.colk;
+  a.dtdv_f = (float)a.dtdv; a.lo_f = (float)a.lo; a.inv_bl_f = (float)(1.0 / a.bl);
+  a.E_const_f = (float)a.E_const;
   int blocks = nblk((a.C + CELL_WARPS - 1) / CELL_WARPS, 1);
   k_collide_cells<<<blocks, CELL_WARPS * 32, CELL_SMEM_BYTES, s>>>(a); note_launches(1);
   cudaError_t e = cudaGetLastError();

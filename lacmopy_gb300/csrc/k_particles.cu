@@ -248,6 +248,7 @@ struct PArgs {
   const float* gvf;             // [2][nx+1][nz+1] FP32 wind field
   double inv_dx, inv_dz;
   float inv_dxf, inv_dzf, dt_subf, dtg_f, dt_posf;
+  float x_minf, x_maxf, z_minf, z_capf;
 };
 
 // FP32 per-cell table of the mixed-precision path
@@ -425,7 +426,7 @@ __device__ __forceinline__ void grid_cell_update(double* gsf, double* gmp, int64
 // one thread per cell: delta_m_l as the ascending-ID fold of dm*xi over the
 // cell's SIPs (integration.py:916-936), then the grid update of the cell and
 // its mass-rate terms for the next sub-step; all lanes carry FP64 work
-__global__ void __launch_bounds__(128) k_cell_update(const int32_t* __restrict__ start,
+__global__ void __launch_bounds__(32) k_cell_update(const int32_t* __restrict__ start,
                                                      const int32_t* __restrict__ perm,
                                                      const double* __restrict__ dmxi,
                                                      double* delta_m_l, double* gsf, double* gmp,
@@ -462,10 +463,14 @@ __global__ void __launch_bounds__(128) k_cell_update(const int32_t* __restrict__
 // The Newton condensation and the drag update run in FP32 (lacmo_physics.cuh)
 // with the FP64 Newton for SIPs near the critical radius.  Per-cell sums and
 // water_removed are formed in arbitrary order.
+// Rare paths are out of line (__noinline__) so that the common path issues
+// no FP64 instruction, not even predicated off.
+__device__ __noinline__ float d2f_slow(double x) { return (float)x; }
+__device__ __noinline__ double f2d_slow(float f) { return (double)f; }
 __device__ __forceinline__ float d2f_int(double x) {
   const uint64_t b = (uint64_t)__double_as_longlong(x);
   const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
-  if (e < 897u || e > 1150u) return (float)x;   // zero, subnormal, huge, inf, nan
+  if (e - 897u > 253u) return d2f_slow(x);   // zero, subnormal, huge, inf, nan
   const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
   const uint64_t m = b & 0x000fffffffffffffull;
   const uint32_t fm = (uint32_t)(m >> 29), rem = (uint32_t)m & 0x1fffffffu;
@@ -476,29 +481,69 @@ __device__ __forceinline__ float d2f_int(double x) {
 __device__ __forceinline__ double f2d_int(float f) {
   const uint32_t b = (uint32_t)__float_as_int(f);
   const uint32_t e = (b >> 23) & 0xffu;
-  if (e == 0u || e == 255u) return (double)f;   // zero, subnormal, inf, nan
+  if (e - 1u > 253u) return f2d_slow(f);   // zero, subnormal, inf, nan
   const uint64_t r = ((uint64_t)(b & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
                      ((uint64_t)(b & 0x7fffffu) << 29);
   return __longlong_as_double((long long)r);
 }
-__global__ void __launch_bounds__(128) k_particles_mixed(PArgs a) {
+
+// removed SIP: only the relative position keeps its per-call division
+__device__ __noinline__ void mixed_inactive_rel(const PArgs& a, int64_t k, int i) {
+  a.rel[k] = a.rel[k] / a.dx - (double)i;
+  a.rel[a.n + k] = a.rel[a.n + k] / a.dz - (-1.0);
+}
+// near the critical radius: FP64 residual and Newton step
+__device__ __noinline__ double mixed_newton_fp64(const PArgs& a, int32_t c, double mw, double ms,
+                                                 double T_p) {
   const int64_t C = a.nx * a.nz;
+  CellAmb amb;
+  amb.T = T_p; amb.p = __ldg(a.gsf + C + c); amb.S = __ldg(a.gsf + 6 * C + c);
+  amb.e_s = __ldg(a.gsf + 7 * C + c); amb.K = __ldg(a.gmp + c);
+  amb.D_v = __ldg(a.gmp + C + c); amb.L_v = __ldg(a.gmp + 2 * C + c);
+  amb.sigw = __ldg(a.aux + c); amb.rhow = __ldg(a.aux + C + c);
+  amb.lap0 = __ldg(a.aux + 2 * C + c); amb.lbp0 = __ldg(a.aux + 3 * C + c);
+  amb.c1 = __ldg(a.aux + 4 * C + c); amb.c2 = __ldg(a.aux + 5 * C + c);
+  const double m_p = mw + ms;
+  const double w_s = ms / m_p;
+  const double rho64 = (a.sol == SOL_AS) ? density_AS_solution_rw(w_s, amb.rhow)
+                                         : density_NaCl_solution(w_s, T_p);
+  const double R64 = radius_from_mass(m_p, rho64);
+  const double sig64 = (a.sol == SOL_AS) ? surface_tension_AS_sw(w_s, amb.sigw)
+                                         : surface_tension_NaCl_sw(w_s, amb.sigw);
+  atomicAdd(a.nfb, 1ull);
+  return newton_full(a.sol, a.dt_sub, a.no_iter, mw, ms, w_s, R64, T_p, rho64, sig64, amb,
+                     nullptr);
+}
+__device__ __noinline__ double mixed_wrap_x(double x, double x_max) { return py_mod(x, x_max); }
+__device__ __noinline__ double mixed_cap_z(double z, double z_cap) { return np_min(z, z_cap); }
+__device__ __noinline__ bool mixed_below(double z, double z_min) { return z <= z_min; }
+__device__ __noinline__ int mixed_floor_div(double x, double d) { return (int)floor(x / d); }
+// SIP reaching the ground (integration.py:606-630)
+__device__ __noinline__ void mixed_remove(const PArgs& a, int64_t k, int i, int j, double x0,
+                                          double z0, double xik, double mw, double* z) {
+  *z = a.z_min - 0.01 * a.dz;
+  atomicAdd(a.rm_val, xik * mw);   // water_removed (FP64, any order)
+  const double rel_x = (x0 - a.x_min) / a.dx - (double)i;
+  const double rel_z = (z0 - a.z_min) / a.dz - (double)j;
+  a.rel[k] = rel_x / a.dx - (double)i;
+  a.rel[a.n + k] = rel_z / a.dz - (-1.0);
+}
+
+__global__ void __launch_bounds__(128) k_particles_mixed(const __grid_constant__ PArgs a) {
+  const int C = (int)(a.nx * a.nz);
+  const int nz = (int)a.nz;
   const GridVelF gvf{a.gvf, a.nx, a.nz};
-  const float x_maxf = (float)a.x_max, z_minf = (float)a.z_min, z_capf = (float)a.z_cap;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n;
        k += (int64_t)gridDim.x * blockDim.x) {
     const int32_t c = a.cell[k];
     const bool active = c >= 0;
-    const int64_t i = active ? (int64_t)c / a.nz : (int64_t)(-1 - c);
-    const int64_t j = active ? (int64_t)c - i * a.nz : -1;
+    const int i = active ? c / nz : -1 - c;
+    const int j = active ? c - i * nz : -1;
     double x = a.pos[k], z = a.pos[a.n + k];
-    const double T_p = __ldg(a.gsf + i * a.nz + (active ? j : a.nz - 1));
+    const double T_p = __ldg(a.gsf + (int64_t)i * nz + (active ? j : nz - 1));
     if (a.write_Tp) a.T_p[k] = T_p;
     if (!active) {
-      // removed SIPs: velocity 0, x fixed under the wrap, z below ground;
-      // only the relative position keeps its per-call division
-      a.rel[k] = a.rel[k] / a.dx - (double)i;
-      a.rel[a.n + k] = a.rel[a.n + k] / a.dz - (-1.0);
+      mixed_inactive_rel(a, k, i);
       continue;
     }
     double mw = a.m_w[k];
@@ -521,37 +566,20 @@ __global__ void __launch_bounds__(128) k_particles_mixed(PArgs a) {
                           (float)LC_PAR_SOL_DENS_NACL_4 * wsf * af.T +
                           (float)LC_PAR_SOL_DENS_NACL_5 * af.T * af.T;
     float R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * mpf / rho);
-    const float sig = af.sigw * (1.0f + (float)(a.sol == SOL_AS ? LC_PAR_SIGMA_AS
-                                                                  : LC_PAR_SIGMA_NACL) *
+    const float sig = af.sigw * (1.0f + (a.sol == SOL_AS ? (float)LC_PAR_SIGMA_AS
+                                                          : (float)LC_PAR_SIGMA_NACL) *
                                              wsf / (1.f - wsf));
     // efflorescence floor m_s (1/0.78 - 1) as an increment, in FP32
     const float d_effl = msf * (float)(LC_W_S_MAX_AS_INV - 1.0) - mwf;
     float d;
-    bool ok = newton_mixed_f(a.sol, a.dt_subf, a.no_iter, mwf, msf, wsf, R, af.T, rho, sig, af,
-                             d_effl, &d);
+    const bool ok = newton_mixed_f(a.sol, a.dt_subf, a.no_iter, mwf, msf, wsf, R, af.T, rho, sig,
+                                   af, d_effl, &d);
     double dm;
     if (ok) {
       dm = f2d_int(d);
     } else {
-      // near the critical radius: FP64 residual and step
-      CellAmb amb;
-      amb.T = T_p; amb.p = __ldg(a.gsf + C + c); amb.S = __ldg(a.gsf + 6 * C + c);
-      amb.e_s = __ldg(a.gsf + 7 * C + c); amb.K = __ldg(a.gmp + c);
-      amb.D_v = __ldg(a.gmp + C + c); amb.L_v = __ldg(a.gmp + 2 * C + c);
-      amb.sigw = __ldg(a.aux + c); amb.rhow = __ldg(a.aux + C + c);
-      amb.lap0 = __ldg(a.aux + 2 * C + c); amb.lbp0 = __ldg(a.aux + 3 * C + c);
-      amb.c1 = __ldg(a.aux + 4 * C + c); amb.c2 = __ldg(a.aux + 5 * C + c);
-      const double m_p = mw + ms;
-      const double w_s = ms / m_p;
-      const double rho64 = (a.sol == SOL_AS) ? density_AS_solution_rw(w_s, amb.rhow)
-                                             : density_NaCl_solution(w_s, T_p);
-      const double R64 = radius_from_mass(m_p, rho64);
-      const double sig64 = (a.sol == SOL_AS) ? surface_tension_AS_sw(w_s, amb.sigw)
-                                             : surface_tension_NaCl_sw(w_s, amb.sigw);
-      dm = newton_full(a.sol, a.dt_sub, a.no_iter, mw, ms, w_s, R64, T_p, rho64, sig64, amb,
-                       nullptr);
+      dm = mixed_newton_fp64(a, c, mw, ms, T_p);
       d = d2f_int(dm);
-      atomicAdd(a.nfb, 1ull);
     }
     mw += dm;
     // per-cell FP64 sum of dm * xi (executed by L2)
@@ -563,8 +591,8 @@ __global__ void __launch_bounds__(128) k_particles_mixed(PArgs a) {
                       (float)LC_PAR_RHO_AS_2) * wn + (float)LC_PAR_RHO_AS_3);
     R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * mpn / rho);
     const float xf = d2f_int(x), zf = d2f_int(z);
-    const float rxf = (xf - (float)a.x_min) * a.inv_dxf - (float)i;
-    const float rzf = (zf - (float)a.z_min) * a.inv_dzf - (float)j;
+    const float rxf = (xf - a.x_minf) * a.inv_dxf - (float)i;
+    const float rzf = (zf - a.z_minf) * a.inv_dzf - (float)j;
     float uf, wf;
     gvf.interp(i, j, rxf, rzf, uf, wf);
     const float mu_f = __ldg(a.auxf + AF_MU * C + c), rho_f = __ldg(a.auxf + AF_RHOF * C + c);
@@ -587,30 +615,25 @@ __global__ void __launch_bounds__(128) k_particles_mixed(PArgs a) {
     const float xnf = xf + a.dt_posf * un, znf = zf + a.dt_posf * wn2;
     double u = f2d_int(un), w = f2d_int(wn2);
     // periodic x / capped z: exact FP64 only when near or past a boundary
-    if (!(xnf > 1e-3f && xnf < x_maxf - 1e-3f)) x = py_mod(x, a.x_max);
-    if (!(znf < z_capf - 1e-3f)) z = np_min(z, a.z_cap);
+    if (!(xnf > 1e-3f && xnf < a.x_maxf - 1e-3f)) x = mixed_wrap_x(x, a.x_max);
+    if (!(znf < a.z_capf - 1e-3f)) z = mixed_cap_z(z, a.z_cap);
     int32_t newc;
-    if (!(znf > z_minf + 1e-3f) && z <= a.z_min) {
-      z = a.z_min - 0.01 * a.dz;
+    if (!(znf > a.z_minf + 1e-3f) && mixed_below(z, a.z_min)) {
+      mixed_remove(a, k, i, j, x0, z0, xik, mw, &z);
       u = 0.0; w = 0.0;
-      atomicAdd(a.rm_val, xik * mw);   // water_removed (FP64, any order)
-      const double rel_x = (x0 - a.x_min) / a.dx - (double)i;
-      const double rel_z = (z0 - a.z_min) / a.dz - (double)j;
-      a.rel[k] = rel_x / a.dx - (double)i;
-      a.rel[a.n + k] = rel_z / a.dz - (-1.0);
       newc = (int32_t)(-1 - i);
     } else {
       const float qx = d2f_int(x) * a.inv_dxf, qz = d2f_int(z) * a.inv_dzf;
-      int64_t ci = (int64_t)floorf(qx), cj = (int64_t)floorf(qz);
+      int ci = __float2int_rd(qx), cj = __float2int_rd(qz);
       const float fx = qx - floorf(qx), fz = qz - floorf(qz);
-      if (!(fx > 1e-4f && fx < 0.9999f)) ci = (int64_t)floor(x / a.dx);
-      if (!(fz > 1e-4f && fz < 0.9999f)) cj = (int64_t)floor(z / a.dz);
-      if (ci >= a.nx || ci < 0 || cj >= a.nz || cj < 0) {
+      if (!(fx > 1e-4f && fx < 0.9999f)) ci = mixed_floor_div(x, a.dx);
+      if (!(fz > 1e-4f && fz < 0.9999f)) cj = mixed_floor_div(z, a.dz);
+      if (ci >= a.nx || ci < 0 || cj >= nz || cj < 0) {
         atomicOr(a.flags, LACMO_FLAG_CELL_CLAMPED);
-        ci = ci < 0 ? 0 : (ci >= a.nx ? a.nx - 1 : ci);
-        cj = cj < 0 ? 0 : (cj >= a.nz ? a.nz - 1 : cj);
+        ci = ci < 0 ? 0 : (ci >= a.nx ? (int)a.nx - 1 : ci);
+        cj = cj < 0 ? 0 : (cj >= nz ? nz - 1 : cj);
       }
-      newc = (int32_t)(ci * a.nz + cj);
+      newc = (int32_t)(ci * nz + cj);
       if (a.hist) a.rank[k] = atomicAdd(a.counts + newc, 1);
     }
     a.pos[k] = x; a.pos[a.n + k] = z;
@@ -725,6 +748,23 @@ __global__ void k_relaxation(const double* f, int64_t nx, int64_t nz, const doub
   }
 }
 
+// both relaxation terms of a sub-step in one launch: r_v into out[0:nz],
+// Theta into out[nz:2nz] (integration.py:325-354)
+__global__ void k_relaxation2(const double* gsf, int64_t nx, int64_t nz, const double* prof_rv,
+                              const double* prof_th, const double* trel, double dt, double* out) {
+  const int64_t C = nx * nz;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 2 * nz;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = t < nz ? t : t - nz;
+    const double* f = gsf + (t < nz ? 4 : 2) * C;
+    const double* prof = t < nz ? prof_rv : prof_th;
+    double s = f[j];
+#pragma unroll 8
+    for (int64_t i = 1; i < nx; ++i) s += f[i * nz + j];
+    out[t] = dt * (prof[j] - s / (double)nx) / trel[j];
+  }
+}
+
 // integration.py:1483-1508 (factor 1) and 1536-1561 (factor 2, minus the
 // previous increment): advective + relaxation increments per sub-step
 __global__ void k_advection(const double* gsf, const double* flux, int64_t nx, int64_t nz,
@@ -806,7 +846,7 @@ cudaError_t launch_cells_export(const int32_t* cell, const double* pos, double* 
 }
 cudaError_t launch_cell_aux(const lacmo_grid_t& g, const Ws& w, cudaStream_t s) {
   int64_t C = g.nx * g.nz;
-  k_cell_aux<<<nblocks(C, 128), 128, 0, s>>>(g.scalar_fields, g.mat_prop, w.aux, C); note_launches(1);
+  k_cell_aux<<<nblocks(C, 32), 32, 0, s>>>(g.scalar_fields, g.mat_prop, w.aux, C); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_histogram(const int32_t* cell, int64_t n, const Ws& w, cudaStream_t s) {
@@ -872,6 +912,8 @@ cudaError_t launch_particles_mixed(const lacmo_sips_t& sp, const lacmo_grid_t& g
   a.inv_dx = 1.0 / g.dx; a.inv_dz = 1.0 / g.dz;
   a.inv_dxf = (float)(1.0 / g.dx); a.inv_dzf = (float)(1.0 / g.dz);
   a.dt_subf = (float)dt_sub; a.dtg_f = (float)(dt_sub * p.g_set); a.dt_posf = (float)dt_sub_pos;
+  a.x_minf = (float)a.x_min; a.x_maxf = (float)a.x_max; a.z_minf = (float)a.z_min;
+  a.z_capf = (float)a.z_cap;
   k_particles_mixed<<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a); note_launches(1);
   return cudaGetLastError();
 }
@@ -882,9 +924,8 @@ cudaError_t launch_wind_float(const lacmo_grid_t& g, const Ws& w, cudaStream_t s
 }
 cudaError_t launch_grid_acc(const lacmo_grid_t& g, const Ws& w, cudaStream_t s) {
   int64_t C = g.nx * g.nz;
-  k_grid_acc<<<nblocks(C, 128), 128, 0, s>>>(w.div, g.delta_m_l, g.scalar_fields, g.mat_prop,
-                                             w.aux, w.dTh, w.drv, C, g.p_ref, g.p_ref_inv,
-                                             g.volume_cell); note_launches(1);
+  k_grid_acc<<<nblocks(C, 32), 32, 0, s>>>(w.div, g.delta_m_l, g.scalar_fields, g.mat_prop, w.aux,
+                                           w.dTh, w.drv, C, g.p_ref, g.p_ref_inv, g.volume_cell); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_cell_update(const lacmo_sips_t& sp, const lacmo_grid_t& g, const Ws& w,
@@ -892,7 +933,7 @@ cudaError_t launch_cell_update(const lacmo_sips_t& sp, const lacmo_grid_t& g, co
                                cudaStream_t s) {
   (void)sp;
   int64_t C = g.nx * g.nz;
-  k_cell_update<<<nblocks(C, 128), 128, 0, s>>>(
+  k_cell_update<<<nblocks(C, 32), 32, 0, s>>>(
       w.start, w.perm, w.dmxi, g.delta_m_l, g.scalar_fields, g.mat_prop, w.aux, dTh, drv, C,
       g.p_ref, g.p_ref_inv, g.volume_cell, grid_update ? 1 : 0); note_launches(1);
   return cudaGetLastError();
@@ -900,7 +941,7 @@ cudaError_t launch_cell_update(const lacmo_sips_t& sp, const lacmo_grid_t& g, co
 cudaError_t launch_grid_only(const lacmo_grid_t& g, const double* dTh, const double* drv,
                              const double* dml, double* aux, cudaStream_t s) {
   int64_t C = g.nx * g.nz;
-  k_grid_only<<<nblocks(C, 128), 128, 0, s>>>(g.scalar_fields, g.mat_prop, aux, dTh, drv, dml, C,
+  k_grid_only<<<nblocks(C, 32), 32, 0, s>>>(g.scalar_fields, g.mat_prop, aux, dTh, drv, dml, C,
                                               g.p_ref, g.p_ref_inv, g.volume_cell); note_launches(1);
   return cudaGetLastError();
 }
@@ -911,15 +952,12 @@ cudaError_t launch_advection(const lacmo_grid_t& g, const lacmo_params_t& p, con
   const bool relax_on = p.act_relaxation && p.init_profile_r_v && p.init_profile_Theta &&
                         p.relaxation_time_profile;
   if (relax_on) {
-    k_relaxation<<<nblocks(g.nz, 128), 128, 0, s>>>(g.scalar_fields + 4 * C, g.nx, g.nz,
-                                                     p.init_profile_r_v, p.relaxation_time_profile,
-                                                     p.dt_sub, w.relax); note_launches(1);
-    k_relaxation<<<nblocks(g.nz, 128), 128, 0, s>>>(g.scalar_fields + 2 * C, g.nx, g.nz,
-                                                     p.init_profile_Theta,
-                                                     p.relaxation_time_profile, p.dt_sub,
-                                                     w.relax + g.nz); note_launches(1);
+    k_relaxation2<<<nblocks(2 * g.nz, 32), 32, 0, s>>>(g.scalar_fields, g.nx, g.nz,
+                                                        p.init_profile_r_v, p.init_profile_Theta,
+                                                        p.relaxation_time_profile, p.dt_sub,
+                                                        w.relax); note_launches(1);
   }
-  k_advection<<<nblocks(C, 128), 128, 0, s>>>(g.scalar_fields, g.mass_flux_air_dry, g.nx, g.nz,
+  k_advection<<<nblocks(C, 32), 32, 0, s>>>(g.scalar_fields, g.mass_flux_air_dry, g.nx, g.nz,
                                               g.dx, g.dz, p.dt_sub, w.relax, relax_on ? 1 : 0,
                                               w.dTh, w.drv, second ? 1 : 0); note_launches(1);
   return cudaGetLastError();

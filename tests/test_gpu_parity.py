@@ -181,6 +181,38 @@ def test_cells_full_size_bit_exact_vs_cr_oracle(oracle_cr, oracle_nb, kernel, bo
     assert diff.sum() <= max(5, n // 1000)
 
 
+@pytest.mark.parametrize("boost", [200.0, 2000.0])
+def test_cells_oversized_bit_exact_vs_cr_oracle(oracle_cr, boost):
+    """Cells above the shared-memory size (~330 SIPs) take the global-memory
+    path; mixed with ordinary cells, results == correctly-rounded oracle."""
+    from lacmopy_gb300 import collision as C
+    st = _full_state(21, nx=6, nz=5, spcm=(150, 180), kernel="Hall_Bott", drizzle_fraction=0.3,
+                     r_tot=12.5E-3)
+    # move a third of the SIPs of cell (0, 0) into (0, 1) so some cells stay small
+    cells = st["cells"].copy()
+    sel = np.flatnonzero((cells[0] == 0) & (cells[1] == 0))[::3]
+    cells[1, sel] = 1
+    draws = np.random.default_rng(5).random(oracle_cr.collision_pair_count(cells,
+                                                                           st["grid_no_cells"]))
+    outs = {}
+    for name, run in (("gpu", None), ("cr", oracle_cr)):
+        xi, mw, ms = st["xi"].copy(), st["m_w"].copy(), st["m_s"].copy()
+        nc = np.zeros(2, dtype=np.int64)
+        args = (xi, mw, ms, st["vel"], st["grid_scalar_fields"][0], cells, st["grid_no_cells"],
+                st["dt_col_over_dV"] * boost, st["E_col_grid"], st["no_kernel_bins"],
+                st["R_kernel_low_log"], st["bin_factor_R_log"], nc, "AS")
+        if run is None:
+            C.collision_step_Ecol_grid_R_all_cells_2D_multicomp_np(*args, draws=draws)
+        else:
+            run.collision_step_Ecol_grid_R_all_cells_2D_multicomp_np(*args, draws)
+        outs[name] = (xi, mw, ms, nc)
+    g, c = outs["gpu"], outs["cr"]
+    assert np.bincount(cells[0] * 5 + cells[1]).max() > 256
+    assert g[3].sum() > 0
+    for k in range(4):
+        assert np.array_equal(g[k], c[k])
+
+
 def test_philox_draws_match_oracle(oracle_cr):
     """Device Philox (performance mode) == the oracle's Philox: same collision
     outcomes bit for bit over two consecutive steps (counter advances)."""
