@@ -26,6 +26,8 @@ extern "C" {
 #endif
 
 #define LACMO_ABI_VERSION 1
+/* tables up to this many kernel bins get an FP32 copy for the pair screen */
+#define LACMO_MAX_KERNEL_BINS 512
 
 /* status codes (negative: error, nothing or part of the work done) */
 #define LACMO_OK 0
@@ -162,6 +164,34 @@ int lacmo_plan_launch(lacmo_plan* plan, void* stream);
 int lacmo_plan_destroy(lacmo_plan* plan);
 /* Kernel launches one replay of the plan performs (-1 on error). */
 int64_t lacmo_plan_kernel_nodes(const lacmo_plan* plan);
+
+/* Batched ensemble: M independent model states (members) advanced together,
+ * each kernel launch covering all members (blockIdx.y = member).  The
+ * reference runs one simulation per process (integration.py:1790-2066
+ * simulate_interval / simulate); a batch is M such simulations with the same
+ * parameters, grid shape and time step, different SIP counts and states, and
+ * Philox collision draws keyed by each member's seed.  The caller owns the
+ * member arrays and one workspace of lacmo_batch_workspace_bytes() bytes;
+ * lacmo_batch_create zeroes it, uploads the member table (synchronously) and
+ * returns a handle that refers to the caller's memory.  prms (optional, M
+ * entries) supplies each member's relaxation profiles (integration.py:
+ * 325-354 relaxes towards the member's own initial profiles); every other
+ * parameter comes from the lacmo_params_t of the stepping calls. */
+typedef struct lacmo_batch lacmo_batch;
+size_t lacmo_batch_workspace_bytes(int M, const int64_t* n, int64_t nx, int64_t nz);
+int lacmo_batch_create(int M, const lacmo_sips_t* sips, const lacmo_grid_t* grids,
+                       const lacmo_params_t* prms, const uint64_t* seeds, void* ws,
+                       size_t ws_bytes, lacmo_batch** batch);
+/* lacmo_prepare for every member */
+int lacmo_batch_prepare(lacmo_batch* batch, const lacmo_params_t* prm, void* stream);
+/* one advection step of every member (lacmo_integrate_adv_step, Philox draws) */
+int lacmo_batch_adv_step(lacmo_batch* batch, const lacmo_params_t* prm, void* stream);
+/* a CUDA graph of n_steps batch advection steps (see lacmo_plan_create) */
+int lacmo_batch_plan_create(lacmo_batch* batch, const lacmo_params_t* prm, int n_steps,
+                            void* stream, lacmo_plan** plan);
+/* member m's workspace slice, for lacmo_read_flags / lacmo_read_fallbacks */
+int lacmo_batch_member_workspace(const lacmo_batch* batch, int m, void** ws, size_t* ws_bytes);
+int lacmo_batch_destroy(lacmo_batch* batch);
 /* Phases of lacmo_integrate_adv_step, for callers that run the collision
  * steps themselves (e.g. to draw each step's uniforms from a host generator
  * exactly as the reference does):

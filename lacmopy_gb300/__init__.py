@@ -7,6 +7,6 @@ Modules mirror the reference's step functions by name and argument list:
 ``collision`` (collision/all_or_nothing.py, collision/box_model.py driver).
 ``DeviceState`` keeps a state resident on the GPU between steps.
 """
-from .device import DeviceState  # noqa: F401
+from .device import BatchState, DeviceState  # noqa: F401
 
-__all__ = ["DeviceState"]
+__all__ = ["BatchState", "DeviceState"]

@@ -79,6 +79,14 @@ PROTOTYPES = {
     "lacmo_plan_launch": (ctypes.c_int, [vp, vp]),
     "lacmo_plan_destroy": (ctypes.c_int, [vp]),
     "lacmo_plan_kernel_nodes": (i64, [vp]),
+    "lacmo_batch_workspace_bytes": (sz, [ctypes.c_int, P(i64), i64, i64]),
+    "lacmo_batch_create": (ctypes.c_int, [ctypes.c_int, P(Sips), P(Grid), P(Params), P(u64), vp,
+                                          sz, P(vp)]),
+    "lacmo_batch_prepare": (ctypes.c_int, [vp, P(Params), vp]),
+    "lacmo_batch_adv_step": (ctypes.c_int, [vp, P(Params), vp]),
+    "lacmo_batch_plan_create": (ctypes.c_int, [vp, P(Params), ctypes.c_int, vp, P(vp)]),
+    "lacmo_batch_member_workspace": (ctypes.c_int, [vp, ctypes.c_int, P(vp), P(sz)]),
+    "lacmo_batch_destroy": (ctypes.c_int, [vp]),
     "lacmo_adv_step_begin": (ctypes.c_int, [P(Sips), P(Grid), P(Params), vp, sz, vp]),
     "lacmo_adv_step_second_half": (ctypes.c_int, [P(Sips), P(Grid), P(Params), vp, sz, vp]),
     "lacmo_adv_substep": (ctypes.c_int, [P(Sips), P(Grid), P(Params), dbl, ctypes.c_int, vp, sz,

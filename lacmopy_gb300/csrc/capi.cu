@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <atomic>
+#include <vector>
 
 #include "lacmo_internal.cuh"
 
@@ -40,6 +41,7 @@ static WsPlan ws_plan(int64_t n, int64_t nx, int64_t nz) {
       4 * N,           // colk
       64,              // scalars
       4 * 2 * (size_t)((nx + 1) * (nz + 1)),  // gvf
+      4 * (size_t)LACMO_MAX_KERNEL_BINS * LACMO_MAX_KERNEL_BINS,  // Ef
   };
   WsPlan p;
   size_t o = 0;
@@ -81,6 +83,7 @@ bool ws_carve(void* base, size_t bytes, int64_t n, int64_t nx, int64_t nz, Ws* w
   w->total_pairs = (int64_t*)(sc + 24);
   w->nfb = (unsigned long long*)(sc + 32);
   w->gvf = (float*)(b + p.off[17]);
+  w->Ef = (float*)(b + p.off[18]);
   return true;
 }
 
@@ -105,84 +108,119 @@ static bool prm_ok(const lacmo_params_t* p) {
     if ((x) != cudaSuccess) return LACMO_ERR_CUDA; \
   } while (0)
 
+Member make_member(const lacmo_sips_t& sp, const lacmo_grid_t& g, const Ws& w, uint64_t seed) {
+  Member m;
+  memset(&m, 0, sizeof(m));
+  m.sp = sp; m.g = g; m.w = w; m.seed = seed;
+  m.z_cap = g.z_max * 0.999999;
+  m.inv_dx = 1.0 / g.dx; m.inv_dz = 1.0 / g.dz;
+  m.x_minf = (float)g.x_min; m.x_maxf = (float)g.x_max; m.z_minf = (float)g.z_min;
+  m.z_capf = (float)m.z_cap; m.inv_dxf = (float)m.inv_dx; m.inv_dzf = (float)m.inv_dz;
+  return m;
+}
+
+Bt single(const lacmo_sips_t& sp, const lacmo_grid_t& g, const Ws& w, uint64_t seed) {
+  Bt B;
+  B.M = 1; B.dev = nullptr; B.one = make_member(sp, g, w, seed);
+  B.n_max = sp.n; B.nx = g.nx; B.nz = g.nz;
+  return B;
+}
+
 // integration.py:1095-1294
-static int subloop(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
-                   const lacmo_draws_t& d, const Ws& w, int no_cond, int no_col, cudaStream_t s) {
-  const int64_t C = g.nx * g.nz;
+static int subloop(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d, int no_cond,
+                   int no_col, cudaStream_t s) {
   const bool col = p.act_collisions != 0;
-  if (col && no_col == 1) LCHK(launch_collide_cells(sp, g, p, d, w, s));
+  if (col && no_col == 1) LCHK(launch_collide_cells(B, p, d, s));
   for (int k = 0; k < no_cond; ++k) {
-    if (col && no_col > 1) LCHK(launch_collide_cells(sp, g, p, d, w, s));
-    LCHK(launch_particles(sp, g, p, p.dt_sub, p.dt_sub, false, w, s));
-    LCHK(launch_cell_update(sp, g, w, w.dTh, w.drv, true, s));
-    LCHK(launch_bin(sp, C, w, s));
+    if (col && no_col > 1) LCHK(launch_collide_cells(B, p, d, s));
+    LCHK(launch_particles(B, p, p.dt_sub, p.dt_sub, false, s));
+    LCHK(launch_cell_update(B, true, s));
+    LCHK(launch_bin(B, s));
   }
-  if (col && no_col > no_cond) LCHK(launch_collide_cells(sp, g, p, d, w, s));
+  if (col && no_col > no_cond) LCHK(launch_collide_cells(B, p, d, s));
   return LACMO_OK;
 }
 
 // Mixed precision sub-loop: the particle sub-steps skip the cell binning
 // unless a collision step follows before the next position update.
-static int subloop_mixed(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
-                         const lacmo_draws_t& d, const Ws& w, int no_cond, int no_col,
-                         bool bin_at_end, cudaStream_t s) {
-  const int64_t C = g.nx * g.nz;
+static int subloop_mixed(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d, int no_cond,
+                         int no_col, bool bin_at_end, cudaStream_t s) {
   const bool col = p.act_collisions != 0;
-  if (col && no_col == 1) LCHK(launch_collide_cells(sp, g, p, d, w, s));
+  if (col && no_col == 1) LCHK(launch_collide_cells(B, p, d, s));
   for (int k = 0; k < no_cond; ++k) {
-    if (col && no_col > 1) LCHK(launch_collide_cells(sp, g, p, d, w, s));
+    if (col && no_col > 1) LCHK(launch_collide_cells(B, p, d, s));
     const bool bin = (col && no_col > 1) || (k == no_cond - 1 && bin_at_end);
-    LCHK(launch_particles_mixed(sp, g, p, p.dt_sub, p.dt_sub, false, bin, w, s));
-    LCHK(launch_grid_acc(g, w, s));
-    if (bin) LCHK(launch_bin(sp, C, w, s));
+    LCHK(launch_particles_mixed(B, p, p.dt_sub, p.dt_sub, false, bin, s));
+    LCHK(launch_grid_acc(B, s));
+    if (bin) LCHK(launch_bin(B, s));
   }
-  if (col && no_col > no_cond) LCHK(launch_collide_cells(sp, g, p, d, w, s));
+  if (col && no_col > no_cond) LCHK(launch_collide_cells(B, p, d, s));
   return LACMO_OK;
 }
 
-static int adv_step_mixed(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
-                          const lacmo_draws_t& d, const Ws& w, cudaStream_t s) {
-  const int64_t C = g.nx * g.nz;
-  LCHK(launch_wind_float(g, w, s));
-  LCHK(launch_move(sp, g, p.dt_sub_half, w, s));
-  LCHK(launch_bin(sp, C, w, s));
-  LCHK(launch_advection(g, p, w, 1.0, false, s));
+static int adv_step_mixed(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d,
+                          cudaStream_t s) {
+  LCHK(launch_wind_float(B, s));
+  LCHK(launch_move(B, p.dt_sub_half, s));
+  LCHK(launch_bin(B, s));
+  LCHK(launch_advection(B, p, false, s));
   const int nc1 = p.no_col_per_adv == 1 ? 0 : (p.no_col_per_adv == 2 ? 1 : p.scale_dt_cond);
   const int nc2 = (p.no_col_per_adv == 1 || p.no_col_per_adv == 2) ? 1 : p.scale_dt_cond;
-  int rc = subloop_mixed(sp, g, p, d, w, p.scale_dt_cond, nc1, p.act_collisions && nc2 >= 1, s);
+  int rc = subloop_mixed(B, p, d, p.scale_dt_cond, nc1, p.act_collisions && nc2 >= 1, s);
   if (rc) return rc;
-  LCHK(launch_advection(g, p, w, 2.0, true, s));
-  rc = subloop_mixed(sp, g, p, d, w, p.scale_dt_cond - 1, nc2, false, s);
+  LCHK(launch_advection(B, p, true, s));
+  rc = subloop_mixed(B, p, d, p.scale_dt_cond - 1, nc2, false, s);
   if (rc) return rc;
   // last sub-step; the binning afterwards keeps it valid for the entry points
   // that use it between advection steps
-  LCHK(launch_particles_mixed(sp, g, p, p.dt_sub, p.dt_sub_half, true, true, w, s));
-  LCHK(launch_grid_acc(g, w, s));
-  LCHK(launch_bin(sp, C, w, s));
+  LCHK(launch_particles_mixed(B, p, p.dt_sub, p.dt_sub_half, true, true, s));
+  LCHK(launch_grid_acc(B, s));
+  LCHK(launch_bin(B, s));
   return LACMO_OK;
 }
 
-static int adv_step(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
-                    const lacmo_draws_t& d, const Ws& w, cudaStream_t s) {
-  if (p.precision == LACMO_PRECISION_MIXED) return adv_step_mixed(sp, g, p, d, w, s);
-  const int64_t C = g.nx * g.nz;
+static int adv_step(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d, cudaStream_t s) {
+  if (p.precision == LACMO_PRECISION_MIXED) return adv_step_mixed(B, p, d, s);
   // b) x_{n+1/2} (integration.py:1474-1481)
-  LCHK(launch_move(sp, g, p.dt_sub_half, w, s));
-  LCHK(launch_bin(sp, C, w, s));
+  LCHK(launch_move(B, p.dt_sub_half, s));
+  LCHK(launch_bin(B, s));
   // c) advective increments (+ relaxation)
-  LCHK(launch_advection(g, p, w, 1.0, false, s));
+  LCHK(launch_advection(B, p, false, s));
   int no_col = p.no_col_per_adv == 1 ? 0 : (p.no_col_per_adv == 2 ? 1 : p.scale_dt_cond);
-  int rc = subloop(sp, g, p, d, w, p.scale_dt_cond, no_col, s);
+  int rc = subloop(B, p, d, p.scale_dt_cond, no_col, s);
   if (rc) return rc;
   // e) second-half increments
-  LCHK(launch_advection(g, p, w, 2.0, true, s));
+  LCHK(launch_advection(B, p, true, s));
   no_col = (p.no_col_per_adv == 1 || p.no_col_per_adv == 2) ? 1 : p.scale_dt_cond;
-  rc = subloop(sp, g, p, d, w, p.scale_dt_cond - 1, no_col, s);
+  rc = subloop(B, p, d, p.scale_dt_cond - 1, no_col, s);
   if (rc) return rc;
   // last sub-step: positions move by dt_sub/2 (integration.py:1593-1610)
-  LCHK(launch_particles(sp, g, p, p.dt_sub, p.dt_sub_half, true, w, s));
-  LCHK(launch_cell_update(sp, g, w, w.dTh, w.drv, true, s));
-  LCHK(launch_bin(sp, C, w, s));
+  LCHK(launch_particles(B, p, p.dt_sub, p.dt_sub_half, true, s));
+  LCHK(launch_cell_update(B, true, s));
+  LCHK(launch_bin(B, s));
+  return LACMO_OK;
+}
+
+// capture n_steps advection steps of B into an executable graph
+static int capture_plan(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d, int n_steps,
+                        cudaStream_t s, cudaGraph_t* graph_out, cudaGraphExec_t* exec_out) {
+  if (s == nullptr) return LACMO_ERR_ARG;  // the legacy default stream cannot be captured
+  LCHK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int rc = LACMO_OK;
+  for (int k = 0; k < n_steps && rc == LACMO_OK; ++k) rc = adv_step(B, p, d, s);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &graph);
+  if (rc != LACMO_OK || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc != LACMO_OK ? rc : LACMO_ERR_CUDA;
+  }
+  cudaGraphExec_t exec = nullptr;
+  if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return LACMO_ERR_CUDA;
+  }
+  *graph_out = graph;
+  *exec_out = exec;
   return LACMO_OK;
 }
 
@@ -201,7 +239,8 @@ int lacmo_particles_only(const lacmo_sips_t* sp, const lacmo_grid_t* g, const la
   if (!sips_ok(sp) || !grid_ok(g) || !prm_ok(p)) return LACMO_ERR_ARG;
   Ws w;
   if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
-  LCHK(launch_particles(*sp, *g, *p, dt_sub, dt_sub_pos, true, w, (cudaStream_t)stream));
+  LCHK(launch_particles(single(*sp, *g, w, 0), *p, dt_sub, dt_sub_pos, true,
+                        (cudaStream_t)stream));
   return LACMO_OK;
 }
 
@@ -209,7 +248,7 @@ int lacmo_bin(const lacmo_sips_t* sp, const lacmo_grid_t* g, void* ws, size_t by
   if (!sips_ok(sp) || !grid_ok(g)) return LACMO_ERR_ARG;
   Ws w;
   if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
-  LCHK(launch_bin(*sp, g->nx * g->nz, w, (cudaStream_t)stream));
+  LCHK(launch_bin(single(*sp, *g, w, 0), (cudaStream_t)stream));
   return LACMO_OK;
 }
 
@@ -278,9 +317,10 @@ int lacmo_prepare(const lacmo_sips_t* sp, const lacmo_grid_t* g, const lacmo_par
   Ws w;
   if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  LCHK(launch_cell_aux(*g, w, s));
-  LCHK(launch_histogram(sp->cell, sp->n, w, s));
-  LCHK(launch_bin(*sp, g->nx * g->nz, w, s));
+  const Bt B = single(*sp, *g, w, 0);
+  LCHK(launch_cell_aux(B, s));
+  LCHK(launch_histogram(B, s));
+  LCHK(launch_bin(B, s));
   return LACMO_OK;
 }
 
@@ -291,7 +331,7 @@ int lacmo_integrate_adv_step(const lacmo_sips_t* sp, const lacmo_grid_t* g,
   if (d->draws && d->n_draws < 0) return LACMO_ERR_ARG;
   Ws w;
   if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
-  return adv_step(*sp, *g, *p, *d, w, (cudaStream_t)stream);
+  return adv_step(single(*sp, *g, w, d->seed), *p, *d, (cudaStream_t)stream);
 }
 
 int lacmo_adv_step_begin(const lacmo_sips_t* sp, const lacmo_grid_t* g, const lacmo_params_t* p,
@@ -300,9 +340,10 @@ int lacmo_adv_step_begin(const lacmo_sips_t* sp, const lacmo_grid_t* g, const la
   Ws w;
   if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  LCHK(launch_move(*sp, *g, p->dt_sub_half, w, s));
-  LCHK(launch_bin(*sp, g->nx * g->nz, w, s));
-  LCHK(launch_advection(*g, *p, w, 1.0, false, s));
+  const Bt B = single(*sp, *g, w, 0);
+  LCHK(launch_move(B, p->dt_sub_half, s));
+  LCHK(launch_bin(B, s));
+  LCHK(launch_advection(B, *p, false, s));
   return LACMO_OK;
 }
 
@@ -311,7 +352,7 @@ int lacmo_adv_step_second_half(const lacmo_sips_t* sp, const lacmo_grid_t* g,
   if (!sips_ok(sp) || !grid_ok(g) || !prm_ok(p)) return LACMO_ERR_ARG;
   Ws w;
   if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
-  LCHK(launch_advection(*g, *p, w, 2.0, true, (cudaStream_t)stream));
+  LCHK(launch_advection(single(*sp, *g, w, 0), *p, true, (cudaStream_t)stream));
   return LACMO_OK;
 }
 
@@ -321,9 +362,10 @@ int lacmo_adv_substep(const lacmo_sips_t* sp, const lacmo_grid_t* g, const lacmo
   Ws w;
   if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  LCHK(launch_particles(*sp, *g, *p, p->dt_sub, dt_sub_pos, write_T_p != 0, w, s));
-  LCHK(launch_cell_update(*sp, *g, w, w.dTh, w.drv, true, s));
-  LCHK(launch_bin(*sp, g->nx * g->nz, w, s));
+  const Bt B = single(*sp, *g, w, 0);
+  LCHK(launch_particles(B, *p, p->dt_sub, dt_sub_pos, write_T_p != 0, s));
+  LCHK(launch_cell_update(B, true, s));
+  LCHK(launch_bin(B, s));
   return LACMO_OK;
 }
 
@@ -341,22 +383,11 @@ int lacmo_plan_create(const lacmo_sips_t* sp, const lacmo_grid_t* g, const lacmo
   if (d->draws && d->n_draws < 0) return LACMO_ERR_ARG;
   Ws w;
   if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
-  cudaStream_t s = (cudaStream_t)stream;
-  if (s == nullptr) return LACMO_ERR_ARG;  // the legacy default stream cannot be captured
-  LCHK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  int rc = LACMO_OK;
-  for (int k = 0; k < n_steps && rc == LACMO_OK; ++k) rc = adv_step(*sp, *g, *p, *d, w, s);
   cudaGraph_t graph = nullptr;
-  cudaError_t e = cudaStreamEndCapture(s, &graph);
-  if (rc != LACMO_OK || e != cudaSuccess) {
-    if (graph) cudaGraphDestroy(graph);
-    return rc != LACMO_OK ? rc : LACMO_ERR_CUDA;
-  }
   cudaGraphExec_t exec = nullptr;
-  if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
-    cudaGraphDestroy(graph);
-    return LACMO_ERR_CUDA;
-  }
+  const int rc = capture_plan(single(*sp, *g, w, d->seed), *p, *d, n_steps, (cudaStream_t)stream,
+                              &graph, &exec);
+  if (rc != LACMO_OK) return rc;
   lacmo_plan* pl = new lacmo_plan{graph, exec};
   *out = pl;
   return LACMO_OK;
@@ -395,6 +426,119 @@ int lacmo_plan_destroy(lacmo_plan* pl) {
   return LACMO_OK;
 }
 
+struct lacmo_batch {
+  Bt B;
+  std::vector<Member> members;
+  std::vector<size_t> ws_off, ws_len;
+  char* ws;
+};
+
+static size_t batch_table_bytes(int M) { return al((size_t)M * sizeof(Member)); }
+
+size_t lacmo_batch_workspace_bytes(int M, const int64_t* n, int64_t nx, int64_t nz) {
+  if (M < 1 || !n || nx <= 0 || nz <= 0) return 0;
+  size_t t = batch_table_bytes(M);
+  for (int m = 0; m < M; ++m) {
+    if (n[m] <= 0) return 0;
+    t += al(ws_bytes(n[m], nx, nz));
+  }
+  return t;
+}
+
+int lacmo_batch_create(int M, const lacmo_sips_t* sips, const lacmo_grid_t* grids,
+                       const lacmo_params_t* prms, const uint64_t* seeds, void* ws, size_t bytes,
+                       lacmo_batch** out) {
+  if (!out || M < 1 || M > 65535 || !sips || !grids || !seeds || !ws) return LACMO_ERR_ARG;
+  *out = nullptr;
+  for (int m = 0; m < M; ++m) {
+    if (!sips_ok(&sips[m]) || !grid_ok(&grids[m])) return LACMO_ERR_ARG;
+    if (prms && !prm_ok(&prms[m])) return LACMO_ERR_ARG;
+    if (grids[m].nx != grids[0].nx || grids[m].nz != grids[0].nz) return LACMO_ERR_ARG;
+  }
+  const int64_t nx = grids[0].nx, nz = grids[0].nz;
+  std::vector<int64_t> ns((size_t)M);
+  for (int m = 0; m < M; ++m) ns[(size_t)m] = sips[m].n;
+  const size_t need = lacmo_batch_workspace_bytes(M, ns.data(), nx, nz);
+  if (need == 0 || bytes < need) return LACMO_ERR_WORKSPACE;
+  lacmo_batch* b = new lacmo_batch;
+  b->ws = (char*)ws;
+  b->members.resize((size_t)M);
+  size_t off = batch_table_bytes(M);
+  int64_t n_max = 0;
+  for (int m = 0; m < M; ++m) {
+    const size_t len = ws_bytes(sips[m].n, nx, nz);
+    Ws w;
+    ws_carve(b->ws + off, len, sips[m].n, nx, nz, &w);
+    Member& mb = b->members[(size_t)m];
+    mb = make_member(sips[m], grids[m], w, seeds[m]);
+    if (prms && prms[m].init_profile_r_v && prms[m].init_profile_Theta &&
+        prms[m].relaxation_time_profile) {
+      mb.prof_rv = prms[m].init_profile_r_v;
+      mb.prof_th = prms[m].init_profile_Theta;
+      mb.t_relax = prms[m].relaxation_time_profile;
+    }
+    b->ws_off.push_back(off);
+    b->ws_len.push_back(len);
+    off += al(len);
+    if (sips[m].n > n_max) n_max = sips[m].n;
+  }
+  if (cudaMemset(ws, 0, need) != cudaSuccess ||
+      cudaMemcpy(ws, b->members.data(), (size_t)M * sizeof(Member), cudaMemcpyHostToDevice) !=
+          cudaSuccess) {
+    delete b;
+    return LACMO_ERR_CUDA;
+  }
+  b->B.M = M;
+  b->B.dev = (const Member*)ws;
+  b->B.one = b->members[0];
+  b->B.n_max = n_max;
+  b->B.nx = nx;
+  b->B.nz = nz;
+  *out = b;
+  return LACMO_OK;
+}
+
+int lacmo_batch_prepare(lacmo_batch* b, const lacmo_params_t* p, void* stream) {
+  if (!b || !prm_ok(p)) return LACMO_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  LCHK(launch_cell_aux(b->B, s));
+  LCHK(launch_histogram(b->B, s));
+  LCHK(launch_bin(b->B, s));
+  return LACMO_OK;
+}
+
+int lacmo_batch_adv_step(lacmo_batch* b, const lacmo_params_t* p, void* stream) {
+  if (!b || !prm_ok(p)) return LACMO_ERR_ARG;
+  const lacmo_draws_t d = {nullptr, 0, 0};
+  return adv_step(b->B, *p, d, (cudaStream_t)stream);
+}
+
+int lacmo_batch_plan_create(lacmo_batch* b, const lacmo_params_t* p, int n_steps, void* stream,
+                            lacmo_plan** out) {
+  if (!out || n_steps < 1) return LACMO_ERR_ARG;
+  *out = nullptr;
+  if (!b || !prm_ok(p)) return LACMO_ERR_ARG;
+  const lacmo_draws_t d = {nullptr, 0, 0};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const int rc = capture_plan(b->B, *p, d, n_steps, (cudaStream_t)stream, &graph, &exec);
+  if (rc != LACMO_OK) return rc;
+  *out = new lacmo_plan{graph, exec};
+  return LACMO_OK;
+}
+
+int lacmo_batch_member_workspace(const lacmo_batch* b, int m, void** ws, size_t* bytes) {
+  if (!b || m < 0 || m >= b->B.M || !ws || !bytes) return LACMO_ERR_ARG;
+  *ws = b->ws + b->ws_off[(size_t)m];
+  *bytes = b->ws_len[(size_t)m];
+  return LACMO_OK;
+}
+
+int lacmo_batch_destroy(lacmo_batch* b) {
+  delete b;
+  return LACMO_OK;
+}
+
 int lacmo_propagate_particles_subloop_step(const lacmo_sips_t* sp, const lacmo_grid_t* g,
                                            const lacmo_params_t* p, double dt_sub,
                                            double dt_sub_pos, void* ws, size_t bytes,
@@ -403,10 +547,11 @@ int lacmo_propagate_particles_subloop_step(const lacmo_sips_t* sp, const lacmo_g
   Ws w;
   if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  LCHK(launch_cell_aux(*g, w, s));
-  LCHK(launch_particles(*sp, *g, *p, dt_sub, dt_sub_pos, true, w, s));
-  LCHK(launch_cell_update(*sp, *g, w, nullptr, nullptr, false, s));
-  LCHK(launch_bin(*sp, g->nx * g->nz, w, s));
+  const Bt B = single(*sp, *g, w, 0);
+  LCHK(launch_cell_aux(B, s));
+  LCHK(launch_particles(B, *p, dt_sub, dt_sub_pos, true, s));
+  LCHK(launch_cell_update(B, false, s));
+  LCHK(launch_bin(B, s));
   return LACMO_OK;
 }
 
@@ -438,7 +583,7 @@ int lacmo_update_grid_r_l(const lacmo_sips_t* sp, const lacmo_grid_t* g, void* w
   if (!sips_ok(sp) || !grid_ok(g)) return LACMO_ERR_ARG;
   Ws w;
   if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
-  LCHK(launch_r_l_binned(*sp, *g, w, (cudaStream_t)stream));
+  LCHK(launch_r_l_binned(single(*sp, *g, w, 0), (cudaStream_t)stream));
   return LACMO_OK;
 }
 
@@ -449,7 +594,7 @@ int lacmo_collision_step_cells(const lacmo_sips_t* sp, const lacmo_grid_t* g,
   Ws w;
   if (!ws_carve(ws, bytes, sp->n, g->nx, g->nz, &w)) return LACMO_ERR_WORKSPACE;
   if (d->draws) LCHK(cudaMemsetAsync(w.cursor, 0, 8, (cudaStream_t)stream));
-  LCHK(launch_collide_cells(*sp, *g, *p, *d, w, (cudaStream_t)stream));
+  LCHK(launch_collide_cells(single(*sp, *g, w, d->seed), *p, *d, (cudaStream_t)stream));
   return LACMO_OK;
 }
 

@@ -17,6 +17,8 @@
 // reference's consumption order or from Philox4x32-10.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "lacmo_crmath.h"
 #include "lacmo_internal.cuh"
 #include "lacmo_physics.cuh"
@@ -101,7 +103,39 @@ struct CellArgs {
   double *gR, *grho;   // per SIP: exact radius and density, or the step-start m_p, m_s
   int32_t* gk;         // per SIP: exact kernel bin, or -1 while gR/grho hold m_p, m_s
   float dtdv_f, lo_f, inv_bl_f, E_const_f;   // FP32 copies for the screen
+  const float* Ef;     // FP32 efficiency table, or null (then E is read and rounded)
 };
+
+// the parameters a collision step shares across members
+struct CellCommon {
+  double dtdv;
+  const double* E;
+  double E_const;
+  int64_t nb;
+  double lo, bl;
+  int sol;
+  const double* draws;
+  int64_t n_draws;
+  float dtdv_f, lo_f, inv_bl_f, E_const_f;
+  const float* Ef;
+};
+struct CK {
+  MRef m;
+  CellCommon cc;
+};
+__device__ __forceinline__ void make_cellargs(CellArgs& a, const Member& mb, const CellCommon& cc) {
+  a.xi = mb.sp.xi; a.m_w = mb.sp.m_w; a.m_s = mb.sp.m_s; a.vel = mb.sp.vel;
+  a.T = mb.g.scalar_fields;
+  a.start = mb.w.start; a.perm = mb.w.perm; a.draw_off = mb.w.draw_off;
+  a.n = mb.sp.n; a.C = mb.g.nx * mb.g.nz;
+  a.dtdv = cc.dtdv; a.E = cc.E; a.E_const = cc.E_const; a.nb = cc.nb; a.lo = cc.lo; a.bl = cc.bl;
+  a.sol = cc.sol; a.draws = cc.draws; a.n_draws = cc.n_draws; a.seed = mb.seed;
+  a.cursor = mb.w.cursor; a.col_step = mb.w.col_step; a.total_pairs = mb.w.total_pairs;
+  a.no_cols = mb.sp.no_cols; a.flags = mb.w.flags;
+  a.gR = mb.w.colR; a.grho = mb.w.colrho; a.gk = mb.w.colk;
+  a.dtdv_f = cc.dtdv_f; a.lo_f = cc.lo_f; a.inv_bl_f = cc.inv_bl_f; a.E_const_f = cc.E_const_f;
+  a.Ef = cc.Ef;
+}
 
 // integer-unit conversions (GB300 runs FP64 conversions on its narrow FP64
 // pipe): round to nearest even, and truncation toward zero for r >= 0
@@ -271,50 +305,46 @@ __device__ __noinline__ double philox_from_bits(uint64_t k53) {
   return (double)k53 * (1.0 / 9007199254740992.0);
 }
 
-// FP32 screen of the pair (i, j) at lexicographic rank rk: 0 = certainly no
-// collision, 1 = certainly one ordinary collection (0 < p_crit <= 1 and
-// p_crit > r), 2 = undecided (the exact FP64 evaluation decides).  Two-sided
-// bounds of p_crit: the FP32 radii are within 1e-6 (relative) of the exact
-// ones, every other FP32 operation and conversion within 2^-24, the velocity
-// difference carries an absolute slack for its cancellation, and the bounds
-// are widened by 2^-14 relative (and 1e-36 absolute).  Non-positive
-// multiplicities (left by multiple collections) are undecided.  The draw is
-// bracketed by a float interval [r_lo, r_hi]; *k53 returns the Philox bits.
-struct ScreenCtx {
-  const double* rnd;
-  uint64_t seed, pc1;
-  bool use_E;
-};
-__device__ __forceinline__ int screen_pair(const CellArgs& a, const CellSmem& S,
-                                           const ScreenCtx& x, int i, int j, int64_t rk,
-                                           uint64_t* k53out) {
+// FP32 screen of the pair (i, j): 0 = certainly no collision, 1 = certainly
+// one ordinary collection (0 < p_crit <= 1 and p_crit > r), 2 = undecided
+// (the exact FP64 evaluation decides).  Two-sided bounds of p_crit: the FP32
+// radii are within 1e-6 (relative) of the exact ones, every other FP32
+// operation and conversion within 2^-24, the velocity difference carries an
+// absolute slack for its cancellation, and the bounds are widened by 2^-14
+// relative (and 1e-36 absolute).  Non-positive multiplicities (left by
+// multiple collections) are undecided.  [r_lo, r_hi] brackets the draw.
+__device__ __forceinline__ int screen_pair(const CellArgs& a, const CellSmem& S, bool use_E, int i,
+                                           int j, float r_lo, float r_hi) {
   const float xa = S.fxi[i], xb = S.fxi[j];
   const float ui = S.fu[i], uj = S.fu[j], wi = S.fw[i], wj = S.fw[j];
   const float du = ui - uj, dw = wi - wj;
   const float slack = 0x1p-21f * (fabsf(ui) + fabsf(uj) + fabsf(wi) + fabsf(wj));
   const float dvm = sqrtf(du * du + dw * dw);
   const float rs = S.fR[i] + S.fR[j];
-  const float ef = x.use_E ? d2f_flush(__ldg(a.E + (int64_t)S.sk[i] * a.nb + S.sk[j])) : a.E_const_f;
+  float ef = a.E_const_f;
+  if (use_E) {
+    const int64_t ke = (int64_t)S.sk[i] * a.nb + S.sk[j];
+    ef = a.Ef ? __ldg(a.Ef + ke) : d2f_flush(__ldg(a.E + ke));
+  }
   const float core = ((fmaxf(xa, xb) * a.dtdv_f) * (float)(LC_PI * 1.0E-12)) * rs * rs * ef;
   const float p_hi = core * (dvm + slack) * (1.0f + 0x1p-14f) + 1e-36f;
   const float p_lo = core * fmaxf(dvm - slack, 0.0f) * (1.0f - 0x1p-14f);
-  float r_lo, r_hi;
-  if (x.rnd) {
-    // an injected draw outside [0, 1) leaves the pair undecided
-    const uint64_t rb = (uint64_t)__double_as_longlong(x.rnd[rk]);
-    const bool in01 = rb < 0x3ff0000000000000ull;
-    r_lo = in01 ? d2f_down_pos(__longlong_as_double((long long)rb)) : 2.0f;
-    r_hi = in01 ? r_lo + 0x1p-24f : -1.0f;
-  } else {
-    const uint64_t k53 = philox_bits53(x.seed, (uint64_t)rk, x.pc1);
-    *k53out = k53;
-    r_lo = (float)(uint32_t)(k53 >> 29) * 0x1p-24f;
-    r_hi = r_lo + 0x1p-24f;
-  }
   const bool sane = xa > 0.0f && xb > 0.0f && p_hi < 1.0f && core >= 1e-30f;
   if (sane && p_hi < r_lo) return 0;
   if (sane && p_lo > r_hi) return 1;
   return 2;
+}
+// draw intervals: Philox bits (exact: r - r_lo < 2^-24) or an injected draw
+// (an injected draw outside [0, 1) gives an empty interval: undecided)
+__device__ __forceinline__ void philox_interval(uint64_t k53, float& r_lo, float& r_hi) {
+  r_lo = (float)(uint32_t)(k53 >> 29) * 0x1p-24f;
+  r_hi = r_lo + 0x1p-24f;
+}
+__device__ __forceinline__ void injected_interval(double r, float& r_lo, float& r_hi) {
+  const uint64_t rb = (uint64_t)__double_as_longlong(r);
+  const bool in01 = rb < 0x3ff0000000000000ull;
+  r_lo = in01 ? d2f_down_pos(r) : 2.0f;
+  r_hi = in01 ? r_lo + 0x1p-24f : -1.0f;
 }
 
 // One warp per cell.  Shared memory holds FP32 copies of xi, R, u, w and the
@@ -328,7 +358,14 @@ __device__ __forceinline__ int screen_pair(const CellArgs& a, const CellSmem& S,
 constexpr size_t CELL_WARP_BYTES = (size_t)CELL_SMEM * (4 * 4 + 4 + 4);
 
 __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
-    k_collide_cells(const __grid_constant__ CellArgs a) {
+    k_collide_cells(const __grid_constant__ CK x) {
+  // the member's arguments, once per block (all warps of a block belong to
+  // the same member); shared memory keeps them addressable without a copy
+  // per thread
+  __shared__ CellArgs s_args;
+  if (threadIdx.x == 0) make_cellargs(s_args, x.m.get(), x.cc);
+  __syncthreads();
+  const CellArgs& a = s_args;
   extern __shared__ float fsm[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   float* wbase = (float*)((char*)fsm + (size_t)wid * CELL_WARP_BYTES);
@@ -416,18 +453,32 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
       S.sid[q] = id;
     }
     __syncwarp();
-    const ScreenCtx X{rnd, a.seed, pc1, use_E};
-    // pass 1: screen all pairs with the step-start state, lexicographic walk
+    // pass 1: screen all pairs with the step-start state.  Lane l takes the
+    // pair couples (2q, 2q + 1), q = l, l + 32, ..., in lexicographic order;
+    // one Philox block serves both pairs of a couple.
     int pstar = 0x7fffffff;
     {
-      int i = 0, j = 1 + lane, p = lane;
+      int i = 0, j = 1 + 2 * lane, p = 2 * lane;
       for (;;) {
         while (j > n - 1 && i < n - 2) { j += i + 2 - n; ++i; }
         if (j > n - 1) break;
-        uint64_t k53;
-        if (screen_pair(a, S, X, i, j, p, &k53) != 0) { pstar = p; break; }
-        j += 32;
-        p += 32;
+        // the next pair in lexicographic order (absent past the last pair)
+        int i2 = i, j2 = j + 1;
+        if (j2 > n - 1) { i2 = i + 1; j2 = i + 2; }
+        const bool has2 = i2 < n - 1;
+        float rl0, rh0, rl1, rh1;
+        if (rnd) {
+          injected_interval(rnd[p], rl0, rh0);
+          if (has2) injected_interval(rnd[p + 1], rl1, rh1);
+        } else {
+          const PhiloxBlock blk = philox_block(a.seed, (uint64_t)(p >> 1), pc1);
+          philox_interval(philox_half53(blk, false), rl0, rh0);
+          philox_interval(philox_half53(blk, true), rl1, rh1);
+        }
+        if (screen_pair(a, S, use_E, i, j, rl0, rh0) != 0) { pstar = p; break; }
+        if (has2 && screen_pair(a, S, use_E, i2, j2, rl1, rh1) != 0) { pstar = p + 1; break; }
+        j += 64;
+        p += 64;
       }
     }
     pstar = __reduce_min_sync(0xffffffffu, pstar);
@@ -449,7 +500,14 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
         const int64_t rk = pair_rank(i, j, n);
         if (rk < pstar) continue;
         uint64_t k53 = 0;
-        const int sc = screen_pair(a, S, X, i, j, rk, &k53);
+        float r_lo, r_hi;
+        if (rnd) {
+          injected_interval(rnd[rk], r_lo, r_hi);
+        } else {
+          k53 = philox_bits53(a.seed, (uint64_t)rk, pc1);
+          philox_interval(k53, r_lo, r_hi);
+        }
+        const int sc = screen_pair(a, S, use_E, i, j, r_lo, r_hi);
         if (sc == 0) continue;
         if (sc == 1) {
           certain_collection(a, wbase, i, j, Tc, use_E);
@@ -478,10 +536,10 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
   }
 }
 
-__global__ void k_col_advance(int64_t* cursor, int64_t* col_step, const int64_t* total,
-                              const uint32_t* flags, int draws) {
-  if (draws && !(*flags & LACMO_FLAG_DRAWS_SHORT)) *cursor += *total;
-  *col_step += 1;
+__global__ void k_col_advance(const __grid_constant__ MRef mr, int draws) {
+  const Ws& w = mr.get().w;
+  if (draws && !(*w.flags & LACMO_FLAG_DRAWS_SHORT)) *w.cursor += *w.total_pairs;
+  *w.col_step += 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -681,37 +739,45 @@ static inline int nblk(int64_t n, int t) {
 }
 static const size_t CELL_SMEM_BYTES = (size_t)CELL_WARPS * CELL_WARP_BYTES;
 
-cudaError_t launch_collide_cells(const lacmo_sips_t& sp, const lacmo_grid_t& g,
-                                 const lacmo_params_t& p, const lacmo_draws_t& d, const Ws& w,
-                                 cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_collide_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)CELL_SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
-  CellArgs a;
-  a.xi = sp.xi; a.m_w = sp.m_w; a.m_s = sp.m_s; a.vel = sp.vel; a.T = g.scalar_fields;
-  a.start = w.start; a.perm = w.perm; a.draw_off = w.draw_off;
-  a.n = sp.n; a.C = g.nx * g.nz; a.dtdv = p.dt_col_over_dV;
-  a.E = p.E_col_grid; a.E_const = p.E_col_const; a.nb = p.no_kernel_bins;
-  a.lo = p.R_kernel_low_log; a.bl = p.bin_factor_R_log; a.sol = p.solute;
-  a.draws = d.draws; a.n_draws = d.n_draws; a.seed = d.seed;
-  a.cursor = w.cursor; a.col_step = w.col_step; a.total_pairs = w.total_pairs;
-  a.no_cols = sp.no_cols; a.flags = w.flags;
-  a.gR = w.colR; a.grho = w.colrho; a.gk = w.colk;
-  a.dtdv_f = (float)a.dtdv; a.lo_f = (float)a.lo; a.inv_bl_f = (float)(1.0 / a.bl);
-  a.E_const_f = (float)a.E_const;
-  int blocks = nblk((a.C + CELL_WARPS - 1) / CELL_WARPS, 1);
-  k_collide_cells<<<blocks, CELL_WARPS * 32, CELL_SMEM_BYTES, s>>>(a); note_launches(1);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  k_col_advance<<<1, 1, 0, s>>>(w.cursor, w.col_step, w.total_pairs, w.flags, d.draws ? 1 : 0); note_launches(1);
-  return cudaGetLastError();
+__global__ void k_table_to_float(const double* __restrict__ E, float* __restrict__ Ef, int64_t m) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m;
+       k += (int64_t)gridDim.x * blockDim.x)
+    Ef[k] = (float)E[k];
 }
-cudaError_t launch_col_advance(const Ws& w, cudaStream_t s) {
-  k_col_advance<<<1, 1, 0, s>>>(w.cursor, w.col_step, w.total_pairs, w.flags, 0); note_launches(1);
+
+cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d,
+                                 cudaStream_t s) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  static std::atomic<uint64_t> attr_done{0};   // one bit per device
+  if (dev < 64 && !(attr_done.load() & (1ull << dev))) {
+    e = cudaFuncSetAttribute(k_collide_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)CELL_SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    attr_done.fetch_or(1ull << dev);
+  }
+  if (B.M > 1 && d.draws) return cudaErrorInvalidValue;   // batches draw from Philox
+  CellCommon cc;
+  cc.dtdv = p.dt_col_over_dV; cc.E = p.E_col_grid; cc.E_const = p.E_col_const;
+  cc.nb = p.no_kernel_bins; cc.lo = p.R_kernel_low_log; cc.bl = p.bin_factor_R_log;
+  cc.sol = p.solute; cc.draws = d.draws; cc.n_draws = d.n_draws;
+  cc.dtdv_f = (float)cc.dtdv; cc.lo_f = (float)cc.lo; cc.inv_bl_f = (float)(1.0 / cc.bl);
+  cc.E_const_f = (float)cc.E_const;
+  cc.Ef = nullptr;
+  float* Ef = B.one.w.Ef;   // member 0's slot serves the whole batch
+  if (p.E_col_grid && Ef && p.no_kernel_bins <= LACMO_MAX_KERNEL_BINS) {
+    const int64_t m = p.no_kernel_bins * p.no_kernel_bins;
+    k_table_to_float<<<nblk(m, 256), 256, 0, s>>>(p.E_col_grid, Ef, m); note_launches(1);
+    cc.Ef = Ef;
+  }
+  CK x{B.ref(), cc};
+  const int64_t C = B.nx * B.nz;
+  dim3 grid((unsigned)nblk((C + CELL_WARPS - 1) / CELL_WARPS, 1), (unsigned)B.M);
+  k_collide_cells<<<grid, CELL_WARPS * 32, CELL_SMEM_BYTES, s>>>(x); note_launches(1);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_col_advance<<<dim3(1, B.M), 1, 0, s>>>(B.ref(), d.draws ? 1 : 0); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_golovin(double* xis, double* m, int64_t n, double dtdv, int64_t* no_cols,

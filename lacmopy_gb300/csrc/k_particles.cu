@@ -72,7 +72,11 @@ __device__ __forceinline__ void write_aux(const double* gsf, const double* gmp, 
   af[9 * C + c] = (float)gmp[6 * C + c];
 }
 
-__global__ void k_cell_aux(const double* gsf, const double* gmp, double* aux, int64_t C) {
+__global__ void k_cell_aux(const __grid_constant__ MRef mr) {
+  const Member& mb = mr.get();
+  const int64_t C = mb.g.nx * mb.g.nz;
+  const double *gsf = mb.g.scalar_fields, *gmp = mb.g.mat_prop;
+  double* aux = mb.w.aux;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
        c += (int64_t)gridDim.x * blockDim.x)
     write_aux(gsf, gmp, aux, c, C);
@@ -80,8 +84,11 @@ __global__ void k_cell_aux(const double* gsf, const double* gmp, double* aux, in
 
 // ---------------------------------------------------------------------------
 // binning: histogram (arrival rank) -> scan -> scatter -> order by ID
-__global__ void k_histogram(const int32_t* __restrict__ cell, int64_t n, int32_t* counts,
-                            int32_t* rank) {
+__global__ void k_histogram(const __grid_constant__ MRef mr) {
+  const Member& mb = mr.get();
+  const int32_t* __restrict__ cell = mb.sp.cell;
+  const int64_t n = mb.sp.n;
+  int32_t *counts = mb.w.counts, *rank = mb.w.rank;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x) {
     int32_t c = cell[k];
@@ -91,10 +98,13 @@ __global__ void k_histogram(const int32_t* __restrict__ cell, int64_t n, int32_t
 
 // Single block: folds the sorted ground-removal list into water_removed, then
 // the exclusive scans of the SIP counts (slots) and pair counts (draws).
-__global__ void __launch_bounds__(1024) k_scan(int32_t* counts, int32_t* start, int64_t* draw_off,
-                                               int64_t* total_pairs, int64_t C, int32_t* rm_count,
-                                               int32_t* rm_id, double* rm_val,
-                                               double* water_removed) {
+__global__ void __launch_bounds__(1024) k_scan(const __grid_constant__ MRef mr) {
+  const Member& mb = mr.get();
+  int32_t *counts = mb.w.counts, *start = mb.w.start, *rm_count = mb.w.rm_count,
+          *rm_id = mb.w.rm_id;
+  int64_t *draw_off = mb.w.draw_off, *total_pairs = mb.w.total_pairs;
+  double *rm_val = mb.w.rm_val, *water_removed = mb.sp.water_removed;
+  const int64_t C = mb.g.nx * mb.g.nz;
   __shared__ int64_t s_slot[1024];
   __shared__ int64_t s_pair[1024];
   __shared__ int32_t s_id[2048];
@@ -175,8 +185,13 @@ __global__ void __launch_bounds__(1024) k_scan(int32_t* counts, int32_t* start, 
   if (t == blockDim.x - 1) { start[C] = (int32_t)os; draw_off[C] = op; *total_pairs = op; }
 }
 
-__global__ void k_scatter(const int32_t* __restrict__ cell, const int32_t* __restrict__ rank,
-                          const int32_t* __restrict__ start, int32_t* perm, int64_t n) {
+__global__ void k_scatter(const __grid_constant__ MRef mr) {
+  const Member& mb = mr.get();
+  const int32_t* __restrict__ cell = mb.sp.cell;
+  const int32_t* __restrict__ rank = mb.w.rank;
+  const int32_t* __restrict__ start = mb.w.start;
+  int32_t* perm = mb.w.perm;
+  const int64_t n = mb.sp.n;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x) {
     int32_t c = cell[k];
@@ -186,8 +201,11 @@ __global__ void k_scatter(const int32_t* __restrict__ cell, const int32_t* __res
 
 // one warp per cell: order the cell's slots by ascending SIP ID
 constexpr int ORDER_SMEM = 256;
-__global__ void __launch_bounds__(256) k_order(const int32_t* __restrict__ start, int32_t* perm,
-                                               int32_t* scratch, int64_t C) {
+__global__ void __launch_bounds__(256) k_order(const __grid_constant__ MRef mr) {
+  const Member& mb = mr.get();
+  const int32_t* __restrict__ start = mb.w.start;
+  int32_t *perm = mb.w.perm, *scratch = mb.w.rank;
+  const int64_t C = mb.g.nx * mb.g.nz;
   __shared__ int32_t s_ids[8][ORDER_SMEM];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int64_t c = blockIdx.x * 8LL + wid; c < C; c += (int64_t)gridDim.x * 8) {
@@ -249,7 +267,44 @@ struct PArgs {
   double inv_dx, inv_dz;
   float inv_dxf, inv_dzf, dt_subf, dtg_f, dt_posf;
   float x_minf, x_maxf, z_minf, z_capf;
+  double* water_removed;
 };
+
+// per-call scalars of a particle sub-step (common to all members)
+struct PCall {
+  double dt_sub, dt_pos, g_set;
+  int no_iter, sol, write_Tp, hist;
+  float dt_subf, dtg_f, dt_posf;
+};
+struct PK {
+  MRef m;
+  PCall c;
+};
+
+__device__ __forceinline__ PArgs make_pargs(const Member& mb, const PCall& c) {
+  PArgs a;
+  const lacmo_sips_t& sp = mb.sp;
+  const lacmo_grid_t& g = mb.g;
+  const Ws& w = mb.w;
+  a.pos = sp.pos; a.vel = sp.vel; a.m_w = sp.m_w; a.rel = sp.rel_pos; a.T_p = sp.T_p;
+  a.m_s = sp.m_s; a.xi = sp.xi; a.cell = sp.cell;
+  a.gsf = g.scalar_fields; a.gmp = g.mat_prop; a.aux = w.aux; a.gv = g.velocity;
+  a.n = sp.n; a.nx = g.nx; a.nz = g.nz;
+  a.x_min = g.x_min; a.x_max = g.x_max; a.z_min = g.z_min; a.z_cap = mb.z_cap;
+  a.dx = g.dx; a.dz = g.dz;
+  a.dt_sub = c.dt_sub; a.dt_pos = c.dt_pos; a.g_set = c.g_set;
+  a.no_iter = c.no_iter; a.sol = c.sol; a.write_Tp = c.write_Tp;
+  a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
+  a.rm_id = w.rm_id; a.rm_val = w.rm_val; a.flags = w.flags;
+  a.acc = w.div; a.hist = c.hist; a.nfb = w.nfb;
+  a.auxf = (const float*)(w.aux + 6 * g.nx * g.nz); a.gvf = w.gvf;
+  a.inv_dx = mb.inv_dx; a.inv_dz = mb.inv_dz;
+  a.inv_dxf = mb.inv_dxf; a.inv_dzf = mb.inv_dzf;
+  a.dt_subf = c.dt_subf; a.dtg_f = c.dtg_f; a.dt_posf = c.dt_posf;
+  a.x_minf = mb.x_minf; a.x_maxf = mb.x_maxf; a.z_minf = mb.z_minf; a.z_capf = mb.z_capf;
+  a.water_removed = sp.water_removed;
+  return a;
+}
 
 // FP32 per-cell table of the mixed-precision path
 enum { AF_T, AF_SM1, AF_SIGW, AF_RHOW, AF_LAP0, AF_LBP0, AF_C1, AF_C2, AF_MU, AF_RHOF, AUXF };
@@ -281,14 +336,19 @@ struct GridVelF {
   }
 };
 
-__global__ void k_to_float(const double* in, float* out, int64_t n) {
+__global__ void k_to_float(const __grid_constant__ MRef mr) {
+  const Member& mb = mr.get();
+  const double* in = mb.g.velocity;
+  float* out = mb.w.gvf;
+  const int64_t n = 2 * (mb.g.nx + 1) * (mb.g.nz + 1);
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x)
     out[k] = (float)in[k];
 }
 
 template <bool PHYS>
-__global__ void __launch_bounds__(128) k_particles(PArgs a) {
+__global__ void __launch_bounds__(128) k_particles(const __grid_constant__ PK x) {
+  const PArgs a = make_pargs(x.m.get(), x.c);
   const int64_t C = a.nx * a.nz;
   const GridVel gv{a.gv, a.nx, a.nz};
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n;
@@ -426,13 +486,17 @@ __device__ __forceinline__ void grid_cell_update(double* gsf, double* gmp, int64
 // one thread per cell: delta_m_l as the ascending-ID fold of dm*xi over the
 // cell's SIPs (integration.py:916-936), then the grid update of the cell and
 // its mass-rate terms for the next sub-step; all lanes carry FP64 work
-__global__ void __launch_bounds__(32) k_cell_update(const int32_t* __restrict__ start,
-                                                     const int32_t* __restrict__ perm,
-                                                     const double* __restrict__ dmxi,
-                                                     double* delta_m_l, double* gsf, double* gmp,
-                                                     double* aux, const double* dTh,
-                                                     const double* drv, int64_t C, double p_ref,
-                                                     double p_ref_inv, double V, int grid_update) {
+__global__ void __launch_bounds__(32) k_cell_update(const __grid_constant__ MRef mr,
+                                                     int grid_update) {
+  const Member& mb = mr.get();
+  const int32_t* __restrict__ start = mb.w.start;
+  const int32_t* __restrict__ perm = mb.w.perm;
+  const double* __restrict__ dmxi = mb.w.dmxi;
+  double *delta_m_l = mb.g.delta_m_l, *gsf = mb.g.scalar_fields, *gmp = mb.g.mat_prop,
+         *aux = mb.w.aux;
+  const double *dTh = mb.w.dTh, *drv = mb.w.drv;
+  const int64_t C = mb.g.nx * mb.g.nz;
+  const double p_ref = mb.g.p_ref, p_ref_inv = mb.g.p_ref_inv, V = mb.g.volume_cell;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
        c += (int64_t)gridDim.x * blockDim.x) {
     const int32_t b = start[c], e = start[c + 1];
@@ -488,14 +552,22 @@ __device__ __forceinline__ double f2d_int(float f) {
 }
 
 // removed SIP: only the relative position keeps its per-call division
-__device__ __noinline__ void mixed_inactive_rel(const PArgs& a, int64_t k, int i) {
-  a.rel[k] = a.rel[k] / a.dx - (double)i;
-  a.rel[a.n + k] = a.rel[a.n + k] / a.dz - (-1.0);
+__device__ __noinline__ void mixed_inactive_rel(double* rel, int64_t n, double dx, double dz,
+                                                int64_t k, int i) {
+  rel[k] = rel[k] / dx - (double)i;
+  rel[n + k] = rel[n + k] / dz - (-1.0);
 }
 // near the critical radius: FP64 residual and Newton step
-__device__ __noinline__ double mixed_newton_fp64(const PArgs& a, int32_t c, double mw, double ms,
+struct NewtonFP64 {
+  const double *gsf, *gmp, *aux;
+  int64_t C;
+  double dt_sub;
+  int sol, no_iter;
+  unsigned long long* nfb;
+};
+__device__ __noinline__ double mixed_newton_fp64(NewtonFP64 a, int32_t c, double mw, double ms,
                                                  double T_p) {
-  const int64_t C = a.nx * a.nz;
+  const int64_t C = a.C;
   CellAmb amb;
   amb.T = T_p; amb.p = __ldg(a.gsf + C + c); amb.S = __ldg(a.gsf + 6 * C + c);
   amb.e_s = __ldg(a.gsf + 7 * C + c); amb.K = __ldg(a.gmp + c);
@@ -519,17 +591,24 @@ __device__ __noinline__ double mixed_cap_z(double z, double z_cap) { return np_m
 __device__ __noinline__ bool mixed_below(double z, double z_min) { return z <= z_min; }
 __device__ __noinline__ int mixed_floor_div(double x, double d) { return (int)floor(x / d); }
 // SIP reaching the ground (integration.py:606-630)
-__device__ __noinline__ void mixed_remove(const PArgs& a, int64_t k, int i, int j, double x0,
-                                          double z0, double xik, double mw, double* z) {
-  *z = a.z_min - 0.01 * a.dz;
-  atomicAdd(a.rm_val, xik * mw);   // water_removed (FP64, any order)
+struct GroundGeo {
+  double* rel;
+  double* water_removed;
+  int64_t n;
+  double x_min, z_min, dx, dz;
+};
+__device__ __noinline__ double mixed_remove(GroundGeo a, int64_t k, int i, int j, double x0,
+                                            double z0, double xik, double mw) {
+  atomicAdd(a.water_removed, xik * mw);   // FP64, any order
   const double rel_x = (x0 - a.x_min) / a.dx - (double)i;
   const double rel_z = (z0 - a.z_min) / a.dz - (double)j;
   a.rel[k] = rel_x / a.dx - (double)i;
   a.rel[a.n + k] = rel_z / a.dz - (-1.0);
+  return a.z_min - 0.01 * a.dz;
 }
 
-__global__ void __launch_bounds__(128) k_particles_mixed(const __grid_constant__ PArgs a) {
+__global__ void __launch_bounds__(128) k_particles_mixed(const __grid_constant__ PK x) {
+  const PArgs a = make_pargs(x.m.get(), x.c);
   const int C = (int)(a.nx * a.nz);
   const int nz = (int)a.nz;
   const GridVelF gvf{a.gvf, a.nx, a.nz};
@@ -543,7 +622,7 @@ __global__ void __launch_bounds__(128) k_particles_mixed(const __grid_constant__
     const double T_p = __ldg(a.gsf + (int64_t)i * nz + (active ? j : nz - 1));
     if (a.write_Tp) a.T_p[k] = T_p;
     if (!active) {
-      mixed_inactive_rel(a, k, i);
+      mixed_inactive_rel(a.rel, a.n, a.dx, a.dz, k, i);
       continue;
     }
     double mw = a.m_w[k];
@@ -578,7 +657,9 @@ __global__ void __launch_bounds__(128) k_particles_mixed(const __grid_constant__
     if (ok) {
       dm = f2d_int(d);
     } else {
-      dm = mixed_newton_fp64(a, c, mw, ms, T_p);
+      dm = mixed_newton_fp64(NewtonFP64{a.gsf, a.gmp, a.aux, (int64_t)C, a.dt_sub, a.sol,
+                                        a.no_iter, a.nfb},
+                             c, mw, ms, T_p);
       d = d2f_int(dm);
     }
     mw += dm;
@@ -619,7 +700,8 @@ __global__ void __launch_bounds__(128) k_particles_mixed(const __grid_constant__
     if (!(znf < a.z_capf - 1e-3f)) z = mixed_cap_z(z, a.z_cap);
     int32_t newc;
     if (!(znf > a.z_minf + 1e-3f) && mixed_below(z, a.z_min)) {
-      mixed_remove(a, k, i, j, x0, z0, xik, mw, &z);
+      z = mixed_remove(GroundGeo{a.rel, a.water_removed, a.n, a.x_min, a.z_min, a.dx, a.dz}, k,
+                       i, j, x0, z0, xik, mw);
       u = 0.0; w = 0.0;
       newc = (int32_t)(-1 - i);
     } else {
@@ -644,9 +726,13 @@ __global__ void __launch_bounds__(128) k_particles_mixed(const __grid_constant__
 }
 
 // mixed precision: the grid sub-step from the per-cell FP64 sums (then zeroed)
-__global__ void k_grid_acc(double* acc, double* delta_m_l, double* gsf, double* gmp, double* aux,
-                           const double* dTh, const double* drv, int64_t C, double p_ref,
-                           double p_ref_inv, double V) {
+__global__ void k_grid_acc(const __grid_constant__ MRef mr) {
+  const Member& mb = mr.get();
+  double *acc = mb.w.div, *delta_m_l = mb.g.delta_m_l, *gsf = mb.g.scalar_fields,
+         *gmp = mb.g.mat_prop, *aux = mb.w.aux;
+  const double *dTh = mb.w.dTh, *drv = mb.w.drv;
+  const int64_t C = mb.g.nx * mb.g.nz;
+  const double p_ref = mb.g.p_ref, p_ref_inv = mb.g.p_ref_inv, V = mb.g.volume_cell;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
        c += (int64_t)gridDim.x * blockDim.x) {
     const double dml = acc[c] * 1.0E-18;
@@ -668,10 +754,14 @@ __global__ void k_grid_only(double* gsf, double* gmp, double* aux, const double*
 }
 
 // grid.py:370-412 (ascending-ID fold per cell)
-__global__ void __launch_bounds__(256) k_r_l(const int32_t* __restrict__ start,
-                                             const int32_t* __restrict__ perm,
-                                             const double* __restrict__ m_w,
-                                             const double* __restrict__ xi, double* gsf, int64_t C) {
+__global__ void __launch_bounds__(256) k_r_l(const __grid_constant__ MRef mr) {
+  const Member& mb = mr.get();
+  const int32_t* __restrict__ start = mb.w.start;
+  const int32_t* __restrict__ perm = mb.w.perm;
+  const double* __restrict__ m_w = mb.sp.m_w;
+  const double* __restrict__ xi = mb.sp.xi;
+  double* gsf = mb.g.scalar_fields;
+  const int64_t C = mb.g.nx * mb.g.nz;
   const int lane = threadIdx.x & 31;
   for (int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; c < C;
        c += ((int64_t)gridDim.x * blockDim.x) >> 5) {
@@ -750,8 +840,13 @@ __global__ void k_relaxation(const double* f, int64_t nx, int64_t nz, const doub
 
 // both relaxation terms of a sub-step in one launch: r_v into out[0:nz],
 // Theta into out[nz:2nz] (integration.py:325-354)
-__global__ void k_relaxation2(const double* gsf, int64_t nx, int64_t nz, const double* prof_rv,
-                              const double* prof_th, const double* trel, double dt, double* out) {
+__global__ void k_relaxation2(const __grid_constant__ MRef mr, const double* prof_rv,
+                              const double* prof_th, const double* trel, double dt) {
+  const Member& mb = mr.get();
+  const double* gsf = mb.g.scalar_fields;
+  const int64_t nx = mb.g.nx, nz = mb.g.nz;
+  double* out = mb.w.relax;
+  if (mb.prof_rv) { prof_rv = mb.prof_rv; prof_th = mb.prof_th; trel = mb.t_relax; }
   const int64_t C = nx * nz;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 2 * nz;
        t += (int64_t)gridDim.x * blockDim.x) {
@@ -767,9 +862,13 @@ __global__ void k_relaxation2(const double* gsf, int64_t nx, int64_t nz, const d
 
 // integration.py:1483-1508 (factor 1) and 1536-1561 (factor 2, minus the
 // previous increment): advective + relaxation increments per sub-step
-__global__ void k_advection(const double* gsf, const double* flux, int64_t nx, int64_t nz,
-                            double dx, double dz, double dt_sub, const double* relax, int relax_on,
-                            double* dTh, double* drv, int second) {
+__global__ void k_advection(const __grid_constant__ MRef mr, double dt_sub, int relax_on,
+                            int second) {
+  const Member& mb = mr.get();
+  const double *gsf = mb.g.scalar_fields, *flux = mb.g.mass_flux_air_dry, *relax = mb.w.relax;
+  const int64_t nx = mb.g.nx, nz = mb.g.nz;
+  const double dx = mb.g.dx, dz = mb.g.dz;
+  double *dTh = mb.w.dTh, *drv = mb.w.drv;
   const int64_t C = nx * nz;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
        c += (int64_t)gridDim.x * blockDim.x) {
@@ -844,98 +943,61 @@ cudaError_t launch_cells_export(const int32_t* cell, const double* pos, double* 
                                                  dx, dz); note_launches(1);
   return cudaGetLastError();
 }
-cudaError_t launch_cell_aux(const lacmo_grid_t& g, const Ws& w, cudaStream_t s) {
-  int64_t C = g.nx * g.nz;
-  k_cell_aux<<<nblocks(C, 32), 32, 0, s>>>(g.scalar_fields, g.mat_prop, w.aux, C); note_launches(1);
+static inline dim3 grid2(int64_t per_member, int t, int M, int cap = 152 * 32) {
+  return dim3((unsigned)nblocks(per_member, t, cap), (unsigned)M);
+}
+static PCall pcall(const lacmo_params_t& p, double dt_sub, double dt_pos, bool write_Tp,
+                   bool hist) {
+  PCall c;
+  c.dt_sub = dt_sub; c.dt_pos = dt_pos; c.g_set = p.g_set;
+  c.no_iter = p.no_iter_impl_mass; c.sol = p.solute; c.write_Tp = write_Tp ? 1 : 0;
+  c.hist = hist ? 1 : 0;
+  c.dt_subf = (float)dt_sub; c.dtg_f = (float)(dt_sub * p.g_set); c.dt_posf = (float)dt_pos;
+  return c;
+}
+cudaError_t launch_cell_aux(const Bt& B, cudaStream_t s) {
+  k_cell_aux<<<grid2(B.nx * B.nz, 32, B.M), 32, 0, s>>>(B.ref()); note_launches(1);
   return cudaGetLastError();
 }
-cudaError_t launch_histogram(const int32_t* cell, int64_t n, const Ws& w, cudaStream_t s) {
-  k_histogram<<<nblocks(n, 256), 256, 0, s>>>(cell, n, w.counts, w.rank); note_launches(1);
+cudaError_t launch_histogram(const Bt& B, cudaStream_t s) {
+  k_histogram<<<grid2(B.n_max, 256, B.M), 256, 0, s>>>(B.ref()); note_launches(1);
   return cudaGetLastError();
 }
-cudaError_t launch_bin(const lacmo_sips_t& sp, int64_t C, const Ws& w, cudaStream_t s) {
-  k_scan<<<1, 1024, 0, s>>>(w.counts, w.start, w.draw_off, w.total_pairs, C, w.rm_count, w.rm_id,
-                            w.rm_val, sp.water_removed); note_launches(1);
-  k_scatter<<<nblocks(sp.n, 256), 256, 0, s>>>(sp.cell, w.rank, w.start, w.perm, sp.n); note_launches(1);
-  k_order<<<nblocks(C * 32, 256, 152 * 16), 256, 0, s>>>(w.start, w.perm, w.rank, C); note_launches(1);
+cudaError_t launch_bin(const Bt& B, cudaStream_t s) {
+  const int64_t C = B.nx * B.nz;
+  k_scan<<<dim3(1, B.M), 1024, 0, s>>>(B.ref()); note_launches(1);
+  k_scatter<<<grid2(B.n_max, 256, B.M), 256, 0, s>>>(B.ref()); note_launches(1);
+  k_order<<<grid2(C * 32, 256, B.M, 152 * 16), 256, 0, s>>>(B.ref()); note_launches(1);
   return cudaGetLastError();
 }
-cudaError_t launch_particles(const lacmo_sips_t& sp, const lacmo_grid_t& g, const lacmo_params_t& p,
-                             double dt_sub, double dt_sub_pos, bool write_Tp, const Ws& w,
-                             cudaStream_t s) {
-  PArgs a;
-  a.pos = sp.pos; a.vel = sp.vel; a.m_w = sp.m_w; a.rel = sp.rel_pos; a.T_p = sp.T_p;
-  a.m_s = sp.m_s; a.xi = sp.xi; a.cell = sp.cell;
-  a.gsf = g.scalar_fields; a.gmp = g.mat_prop; a.aux = w.aux; a.gv = g.velocity;
-  a.n = sp.n; a.nx = g.nx; a.nz = g.nz;
-  a.x_min = g.x_min; a.x_max = g.x_max; a.z_min = g.z_min; a.z_cap = g.z_max * 0.999999;
-  a.dx = g.dx; a.dz = g.dz;
-  a.dt_sub = dt_sub; a.dt_pos = dt_sub_pos; a.g_set = p.g_set;
-  a.no_iter = p.no_iter_impl_mass; a.sol = p.solute; a.write_Tp = write_Tp ? 1 : 0;
-  a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
-  a.rm_id = w.rm_id; a.rm_val = w.rm_val; a.flags = w.flags;
-  k_particles<true><<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a); note_launches(1);
+cudaError_t launch_particles(const Bt& B, const lacmo_params_t& p, double dt_sub,
+                             double dt_sub_pos, bool write_Tp, cudaStream_t s) {
+  PK x{B.ref(), pcall(p, dt_sub, dt_sub_pos, write_Tp, true)};
+  k_particles<true><<<grid2(B.n_max, 128, B.M, 152 * 16), 128, 0, s>>>(x); note_launches(1);
   return cudaGetLastError();
 }
-cudaError_t launch_move(const lacmo_sips_t& sp, const lacmo_grid_t& g, double dt_pos, const Ws& w,
-                        cudaStream_t s) {
-  PArgs a;
-  a.pos = sp.pos; a.vel = sp.vel; a.m_w = sp.m_w; a.rel = sp.rel_pos; a.T_p = sp.T_p;
-  a.m_s = sp.m_s; a.xi = sp.xi; a.cell = sp.cell;
-  a.gsf = g.scalar_fields; a.gmp = g.mat_prop; a.aux = w.aux; a.gv = g.velocity;
-  a.n = sp.n; a.nx = g.nx; a.nz = g.nz;
-  a.x_min = g.x_min; a.x_max = g.x_max; a.z_min = g.z_min; a.z_cap = g.z_max * 0.999999;
-  a.dx = g.dx; a.dz = g.dz;
-  a.dt_sub = 0.0; a.dt_pos = dt_pos; a.g_set = 0.0;
-  a.no_iter = 0; a.sol = 0; a.write_Tp = 0;
-  a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
-  a.rm_id = w.rm_id; a.rm_val = w.rm_val; a.flags = w.flags;
-  k_particles<false><<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a); note_launches(1);
+cudaError_t launch_move(const Bt& B, double dt_pos, cudaStream_t s) {
+  lacmo_params_t p = {};
+  PK x{B.ref(), pcall(p, 0.0, dt_pos, false, true)};
+  k_particles<false><<<grid2(B.n_max, 128, B.M, 152 * 16), 128, 0, s>>>(x); note_launches(1);
   return cudaGetLastError();
 }
-cudaError_t launch_particles_mixed(const lacmo_sips_t& sp, const lacmo_grid_t& g,
-                                   const lacmo_params_t& p, double dt_sub, double dt_sub_pos,
-                                   bool write_Tp, bool hist, const Ws& w, cudaStream_t s) {
-  PArgs a;
-  a.pos = sp.pos; a.vel = sp.vel; a.m_w = sp.m_w; a.rel = sp.rel_pos; a.T_p = sp.T_p;
-  a.m_s = sp.m_s; a.xi = sp.xi; a.cell = sp.cell;
-  a.gsf = g.scalar_fields; a.gmp = g.mat_prop; a.aux = w.aux; a.gv = g.velocity;
-  a.n = sp.n; a.nx = g.nx; a.nz = g.nz;
-  a.x_min = g.x_min; a.x_max = g.x_max; a.z_min = g.z_min; a.z_cap = g.z_max * 0.999999;
-  a.dx = g.dx; a.dz = g.dz;
-  a.dt_sub = dt_sub; a.dt_pos = dt_sub_pos; a.g_set = p.g_set;
-  a.no_iter = p.no_iter_impl_mass; a.sol = p.solute; a.write_Tp = write_Tp ? 1 : 0;
-  a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
-  a.rm_id = w.rm_id; a.rm_val = sp.water_removed; a.flags = w.flags;
-  a.acc = w.div; a.hist = hist ? 1 : 0; a.nfb = w.nfb;
-  a.auxf = (const float*)(w.aux + 6 * g.nx * g.nz); a.gvf = w.gvf;
-  a.inv_dx = 1.0 / g.dx; a.inv_dz = 1.0 / g.dz;
-  a.inv_dxf = (float)(1.0 / g.dx); a.inv_dzf = (float)(1.0 / g.dz);
-  a.dt_subf = (float)dt_sub; a.dtg_f = (float)(dt_sub * p.g_set); a.dt_posf = (float)dt_sub_pos;
-  a.x_minf = (float)a.x_min; a.x_maxf = (float)a.x_max; a.z_minf = (float)a.z_min;
-  a.z_capf = (float)a.z_cap;
-  k_particles_mixed<<<nblocks(sp.n, 128, 152 * 16), 128, 0, s>>>(a); note_launches(1);
+cudaError_t launch_particles_mixed(const Bt& B, const lacmo_params_t& p, double dt_sub,
+                                   double dt_sub_pos, bool write_Tp, bool hist, cudaStream_t s) {
+  PK x{B.ref(), pcall(p, dt_sub, dt_sub_pos, write_Tp, hist)};
+  k_particles_mixed<<<grid2(B.n_max, 128, B.M, 152 * 16), 128, 0, s>>>(x); note_launches(1);
   return cudaGetLastError();
 }
-cudaError_t launch_wind_float(const lacmo_grid_t& g, const Ws& w, cudaStream_t s) {
-  const int64_t m = 2 * (g.nx + 1) * (g.nz + 1);
-  k_to_float<<<nblocks(m, 256), 256, 0, s>>>(g.velocity, w.gvf, m); note_launches(1);
+cudaError_t launch_wind_float(const Bt& B, cudaStream_t s) {
+  k_to_float<<<grid2(2 * (B.nx + 1) * (B.nz + 1), 256, B.M), 256, 0, s>>>(B.ref()); note_launches(1);
   return cudaGetLastError();
 }
-cudaError_t launch_grid_acc(const lacmo_grid_t& g, const Ws& w, cudaStream_t s) {
-  int64_t C = g.nx * g.nz;
-  k_grid_acc<<<nblocks(C, 32), 32, 0, s>>>(w.div, g.delta_m_l, g.scalar_fields, g.mat_prop, w.aux,
-                                           w.dTh, w.drv, C, g.p_ref, g.p_ref_inv, g.volume_cell); note_launches(1);
+cudaError_t launch_grid_acc(const Bt& B, cudaStream_t s) {
+  k_grid_acc<<<grid2(B.nx * B.nz, 32, B.M), 32, 0, s>>>(B.ref()); note_launches(1);
   return cudaGetLastError();
 }
-cudaError_t launch_cell_update(const lacmo_sips_t& sp, const lacmo_grid_t& g, const Ws& w,
-                               const double* dTh, const double* drv, bool grid_update,
-                               cudaStream_t s) {
-  (void)sp;
-  int64_t C = g.nx * g.nz;
-  k_cell_update<<<nblocks(C, 32), 32, 0, s>>>(
-      w.start, w.perm, w.dmxi, g.delta_m_l, g.scalar_fields, g.mat_prop, w.aux, dTh, drv, C,
-      g.p_ref, g.p_ref_inv, g.volume_cell, grid_update ? 1 : 0); note_launches(1);
+cudaError_t launch_cell_update(const Bt& B, bool grid_update, cudaStream_t s) {
+  k_cell_update<<<grid2(B.nx * B.nz, 32, B.M), 32, 0, s>>>(B.ref(), grid_update ? 1 : 0); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_grid_only(const lacmo_grid_t& g, const double* dTh, const double* drv,
@@ -945,21 +1007,16 @@ cudaError_t launch_grid_only(const lacmo_grid_t& g, const double* dTh, const dou
                                               g.p_ref, g.p_ref_inv, g.volume_cell); note_launches(1);
   return cudaGetLastError();
 }
-cudaError_t launch_advection(const lacmo_grid_t& g, const lacmo_params_t& p, const Ws& w,
-                             double factor, bool second, cudaStream_t s) {
-  (void)factor;
-  int64_t C = g.nx * g.nz;
+cudaError_t launch_advection(const Bt& B, const lacmo_params_t& p, bool second, cudaStream_t s) {
   const bool relax_on = p.act_relaxation && p.init_profile_r_v && p.init_profile_Theta &&
                         p.relaxation_time_profile;
   if (relax_on) {
-    k_relaxation2<<<nblocks(2 * g.nz, 32), 32, 0, s>>>(g.scalar_fields, g.nx, g.nz,
-                                                        p.init_profile_r_v, p.init_profile_Theta,
-                                                        p.relaxation_time_profile, p.dt_sub,
-                                                        w.relax); note_launches(1);
+    k_relaxation2<<<grid2(2 * B.nz, 32, B.M), 32, 0, s>>>(B.ref(), p.init_profile_r_v,
+                                                           p.init_profile_Theta,
+                                                           p.relaxation_time_profile, p.dt_sub); note_launches(1);
   }
-  k_advection<<<nblocks(C, 32), 32, 0, s>>>(g.scalar_fields, g.mass_flux_air_dry, g.nx, g.nz,
-                                              g.dx, g.dz, p.dt_sub, w.relax, relax_on ? 1 : 0,
-                                              w.dTh, w.drv, second ? 1 : 0); note_launches(1);
+  k_advection<<<grid2(B.nx * B.nz, 32, B.M), 32, 0, s>>>(B.ref(), p.dt_sub, relax_on ? 1 : 0,
+                                                          second ? 1 : 0); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_divergence(const double* f, const double* flux, int64_t nx, int64_t nz,
@@ -972,11 +1029,8 @@ cudaError_t launch_relaxation(const double* f, int64_t nx, int64_t nz, const dou
   k_relaxation<<<nblocks(nz, 128), 128, 0, s>>>(f, nx, nz, prof, trel, dt, out); note_launches(1);
   return cudaGetLastError();
 }
-cudaError_t launch_r_l_binned(const lacmo_sips_t& sp, const lacmo_grid_t& g, const Ws& w,
-                              cudaStream_t s) {
-  int64_t C = g.nx * g.nz;
-  k_r_l<<<nblocks(C * 32, 256, 152 * 16), 256, 0, s>>>(w.start, w.perm, sp.m_w, sp.xi,
-                                                       g.scalar_fields, C); note_launches(1);
+cudaError_t launch_r_l_binned(const Bt& B, cudaStream_t s) {
+  k_r_l<<<grid2(B.nx * B.nz * 32, 256, B.M, 152 * 16), 256, 0, s>>>(B.ref()); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_mass_rate(int sol, int64_t n, const InPtrs& in, double* g, double* dg,

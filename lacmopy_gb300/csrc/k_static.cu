@@ -121,8 +121,9 @@ extern "C" int lacmo_collision_step_cells_noalloc(double* xi, double* m_w, doubl
                                                          (int64_t)step);
   note_launches(1);
   if (cudaGetLastError() != cudaSuccess) return LACMO_ERR_CUDA;
-  if (launch_histogram(cell, n, w, s) != cudaSuccess) return LACMO_ERR_CUDA;
-  if (launch_bin(sp, C, w, s) != cudaSuccess) return LACMO_ERR_CUDA;
-  if (launch_collide_cells(sp, g, *prm, *draws, w, s) != cudaSuccess) return LACMO_ERR_CUDA;
+  const Bt B = single(sp, g, w, draws->seed);
+  if (launch_histogram(B, s) != cudaSuccess) return LACMO_ERR_CUDA;
+  if (launch_bin(B, s) != cudaSuccess) return LACMO_ERR_CUDA;
+  if (launch_collide_cells(B, *prm, *draws, s) != cudaSuccess) return LACMO_ERR_CUDA;
   return LACMO_OK;
 }

@@ -51,7 +51,8 @@ class DeviceState:
     GRID_KEYS = ("grid_scalar_fields", "grid_mat_prop", "grid_velocity",
                  "grid_mass_flux_air_dry")
 
-    def __init__(self, st, device="cuda", draws="philox", seed=1001, precision="fp64"):
+    def __init__(self, st, device="cuda", draws="philox", seed=1001, precision="fp64",
+                 workspace=True):
         self.lib = _lib.load()
         self.device = device
         g = st["grid_no_cells"]
@@ -96,13 +97,16 @@ class DeviceState:
             raise ValueError(f"precision must be 'fp64' or 'mixed', got {precision!r}")
         self.precision = precision
         self.set_params(st)
+        self.draw_mode = draws if isinstance(draws, str) else "buffer"
+        self.seed = int(seed)
+        self.draw_buf = None
+        if not workspace:   # a batch member: the batch owns the workspace
+            self.ws, self.ws_bytes = None, 0
+            return
         self.ws_bytes = int(self.lib.lacmo_workspace_bytes(self.n, self.nx, self.nz))
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
         _lib.check(self.lib.lacmo_workspace_reset(_ptr(self.ws), self.ws_bytes, self.n, self.nx,
                                                   self.nz, s), "workspace_reset")
-        self.draw_mode = draws if isinstance(draws, str) else "buffer"
-        self.seed = int(seed)
-        self.draw_buf = None
         if not isinstance(draws, str):
             self.draw_buf = to_device(draws, device=dev)
         self.prepare()
@@ -321,3 +325,112 @@ class DeviceState:
                 "grid_mat_prop": self.gmp.cpu().numpy(), "delta_m_l": self.delta_m_l.cpu().numpy(),
                 "no_cols": self.no_cols.cpu().numpy(), "cells": cells.cpu().numpy(),
                 "active_ids": act.cpu().numpy().astype(bool)}
+
+
+class BatchState:
+    """A batched ensemble: M independent ``DeviceState`` members (same grid
+    shape and parameters, own SIP counts and states) advanced together, each
+    kernel launch covering every member.  Collision draws come from Philox
+    keyed by each member's seed, so member m evolves exactly like a
+    ``DeviceState(states[m], draws="philox", seed=seeds[m])`` on its own."""
+
+    def __init__(self, states, seeds, device="cuda", precision="mixed"):
+        if len(states) != len(seeds) or not states:
+            raise ValueError("one seed per member state is required")
+        self.lib = _lib.load()
+        self.members = [DeviceState(st, device=device, draws="philox", seed=int(sd),
+                                    precision=precision, workspace=False)
+                        for st, sd in zip(states, seeds)]
+        self.M = len(self.members)
+        self.params = self.members[0].params
+        self.nx, self.nz = self.members[0].nx, self.members[0].nz
+        M = self.M
+        sips = (_lib.Sips * M)(*[m.sips for m in self.members])
+        grids = (_lib.Grid * M)(*[m.grid for m in self.members])
+        prms = (_lib.Params * M)(*[m.params for m in self.members])
+        seed_arr = (ctypes.c_uint64 * M)(*[m.seed for m in self.members])
+        ns = (ctypes.c_int64 * M)(*[m.n for m in self.members])
+        self.ws_bytes = int(self.lib.lacmo_batch_workspace_bytes(M, ns, self.nx, self.nz))
+        if self.ws_bytes == 0:
+            raise _lib.LacmoError("batch_workspace_bytes: invalid member shapes")
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=device)
+        torch.cuda.current_stream().synchronize()
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.lacmo_batch_create(M, sips, grids, prms, seed_arr, _ptr(self.ws),
+                                               self.ws_bytes, ctypes.byref(h)), "batch_create")
+        self.handle = h
+        self._keep = (sips, grids, prms, seed_arr, ns)
+        self._plan_handle = None
+        _lib.check(self.lib.lacmo_batch_prepare(self.handle, ctypes.byref(self.params), _stream()),
+                   "batch_prepare")
+
+    @property
+    def n_total(self):
+        return sum(m.n for m in self.members)
+
+    def adv_step(self, n_steps=1, graph=False):
+        s = _stream()
+        if graph:
+            plan = self._plan()
+            for _ in range(n_steps):
+                _lib.check(self.lib.lacmo_plan_launch(plan, s), "plan_launch")
+            return
+        for _ in range(n_steps):
+            _lib.check(self.lib.lacmo_batch_adv_step(self.handle, ctypes.byref(self.params), s),
+                       "batch_adv_step")
+
+    def _plan(self):
+        if self._plan_handle is not None:
+            return self._plan_handle
+        cur = torch.cuda.current_stream()
+        side = torch.cuda.Stream()
+        side.wait_stream(cur)
+        handle = ctypes.c_void_p()
+        with torch.cuda.stream(side):
+            _lib.check(self.lib.lacmo_batch_plan_create(
+                self.handle, ctypes.byref(self.params), 1, ctypes.c_void_p(side.cuda_stream),
+                ctypes.byref(handle)), "batch_plan_create")
+        cur.wait_stream(side)
+        self._plan_handle = handle
+        return handle
+
+    def graph_kernel_count(self):
+        if self._plan_handle is None:
+            return 0
+        return int(self.lib.lacmo_plan_kernel_nodes(self._plan_handle))
+
+    def _member_ws(self, m):
+        ws, nb = ctypes.c_void_p(), ctypes.c_size_t()
+        _lib.check(self.lib.lacmo_batch_member_workspace(self.handle, m, ctypes.byref(ws),
+                                                         ctypes.byref(nb)), "member_workspace")
+        return ws
+
+    def fallbacks(self, m=None):
+        ms = range(self.M) if m is None else [m]
+        tot = 0
+        for k in ms:
+            f = ctypes.c_uint64(0)
+            mb = self.members[k]
+            _lib.check(self.lib.lacmo_read_fallbacks(self._member_ws(k), mb.n, mb.nx, mb.nz,
+                                                     ctypes.byref(f), _stream()), "read_fallbacks")
+            tot += int(f.value)
+        return tot
+
+    def flags(self, m):
+        f = ctypes.c_uint32(0)
+        mb = self.members[m]
+        _lib.check(self.lib.lacmo_read_flags(self._member_ws(m), mb.n, mb.nx, mb.nz,
+                                             ctypes.byref(f), _stream()), "read_flags")
+        return int(f.value)
+
+    def snapshot(self, m):
+        return self.members[m].snapshot()
+
+    def __del__(self):
+        try:
+            if getattr(self, "_plan_handle", None) is not None:
+                self.lib.lacmo_plan_destroy(self._plan_handle)
+            if getattr(self, "handle", None) is not None:
+                self.lib.lacmo_batch_destroy(self.handle)
+        except Exception:
+            pass

@@ -329,9 +329,12 @@ ORC_EXPORT void orc_update_velocity_Beard(double* vel, const double* R, int64_t 
 
 /* Philox4x32-10 (Salmon et al., SC'11) uniform double with 53 random bits;
    the same generator and counter layout as the GPU kernels use when no draw
-   buffer is given: key = seed, counter = (pair rank, collision step << 32 | cell). */
+   buffer is given: key = seed; pair rank k reads block (k >> 1, collision
+   step << 32 | cell) and takes (x0 >> 5, x1 >> 6) for even k, (x2 >> 5,
+   x3 >> 6) for odd k. */
 static uint32_t mulhi32(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a * b) >> 32); }
-static double philox_uniform(uint64_t key, uint64_t c0, uint64_t c1) {
+static double philox_uniform(uint64_t key, uint64_t k, uint64_t c1) {
+  const uint64_t c0 = k >> 1;
   uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
   uint32_t x0 = (uint32_t)c0, x1 = (uint32_t)(c0 >> 32), x2 = (uint32_t)c1, x3 = (uint32_t)(c1 >> 32);
   for (int r = 0; r < 10; ++r) {
@@ -341,8 +344,21 @@ static double philox_uniform(uint64_t key, uint64_t c0, uint64_t c1) {
     x0 = y0; x1 = y1; x2 = y2; x3 = y3;
     k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
   }
-  uint64_t a = x0 >> 5, b = x1 >> 6;
+  uint64_t a = (k & 1) ? (x2 >> 5) : (x0 >> 5), b = (k & 1) ? (x3 >> 6) : (x1 >> 6);
   return (double)(a * 67108864ull + b) * (1.0 / 9007199254740992.0);
+}
+/* the raw Philox4x32-10 block, for known-answer tests */
+ORC_EXPORT void orc_philox_block(uint64_t key, uint64_t c0, uint64_t c1, uint32_t* out) {
+  uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
+  uint32_t x0 = (uint32_t)c0, x1 = (uint32_t)(c0 >> 32), x2 = (uint32_t)c1, x3 = (uint32_t)(c1 >> 32);
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0 = mulhi32(0xD2511F53u, x0), lo0 = 0xD2511F53u * x0;
+    uint32_t hi1 = mulhi32(0xCD9E8D57u, x2), lo1 = 0xCD9E8D57u * x2;
+    uint32_t y0 = hi1 ^ x1 ^ k0, y1 = lo1, y2 = hi0 ^ x3 ^ k1, y3 = lo0;
+    x0 = y0; x1 = y1; x2 = y2; x3 = y3;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  out[0] = x0; out[1] = x1; out[2] = x2; out[3] = x3;
 }
 ORC_EXPORT void orc_philox_uniform(uint64_t key, const uint64_t* c0, const uint64_t* c1, int64_t n,
                                    double* out) {

@@ -80,6 +80,8 @@ def _lib(variant):
     lib.orc_collision_step_all_cells_2d_philox.restype = cint
     U64 = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
     lib.orc_philox_uniform.argtypes = [ctypes.c_uint64, U64, U64, i64, D]
+    lib.orc_philox_block.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                     np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")]
     lib.orc_integrate_adv_step.restype = cint
     lib.orc_set_threads.argtypes = [cint]
     lib.orc_get_threads.restype = cint
@@ -305,11 +307,20 @@ class Oracle:
             float(R_kernel_low_log or 0.0), float(bin_factor_R_log or 1.0), _c(no_cols, np.int64),
             _sol(solute_type), int(seed), _c(col_step, np.int64))
 
-    def philox_uniform(self, key, c0, c1):
-        c0 = np.ascontiguousarray(c0, dtype=np.uint64)
+    def philox_uniform(self, key, k, c1):
+        """Uniforms of pair ranks ``k`` (block k >> 1, half k & 1) under
+        counter word ``c1`` (collision step << 32 | cell)."""
+        k = np.ascontiguousarray(k, dtype=np.uint64)
         c1 = np.ascontiguousarray(c1, dtype=np.uint64)
-        out = np.empty(c0.size)
-        self.lib.orc_philox_uniform(int(key), c0, c1, c0.size, out)
+        out = np.empty(k.size)
+        self.lib.orc_philox_uniform(int(key), k, c1, k.size, out)
+        return out
+
+    def philox_block(self, key, c0, c1):
+        """The raw Philox4x32-10 output block (x0, x1, x2, x3) for key and the
+        128-bit counter (c0 low 64 bits, c1 high 64 bits)."""
+        out = np.zeros(4, dtype=np.uint32)
+        self.lib.orc_philox_block(int(key), int(c0), int(c1), out)
         return out
 
     # -- correctly-rounded routines (variant 'cr') -----------------------------
