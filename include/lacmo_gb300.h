@@ -40,6 +40,7 @@ extern "C" {
 #define LACMO_FLAG_DRAWS_SHORT 0x1u     /* a collision step skipped: draws   */
 #define LACMO_FLAG_CELL_CLAMPED 0x2u    /* x == x_max after the periodic wrap */
 #define LACMO_FLAG_NONFINITE 0x4u       /* NaN/inf met in a SIP mass         */
+#define LACMO_FLAG_CELL_TOO_BIG 0x8u    /* a cell above 65535 SIPs was not collided */
 
 #define LACMO_SOLUTE_AS 0
 #define LACMO_SOLUTE_NACL 1

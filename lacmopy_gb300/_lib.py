@@ -15,6 +15,7 @@ ERRORS = {-1: "invalid argument", -2: "CUDA runtime error", -3: "injected draw b
 FLAG_DRAWS_SHORT = 0x1
 FLAG_CELL_CLAMPED = 0x2
 FLAG_NONFINITE = 0x4
+FLAG_CELL_TOO_BIG = 0x8
 BOX_MAX_SIPS = 8192
 ECOL_BOX_MAX_SIPS = 4096
 

@@ -42,6 +42,8 @@ static WsPlan ws_plan(int64_t n, int64_t nx, int64_t nz) {
       64,              // scalars
       4 * 2 * (size_t)((nx + 1) * (nz + 1)),  // gvf
       4 * (size_t)LACMO_MAX_KERNEL_BINS * LACMO_MAX_KERNEL_BINS,  // Ef
+      4 * C,           // cell_order
+      24 * N,          // gcopy
   };
   WsPlan p;
   size_t o = 0;
@@ -84,6 +86,9 @@ bool ws_carve(void* base, size_t bytes, int64_t n, int64_t nx, int64_t nz, Ws* w
   w->nfb = (unsigned long long*)(sc + 32);
   w->gvf = (float*)(b + p.off[17]);
   w->Ef = (float*)(b + p.off[18]);
+  w->cell_order = (int32_t*)(b + p.off[19]);
+  w->cell_ctr = (int32_t*)(sc + 40);
+  w->gcopy = (float*)(b + p.off[20]);
   return true;
 }
 

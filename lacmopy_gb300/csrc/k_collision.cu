@@ -104,6 +104,9 @@ struct CellArgs {
   int32_t* gk;         // per SIP: exact kernel bin, or -1 while gR/grho hold m_p, m_s
   float dtdv_f, lo_f, inv_bl_f, E_const_f;   // FP32 copies for the screen
   const float* Ef;     // FP32 efficiency table, or null (then E is read and rounded)
+  const int32_t* cell_order;   // cells, largest first
+  int32_t* cell_ctr;           // next cell_order entry to take
+  float* gcopy;                // [6][n] FP32 copies by slot, for cells above CELL_SMEM
 };
 
 // the parameters a collision step shares across members
@@ -135,6 +138,8 @@ __device__ __forceinline__ void make_cellargs(CellArgs& a, const Member& mb, con
   a.gR = mb.w.colR; a.grho = mb.w.colrho; a.gk = mb.w.colk;
   a.dtdv_f = cc.dtdv_f; a.lo_f = cc.lo_f; a.inv_bl_f = cc.inv_bl_f; a.E_const_f = cc.E_const_f;
   a.Ef = cc.Ef;
+  a.cell_order = mb.w.cell_order; a.cell_ctr = mb.w.cell_ctr;
+  a.gcopy = mb.w.gcopy;
 }
 
 // integer-unit conversions (GB300 runs FP64 conversions on its narrow FP64
@@ -198,13 +203,15 @@ __device__ __forceinline__ void ensure_exact(const CellArgs& a, int32_t id, doub
   if (a.gk[id] < 0) compute_exact(a, id, Tc, use_E);
 }
 
-// FP32 shared-memory copies of a cell's SIPs (one warp's slice)
+// FP32 copies of a cell's SIPs: six arrays of `stride` entries from w (a
+// warp's shared-memory slice, or the cell's slots of the global scratch for
+// cells above the shared-memory size)
 struct CellSmem {
   float *fxi, *fR, *fu, *fw;
   int32_t *sk, *sid;
-  __device__ __forceinline__ explicit CellSmem(float* w)
-      : fxi(w), fR(w + CELL_SMEM), fu(w + 2 * CELL_SMEM), fw(w + 3 * CELL_SMEM),
-        sk((int32_t*)(w + 4 * CELL_SMEM)), sid((int32_t*)(w + 5 * CELL_SMEM)) {}
+  __device__ __forceinline__ CellSmem(float* w, int64_t stride)
+      : fxi(w), fR(w + stride), fu(w + 2 * stride), fw(w + 3 * stride),
+        sk((int32_t*)(w + 4 * stride)), sid((int32_t*)(w + 5 * stride)) {}
 };
 
 // One ordinary collection (p_crit <= 1 and p_crit > r) of the pair imin/imax
@@ -254,10 +261,11 @@ __device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* 
 // 553-633) in the reference's operation order, on the global arrays.  Returns
 // 0 (no collision), 1 (one collection) or 2 (multiple collection).  wsm is
 // the warp's shared-memory slice, or null (cells above its size).
-__device__ __noinline__ int exact_pair(const CellArgs& a, float* wsm, int32_t ii, int32_t jj,
-                                       int li, int lj, double Tc, bool use_E, double r) {
-  CellSmem Sm(wsm);
-  const CellSmem* S = wsm ? &Sm : nullptr;
+__device__ __noinline__ int exact_pair(const CellArgs& a, float* wsm, int64_t stride, int32_t ii,
+                                       int32_t jj, int li, int lj, double Tc, bool use_E,
+                                       double r) {
+  CellSmem Sm(wsm, stride);
+  const CellSmem* S = &Sm;
   ensure_exact(a, ii, Tc, use_E);
   ensure_exact(a, jj, Tc, use_E);
   double *XI = a.xi, *MW = a.m_w, *MS = a.m_s, *RR = a.gR;
@@ -291,9 +299,9 @@ __device__ __noinline__ int exact_pair(const CellArgs& a, float* wsm, int32_t ii
 }
 
 // A pair the FP32 bounds place certainly in an ordinary collection.
-__device__ __noinline__ void certain_collection(const CellArgs& a, float* wsm, int i, int j,
-                                                double Tc, bool use_E) {
-  CellSmem S(wsm);
+__device__ __noinline__ void certain_collection(const CellArgs& a, float* wsm, int64_t stride,
+                                                int i, int j, double Tc, bool use_E) {
+  CellSmem S(wsm, stride);
   const int32_t ii = S.sid[i], jj = S.sid[j];
   const bool lo_i = a.xi[ii] <= a.xi[jj];
   const int32_t imin = lo_i ? ii : jj, imax = lo_i ? jj : ii;
@@ -368,8 +376,7 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
   const CellArgs& a = s_args;
   extern __shared__ float fsm[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  float* wbase = (float*)((char*)fsm + (size_t)wid * CELL_WARP_BYTES);
-  const CellSmem S(wbase);
+  float* const wslice = (float*)((char*)fsm + (size_t)wid * CELL_WARP_BYTES);
   const int64_t cursor = a.draws ? *a.cursor : 0;
   if (a.draws && cursor + *a.total_pairs > a.n_draws) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.flags, LACMO_FLAG_DRAWS_SHORT);
@@ -379,41 +386,29 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
   const bool use_E = a.E != nullptr;
   const float c43 = (float)LC_FOUR_PI_OVER_THREE_INV;
   int64_t c0 = 0, c1 = 0;
-  for (int64_t c = blockIdx.x * (int64_t)CELL_WARPS + wid; c < a.C;
-       c += (int64_t)gridDim.x * CELL_WARPS) {
+  // persistent warps take the member's cells, largest first, from a counter
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(a.cell_ctr, 1);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= a.C) break;
+    const int64_t c = a.cell_order[idx];
     const int32_t b = a.start[c];
     const int n = a.start[c + 1] - b;
-    if (n < 2) continue;
+    if (n < 2) break;   // the remaining cells hold fewer than two SIPs
+    if (n > 65535) {    // pair ranks would leave 32 bits
+      if (lane == 0) atomicOr(a.flags, LACMO_FLAG_CELL_TOO_BIG);
+      continue;
+    }
     const double Tc = a.T[c];
     const double* rnd = a.draws ? a.draws + cursor + a.draw_off[c] : nullptr;
     const uint64_t pc1 = (cstep << 32) | (uint64_t)c;
     const int32_t* ids = a.perm + b;
-    if (n > CELL_SMEM) {
-      // rare oversized cell: exact evaluation of every pair on global data
-      for (int q = lane; q < n; q += 32) {
-        const int32_t id = ids[q];
-        a.gR[id] = a.m_w[id] + a.m_s[id];
-        a.grho[id] = a.m_s[id];
-        a.gk[id] = -1;
-      }
-      __syncwarp();
-      for (int s = 1; s <= 2 * n - 3; ++s) {
-        const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
-        const int ihi = (s - 1) >> 1;
-        for (int i = ilo + lane; i <= ihi; i += 32) {
-          const int j = s - i;
-          const int32_t ii = ids[i], jj = ids[j];
-          const int64_t rk = pair_rank(i, j, n);
-          const double r = rnd ? rnd[rk] : philox_uniform(a.seed, (uint64_t)rk, pc1);
-          const int o = exact_pair(a, nullptr, ii, jj, i, j, Tc, use_E, r);
-          c0 += o == 1;
-          c1 += o == 2;
-        }
-        __threadfence_block();
-        __syncwarp();
-      }
-      continue;
-    }
+    // cells above the shared-memory size keep their copies in global scratch
+    const bool big = n > CELL_SMEM;
+    float* const wbase = big ? a.gcopy + b : wslice;
+    const int64_t stride = big ? a.n : (int64_t)CELL_SMEM;
+    const CellSmem S(wbase, stride);
     const float Tf = d2f_rn(Tc);
     const float rhow_f = (float)LC_PAR_WATER_DENS_0 +
                          (float)LC_PAR_WATER_DENS_1 * ((Tf - (float)LC_PAR_WATER_DENS_2) *
@@ -510,11 +505,11 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
         const int sc = screen_pair(a, S, use_E, i, j, r_lo, r_hi);
         if (sc == 0) continue;
         if (sc == 1) {
-          certain_collection(a, wbase, i, j, Tc, use_E);
+          certain_collection(a, wbase, stride, i, j, Tc, use_E);
           c0 += 1;
           continue;
         }
-        const int o = exact_pair(a, wbase, S.sid[i], S.sid[j], i, j, Tc, use_E,
+        const int o = exact_pair(a, wbase, stride, S.sid[i], S.sid[j], i, j, Tc, use_E,
                                  rnd ? rnd[rk] : philox_from_bits(k53));
         c0 += o == 1;
         c1 += o == 2;
@@ -540,6 +535,7 @@ __global__ void k_col_advance(const __grid_constant__ MRef mr, int draws) {
   const Ws& w = mr.get().w;
   if (draws && !(*w.flags & LACMO_FLAG_DRAWS_SHORT)) *w.cursor += *w.total_pairs;
   *w.col_step += 1;
+  *w.cell_ctr = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -772,8 +768,25 @@ cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lac
     cc.Ef = Ef;
   }
   CK x{B.ref(), cc};
+  // persistent blocks: as many as are resident at once, split over members
+  static std::atomic<int> resident[64];
+  int res = dev < 64 ? resident[dev].load() : 0;
+  if (res <= 0) {
+    int per_sm = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collide_cells, CELL_WARPS * 32,
+                                                      CELL_SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    res = per_sm * sms > 0 ? per_sm * sms : 1;
+    if (dev < 64) resident[dev].store(res);
+  }
   const int64_t C = B.nx * B.nz;
-  dim3 grid((unsigned)nblk((C + CELL_WARPS - 1) / CELL_WARPS, 1), (unsigned)B.M);
+  int64_t bx = res / B.M;
+  const int64_t need = (C + CELL_WARPS - 1) / CELL_WARPS;
+  if (bx > need) bx = need;
+  if (bx < 1) bx = 1;
+  dim3 grid((unsigned)bx, (unsigned)B.M);
   k_collide_cells<<<grid, CELL_WARPS * 32, CELL_SMEM_BYTES, s>>>(x); note_launches(1);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

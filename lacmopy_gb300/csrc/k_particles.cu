@@ -183,6 +183,32 @@ __global__ void __launch_bounds__(1024) k_scan(const __grid_constant__ MRef mr) 
     counts[c] = 0;
   }
   if (t == blockDim.x - 1) { start[C] = (int32_t)os; draw_off[C] = op; *total_pairs = op; }
+  // ---- collision work order: cells by descending SIP count (a counting
+  // sort on min(count, 1023); the order inside a size class is arbitrary) ----
+  __shared__ int32_t s_hist[1024];
+  int32_t* order = mb.w.cell_order;
+  s_hist[t] = 0;
+  __syncthreads();
+  for (int64_t c = b0; c < b1; ++c) {
+    const int32_t m = start[c + 1] - start[c];
+    atomicAdd(&s_hist[1023 - (m < 1023 ? m : 1023)], 1);
+  }
+  __syncthreads();
+  const int32_t hv = s_hist[t];
+  s_slot[t] = hv;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const int64_t add = t >= off ? s_slot[t - off] : 0;
+    __syncthreads();
+    s_slot[t] += add;
+    __syncthreads();
+  }
+  s_hist[t] = (int32_t)(s_slot[t] - hv);
+  __syncthreads();
+  for (int64_t c = b0; c < b1; ++c) {
+    const int32_t m = start[c + 1] - start[c];
+    order[atomicAdd(&s_hist[1023 - (m < 1023 ? m : 1023)], 1)] = (int32_t)c;
+  }
 }
 
 __global__ void k_scatter(const __grid_constant__ MRef mr) {

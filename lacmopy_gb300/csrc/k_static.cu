@@ -34,7 +34,9 @@ constexpr size_t st_off_rank = a256(st_off_perm + 4 * STATIC_MAX_SIPS);
 constexpr size_t st_off_colR = a256(st_off_rank + 4 * STATIC_MAX_SIPS);
 constexpr size_t st_off_colrho = a256(st_off_colR + 8 * STATIC_MAX_SIPS);
 constexpr size_t st_off_colk = a256(st_off_colrho + 8 * STATIC_MAX_SIPS);
-constexpr size_t st_off_scalars = a256(st_off_colk + 4 * STATIC_MAX_SIPS);
+constexpr size_t st_off_order = a256(st_off_colk + 4 * STATIC_MAX_SIPS);
+constexpr size_t st_off_gcopy = a256(st_off_order + 4 * STATIC_MAX_CELLS);
+constexpr size_t st_off_scalars = a256(st_off_gcopy + 24 * STATIC_MAX_SIPS);
 constexpr size_t STATIC_BYTES = st_off_scalars + 256;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[STATIC_BYTES];
@@ -64,12 +66,13 @@ static cudaError_t scratch_address(void** out) {
 
 // zero the cell counters and the scalars; set the collision-step counter
 __global__ void k_static_clear(int32_t* counts, int64_t C, uint32_t* flags, int32_t* rm_count,
-                               int64_t* cursor, int64_t* col_step, int64_t* total, int64_t step) {
+                               int64_t* cursor, int64_t* col_step, int64_t* total,
+                               int32_t* cell_ctr, int64_t step) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
        c += (int64_t)gridDim.x * blockDim.x)
     counts[c] = 0;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    *flags = 0; *rm_count = 0; *cursor = 0; *col_step = step; *total = 0;
+    *flags = 0; *rm_count = 0; *cursor = 0; *col_step = step; *total = 0; *cell_ctr = 0;
   }
 }
 
@@ -101,12 +104,15 @@ extern "C" int lacmo_collision_step_cells_noalloc(double* xi, double* m_w, doubl
   w.colR = (double*)(b + st_off_colR);
   w.colrho = (double*)(b + st_off_colrho);
   w.colk = (int32_t*)(b + st_off_colk);
+  w.cell_order = (int32_t*)(b + st_off_order);
+  w.gcopy = (float*)(b + st_off_gcopy);
   char* sc = b + st_off_scalars;
   w.flags = (uint32_t*)sc;
   w.rm_count = (int32_t*)(sc + 4);
   w.cursor = (int64_t*)(sc + 8);
   w.col_step = (int64_t*)(sc + 16);
   w.total_pairs = (int64_t*)(sc + 24);
+  w.cell_ctr = (int32_t*)(sc + 40);
   cudaStream_t s = (cudaStream_t)stream;
   const int64_t C = nx * nz;
   // the entry points below read only these members of the SIP and grid state
@@ -118,7 +124,7 @@ extern "C" int lacmo_collision_step_cells_noalloc(double* xi, double* m_w, doubl
   int blocks = (int)((C + 255) / 256 < 1024 ? (C + 255) / 256 : 1024);
   k_static_clear<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(w.counts, C, w.flags, w.rm_count,
                                                          w.cursor, w.col_step, w.total_pairs,
-                                                         (int64_t)step);
+                                                         w.cell_ctr, (int64_t)step);
   note_launches(1);
   if (cudaGetLastError() != cudaSuccess) return LACMO_ERR_CUDA;
   const Bt B = single(sp, g, w, draws->seed);

@@ -35,6 +35,9 @@ struct Ws {
   unsigned long long* nfb;   // mixed precision: Newton repeats in FP64
   float* gvf;                // [2][nx+1][nz+1] FP32 copy of the wind (mixed precision)
   float* Ef;                 // [LACMO_MAX_KERNEL_BINS^2] FP32 copy of the efficiency table
+  int32_t* cell_order;       // [C]   cells by descending SIP count (collision work order)
+  int32_t* cell_ctr;         // next entry of cell_order a collision warp takes
+  float* gcopy;              // [6][n] collision FP32 copies of cells above the shared-memory size
 };
 
 size_t ws_bytes(int64_t n, int64_t nx, int64_t nz);
