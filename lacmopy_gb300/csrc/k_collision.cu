@@ -356,13 +356,9 @@ __device__ __forceinline__ void injected_interval(double r, float& r_lo, float& 
 }
 
 // One warp per cell.  Shared memory holds FP32 copies of xi, R, u, w and the
-// kernel bin (24 B per SIP with the SIP ID).  A first pass screens every pair
-// of the cell with the step-start state, lanes striding through the pairs in
-// lexicographic order.  Most cells have no pair the screen does not skip and
-// are done.  Otherwise let p* be the first such pair: every pair before p*
-// is skipped in the sequential order too (nothing changed before it), and the
-// anti-diagonal schedule runs the pairs from p* on, with the screen deciding
-// most of them and the exact FP64 evaluation the rest.
+// kernel bin (24 B per SIP with the SIP ID); the pairs are screened in
+// parallel in lexicographic order and only the events of the sequential
+// order (collections and undecided pairs) are processed one at a time.
 constexpr size_t CELL_WARP_BYTES = (size_t)CELL_SMEM * (4 * 4 + 4 + 4);
 
 __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
@@ -448,74 +444,127 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
       S.sid[q] = id;
     }
     __syncwarp();
-    // pass 1: screen all pairs with the step-start state.  Lane l takes the
-    // pair couples (2q, 2q + 1), q = l, l + 32, ..., in lexicographic order;
-    // one Philox block serves both pairs of a couple.
-    int pstar = 0x7fffffff;
-    {
-      int i = 0, j = 1 + 2 * lane, p = 2 * lane;
-      for (;;) {
-        while (j > n - 1 && i < n - 2) { j += i + 2 - n; ++i; }
-        if (j > n - 1) break;
-        // the next pair in lexicographic order (absent past the last pair)
-        int i2 = i, j2 = j + 1;
-        if (j2 > n - 1) { i2 = i + 1; j2 = i + 2; }
-        const bool has2 = i2 < n - 1;
-        float rl0, rh0, rl1, rh1;
-        if (rnd) {
-          injected_interval(rnd[p], rl0, rh0);
-          if (has2) injected_interval(rnd[p + 1], rl1, rh1);
-        } else {
-          const PhiloxBlock blk = philox_block(a.seed, (uint64_t)(p >> 1), pc1);
-          philox_interval(philox_half53(blk, false), rl0, rh0);
-          philox_interval(philox_half53(blk, true), rl1, rh1);
+    // Speculative sequential order.  From rank pos on, the lanes screen the
+    // pairs in parallel with the current state: lane l takes the couples
+    // (p0 + 2l + 64t, p0 + 2l + 64t + 1), p0 = pos rounded down to even, in
+    // lexicographic order, one Philox block per couple.  The first pair p*
+    // the screen does not skip is the next event of the sequential order:
+    // every pair before it is skipped with the very state it would see.  The
+    // lane that found p* processes it (certain collection or exact FP64
+    // evaluation), then screening resumes at p* + 1.  Most cells have no
+    // event at all.  A cell with many events finishes with the anti-diagonal
+    // schedule from its current position.
+    const int P = (int)((int64_t)n * (n - 1) / 2);
+    const int event_limit = 16 + P / 64;
+    int pos = 0;           // first rank not processed yet
+    int bi = 0, bj = 1;    // the pair of rank pos & ~1
+    int events = 0;
+    bool diagonal = false;
+    for (;;) {
+      int my_p = 0x7fffffff, my_i = 0, my_j = 0, my_sc = 0;
+      uint64_t my_k53 = 0;
+      {
+        int i = bi, j = bj + 2 * lane, p = (pos & ~1) + 2 * lane;
+        for (;;) {
+          while (j > n - 1 && i < n - 2) { j += i + 2 - n; ++i; }
+          if (j > n - 1) break;
+          // the next pair in lexicographic order (absent past the last pair)
+          int i2 = i, j2 = j + 1;
+          if (j2 > n - 1) { i2 = i + 1; j2 = i + 2; }
+          const bool has2 = i2 < n - 1;
+          float rl0, rh0, rl1 = 0.f, rh1 = 0.f;
+          uint64_t k0 = 0, k1 = 0;
+          if (rnd) {
+            injected_interval(rnd[p], rl0, rh0);
+            if (has2) injected_interval(rnd[p + 1], rl1, rh1);
+          } else {
+            const PhiloxBlock blk = philox_block(a.seed, (uint64_t)(p >> 1), pc1);
+            k0 = philox_half53(blk, false);
+            k1 = philox_half53(blk, true);
+            philox_interval(k0, rl0, rh0);
+            philox_interval(k1, rl1, rh1);
+          }
+          if (p >= pos) {
+            const int sc = screen_pair(a, S, use_E, i, j, rl0, rh0);
+            if (sc != 0) { my_p = p; my_i = i; my_j = j; my_sc = sc; my_k53 = k0; break; }
+          }
+          if (has2) {
+            const int sc = screen_pair(a, S, use_E, i2, j2, rl1, rh1);
+            if (sc != 0) { my_p = p + 1; my_i = i2; my_j = j2; my_sc = sc; my_k53 = k1; break; }
+          }
+          j += 64;
+          p += 64;
         }
-        if (screen_pair(a, S, use_E, i, j, rl0, rh0) != 0) { pstar = p; break; }
-        if (has2 && screen_pair(a, S, use_E, i2, j2, rl1, rh1) != 0) { pstar = p + 1; break; }
-        j += 64;
-        p += 64;
       }
-    }
-    pstar = __reduce_min_sync(0xffffffffu, pstar);
-    if (pstar == 0x7fffffff) continue;   // nothing collides in this cell
-    // exact data of the cell's SIPs, computed lazily from the step-start masses
-    for (int q = lane; q < n; q += 32) {
-      const int32_t id = S.sid[q];
-      a.gR[id] = a.m_w[id] + a.m_s[id];
-      a.grho[id] = a.m_s[id];
-      a.gk[id] = -1;
-    }
-    __syncwarp();
-    // pass 2: anti-diagonal schedule of the pairs from p* on
-    for (int s = 1; s <= 2 * n - 3; ++s) {
-      const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
-      const int ihi = (s - 1) >> 1;
-      for (int i = ilo + lane; i <= ihi; i += 32) {
-        const int j = s - i;
-        const int64_t rk = pair_rank(i, j, n);
-        if (rk < pstar) continue;
-        uint64_t k53 = 0;
-        float r_lo, r_hi;
-        if (rnd) {
-          injected_interval(rnd[rk], r_lo, r_hi);
-        } else {
-          k53 = philox_bits53(a.seed, (uint64_t)rk, pc1);
-          philox_interval(k53, r_lo, r_hi);
+      const int pstar = __reduce_min_sync(0xffffffffu, my_p);
+      if (pstar == 0x7fffffff) break;   // no further event in this cell
+      if (events == 0) {
+        // exact data of the cell's SIPs, computed lazily from the step-start masses
+        for (int q = lane; q < n; q += 32) {
+          const int32_t id = S.sid[q];
+          a.gR[id] = a.m_w[id] + a.m_s[id];
+          a.grho[id] = a.m_s[id];
+          a.gk[id] = -1;
         }
-        const int sc = screen_pair(a, S, use_E, i, j, r_lo, r_hi);
-        if (sc == 0) continue;
-        if (sc == 1) {
-          certain_collection(a, wbase, stride, i, j, Tc, use_E);
+        __syncwarp();
+      }
+      const int L = __ffs(__ballot_sync(0xffffffffu, my_p == pstar)) - 1;
+      if (lane == L) {
+        if (my_sc == 1) {
+          certain_collection(a, wbase, stride, my_i, my_j, Tc, use_E);
           c0 += 1;
-          continue;
+        } else {
+          const int o = exact_pair(a, wbase, stride, S.sid[my_i], S.sid[my_j], my_i, my_j, Tc,
+                                   use_E, rnd ? rnd[pstar] : philox_from_bits(my_k53));
+          c0 += o == 1;
+          c1 += o == 2;
         }
-        const int o = exact_pair(a, wbase, stride, S.sid[i], S.sid[j], i, j, Tc, use_E,
-                                 rnd ? rnd[rk] : philox_from_bits(k53));
-        c0 += o == 1;
-        c1 += o == 2;
       }
       __threadfence_block();
       __syncwarp();
+      const int si = __shfl_sync(0xffffffffu, my_i, L), sj = __shfl_sync(0xffffffffu, my_j, L);
+      pos = pstar + 1;
+      if (pstar & 1) {   // rank pos is even: the successor of p*
+        bi = si; bj = sj + 1;
+        if (bj > n - 1) { bi = si + 1; bj = si + 2; }
+      } else {           // rank pos is odd: its couple starts at p* itself
+        bi = si; bj = sj;
+      }
+      if (pos >= P) break;
+      if (++events >= event_limit) { diagonal = true; break; }
+    }
+    if (diagonal) {
+      // anti-diagonal schedule of the pairs from rank pos on
+      for (int s = 1; s <= 2 * n - 3; ++s) {
+        const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
+        const int ihi = (s - 1) >> 1;
+        for (int i = ilo + lane; i <= ihi; i += 32) {
+          const int j = s - i;
+          const int64_t rk = pair_rank(i, j, n);
+          if (rk < pos) continue;
+          uint64_t k53 = 0;
+          float r_lo, r_hi;
+          if (rnd) {
+            injected_interval(rnd[rk], r_lo, r_hi);
+          } else {
+            k53 = philox_bits53(a.seed, (uint64_t)rk, pc1);
+            philox_interval(k53, r_lo, r_hi);
+          }
+          const int sc = screen_pair(a, S, use_E, i, j, r_lo, r_hi);
+          if (sc == 0) continue;
+          if (sc == 1) {
+            certain_collection(a, wbase, stride, i, j, Tc, use_E);
+            c0 += 1;
+            continue;
+          }
+          const int o = exact_pair(a, wbase, stride, S.sid[i], S.sid[j], i, j, Tc, use_E,
+                                   rnd ? rnd[rk] : philox_from_bits(k53));
+          c0 += o == 1;
+          c1 += o == 2;
+        }
+        __threadfence_block();
+        __syncwarp();
+      }
     }
     __syncwarp();
   }
