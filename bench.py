@@ -1,15 +1,20 @@
 #!/usr/bin/env python3
 """Benchmark of the super-droplet (SIP) hot path on GB300.
 
-One step = one advection step dt = 1 s of the 2-D ICMW 2012 case 1 state:
-75 x 75 cells of 20 m, 64 SIPs per cell (~360k SIPs), 10 condensation
-sub-steps with the 3-iteration implicit Newton, 2 all-or-nothing collision
-steps with the Long/Bott efficiency table, FP64 (the reference's precision).
-Synthetic seeded state with the case's shapes and distributions.
+Headline workload (the "mixed/batched" side of the metric): an ensemble of 64
+independent 2-D ICMW 2012 case 1 states, 75 x 75 cells of 20 m, SIPs per cell
+drawn uniformly in [32, 256] per cell and member (~52M SIPs), Hall/Bott
+collision efficiencies, mixed precision, Philox collision draws, one advection
+step dt = 1 s per step (10 condensation sub-steps with the 3-iteration
+implicit Newton, 2 all-or-nothing collision steps), each kernel launch covering
+all members, the step replayed from a CUDA graph.  The "FP64 plain" side is
+the single 75 x 75 x 64-SIPs/cell state with the Long/Bott table in FP64;
+both sides and the mixed single state are reported under "modes".  Seeded
+synthetic states with the case's shapes and distributions.
 
 Metric: SIP-updates/s = active SIPs advanced one dt per second (whole job).
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-With N > 1 (torchrun) every rank advances its own independent replica
+With N > 1 (torchrun) every rank advances its own independent ensemble
 (replicas only; the path needs no collective).
 """
 import argparse
@@ -21,6 +26,8 @@ import subprocess
 import sys
 import threading
 import time
+from concurrent.futures import ProcessPoolExecutor
+import multiprocessing as mp
 
 import numpy as np
 
@@ -31,7 +38,8 @@ METRIC = "SIP-updates/s per timestep on 1 GB300, mixed/batched vs FP64 plain; % 
 UNIT = "SIP-updates/s"
 # algorithmic bytes per SIP of one condensation sub-step (the fused particle
 # kernel): reads x, z, u, w, m_w, m_s, xi (8 B each), cell (4 B), flag (1 B)
-# = 61 B; writes x, z, u, w, m_w (8 B each) and cell (4 B) = 44 B
+# = 61 B; writes x, z, u, w, m_w (8 B each) and cell (4 B) = 44 B.  The
+# state stays FP64 in mixed precision, so the figure holds for both modes.
 BYTES_PARTICLE_SUBSTEP = 105
 # per SIP-update (adv step): 53 (half-step move) + 10 * 105 + 2 * 68 (collisions)
 BYTES_PER_SIP_UPDATE = 1239
@@ -43,36 +51,57 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--members", type=int, default=64, help="ensemble size of the headline")
+    ap.add_argument("--uneven", type=int, nargs=2, default=[32, 256],
+                    help="range of SIPs per cell of the ensemble members")
     ap.add_argument("--nx", type=int, default=75)
     ap.add_argument("--nz", type=int, default=75)
-    ap.add_argument("--spcm", type=int, nargs=2, default=[26, 38])
-    ap.add_argument("--kernel", default="Long_Bott")
-    ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--spcm", type=int, nargs=2, default=[26, 38],
+                    help="SIPs per cell per aerosol mode of the single-state modes")
+    ap.add_argument("--e2e-members", type=int, default=4)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
-                    help="arithmetic of the headline line; the other mode is reported beside it")
+    ap.add_argument("--no-single", action="store_true", help="skip the single-state modes")
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one")
-    ap.add_argument("--only", action="store_true", help="skip the second precision mode")
     return ap.parse_args()
 
 
 def workload_config(args, n_sips):
-    mode = "fp64_plain" if args.precision == "fp64" else "mixed"
-    return {"workload": f"icmw2012_case1_{args.nx}x{args.nz}_{sum(args.spcm)}spc_{mode}",
-            "precision_mode": mode, "nx": args.nx, "nz": args.nz,
-            "cuda_graph": not getattr(args, "no_graph", False),
-            "sips_per_cell": sum(args.spcm), "n_sips": int(n_sips), "kernel": args.kernel,
+    return {"workload": f"icmw2012_case1_{args.nx}x{args.nz}_ensemble{args.members}_"
+                        f"uneven{args.uneven[0]}-{args.uneven[1]}spc_hall_bott_mixed",
+            "members": args.members, "nx": args.nx, "nz": args.nz,
+            "sips_per_cell": f"uniform in [{args.uneven[0]}, {args.uneven[1]}] per cell and member",
+            "n_sips": int(n_sips), "kernel": "Hall_Bott", "precision_mode": "mixed",
             "dt_s": 1.0, "cond_substeps": 10, "collision_steps": 2, "newton_iterations": 3,
-            "draws": "philox4x32-10 (device)",
-            "l2": "flushed between timed steps (512 MiB device memset)",
+            "draws": "philox4x32-10 (device), keyed per member",
+            "cuda_graph": not args.no_graph,
+            "l2": "inputs larger than L2 (state ~8 GB); L2 also flushed between timed steps "
+                  "(512 MiB device memset)",
             "parallelism": "replicas"}
 
 
-def make_state(args, rank):
+def _member_state(a):
+    nx, nz, lo, hi, seed = a
+    from lacmopy_gb300 import synthetic
+    return synthetic.make_icmw_state(Nx=nx, Nz=nz, seed=seed, kernel_type="Hall_Bott",
+                                     uneven=(lo, hi))
+
+
+def make_members(args, rank):
+    """The ensemble's states, generated on the host cores in parallel (spawned
+    workers: no CUDA context is forked)."""
+    jobs = [(args.nx, args.nz, args.uneven[0], args.uneven[1], 5000 + 1000 * rank + m)
+            for m in range(args.members)]
+    workers = max(1, min(len(jobs), (os.cpu_count() or 1)))
+    with ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_member_state, jobs))
+
+
+def make_single(args, rank):
     from lacmopy_gb300 import synthetic
     return synthetic.make_icmw_state(Nx=args.nx, Nz=args.nz, no_spcm=tuple(args.spcm),
-                                     seed=1001 + rank, kernel_type=args.kernel)
+                                     seed=1001 + rank, kernel_type="Long_Bott")
 
 
 def measured_peaks():
@@ -147,29 +176,32 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-def cpu_port_rate(st, steps, threads):
+def cpu_port_rate(states, steps, threads):
     """Oracle (C port of the reference path, OpenMP over SIPs and cells) on the
-    host cores, Philox draws; returns SIP-updates/s and the seconds spent."""
+    host cores, Philox draws, over the given member states one after another;
+    returns SIP-updates/s and the seconds spent."""
     from oracle.oracle import Oracle, build
     build()
     orc = Oracle("numba")
     orc.set_threads(threads)
-    s = copy.deepcopy(st)
-    col_step = np.zeros(1, np.int64)
     n_up = 0
     t0 = time.perf_counter()
-    for _ in range(steps):
-        n_up += int(np.count_nonzero(s["active_ids"]))
-        orc.integrate_adv_step_np(
-            s["grid_scalar_fields"], s["grid_mat_prop"], s["grid_velocity"],
-            s["grid_mass_flux_air_dry"], s["p_ref"], s["p_ref_inv"], s["grid_no_cells"],
-            s["grid_ranges"], s["grid_steps"], s["grid_volume_cell"], s["pos"], s["vel"],
-            s["cells"], s["rel_pos"], s["m_w"], s["m_s"], s["xi"], "AS", s["water_removed"], None,
-            s["active_ids"], s["T_p"], s["delta_m_l"], s["dt"], s["dt_sub"], s["dt_sub_half"],
-            s["dt_col_over_dV"], s["scale_dt_cond"], s["no_col_per_adv"], True, True,
-            s["init_profile_r_v"], s["init_profile_Theta"], s["relaxation_time_profile"], 3,
-            s["g_set"], s["E_col_grid"], s["no_kernel_bins"], s["R_kernel_low_log"],
-            s["bin_factor_R_log"], s["no_cols"], None, None, 1001, col_step)
+    for m, st in enumerate(states):
+        s = copy.deepcopy(st)
+        col_step = np.zeros(1, np.int64)
+        for _ in range(steps):
+            n_up += int(np.count_nonzero(s["active_ids"]))
+            orc.integrate_adv_step_np(
+                s["grid_scalar_fields"], s["grid_mat_prop"], s["grid_velocity"],
+                s["grid_mass_flux_air_dry"], s["p_ref"], s["p_ref_inv"], s["grid_no_cells"],
+                s["grid_ranges"], s["grid_steps"], s["grid_volume_cell"], s["pos"], s["vel"],
+                s["cells"], s["rel_pos"], s["m_w"], s["m_s"], s["xi"], "AS", s["water_removed"],
+                None, s["active_ids"], s["T_p"], s["delta_m_l"], s["dt"], s["dt_sub"],
+                s["dt_sub_half"], s["dt_col_over_dV"], s["scale_dt_cond"], s["no_col_per_adv"],
+                True, True, s["init_profile_r_v"], s["init_profile_Theta"],
+                s["relaxation_time_profile"], 3, s["g_set"], s["E_col_grid"],
+                s["no_kernel_bins"], s["R_kernel_low_log"], s["bin_factor_R_log"], s["no_cols"],
+                None, None, 1 + m, col_step)
     dt = time.perf_counter() - t0
     return n_up / dt, dt
 
@@ -178,22 +210,28 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    st = make_state(args, 0)
+    from lacmopy_gb300 import synthetic
+    # a bounded sample of the ensemble workload: one member, the oracle's
+    # restatement of the reference algorithm on all host cores
+    st = synthetic.make_icmw_state(Nx=args.nx, Nz=args.nz, seed=5000, kernel_type="Hall_Bott",
+                                   uneven=tuple(args.uneven))
     threads = os.cpu_count() or 1
+    steps = max(1, min(args.steps, 2))
     if args.warmup > 0:
-        cpu_port_rate(st, min(args.warmup, 1), threads)
-    rate, secs = cpu_port_rate(st, args.steps, threads)
-    n = int(st["xi"].size)
+        cpu_port_rate([st], 1, threads)
+    rate, secs = cpu_port_rate([st], steps, threads)
+    n_total_est = int(st["xi"].size) * args.members
     line = {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True,
+            "steps": steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * secs / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload_config(args, n), "impl": "reference",
+            "config": workload_config(args, n_total_est), "impl": "reference",
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} full advection steps of the workload; "
-                                       "reference Numba path unavailable on this box (numba "
-                                       "not installed), so the C port of the reference "
-                                       "algorithm with OpenMP on all host cores"},
+                             "sample": f"{steps} advection steps of one ensemble member "
+                                       f"({st['xi'].size} SIPs) of the workload; the reference's "
+                                       "Numba path is unavailable on this box (numba not "
+                                       "installed), so the C restatement of the reference "
+                                       "algorithm (FP64, OpenMP over SIPs and cells) runs"},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -202,33 +240,32 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 def run_ours(args):
     import torch
-    from lacmopy_gb300 import DeviceState, _lib
+    from lacmopy_gb300 import BatchState, DeviceState, _lib
     from lacmopy_gb300 import integration as I
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    members = make_members(args, rank)          # host work before the first CUDA call
+    single = None if args.no_single else make_single(args, rank)
     torch.cuda.set_device(local)
     dist = None
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
     lib = _lib.load()
-    st = make_state(args, rank)
-    n = int(st["xi"].size)
-    st0 = copy.deepcopy(st)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     graph = not args.no_graph
+    peak, peak_kind = measured_peaks()
 
-    def timed(precision, sample_clocks):
-        ds = DeviceState(copy.deepcopy(st), draws="philox", seed=1001 + rank,
-                         precision=precision)
+    def timed(obj, sample_clocks):
         for _ in range(args.warmup):
-            ds.adv_step(1, graph=graph)
+            obj.adv_step(1, graph=graph)
         torch.cuda.synchronize()
-        n_active = []
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(args.steps)]
+        cells = [m.cell for m in obj.members] if isinstance(obj, BatchState) else [obj.cell]
+        n_active = []
         sampler = ClockSampler(local) if sample_clocks else None
         if sampler:
             sampler.start()
@@ -238,16 +275,15 @@ def run_ours(args):
         launches0 = lib.lacmo_kernel_launches()
         for k in range(args.steps):
             flush.zero_()
-            n_active.append(ds.cell.ge(0).sum())
+            n_active.append(sum(c.ge(0).sum() for c in cells))
             ev[k][0].record()
-            ds.adv_step(1, graph=graph)
+            obj.adv_step(1, graph=graph)
             ev[k][1].record()
         torch.cuda.synchronize()
         launches = lib.lacmo_kernel_launches() - launches0
         if graph:
             # kernels replayed from the captured graph: count them per step
-            per_step = ds.graph_kernel_count()
-            launches = per_step * args.steps
+            launches = obj.graph_kernel_count() * args.steps
         clocks = sampler.stop() if sampler else None
         if dist:
             dist.barrier()
@@ -259,90 +295,113 @@ def run_ours(args):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             dist.all_reduce(u, op=dist.ReduceOp.SUM)
             ms, ups = float(t.item()), float(u.item())
-        return ds, ms, ups, launches, clocks
+        return ms, ups, launches, clocks
 
-    ds, ms, ups, launches, clocks = timed(args.precision, True)
+    # ---- headline: the batched mixed-precision ensemble ----
+    seeds = [1 + 64 * rank + m for m in range(args.members)]
+    batch = BatchState(members, seeds, precision="mixed")   # copies the states to the GPU
+    n_total = batch.n_total
+    ms, ups, launches, clocks = timed(batch, True)
     value = ups / (ms / 1000.0)
-    modes = {("fp64_plain" if args.precision == "fp64" else "mixed"):
-             {"value": value, "ms_per_step": ms / args.steps}}
-    if not args.only:
-        other = "mixed" if args.precision == "fp64" else "fp64"
-        ds2, ms2, ups2, _, _ = timed(other, False)
-        modes["mixed" if other == "mixed" else "fp64_plain"] = {
-            "value": ups2 / (ms2 / 1000.0), "ms_per_step": ms2 / args.steps}
-        del ds2
-    if "mixed" in modes and "fp64_plain" in modes:
-        modes["mixed_over_fp64"] = modes["mixed"]["value"] / modes["fp64_plain"]["value"]
+    modes = {"batched_mixed": {"value": value, "ms_per_step": ms / args.steps,
+                               "n_sips": n_total, "members": args.members}}
 
-    # roofline of the dominant kernel: the fused particle sub-step
-    sp, g, p = ds.sips, ds.grid, ds.params
+    # roofline of the dominant kernel: the fused mixed particle sub-step over
+    # all members (one launch; state advanced afterwards is not used)
+    p = batch.params
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     kt = []
-    for _ in range(10):
+    n_act = float(sum(int(m.cell.ge(0).sum()) for m in batch.members))
+    for _ in range(5):
         flush.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        na = int(ds.cell.ge(0).sum())
         a.record()
-        _lib.check(lib.lacmo_particles_only(ctypes.byref(sp), ctypes.byref(g), ctypes.byref(p),
-                                            p.dt_sub, p.dt_sub, ctypes.c_void_p(ds.ws.data_ptr()),
-                                            ds.ws_bytes, s), "particles_only")
+        _lib.check(lib.lacmo_batch_particles_only(batch.handle, ctypes.byref(p), s),
+                   "batch_particles_only")
         b.record()
-        _lib.check(lib.lacmo_bin(ctypes.byref(sp), ctypes.byref(g),
-                                 ctypes.c_void_p(ds.ws.data_ptr()), ds.ws_bytes, s), "bin")
         torch.cuda.synchronize()
-        kt.append((a.elapsed_time(b), na))
-    k_ms = float(np.mean([x[0] for x in kt]))
-    k_bytes = BYTES_PARTICLE_SUBSTEP * float(np.mean([x[1] for x in kt]))
-    peak, peak_kind = measured_peaks()
+        kt.append(a.elapsed_time(b))
+    k_ms = float(np.mean(kt))
+    k_bytes = BYTES_PARTICLE_SUBSTEP * n_act
     achieved = k_bytes / (k_ms / 1000.0) / 1e9
-    roofline = {"bound": "hbm", "kernel": "k_particles (fused condensation/drag/move sub-step)",
+    tr = traffic_for("k_particles_mixed_batch_per_sip")
+    roofline = {"bound": "hbm", "kernel": "k_particles_mixed (fused condensation/drag/move "
+                                          "sub-step, all members in one launch)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": peak_kind, "traffic": traffic_for("k_particles_icmw75"),
+                "peak_source": peak_kind,
+                "traffic": (tr * n_act if tr is not None else None),
                 "kernel_ms": k_ms, "algorithmic_bytes_per_launch": k_bytes,
-                "note": "FP64 plain mode is FP64-pipe bound on GB300, not HBM bound"}
+                "bytes_per_sip": BYTES_PARTICLE_SUBSTEP}
+    del batch
+    torch.cuda.empty_cache()
 
-    # end to end through the reference-facing API with host NumPy arrays
+    # ---- the FP64 plain path and the mixed single state (75 x 75 x 64) ----
+    if single is not None:
+        for prec, key in (("fp64", "fp64_plain"), ("mixed", "mixed_single")):
+            ds = DeviceState(copy.deepcopy(single), draws="philox", seed=1001 + rank,
+                             precision=prec)
+            ms2, ups2, _, _ = timed(ds, False)
+            modes[key] = {"value": ups2 / (ms2 / 1000.0), "ms_per_step": ms2 / args.steps,
+                          "n_sips": int(single["xi"].size),
+                          "workload": f"icmw2012_case1_{args.nx}x{args.nz}_{sum(args.spcm)}spc_"
+                                      f"long_bott_{prec}"}
+            del ds
+        modes["batched_mixed_over_fp64_plain"] = value / modes["fp64_plain"]["value"]
+        modes["mixed_single_over_fp64_plain"] = (modes["mixed_single"]["value"]
+                                                 / modes["fp64_plain"]["value"])
+
+    # ---- end to end through the reference-facing drop-in API: each member's
+    # NumPy state copied in and out by integrate_adv_step_np every step ----
     e2e = None
-    if rank == 0 and args.e2e_steps > 0:
-        se = copy.deepcopy(st0)
+    if rank == 0 and args.e2e_steps > 0 and args.e2e_members > 0:
         keys = I._STATE_KEYS
-        h2d = sum(np.asarray(se[k]).nbytes for k in
-                  ("pos", "vel", "rel_pos", "m_w", "m_s", "xi", "T_p", "water_removed", "cells",
-                   "grid_scalar_fields", "grid_mat_prop", "grid_velocity",
-                   "grid_mass_flux_air_dry", "delta_m_l", "init_profile_r_v",
-                   "init_profile_Theta", "relaxation_time_profile", "E_col_grid", "no_cols"))
-        h2d += n  # active_ids as uint8
-        d2h = sum(np.asarray(se[k]).nbytes for k in
-                  ("pos", "vel", "rel_pos", "m_w", "m_s", "xi", "T_p", "water_removed", "cells",
-                   "grid_scalar_fields", "grid_mat_prop", "delta_m_l", "no_cols")) + n
-        I.integrate_adv_step_np(*[se[k] for k in keys], draws="philox", seed=7)  # warm-up
+        sts = [copy.deepcopy(members[m]) for m in range(min(args.e2e_members, args.members))]
+        h2d = d2h = 0
+        for se in sts:
+            n = int(se["xi"].size)
+            h2d += sum(np.asarray(se[k]).nbytes for k in
+                       ("pos", "vel", "rel_pos", "m_w", "m_s", "xi", "T_p", "water_removed",
+                        "cells", "grid_scalar_fields", "grid_mat_prop", "grid_velocity",
+                        "grid_mass_flux_air_dry", "delta_m_l", "init_profile_r_v",
+                        "init_profile_Theta", "relaxation_time_profile", "E_col_grid",
+                        "no_cols")) + n
+            d2h += sum(np.asarray(se[k]).nbytes for k in
+                       ("pos", "vel", "rel_pos", "m_w", "m_s", "xi", "T_p", "water_removed",
+                        "cells", "grid_scalar_fields", "grid_mat_prop", "delta_m_l",
+                        "no_cols")) + n
+        I.integrate_adv_step_np(*[sts[0][k] for k in keys], draws="philox", seed=7)  # warm-up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ups_e = 0
         for _ in range(args.e2e_steps):
-            ups_e += int(np.count_nonzero(se["active_ids"]))
-            I.integrate_adv_step_np(*[se[k] for k in keys], draws="philox", seed=7)
+            for m, se in enumerate(sts):
+                ups_e += int(np.count_nonzero(se["active_ids"]))
+                I.integrate_adv_step_np(*[se[k] for k in keys], draws="philox", seed=7 + m)
         torch.cuda.synchronize()
         te = time.perf_counter() - t0
         e2e = {"value": ups_e / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h),
                "api": "lacmopy_gb300.integration.integrate_adv_step_np (reference argument "
-                      "list, NumPy host arrays copied in and out every call)"}
+                      "list) per member, NumPy host state copied in and out every call",
+               "sample": f"{len(sts)} members x {args.e2e_steps} steps of the workload"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        rate, secs = cpu_port_rate(st0, args.cpu_steps, threads)
+        rate, secs = cpu_port_rate(members[:1], args.cpu_steps, threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_steps} advection steps of the same {n}-SIP workload, "
-                         f"{secs:.1f} s, C port of the reference algorithm, OpenMP"}
+               "sample": f"{args.cpu_steps} advection step(s) of one ensemble member "
+                         f"({members[0]['xi'].size} SIPs), {secs:.1f} s; C restatement of "
+                         "the reference algorithm in FP64, OpenMP on all host cores"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": workload_config(args, n), "roofline": roofline,
-                "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "mixed f32/f64 (f32 Newton, drag and pair screen; f64 state, "
+                         "per-cell sums, near-critical Newton and collision updates)",
+                "data": "synthetic", "config": workload_config(args, n_total),
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": int(launches), "modes": modes,
                 "hbm_frac_whole_step": value * BYTES_PER_SIP_UPDATE / 1e9 / peak}
         print(json.dumps(line), flush=True)

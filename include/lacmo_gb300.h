@@ -190,6 +190,9 @@ int lacmo_batch_adv_step(lacmo_batch* batch, const lacmo_params_t* prm, void* st
 /* a CUDA graph of n_steps batch advection steps (see lacmo_plan_create) */
 int lacmo_batch_plan_create(lacmo_batch* batch, const lacmo_params_t* prm, int n_steps,
                             void* stream, lacmo_plan** plan);
+/* one particle sub-step kernel of every member alone (no grid update, no
+ * binning): for timing the fused particle pass; leaves the step incomplete */
+int lacmo_batch_particles_only(lacmo_batch* batch, const lacmo_params_t* prm, void* stream);
 /* member m's workspace slice, for lacmo_read_flags / lacmo_read_fallbacks */
 int lacmo_batch_member_workspace(const lacmo_batch* batch, int m, void** ws, size_t* ws_bytes);
 int lacmo_batch_destroy(lacmo_batch* batch);

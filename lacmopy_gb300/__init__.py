@@ -7,6 +7,13 @@ Modules mirror the reference's step functions by name and argument list:
 ``collision`` (collision/all_or_nothing.py, collision/box_model.py driver).
 ``DeviceState`` keeps a state resident on the GPU between steps.
 """
-from .device import BatchState, DeviceState  # noqa: F401
-
 __all__ = ["BatchState", "DeviceState"]
+
+
+def __getattr__(name):
+    # the device classes import torch; the pure-NumPy modules (synthetic,
+    # tables, constants) stay importable without it
+    if name in __all__:
+        from . import device
+        return getattr(device, name)
+    raise AttributeError(name)

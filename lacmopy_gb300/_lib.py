@@ -86,6 +86,7 @@ PROTOTYPES = {
     "lacmo_batch_prepare": (ctypes.c_int, [vp, P(Params), vp]),
     "lacmo_batch_adv_step": (ctypes.c_int, [vp, P(Params), vp]),
     "lacmo_batch_plan_create": (ctypes.c_int, [vp, P(Params), ctypes.c_int, vp, P(vp)]),
+    "lacmo_batch_particles_only": (ctypes.c_int, [vp, P(Params), vp]),
     "lacmo_batch_member_workspace": (ctypes.c_int, [vp, ctypes.c_int, P(vp), P(sz)]),
     "lacmo_batch_destroy": (ctypes.c_int, [vp]),
     "lacmo_adv_step_begin": (ctypes.c_int, [P(Sips), P(Grid), P(Params), vp, sz, vp]),

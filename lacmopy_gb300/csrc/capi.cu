@@ -532,6 +532,15 @@ int lacmo_batch_plan_create(lacmo_batch* b, const lacmo_params_t* p, int n_steps
   return LACMO_OK;
 }
 
+int lacmo_batch_particles_only(lacmo_batch* b, const lacmo_params_t* p, void* stream) {
+  if (!b || !prm_ok(p)) return LACMO_ERR_ARG;
+  if (p->precision == LACMO_PRECISION_MIXED)
+    LCHK(launch_particles_mixed(b->B, *p, p->dt_sub, p->dt_sub, false, false, (cudaStream_t)stream));
+  else
+    LCHK(launch_particles(b->B, *p, p->dt_sub, p->dt_sub, false, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
 int lacmo_batch_member_workspace(const lacmo_batch* b, int m, void** ws, size_t* bytes) {
   if (!b || m < 0 || m >= b->B.M || !ws || !bytes) return LACMO_ERR_ARG;
   *ws = b->ws + b->ws_off[(size_t)m];
