@@ -262,7 +262,7 @@ int lacmo_collision_step_cells(const lacmo_sips_t* sips, const lacmo_grid_t* gri
  * memory pool or under a fixed memory budget, plugin hosts that forbid
  * cudaMalloc after start-up).  It does the work of lacmo_collision_step_cells
  * from the SIP cell indices alone (binning included), with its scratch in a
- * fixed array inside the library (about 15 MB of device memory, held by every
+ * fixed array inside the library (about 27 MB of device memory, held by every
  * GPU that loads the library until the process exits) instead of a
  * workspace.  The caller still passes all inputs and outputs: xi, m_w, m_s
  * are updated in place, vel is [2][n], grid_T is the [nx][nz] temperature,
