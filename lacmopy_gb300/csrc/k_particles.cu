@@ -633,7 +633,7 @@ __device__ __noinline__ double mixed_remove(GroundGeo a, int64_t k, int i, int j
   return a.z_min - 0.01 * a.dz;
 }
 
-__global__ void __launch_bounds__(128) k_particles_mixed(const __grid_constant__ PK x) {
+__global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constant__ PK x) {
   const PArgs a = make_pargs(x.m.get(), x.c);
   const int C = (int)(a.nx * a.nz);
   const int nz = (int)a.nz;
@@ -661,7 +661,7 @@ __global__ void __launch_bounds__(128) k_particles_mixed(const __grid_constant__
     af.c1 = __ldg(a.auxf + AF_C1 * C + c); af.c2 = __ldg(a.auxf + AF_C2 * C + c);
     const float msf = d2f_int(ms), mwf = d2f_int(mw), xif = d2f_int(xik);
     const float mpf = mwf + msf;
-    const float wsf = msf / mpf;
+    const float wsf = msf * f_rcp(mpf);
     float rho = (a.sol == SOL_AS)
                     ? af.rhow * ((((float)LC_PAR_RHO_AS_0 * wsf + (float)LC_PAR_RHO_AS_1) * wsf +
                                   (float)LC_PAR_RHO_AS_2) * wsf + (float)LC_PAR_RHO_AS_3)
@@ -670,10 +670,10 @@ __global__ void __launch_bounds__(128) k_particles_mixed(const __grid_constant__
                           (float)LC_PAR_SOL_DENS_NACL_3 * wsf * wsf +
                           (float)LC_PAR_SOL_DENS_NACL_4 * wsf * af.T +
                           (float)LC_PAR_SOL_DENS_NACL_5 * af.T * af.T;
-    float R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * mpf / rho);
+    float R = f_cbrt((float)LC_FOUR_PI_OVER_THREE_INV * mpf * f_rcp(rho));
     const float sig = af.sigw * (1.0f + (a.sol == SOL_AS ? (float)LC_PAR_SIGMA_AS
                                                           : (float)LC_PAR_SIGMA_NACL) *
-                                             wsf / (1.f - wsf));
+                                             wsf * f_rcp(1.f - wsf));
     // efflorescence floor m_s (1/0.78 - 1) as an increment, in FP32
     const float d_effl = msf * (float)(LC_W_S_MAX_AS_INV - 1.0) - mwf;
     float d;
@@ -693,10 +693,10 @@ __global__ void __launch_bounds__(128) k_particles_mixed(const __grid_constant__
     atomicAdd(a.acc + c, f2d_int(d * xif));
     // drag (integration.py:699-718) in FP32 with the ammonium-sulfate radius
     const float mpn = (mwf + d) + msf;
-    const float wn = msf / mpn;
+    const float wn = msf * f_rcp(mpn);
     rho = af.rhow * ((((float)LC_PAR_RHO_AS_0 * wn + (float)LC_PAR_RHO_AS_1) * wn +
                       (float)LC_PAR_RHO_AS_2) * wn + (float)LC_PAR_RHO_AS_3);
-    R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * mpn / rho);
+    R = f_cbrt((float)LC_FOUR_PI_OVER_THREE_INV * mpn * f_rcp(rho));
     const float xf = d2f_int(x), zf = d2f_int(z);
     const float rxf = (xf - a.x_minf) * a.inv_dxf - (float)i;
     const float rzf = (zf - a.z_minf) * a.inv_dzf - (float)j;
@@ -706,13 +706,14 @@ __global__ void __launch_bounds__(128) k_particles_mixed(const __grid_constant__
     const float uo = d2f_int(a.vel[k]), wo = d2f_int(a.vel[a.n + k]);
     const float d0 = uf - uo, d1 = wf - wo;
     const float vel_dev = sqrtf(d0 * d0 + d1 * d1);
-    const float Re_p = 2.0E-6f * rho_f * R * vel_dev / mu_f;
-    float k_dt = 4.5E12f * a.dt_subf * mu_f / (rho * R * R);
+    const float inv_mu = f_rcp(mu_f);
+    const float Re_p = 2.0E-6f * rho_f * R * vel_dev * inv_mu;
+    float k_dt = 4.5E12f * a.dt_subf * mu_f * f_rcp(rho * R * R);
     if (Re_p > 0.5f) {
-      if (Re_p < 1000.0f) k_dt *= (1.f + 0.15f * powf(Re_p, 0.687f));
+      if (Re_p < 1000.0f) k_dt *= (1.f + 0.15f * f_pow(Re_p, 0.687f));
       else k_dt *= 0.0183333333333f * Re_p;
     }
-    const float inv = 1.0f / (1.0f + k_dt);
+    const float inv = f_rcp(1.0f + k_dt);
     const float un = (uo + k_dt * uf) * inv;
     const float wn2 = (wo + k_dt * wf - a.dtg_f) * inv;
     // position (integration.py:552-630)

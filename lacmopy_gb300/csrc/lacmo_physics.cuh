@@ -177,6 +177,38 @@ LACMO_DEV double newton_full(int sol, double dt_sub, int no_iter, double m_w, do
 
 // ---------------------------------------------------------------------------
 // Mixed precision: the same Fukuta-Walter mass rate, derivative and implicit
+// ---------------------------------------------------------------------------
+// FP32 building blocks of the mixed-precision path, on the hardware's special
+// function unit.  Each stays far inside the path's FP32 budget:
+//  f_div(a, b) = a * rcp.approx(b) (__fdividef): 2 ulp for 2^-126 < |b| < 2^126
+//    (all divisors here are masses, densities, radii and 1 - w terms);
+//  f_cbrt(x): 2^(log2(x)/3) from lg2/ex2 (relative error below 4e-6), then one
+//    Newton step on y^3 = x, which squares it: within a few ulp for x > 0;
+//  f_expm1(e): Taylor series to e^8 for |e| <= 0.5 (truncation below 1e-8
+//    relative), expm1f beyond;
+//  f_pow(x, y) = 2^(y log2 x) for x > 0 (relative error near 1e-6 for the
+//    drag's Reynolds factor, whose exponent is 0.687).
+LACMO_DEV float f_div(float a, float b) { return __fdividef(a, b); }
+LACMO_DEV float f_rcp(float b) { return __fdividef(1.0f, b); }
+LACMO_DEV float f_cbrt(float x) {
+  const float y = exp2f(__log2f(x) * (1.0f / 3.0f));
+  return (2.0f / 3.0f) * y + (1.0f / 3.0f) * x * f_rcp(y * y);
+}
+static __device__ __noinline__ float f_expm1_wide(float e) { return expm1f(e); }
+LACMO_DEV float f_expm1(float e) {
+  if (!(fabsf(e) <= 0.5f)) return f_expm1_wide(e);
+  float p = 2.4801587e-05f;                 // 1/8!
+  p = p * e + 1.9841270e-04f;               // 1/7!
+  p = p * e + 1.3888889e-03f;               // 1/6!
+  p = p * e + 8.3333333e-03f;               // 1/5!
+  p = p * e + 4.1666667e-02f;               // 1/4!
+  p = p * e + 1.6666667e-01f;               // 1/3!
+  p = p * e + 0.5f;
+  p = p * e + 1.0f;
+  return p * e;
+}
+LACMO_DEV float f_pow(float x, float y) { return exp2f(y * __log2f(x)); }
+
 // Newton in FP32.  The residual f2 = S_amb - S_eq is formed from the two
 // deviations from saturation, S_amb - 1 (exact in FP64, rounded once) and
 // S_eq - 1 = (a_w - 1) + a_w (exp(eps_k) - 1) with a_w - 1 from the water-
@@ -192,13 +224,15 @@ LACMO_DEV void mass_rate_and_derivative_f(int sol, float m_w, float m_s, float w
                                           const CellAmbF& a, float& g, float& dg, float& f2o) {
   const float l_alpha_plus_R_p = 1.0E-6f * (R_p + a.lap0);
   const float l_beta_plus_R_p = 1.0E-6f * (R_p + a.lbp0);
-  const float m_p_inv_SI = 1.0E18f / (m_w + m_s);
-  const float wfac = w_s / ((1.f - w_s) * (1.f - w_s));
+  const float m_p_inv_SI = 1.0E18f * f_rcp(m_w + m_s);
+  const float inv_1mw = f_rcp(1.f - w_s);
+  const float wfac = w_s * inv_1mw * inv_1mw;
+  const float inv_rho = f_rcp(rho_p);
   float drho_dm_over_rho, aw_m1, da_w_dm, dsigma_dm;
   if (sol == SOL_AS) {
     const float pd = ((float)LC_PAR_RHO_DERIV_AS_0 * w_s + (float)LC_PAR_RHO_DERIV_AS_1) * w_s +
                      (float)LC_PAR_RHO_DERIV_AS_2;
-    drho_dm_over_rho = -rhow_p * m_p_inv_SI / rho_p * w_s * pd;
+    drho_dm_over_rho = -rhow_p * m_p_inv_SI * inv_rho * w_s * pd;
     aw_m1 = w_s * ((((float)LC_PAR_WAT_ACT_AS_0 * w_s + (float)LC_PAR_WAT_ACT_AS_1) * w_s +
                     (float)LC_PAR_WAT_ACT_AS_2) * w_s + (float)LC_PAR_WAT_ACT_AS_3);
     const float da = (((float)LC_PAR_WAT_ACT_DERIV_AS_0 * w_s + (float)LC_PAR_WAT_ACT_DERIV_AS_1) *
@@ -207,7 +241,7 @@ LACMO_DEV void mass_rate_and_derivative_f(int sol, float m_w, float m_s, float w
     da_w_dm = -m_p_inv_SI * w_s * da;
     dsigma_dm = -(float)LC_PAR_SIGMA_AS * a.sigw * m_p_inv_SI * wfac;
   } else {
-    drho_dm_over_rho = -w_s * m_p_inv_SI / rho_p *
+    drho_dm_over_rho = -w_s * m_p_inv_SI * inv_rho *
                        ((float)LC_PAR_SOL_DENS_NACL_1 + 2.0f * (float)LC_PAR_SOL_DENS_NACL_3 * w_s +
                         (float)LC_PAR_SOL_DENS_NACL_4 * T_p);
     aw_m1 = w_s * ((((float)LC_PAR_WAT_ACT_NACL_0 * w_s + (float)LC_PAR_WAT_ACT_NACL_1) * w_s +
@@ -221,14 +255,15 @@ LACMO_DEV void mass_rate_and_derivative_f(int sol, float m_w, float m_s, float w
   }
   const float dR_p_dm_over_R_p = (1.0f / 3.0f) * (m_p_inv_SI - drho_dm_over_rho);
   const float dR_p_dm = 1.0E-6f * dR_p_dm_over_R_p * R_p;
-  const float eps_k = 2.0E6f * sigma_p / ((float)LC_R_V * T_p * rho_p * R_p);
-  const float em1 = expm1f(eps_k);
+  const float eps_k = 2.0E6f * sigma_p * inv_rho * f_rcp((float)LC_R_V * T_p * R_p);
+  const float em1 = f_expm1(eps_k);
   const float kelvin_term = 1.0f + em1;
   const float Seq_m1 = aw_m1 + (1.0f + aw_m1) * em1;
   const float S_eq = 1.0f + Seq_m1;
-  const float dSeq_dm =
-      da_w_dm * kelvin_term + S_eq * eps_k * (dsigma_dm / sigma_p - drho_dm_over_rho - dR_p_dm_over_R_p);
-  const float f3 = 1.0f / (l_alpha_plus_R_p * S_eq * a.c1 + l_beta_plus_R_p * a.c2);
+  const float dSeq_dm = da_w_dm * kelvin_term +
+                        S_eq * eps_k *
+                            (dsigma_dm * f_rcp(sigma_p) - drho_dm_over_rho - dR_p_dm_over_R_p);
+  const float f3 = f_rcp(l_alpha_plus_R_p * S_eq * a.c1 + l_beta_plus_R_p * a.c2);
   const float f1f3 = (float)LC_FOUR_PI * R_p * R_p * f3;
   const float dg1_dm = (dSeq_dm * l_alpha_plus_R_p + S_eq * dR_p_dm) * a.c1 + dR_p_dm * a.c2;
   const float f2 = a.S_m1 - Seq_m1;
@@ -237,45 +272,11 @@ LACMO_DEV void mass_rate_and_derivative_f(int sol, float m_w, float m_s, float w
   f2o = f2;
 }
 
-// FP32 implicit Newton on the increment (integration.py:728-836 restated on
-// dm).  Returns false when the SIP is near the critical radius of activation
-// (residual |S_amb - S_eq| < 1e-6 while the step is not stiff, |dt dgamma/dm|
-// < 0.5): the caller then repeats the SIP's Newton in FP64.
-LACMO_DEV bool newton_mixed(int sol, float dt_sub, int no_iter, double m_w, float m_s, float w_s,
-                            float R_p, float T_p, float rho_p, float sigma_p, const CellAmbF& a,
-                            double m_w_effl, double* dm_out) {
-  float g, dg, f2;
-  mass_rate_and_derivative_f(sol, (float)m_w, m_s, w_s, R_p, rho_p, sigma_p, T_p, a.rhow, a, g, dg,
-                             f2);
-  float x = dt_sub * dg;
-  bool near_crit = (fabsf(f2) < 1.0e-6f) && (fabsf(x) < 0.5f);
-  float denom_inv = (x < 0.9f) ? 1.0f / (1.0f - x) : 10.0f;
-  const float d_effl = (float)(m_w_effl - m_w);
-  const float d0 = dt_sub * g * denom_inv;
-  float d = (d0 != d0) ? d0 : fmaxf(d_effl, d0);  // NaN propagates as in np.maximum
-  const float m_w32 = (float)m_w;
-  for (int it = 0; it < no_iter - 1; ++it) {
-    const float mass = m_w32 + d;
-    const float m_p = mass + m_s;
-    const float w = m_s / m_p;
-    const float pr = (((float)LC_PAR_RHO_AS_0 * w + (float)LC_PAR_RHO_AS_1) * w +
-                      (float)LC_PAR_RHO_AS_2) * w + (float)LC_PAR_RHO_AS_3;
-    const float rho = a.rhow * pr;
-    const float R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * m_p / rho);
-    const float sig = a.sigw * (1.0f + (float)LC_PAR_SIGMA_AS * w / (1.f - w));
-    mass_rate_and_derivative_f(sol, mass, m_s, w, R, rho, sig, T_p, a.rhow, a, g, dg, f2);
-    x = dt_sub * dg;
-    near_crit = near_crit || ((fabsf(f2) < 1.0e-6f) && (fabsf(x) < 0.5f));
-    denom_inv = (x < 0.9f) ? 1.0f / (1.0f - x) : 10.0f;
-    d += (dt_sub * g - d) * denom_inv;
-    const float dm2 = fmaxf(d_effl, d);
-    d = (d != d) ? d : dm2;
-  }
-  *dm_out = (double)d;
-  return !near_crit;
-}
-
-// The same Newton with the masses in FP32 (increment d, floor d_effl).
+// The FP32 Newton of integration.py:728-836 on the increment d = m_new - m_w
+// (m_w32 = m_w rounded), with the ammonium-sulfate density and surface
+// tension inside the iterations as the reference hard-wires them.  Returns
+// false when a residual came near the critical radius (|f2| < 1e-6 with
+// |dt gamma'| < 0.5), where the caller repeats the solve in FP64.
 LACMO_DEV bool newton_mixed_f(int sol, float dt_sub, int no_iter, float m_w32, float m_s,
                               float w_s, float R_p, float T_p, float rho_p, float sigma_p,
                               const CellAmbF& a, float d_effl, float* d_out) {
@@ -283,22 +284,22 @@ LACMO_DEV bool newton_mixed_f(int sol, float dt_sub, int no_iter, float m_w32, f
   mass_rate_and_derivative_f(sol, m_w32, m_s, w_s, R_p, rho_p, sigma_p, T_p, a.rhow, a, g, dg, f2);
   float x = dt_sub * dg;
   bool near_crit = (fabsf(f2) < 1.0e-6f) && (fabsf(x) < 0.5f);
-  float denom_inv = (x < 0.9f) ? 1.0f / (1.0f - x) : 10.0f;
+  float denom_inv = (x < 0.9f) ? f_rcp(1.0f - x) : 10.0f;
   const float d0 = dt_sub * g * denom_inv;
   float d = (d0 != d0) ? d0 : fmaxf(d_effl, d0);
   for (int it = 0; it < no_iter - 1; ++it) {
     const float mass = m_w32 + d;
     const float m_p = mass + m_s;
-    const float w = m_s / m_p;
+    const float w = m_s * f_rcp(m_p);
     const float pr = (((float)LC_PAR_RHO_AS_0 * w + (float)LC_PAR_RHO_AS_1) * w +
                       (float)LC_PAR_RHO_AS_2) * w + (float)LC_PAR_RHO_AS_3;
     const float rho = a.rhow * pr;
-    const float R = cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * m_p / rho);
-    const float sig = a.sigw * (1.0f + (float)LC_PAR_SIGMA_AS * w / (1.f - w));
+    const float R = f_cbrt((float)LC_FOUR_PI_OVER_THREE_INV * m_p * f_rcp(rho));
+    const float sig = a.sigw * (1.0f + (float)LC_PAR_SIGMA_AS * w * f_rcp(1.f - w));
     mass_rate_and_derivative_f(sol, mass, m_s, w, R, rho, sig, T_p, a.rhow, a, g, dg, f2);
     x = dt_sub * dg;
     near_crit = near_crit || ((fabsf(f2) < 1.0e-6f) && (fabsf(x) < 0.5f));
-    denom_inv = (x < 0.9f) ? 1.0f / (1.0f - x) : 10.0f;
+    denom_inv = (x < 0.9f) ? f_rcp(1.0f - x) : 10.0f;
     d += (dt_sub * g - d) * denom_inv;
     d = (d != d) ? d : fmaxf(d_effl, d);
   }
