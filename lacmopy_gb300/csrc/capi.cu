@@ -31,7 +31,7 @@ static WsPlan ws_plan(int64_t n, int64_t nx, int64_t nz) {
       8 * N,           // dmxi
       4 * N,           // rm_id
       8 * N,           // rm_val
-      8 * 6 * C + 4 * 10 * C,  // aux: 6 doubles + 10 floats per cell
+      8 * 6 * C + 4 * 12 * C,  // aux: 6 doubles + 12 floats per cell
       8 * C,           // dTh
       8 * C,           // drv
       8 * C,           // div

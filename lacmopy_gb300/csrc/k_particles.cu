@@ -57,7 +57,8 @@ __global__ void k_cells_export(const int32_t* __restrict__ cell, const double* _
 }
 
 // per-cell terms of the mass rate for the next sub-step; the FP32 table that
-// follows them in the workspace (10 floats per cell) feeds the mixed-precision
+// follows them in the workspace (12 floats per cell, cell-major, so a SIP
+// reads its cell's entry with three 16-byte loads) feeds the mixed-precision
 // kernel without double->float conversions there
 __device__ __forceinline__ void write_aux(const double* gsf, const double* gmp, double* aux,
                                           int64_t c, int64_t C) {
@@ -65,11 +66,10 @@ __device__ __forceinline__ void write_aux(const double* gsf, const double* gmp, 
                             gmp[c], gmp[C + c]);
   aux[c] = a.sigw; aux[C + c] = a.rhow; aux[2 * C + c] = a.lap0; aux[3 * C + c] = a.lbp0;
   aux[4 * C + c] = a.c1; aux[5 * C + c] = a.c2;
-  float* af = (float*)(aux + 6 * C);
-  af[c] = (float)a.T; af[C + c] = (float)(a.S - 1.0); af[2 * C + c] = (float)a.sigw;
-  af[3 * C + c] = (float)a.rhow; af[4 * C + c] = (float)a.lap0; af[5 * C + c] = (float)a.lbp0;
-  af[6 * C + c] = (float)a.c1; af[7 * C + c] = (float)a.c2; af[8 * C + c] = (float)gmp[5 * C + c];
-  af[9 * C + c] = (float)gmp[6 * C + c];
+  float4* af = (float4*)(aux + 6 * C) + 3 * c;
+  af[0] = make_float4((float)a.T, (float)(a.S - 1.0), (float)a.sigw, (float)a.rhow);
+  af[1] = make_float4((float)a.lap0, (float)a.lbp0, (float)a.c1, (float)a.c2);
+  af[2] = make_float4((float)gmp[5 * C + c], (float)gmp[6 * C + c], 0.0f, 0.0f);
 }
 
 __global__ void k_cell_aux(const __grid_constant__ MRef mr) {
@@ -288,7 +288,7 @@ struct PArgs {
   double* acc;                  // [C] per-cell FP64 sums of dm * xi
   int hist;                     // count SIPs per new cell for a following binning
   unsigned long long* nfb;      // SIPs whose Newton fell back to FP64
-  const float* auxf;            // [AUXF][C] FP32 per-cell terms (see write_aux)
+  const float4* auxf;           // [C][3] FP32 per-cell terms (see write_aux)
   const float* gvf;             // [2][nx+1][nz+1] FP32 wind field
   double inv_dx, inv_dz;
   float inv_dxf, inv_dzf, dt_subf, dtg_f, dt_posf;
@@ -323,7 +323,7 @@ __device__ __forceinline__ PArgs make_pargs(const Member& mb, const PCall& c) {
   a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
   a.rm_id = w.rm_id; a.rm_val = w.rm_val; a.flags = w.flags;
   a.acc = w.div; a.hist = c.hist; a.nfb = w.nfb;
-  a.auxf = (const float*)(w.aux + 6 * g.nx * g.nz); a.gvf = w.gvf;
+  a.auxf = (const float4*)(w.aux + 6 * g.nx * g.nz); a.gvf = w.gvf;
   a.inv_dx = mb.inv_dx; a.inv_dz = mb.inv_dz;
   a.inv_dxf = mb.inv_dxf; a.inv_dzf = mb.inv_dzf;
   a.dt_subf = c.dt_subf; a.dtg_f = c.dtg_f; a.dt_posf = c.dt_posf;
@@ -332,8 +332,6 @@ __device__ __forceinline__ PArgs make_pargs(const Member& mb, const PCall& c) {
   return a;
 }
 
-// FP32 per-cell table of the mixed-precision path
-enum { AF_T, AF_SM1, AF_SIGW, AF_RHOW, AF_LAP0, AF_LBP0, AF_C1, AF_C2, AF_MU, AF_RHOF, AUXF };
 
 struct GridVelF {
   const float* gv;
@@ -374,7 +372,10 @@ __global__ void k_to_float(const __grid_constant__ MRef mr) {
 
 template <bool PHYS>
 __global__ void __launch_bounds__(128) k_particles(const __grid_constant__ PK x) {
-  const PArgs a = make_pargs(x.m.get(), x.c);
+  __shared__ PArgs s_a;
+  if (threadIdx.x == 0) s_a = make_pargs(x.m.get(), x.c);
+  __syncthreads();
+  const PArgs& a = s_a;
   const int64_t C = a.nx * a.nz;
   const GridVel gv{a.gv, a.nx, a.nz};
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n;
@@ -634,7 +635,12 @@ __device__ __noinline__ double mixed_remove(GroundGeo a, int64_t k, int i, int j
 }
 
 __global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constant__ PK x) {
-  const PArgs a = make_pargs(x.m.get(), x.c);
+  // the member's arguments, once per block in shared memory: threads read
+  // them on use instead of holding some 60 registers of pointers and sizes
+  __shared__ PArgs s_a;
+  if (threadIdx.x == 0) s_a = make_pargs(x.m.get(), x.c);
+  __syncthreads();
+  const PArgs& a = s_a;
   const int C = (int)(a.nx * a.nz);
   const int nz = (int)a.nz;
   const GridVelF gvf{a.gvf, a.nx, a.nz};
@@ -655,10 +661,9 @@ __global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constan
     const double ms = a.m_s[k];
     const double xik = a.xi[k];
     CellAmbF af;
-    af.T = __ldg(a.auxf + AF_T * C + c); af.S_m1 = __ldg(a.auxf + AF_SM1 * C + c);
-    af.sigw = __ldg(a.auxf + AF_SIGW * C + c); af.rhow = __ldg(a.auxf + AF_RHOW * C + c);
-    af.lap0 = __ldg(a.auxf + AF_LAP0 * C + c); af.lbp0 = __ldg(a.auxf + AF_LBP0 * C + c);
-    af.c1 = __ldg(a.auxf + AF_C1 * C + c); af.c2 = __ldg(a.auxf + AF_C2 * C + c);
+    const float4 q0 = __ldg(a.auxf + 3 * c), q1 = __ldg(a.auxf + 3 * c + 1);
+    af.T = q0.x; af.S_m1 = q0.y; af.sigw = q0.z; af.rhow = q0.w;
+    af.lap0 = q1.x; af.lbp0 = q1.y; af.c1 = q1.z; af.c2 = q1.w;
     const float msf = d2f_int(ms), mwf = d2f_int(mw), xif = d2f_int(xik);
     const float mpf = mwf + msf;
     const float wsf = msf * f_rcp(mpf);
@@ -702,7 +707,8 @@ __global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constan
     const float rzf = (zf - a.z_minf) * a.inv_dzf - (float)j;
     float uf, wf;
     gvf.interp(i, j, rxf, rzf, uf, wf);
-    const float mu_f = __ldg(a.auxf + AF_MU * C + c), rho_f = __ldg(a.auxf + AF_RHOF * C + c);
+    const float2 q2 = __ldg((const float2*)(a.auxf + 3 * c + 2));
+    const float mu_f = q2.x, rho_f = q2.y;
     const float uo = d2f_int(a.vel[k]), wo = d2f_int(a.vel[a.n + k]);
     const float d0 = uf - uo, d1 = wf - wo;
     const float vel_dev = sqrtf(d0 * d0 + d1 * d1);

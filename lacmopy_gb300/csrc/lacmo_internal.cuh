@@ -18,7 +18,8 @@ struct Ws {
   double* dmxi;        // [n]   dm * xi of the last condensation sub-step
   int32_t* rm_id;      // [n]   SIPs removed at the ground in the last sub-step
   double* rm_val;      // [n]   their xi * m_w
-  double* aux;         // [6][C] per-cell terms: sigma_w, rho_w, l_alpha, l_beta, c1, c2
+  double* aux;         // [6][C] per-cell terms: sigma_w, rho_w, l_alpha, l_beta, c1, c2,
+                       // then the mixed path's FP32 table [C][12]
   double* dTh;         // [C]   Delta Theta (advection + relaxation) per sub-step
   double* drv;         // [C]   Delta r_v per sub-step
   double* div;         // [C]   divergence scratch
