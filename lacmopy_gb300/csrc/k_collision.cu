@@ -203,15 +203,12 @@ __device__ __forceinline__ void ensure_exact(const CellArgs& a, int32_t id, doub
   if (a.gk[id] < 0) compute_exact(a, id, Tc, use_E);
 }
 
-// FP32 copies of a cell's SIPs: six arrays of `stride` entries from w (a
-// warp's shared-memory slice, or the cell's slots of the global scratch for
-// cells above the shared-memory size)
+// FP32 copies of a cell's SIPs: v = (xi, R, u, w) per SIP, the kernel bin
+// and the SIP ID; in a warp's shared-memory slice, or in the cell's slots of
+// the global scratch for cells above the shared-memory size
 struct CellSmem {
-  float *fxi, *fR, *fu, *fw;
+  float4* v;
   int32_t *sk, *sid;
-  __device__ __forceinline__ CellSmem(float* w, int64_t stride)
-      : fxi(w), fR(w + stride), fu(w + 2 * stride), fw(w + 3 * stride),
-        sk((int32_t*)(w + 4 * stride)), sid((int32_t*)(w + 5 * stride)) {}
 };
 
 // One ordinary collection (p_crit <= 1 and p_crit > r) of the pair imin/imax
@@ -240,8 +237,8 @@ __device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* 
     XI[imin] = 0.5 * xi_ges - XI[imax];
     if (use_E) { a.gk[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb); a.gk[imax] = a.gk[imin]; }
     if (S) {
-      S->fxi[lmin] = d2f_rn(XI[imin]); S->fxi[lmax] = d2f_rn(XI[imax]);
-      S->fR[lmin] = d2f_rn(RR[imin]); S->fR[lmax] = S->fR[lmin];
+      S->v[lmin].x = d2f_rn(XI[imin]); S->v[lmax].x = d2f_rn(XI[imax]);
+      S->v[lmin].y = d2f_rn(RR[imin]); S->v[lmax].y = S->v[lmin].y;
       S->sk[lmin] = a.gk[imin]; S->sk[lmax] = a.gk[imax];
     }
   } else {
@@ -251,7 +248,7 @@ __device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* 
     XI[imax] -= xi_min;
     if (use_E) a.gk[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
     if (S) {
-      S->fxi[lmax] = d2f_rn(XI[imax]); S->fR[lmin] = d2f_rn(RR[imin]);
+      S->v[lmax].x = d2f_rn(XI[imax]); S->v[lmin].y = d2f_rn(RR[imin]);
       S->sk[lmin] = a.gk[imin];
     }
   }
@@ -259,12 +256,10 @@ __device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* 
 
 // Exact FP64 evaluation of the pair ii/jj (collision/all_or_nothing.py:
 // 553-633) in the reference's operation order, on the global arrays.  Returns
-// 0 (no collision), 1 (one collection) or 2 (multiple collection).  wsm is
+// 0 (no collision), 1 (one collection) or 2 (multiple collection).  Sm holds
 // the warp's shared-memory slice, or null (cells above its size).
-__device__ __noinline__ int exact_pair(const CellArgs& a, float* wsm, int64_t stride, int32_t ii,
-                                       int32_t jj, int li, int lj, double Tc, bool use_E,
-                                       double r) {
-  CellSmem Sm(wsm, stride);
+__device__ __noinline__ int exact_pair(const CellArgs& a, CellSmem Sm, int32_t ii, int32_t jj,
+                                       int li, int lj, double Tc, bool use_E, double r) {
   const CellSmem* S = &Sm;
   ensure_exact(a, ii, Tc, use_E);
   ensure_exact(a, jj, Tc, use_E);
@@ -288,7 +283,7 @@ __device__ __noinline__ int exact_pair(const CellArgs& a, float* wsm, int64_t st
     XI[imax] -= xi_col;
     if (use_E) a.gk[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
     if (S) {
-      S->fxi[lmax] = d2f_rn(XI[imax]); S->fR[lmin] = d2f_rn(RR[imin]);
+      S->v[lmax].x = d2f_rn(XI[imax]); S->v[lmin].y = d2f_rn(RR[imin]);
       S->sk[lmin] = a.gk[imin];
     }
     return 2;
@@ -299,9 +294,8 @@ __device__ __noinline__ int exact_pair(const CellArgs& a, float* wsm, int64_t st
 }
 
 // A pair the FP32 bounds place certainly in an ordinary collection.
-__device__ __noinline__ void certain_collection(const CellArgs& a, float* wsm, int64_t stride,
-                                                int i, int j, double Tc, bool use_E) {
-  CellSmem S(wsm, stride);
+__device__ __noinline__ void certain_collection(const CellArgs& a, CellSmem S, int i, int j,
+                                                double Tc, bool use_E) {
   const int32_t ii = S.sid[i], jj = S.sid[j];
   const bool lo_i = a.xi[ii] <= a.xi[jj];
   const int32_t imin = lo_i ? ii : jj, imax = lo_i ? jj : ii;
@@ -321,23 +315,21 @@ __device__ __noinline__ double philox_from_bits(uint64_t k53) {
 // absolute slack for its cancellation, and the bounds are widened by 2^-14
 // relative (and 1e-36 absolute).  Non-positive multiplicities (left by
 // multiple collections) are undecided.  [r_lo, r_hi] brackets the draw.
-__device__ __forceinline__ int screen_pair(const CellArgs& a, const CellSmem& S, bool use_E, int i,
-                                           int j, float r_lo, float r_hi) {
-  const float xa = S.fxi[i], xb = S.fxi[j];
-  const float ui = S.fu[i], uj = S.fu[j], wi = S.fw[i], wj = S.fw[j];
-  const float du = ui - uj, dw = wi - wj;
-  const float slack = 0x1p-21f * (fabsf(ui) + fabsf(uj) + fabsf(wi) + fabsf(wj));
+__device__ __forceinline__ int screen_pair(const CellArgs& a, bool use_E, float4 vi, int32_t ki,
+                                           float4 vj, int32_t kj, float r_lo, float r_hi) {
+  const float du = vi.z - vj.z, dw = vi.w - vj.w;
+  const float slack = 0x1p-21f * (fabsf(vi.z) + fabsf(vj.z) + fabsf(vi.w) + fabsf(vj.w));
   const float dvm = sqrtf(du * du + dw * dw);
-  const float rs = S.fR[i] + S.fR[j];
+  const float rs = vi.y + vj.y;
   float ef = a.E_const_f;
   if (use_E) {
-    const int64_t ke = (int64_t)S.sk[i] * a.nb + S.sk[j];
+    const int64_t ke = (int64_t)ki * a.nb + kj;
     ef = a.Ef ? __ldg(a.Ef + ke) : d2f_flush(__ldg(a.E + ke));
   }
-  const float core = ((fmaxf(xa, xb) * a.dtdv_f) * (float)(LC_PI * 1.0E-12)) * rs * rs * ef;
+  const float core = ((fmaxf(vi.x, vj.x) * a.dtdv_f) * (float)(LC_PI * 1.0E-12)) * rs * rs * ef;
   const float p_hi = core * (dvm + slack) * (1.0f + 0x1p-14f) + 1e-36f;
   const float p_lo = core * fmaxf(dvm - slack, 0.0f) * (1.0f - 0x1p-14f);
-  const bool sane = xa > 0.0f && xb > 0.0f && p_hi < 1.0f && core >= 1e-30f;
+  const bool sane = vi.x > 0.0f && vj.x > 0.0f && p_hi < 1.0f && core >= 1e-30f;
   if (sane && p_hi < r_lo) return 0;
   if (sane && p_lo > r_hi) return 1;
   return 2;
@@ -370,7 +362,7 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
   if (threadIdx.x == 0) make_cellargs(s_args, x.m.get(), x.cc);
   __syncthreads();
   const CellArgs& a = s_args;
-  extern __shared__ float fsm[];
+  extern __shared__ float4 fsm[];   // 16-byte aligned warp slices
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   float* const wslice = (float*)((char*)fsm + (size_t)wid * CELL_WARP_BYTES);
   const int64_t cursor = a.draws ? *a.cursor : 0;
@@ -402,9 +394,16 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
     const int32_t* ids = a.perm + b;
     // cells above the shared-memory size keep their copies in global scratch
     const bool big = n > CELL_SMEM;
-    float* const wbase = big ? a.gcopy + b : wslice;
-    const int64_t stride = big ? a.n : (int64_t)CELL_SMEM;
-    const CellSmem S(wbase, stride);
+    CellSmem S;
+    if (big) {
+      S.v = (float4*)a.gcopy + b;
+      S.sk = (int32_t*)((float4*)a.gcopy + a.n) + b;
+      S.sid = S.sk + a.n;
+    } else {
+      S.v = (float4*)wslice;
+      S.sk = (int32_t*)(S.v + CELL_SMEM);
+      S.sid = S.sk + CELL_SMEM;
+    }
     const float Tf = d2f_rn(Tc);
     const float rhow_f = (float)LC_PAR_WATER_DENS_0 +
                          (float)LC_PAR_WATER_DENS_1 * ((Tf - (float)LC_PAR_WATER_DENS_2) *
@@ -436,10 +435,7 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
           kb = exact_bin_of(a, id, Tc);
         }
       }
-      S.fxi[q] = d2f_rn(a.xi[id]);
-      S.fR[q] = Rf;
-      S.fu[q] = d2f_rn(a.vel[id]);
-      S.fw[q] = d2f_rn(a.vel[a.n + id]);
+      S.v[q] = make_float4(d2f_rn(a.xi[id]), Rf, d2f_rn(a.vel[id]), d2f_rn(a.vel[a.n + id]));
       S.sk[q] = kb;
       S.sid[q] = id;
     }
@@ -484,12 +480,18 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
             philox_interval(k0, rl0, rh0);
             philox_interval(k1, rl1, rh1);
           }
+          const float4 vi = S.v[i], vj = S.v[j];
+          const int32_t ki = S.sk[i], kj = S.sk[j];
           if (p >= pos) {
-            const int sc = screen_pair(a, S, use_E, i, j, rl0, rh0);
+            const int sc = screen_pair(a, use_E, vi, ki, vj, kj, rl0, rh0);
             if (sc != 0) { my_p = p; my_i = i; my_j = j; my_sc = sc; my_k53 = k0; break; }
           }
           if (has2) {
-            const int sc = screen_pair(a, S, use_E, i2, j2, rl1, rh1);
+            // the couple's second pair shares SIP i unless it starts a new row
+            const bool same = i2 == i;
+            const float4 vi2 = same ? vi : S.v[i2];
+            const int32_t ki2 = same ? ki : S.sk[i2];
+            const int sc = screen_pair(a, use_E, vi2, ki2, S.v[j2], S.sk[j2], rl1, rh1);
             if (sc != 0) { my_p = p + 1; my_i = i2; my_j = j2; my_sc = sc; my_k53 = k1; break; }
           }
           j += 64;
@@ -511,10 +513,10 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
       const int L = __ffs(__ballot_sync(0xffffffffu, my_p == pstar)) - 1;
       if (lane == L) {
         if (my_sc == 1) {
-          certain_collection(a, wbase, stride, my_i, my_j, Tc, use_E);
+          certain_collection(a, S, my_i, my_j, Tc, use_E);
           c0 += 1;
         } else {
-          const int o = exact_pair(a, wbase, stride, S.sid[my_i], S.sid[my_j], my_i, my_j, Tc,
+          const int o = exact_pair(a, S, S.sid[my_i], S.sid[my_j], my_i, my_j, Tc,
                                    use_E, rnd ? rnd[pstar] : philox_from_bits(my_k53));
           c0 += o == 1;
           c1 += o == 2;
@@ -550,14 +552,14 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
             k53 = philox_bits53(a.seed, (uint64_t)rk, pc1);
             philox_interval(k53, r_lo, r_hi);
           }
-          const int sc = screen_pair(a, S, use_E, i, j, r_lo, r_hi);
+          const int sc = screen_pair(a, use_E, S.v[i], S.sk[i], S.v[j], S.sk[j], r_lo, r_hi);
           if (sc == 0) continue;
           if (sc == 1) {
-            certain_collection(a, wbase, stride, i, j, Tc, use_E);
+            certain_collection(a, S, i, j, Tc, use_E);
             c0 += 1;
             continue;
           }
-          const int o = exact_pair(a, wbase, stride, S.sid[i], S.sid[j], i, j, Tc, use_E,
+          const int o = exact_pair(a, S, S.sid[i], S.sid[j], i, j, Tc, use_E,
                                    rnd ? rnd[rk] : philox_from_bits(k53));
           c0 += o == 1;
           c1 += o == 2;
