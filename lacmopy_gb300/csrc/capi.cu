@@ -166,7 +166,7 @@ static int subloop_mixed(const Bt& B, const lacmo_params_t& p, const lacmo_draws
 static int adv_step_mixed(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d,
                           cudaStream_t s) {
   LCHK(launch_wind_float(B, s));
-  LCHK(launch_move(B, p.dt_sub_half, s));
+  LCHK(launch_move_mixed(B, p.dt_sub_half, s));
   LCHK(launch_bin(B, s));
   LCHK(launch_advection(B, p, false, s));
   const int nc1 = p.no_col_per_adv == 1 ? 0 : (p.no_col_per_adv == 2 ? 1 : p.scale_dt_cond);

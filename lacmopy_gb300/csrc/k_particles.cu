@@ -634,6 +634,7 @@ __device__ __noinline__ double mixed_remove(GroundGeo a, int64_t k, int i, int j
   return a.z_min - 0.01 * a.dz;
 }
 
+template <bool PHYS>
 __global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constant__ PK x) {
   // the member's arguments, once per block in shared memory: threads read
   // them on use instead of holding some 60 registers of pointers and sizes
@@ -657,71 +658,80 @@ __global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constan
       mixed_inactive_rel(a.rel, a.n, a.dx, a.dz, k, i);
       continue;
     }
-    double mw = a.m_w[k];
-    const double ms = a.m_s[k];
-    const double xik = a.xi[k];
-    CellAmbF af;
-    const float4 q0 = __ldg(a.auxf + 3 * c), q1 = __ldg(a.auxf + 3 * c + 1);
-    af.T = q0.x; af.S_m1 = q0.y; af.sigw = q0.z; af.rhow = q0.w;
-    af.lap0 = q1.x; af.lbp0 = q1.y; af.c1 = q1.z; af.c2 = q1.w;
-    const float msf = d2f_int(ms), mwf = d2f_int(mw), xif = d2f_int(xik);
-    const float mpf = mwf + msf;
-    const float wsf = msf * f_rcp(mpf);
-    float rho = (a.sol == SOL_AS)
-                    ? af.rhow * ((((float)LC_PAR_RHO_AS_0 * wsf + (float)LC_PAR_RHO_AS_1) * wsf +
-                                  (float)LC_PAR_RHO_AS_2) * wsf + (float)LC_PAR_RHO_AS_3)
-                    : (float)LC_PAR_SOL_DENS_NACL_0 + (float)LC_PAR_SOL_DENS_NACL_1 * wsf +
-                          (float)LC_PAR_SOL_DENS_NACL_2 * af.T +
-                          (float)LC_PAR_SOL_DENS_NACL_3 * wsf * wsf +
-                          (float)LC_PAR_SOL_DENS_NACL_4 * wsf * af.T +
-                          (float)LC_PAR_SOL_DENS_NACL_5 * af.T * af.T;
-    float R = f_cbrt((float)LC_FOUR_PI_OVER_THREE_INV * mpf * f_rcp(rho));
-    const float sig = af.sigw * (1.0f + (a.sol == SOL_AS ? (float)LC_PAR_SIGMA_AS
-                                                          : (float)LC_PAR_SIGMA_NACL) *
-                                             wsf * f_rcp(1.f - wsf));
-    // efflorescence floor m_s (1/0.78 - 1) as an increment, in FP32
-    const float d_effl = msf * (float)(LC_W_S_MAX_AS_INV - 1.0) - mwf;
-    float d;
-    const bool ok = newton_mixed_f(a.sol, a.dt_subf, a.no_iter, mwf, msf, wsf, R, af.T, rho, sig,
-                                   af, d_effl, &d);
-    double dm;
-    if (ok) {
-      dm = f2d_int(d);
-    } else {
-      dm = mixed_newton_fp64(NewtonFP64{a.gsf, a.gmp, a.aux, (int64_t)C, a.dt_sub, a.sol,
-                                        a.no_iter, a.nfb},
-                             c, mw, ms, T_p);
-      d = d2f_int(dm);
-    }
-    mw += dm;
-    // per-cell FP64 sum of dm * xi (executed by L2)
-    atomicAdd(a.acc + c, f2d_int(d * xif));
-    // drag (integration.py:699-718) in FP32 with the ammonium-sulfate radius
-    const float mpn = (mwf + d) + msf;
-    const float wn = msf * f_rcp(mpn);
-    rho = af.rhow * ((((float)LC_PAR_RHO_AS_0 * wn + (float)LC_PAR_RHO_AS_1) * wn +
-                      (float)LC_PAR_RHO_AS_2) * wn + (float)LC_PAR_RHO_AS_3);
-    R = f_cbrt((float)LC_FOUR_PI_OVER_THREE_INV * mpn * f_rcp(rho));
+    double mw = 0.0;
+    double xik = 0.0;
+    float un, wn2;
     const float xf = d2f_int(x), zf = d2f_int(z);
-    const float rxf = (xf - a.x_minf) * a.inv_dxf - (float)i;
-    const float rzf = (zf - a.z_minf) * a.inv_dzf - (float)j;
-    float uf, wf;
-    gvf.interp(i, j, rxf, rzf, uf, wf);
-    const float2 q2 = __ldg((const float2*)(a.auxf + 3 * c + 2));
-    const float mu_f = q2.x, rho_f = q2.y;
-    const float uo = d2f_int(a.vel[k]), wo = d2f_int(a.vel[a.n + k]);
-    const float d0 = uf - uo, d1 = wf - wo;
-    const float vel_dev = sqrtf(d0 * d0 + d1 * d1);
-    const float inv_mu = f_rcp(mu_f);
-    const float Re_p = 2.0E-6f * rho_f * R * vel_dev * inv_mu;
-    float k_dt = 4.5E12f * a.dt_subf * mu_f * f_rcp(rho * R * R);
-    if (Re_p > 0.5f) {
-      if (Re_p < 1000.0f) k_dt *= (1.f + 0.15f * f_pow(Re_p, 0.687f));
-      else k_dt *= 0.0183333333333f * Re_p;
+    if (PHYS) {
+      mw = a.m_w[k];
+      const double ms = a.m_s[k];
+      xik = a.xi[k];
+      CellAmbF af;
+      const float4 q0 = __ldg(a.auxf + 3 * c), q1 = __ldg(a.auxf + 3 * c + 1);
+      af.T = q0.x; af.S_m1 = q0.y; af.sigw = q0.z; af.rhow = q0.w;
+      af.lap0 = q1.x; af.lbp0 = q1.y; af.c1 = q1.z; af.c2 = q1.w;
+      const float msf = d2f_int(ms), mwf = d2f_int(mw), xif = d2f_int(xik);
+      const float mpf = mwf + msf;
+      const float wsf = msf * f_rcp(mpf);
+      float rho = (a.sol == SOL_AS)
+                      ? af.rhow * ((((float)LC_PAR_RHO_AS_0 * wsf + (float)LC_PAR_RHO_AS_1) * wsf +
+                                    (float)LC_PAR_RHO_AS_2) * wsf + (float)LC_PAR_RHO_AS_3)
+                      : (float)LC_PAR_SOL_DENS_NACL_0 + (float)LC_PAR_SOL_DENS_NACL_1 * wsf +
+                            (float)LC_PAR_SOL_DENS_NACL_2 * af.T +
+                            (float)LC_PAR_SOL_DENS_NACL_3 * wsf * wsf +
+                            (float)LC_PAR_SOL_DENS_NACL_4 * wsf * af.T +
+                            (float)LC_PAR_SOL_DENS_NACL_5 * af.T * af.T;
+      float R = f_cbrt((float)LC_FOUR_PI_OVER_THREE_INV * mpf * f_rcp(rho));
+      const float sig = af.sigw * (1.0f + (a.sol == SOL_AS ? (float)LC_PAR_SIGMA_AS
+                                                            : (float)LC_PAR_SIGMA_NACL) *
+                                               wsf * f_rcp(1.f - wsf));
+      // efflorescence floor m_s (1/0.78 - 1) as an increment, in FP32
+      const float d_effl = msf * (float)(LC_W_S_MAX_AS_INV - 1.0) - mwf;
+      float d;
+      const bool ok = newton_mixed_f(a.sol, a.dt_subf, a.no_iter, mwf, msf, wsf, R, af.T, rho, sig,
+                                     af, d_effl, &d);
+      double dm;
+      if (ok) {
+        dm = f2d_int(d);
+      } else {
+        dm = mixed_newton_fp64(NewtonFP64{a.gsf, a.gmp, a.aux, (int64_t)C, a.dt_sub, a.sol,
+                                          a.no_iter, a.nfb},
+                               c, mw, ms, T_p);
+        d = d2f_int(dm);
+      }
+      mw += dm;
+      // per-cell FP64 sum of dm * xi (executed by L2)
+      atomicAdd(a.acc + c, f2d_int(d * xif));
+      // drag (integration.py:699-718) in FP32 with the ammonium-sulfate radius
+      const float mpn = (mwf + d) + msf;
+      const float wn = msf * f_rcp(mpn);
+      rho = af.rhow * ((((float)LC_PAR_RHO_AS_0 * wn + (float)LC_PAR_RHO_AS_1) * wn +
+                        (float)LC_PAR_RHO_AS_2) * wn + (float)LC_PAR_RHO_AS_3);
+      R = f_cbrt((float)LC_FOUR_PI_OVER_THREE_INV * mpn * f_rcp(rho));
+      const float rxf = (xf - a.x_minf) * a.inv_dxf - (float)i;
+      const float rzf = (zf - a.z_minf) * a.inv_dzf - (float)j;
+      float uf, wf;
+      gvf.interp(i, j, rxf, rzf, uf, wf);
+      const float2 q2 = __ldg((const float2*)(a.auxf + 3 * c + 2));
+      const float mu_f = q2.x, rho_f = q2.y;
+      const float uo = d2f_int(a.vel[k]), wo = d2f_int(a.vel[a.n + k]);
+      const float d0 = uf - uo, d1 = wf - wo;
+      const float vel_dev = sqrtf(d0 * d0 + d1 * d1);
+      const float inv_mu = f_rcp(mu_f);
+      const float Re_p = 2.0E-6f * rho_f * R * vel_dev * inv_mu;
+      float k_dt = 4.5E12f * a.dt_subf * mu_f * f_rcp(rho * R * R);
+      if (Re_p > 0.5f) {
+        if (Re_p < 1000.0f) k_dt *= (1.f + 0.15f * f_pow(Re_p, 0.687f));
+        else k_dt *= 0.0183333333333f * Re_p;
+      }
+      const float inv = f_rcp(1.0f + k_dt);
+      un = (uo + k_dt * uf) * inv;
+      wn2 = (wo + k_dt * wf - a.dtg_f) * inv;
+    } else {
+      // the half-step move of integration.py:1474-1481: positions only
+      un = d2f_int(a.vel[k]);
+      wn2 = d2f_int(a.vel[a.n + k]);
     }
-    const float inv = f_rcp(1.0f + k_dt);
-    const float un = (uo + k_dt * uf) * inv;
-    const float wn2 = (wo + k_dt * wf - a.dtg_f) * inv;
     // position (integration.py:552-630)
     const double x0 = x, z0 = z;
     x += f2d_int(a.dt_posf * un);
@@ -732,10 +742,13 @@ __global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constan
     if (!(xnf > 1e-3f && xnf < a.x_maxf - 1e-3f)) x = mixed_wrap_x(x, a.x_max);
     if (!(znf < a.z_capf - 1e-3f)) z = mixed_cap_z(z, a.z_cap);
     int32_t newc;
+    bool removed = false;
     if (!(znf > a.z_minf + 1e-3f) && mixed_below(z, a.z_min)) {
+      if (!PHYS) { xik = a.xi[k]; mw = a.m_w[k]; }
       z = mixed_remove(GroundGeo{a.rel, a.water_removed, a.n, a.x_min, a.z_min, a.dx, a.dz}, k,
                        i, j, x0, z0, xik, mw);
       u = 0.0; w = 0.0;
+      removed = true;
       newc = (int32_t)(-1 - i);
     } else {
       const float qx = d2f_int(x) * a.inv_dxf, qz = d2f_int(z) * a.inv_dzf;
@@ -752,10 +765,59 @@ __global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constan
       if (a.hist) a.rank[k] = atomicAdd(a.counts + newc, 1);
     }
     a.pos[k] = x; a.pos[a.n + k] = z;
-    a.vel[k] = u; a.vel[a.n + k] = w;
-    a.m_w[k] = mw;
+    if (PHYS || removed) { a.vel[k] = u; a.vel[a.n + k] = w; }
+    if (PHYS) a.m_w[k] = mw;
     a.cell[k] = newc;
   }
+}
+
+// Mixed precision: the grid update of one cell (integration.py:402-484,
+// update_material_properties :359-400) in FP64 with exp/log in place of pow,
+// pow(x, y) = exp(y log x) to a few 1e-15 relative, and the chained powers of
+// the Exner function folded into one log; then the per-cell Newton terms
+// (FP64 and the FP32 table) from the same values.
+__device__ __forceinline__ void grid_cell_update_mixed(double* gsf, double* gmp, double* aux,
+                                                       int64_t c, int64_t C, double p_ref,
+                                                       double p_ref_inv, double dTh, double drv,
+                                                       double dml, double V) {
+  double Th = gsf[2 * C + c];
+  const double rho_d = gsf[3 * C + c];
+  double r_v = gsf[4 * C + c];
+  const double mdi = gsf[8 * C + c];
+  const double L_v0 = gmp[2 * C + c];
+  Th += dTh;
+  r_v += drv - dml * mdi;
+  const double ToT = exp(LC_KAPPA_FACTOR2 * log(p_ref_inv * LC_R_D * rho_d * Th));
+  Th += ToT * (L_v0 * dml) / (LC_C_PD * rho_d * V * (1.0 + r_v * LC_HEAT_FACTOR_R_V));
+  const double L2 = log(rho_d * Th * LC_R_D * p_ref_inv);
+  const double pdr = exp(LC_KAPPA_FACTOR * L2);
+  const double T = Th * exp((LC_KAPPA_FACTOR * LC_KAPPA_AIR_DRY) * L2);
+  const double p = pdr * p_ref * (1 + r_v / LC_EPSILON_GC);
+  const double e_s = 2.53E11 * exp(-5420.0 / T);
+  const double S = rho_d * r_v * T * LC_R_V / e_s;
+  const double K = 4.1868E-3 * (5.69 + 0.017 * (T - 273.15));
+  const double D_v = 4.01218E-5 * exp(1.94 * log(T)) / p;
+  const double L_v = 1.0E3 * (2500.82 - 2.358 * (T - 273.0));
+  const double tau = 1 - T / 647.096;
+  const double sigw = 0.2358 * exp(1.256 * log(tau)) * (1 - 0.625 * tau);
+  const double mu = 1.458E-6 * T * sqrt(T) / (T + 110.4);
+  const double rho_f = rho_d * (1.0 + r_v);
+  gsf[c] = T; gsf[C + c] = p; gsf[2 * C + c] = Th; gsf[4 * C + c] = r_v;
+  gsf[6 * C + c] = S; gsf[7 * C + c] = e_s;
+  gmp[c] = K; gmp[C + c] = D_v; gmp[2 * C + c] = L_v; gmp[3 * C + c] = sigw;
+  gmp[4 * C + c] = LC_C_PD * (1 + 0.897 * r_v); gmp[5 * C + c] = mu; gmp[6 * C + c] = rho_f;
+  // the terms of make_cell_amb (lacmo_physics.cuh) from the values above
+  const double rhow = density_water(T);
+  const double lap0 = (LC_C_ALPHA_1 + LC_C_ALPHA_2 * (T - LC_T_ALPHA_0)) * K / p;
+  const double lbp0 = LC_C_BETA_1 * (1.0 + LC_C_BETA_2 * (T - LC_T_ALPHA_0)) * D_v;
+  const double c1 = L_v * L_v / (LC_R_V * K * T * T);
+  const double c2 = LC_R_V * T / (D_v * e_s);
+  aux[c] = sigw; aux[C + c] = rhow; aux[2 * C + c] = lap0; aux[3 * C + c] = lbp0;
+  aux[4 * C + c] = c1; aux[5 * C + c] = c2;
+  float4* af = (float4*)(aux + 6 * C) + 3 * c;
+  af[0] = make_float4((float)T, (float)(S - 1.0), (float)sigw, (float)rhow);
+  af[1] = make_float4((float)lap0, (float)lbp0, (float)c1, (float)c2);
+  af[2] = make_float4((float)mu, (float)rho_f, 0.0f, 0.0f);
 }
 
 // mixed precision: the grid sub-step from the per-cell FP64 sums (then zeroed)
@@ -771,8 +833,7 @@ __global__ void k_grid_acc(const __grid_constant__ MRef mr) {
     const double dml = acc[c] * 1.0E-18;
     acc[c] = 0.0;
     delta_m_l[c] = dml;
-    grid_cell_update(gsf, gmp, c, C, p_ref, p_ref_inv, dTh[c], drv[c], dml, V);
-    write_aux(gsf, gmp, aux, c, C);
+    grid_cell_update_mixed(gsf, gmp, aux, c, C, p_ref, p_ref_inv, dTh[c], drv[c], dml, V);
   }
 }
 
@@ -1018,7 +1079,13 @@ cudaError_t launch_move(const Bt& B, double dt_pos, cudaStream_t s) {
 cudaError_t launch_particles_mixed(const Bt& B, const lacmo_params_t& p, double dt_sub,
                                    double dt_sub_pos, bool write_Tp, bool hist, cudaStream_t s) {
   PK x{B.ref(), pcall(p, dt_sub, dt_sub_pos, write_Tp, hist)};
-  k_particles_mixed<<<grid2(B.n_max, 128, B.M, 152 * 16), 128, 0, s>>>(x); note_launches(1);
+  k_particles_mixed<true><<<grid2(B.n_max, 128, B.M, 152 * 16), 128, 0, s>>>(x); note_launches(1);
+  return cudaGetLastError();
+}
+cudaError_t launch_move_mixed(const Bt& B, double dt_pos, cudaStream_t s) {
+  lacmo_params_t p = {};
+  PK x{B.ref(), pcall(p, 0.0, dt_pos, false, true)};
+  k_particles_mixed<false><<<grid2(B.n_max, 128, B.M, 152 * 16), 128, 0, s>>>(x); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_wind_float(const Bt& B, cudaStream_t s) {

@@ -124,6 +124,7 @@ cudaError_t launch_particles(const Bt& B, const lacmo_params_t& p, double dt_sub
 cudaError_t launch_move(const Bt& B, double dt_pos, cudaStream_t s);
 cudaError_t launch_particles_mixed(const Bt& B, const lacmo_params_t& p, double dt_sub,
                                    double dt_sub_pos, bool write_Tp, bool hist, cudaStream_t s);
+cudaError_t launch_move_mixed(const Bt& B, double dt_pos, cudaStream_t s);
 cudaError_t launch_grid_acc(const Bt& B, cudaStream_t s);
 cudaError_t launch_wind_float(const Bt& B, cudaStream_t s);
 cudaError_t launch_cell_update(const Bt& B, bool grid_update, cudaStream_t s);
