@@ -634,8 +634,47 @@ __device__ __noinline__ double mixed_remove(GroundGeo a, int64_t k, int i, int j
   return a.z_min - 0.01 * a.dz;
 }
 
+// per-thread asynchronous global->shared copies (cp.async, completion waited
+// per thread with cp.async.wait_group)
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(smem)), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(smem)), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n"); }
+__device__ __forceinline__ void cp_async_wait1() {
+  asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait0() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// The SIP state a sub-step reads, staged one SIP ahead: each thread copies its
+// next SIP's attributes into its own shared-memory slots while it works on
+// the current one (two stages, field-major so a warp's slots are contiguous).
+constexpr int PM_THREADS = 128;
+enum { PF_X, PF_Z, PF_U, PF_W, PF_MW, PF_MS, PF_XI, PF_N };
 template <bool PHYS>
-__global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constant__ PK x) {
+__device__ __forceinline__ void prefetch_sip(double (*st)[PM_THREADS], int32_t* sc,
+                                             const PArgs& a, int64_t k) {
+  const int t = threadIdx.x;
+  cp_async4(sc + t, a.cell + k);
+  cp_async8(&st[PF_X][t], a.pos + k);
+  cp_async8(&st[PF_Z][t], a.pos + a.n + k);
+  cp_async8(&st[PF_U][t], a.vel + k);
+  cp_async8(&st[PF_W][t], a.vel + a.n + k);
+  if (PHYS) {
+    cp_async8(&st[PF_MW][t], a.m_w + k);
+    cp_async8(&st[PF_MS][t], a.m_s + k);
+    cp_async8(&st[PF_XI][t], a.xi + k);
+  }
+}
+
+template <bool PHYS>
+__global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_constant__ PK x) {
   // the member's arguments, once per block in shared memory: threads read
   // them on use instead of holding some 60 registers of pointers and sizes
   __shared__ PArgs s_a;
@@ -645,13 +684,23 @@ __global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constan
   const int C = (int)(a.nx * a.nz);
   const int nz = (int)a.nz;
   const GridVelF gvf{a.gvf, a.nx, a.nz};
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t c = a.cell[k];
+  __shared__ double s_pf[2][PF_N][PM_THREADS];
+  __shared__ int32_t s_pc[2][PM_THREADS];
+  const int t = threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + t;
+  int sg = 0;
+  if (k < a.n) prefetch_sip<PHYS>(s_pf[0], s_pc[0], a, k);
+  cp_async_commit();
+  for (; k < a.n; k += stride, sg ^= 1) {
+    if (k + stride < a.n) prefetch_sip<PHYS>(s_pf[sg ^ 1], s_pc[sg ^ 1], a, k + stride);
+    cp_async_commit();
+    cp_async_wait1();   // this SIP's copies have landed
+    const int32_t c = s_pc[sg][t];
     const bool active = c >= 0;
     const int i = active ? c / nz : -1 - c;
     const int j = active ? c - i * nz : -1;
-    double x = a.pos[k], z = a.pos[a.n + k];
+    double x = s_pf[sg][PF_X][t], z = s_pf[sg][PF_Z][t];
     const double T_p = __ldg(a.gsf + (int64_t)i * nz + (active ? j : nz - 1));
     if (a.write_Tp) a.T_p[k] = T_p;
     if (!active) {
@@ -663,9 +712,9 @@ __global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constan
     float un, wn2;
     const float xf = d2f_int(x), zf = d2f_int(z);
     if (PHYS) {
-      mw = a.m_w[k];
-      const double ms = a.m_s[k];
-      xik = a.xi[k];
+      mw = s_pf[sg][PF_MW][t];
+      const double ms = s_pf[sg][PF_MS][t];
+      xik = s_pf[sg][PF_XI][t];
       CellAmbF af;
       const float4 q0 = __ldg(a.auxf + 3 * c), q1 = __ldg(a.auxf + 3 * c + 1);
       af.T = q0.x; af.S_m1 = q0.y; af.sigw = q0.z; af.rhow = q0.w;
@@ -714,7 +763,7 @@ __global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constan
       gvf.interp(i, j, rxf, rzf, uf, wf);
       const float2 q2 = __ldg((const float2*)(a.auxf + 3 * c + 2));
       const float mu_f = q2.x, rho_f = q2.y;
-      const float uo = d2f_int(a.vel[k]), wo = d2f_int(a.vel[a.n + k]);
+      const float uo = d2f_int(s_pf[sg][PF_U][t]), wo = d2f_int(s_pf[sg][PF_W][t]);
       const float d0 = uf - uo, d1 = wf - wo;
       const float vel_dev = sqrtf(d0 * d0 + d1 * d1);
       const float inv_mu = f_rcp(mu_f);
@@ -729,8 +778,8 @@ __global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constan
       wn2 = (wo + k_dt * wf - a.dtg_f) * inv;
     } else {
       // the half-step move of integration.py:1474-1481: positions only
-      un = d2f_int(a.vel[k]);
-      wn2 = d2f_int(a.vel[a.n + k]);
+      un = d2f_int(s_pf[sg][PF_U][t]);
+      wn2 = d2f_int(s_pf[sg][PF_W][t]);
     }
     // position (integration.py:552-630)
     const double x0 = x, z0 = z;
@@ -769,6 +818,7 @@ __global__ void __launch_bounds__(128, 6) k_particles_mixed(const __grid_constan
     if (PHYS) a.m_w[k] = mw;
     a.cell[k] = newc;
   }
+  cp_async_wait0();
 }
 
 // Mixed precision: the grid update of one cell (integration.py:402-484,
@@ -1076,16 +1126,51 @@ cudaError_t launch_move(const Bt& B, double dt_pos, cudaStream_t s) {
   k_particles<false><<<grid2(B.n_max, 128, B.M, 152 * 16), 128, 0, s>>>(x); note_launches(1);
   return cudaGetLastError();
 }
+// Resident-sized grid for the pipelined mixed kernel: each thread walks many
+// SIPs so the one-ahead staging hides the loads of all but the first.
+template <bool PHYS>
+static cudaError_t mixed_grid(const Bt& B, dim3* grid) {
+  static int cached[2][64];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int res = dev < 64 ? cached[PHYS][dev] : 0;
+  if (res <= 0) {
+    int per_sm = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_particles_mixed<PHYS>,
+                                                      PM_THREADS, 0);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    res = per_sm * sms > 0 ? per_sm * sms : 1;
+    if (dev < 64) cached[PHYS][dev] = res;
+  }
+  int64_t bx = res / B.M;
+  const int64_t need = (B.n_max + PM_THREADS - 1) / PM_THREADS;
+  // small states: below 8 SIPs per thread the staging gains little, and more
+  // blocks in flight hide the latency better
+  if (bx * PM_THREADS * 8 > B.n_max) bx = need < 152 * 16 ? need : 152 * 16;
+  if (bx > need) bx = need;
+  if (bx < 1) bx = 1;
+  *grid = dim3((unsigned)bx, (unsigned)B.M);
+  return cudaSuccess;
+}
 cudaError_t launch_particles_mixed(const Bt& B, const lacmo_params_t& p, double dt_sub,
                                    double dt_sub_pos, bool write_Tp, bool hist, cudaStream_t s) {
   PK x{B.ref(), pcall(p, dt_sub, dt_sub_pos, write_Tp, hist)};
-  k_particles_mixed<true><<<grid2(B.n_max, 128, B.M, 152 * 16), 128, 0, s>>>(x); note_launches(1);
+  dim3 grid;
+  cudaError_t e = mixed_grid<true>(B, &grid);
+  if (e != cudaSuccess) return e;
+  k_particles_mixed<true><<<grid, PM_THREADS, 0, s>>>(x); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_move_mixed(const Bt& B, double dt_pos, cudaStream_t s) {
   lacmo_params_t p = {};
   PK x{B.ref(), pcall(p, 0.0, dt_pos, false, true)};
-  k_particles_mixed<false><<<grid2(B.n_max, 128, B.M, 152 * 16), 128, 0, s>>>(x); note_launches(1);
+  dim3 grid;
+  cudaError_t e = mixed_grid<false>(B, &grid);
+  if (e != cudaSuccess) return e;
+  k_particles_mixed<false><<<grid, PM_THREADS, 0, s>>>(x); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_wind_float(const Bt& B, cudaStream_t s) {
