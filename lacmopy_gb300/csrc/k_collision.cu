@@ -313,13 +313,15 @@ __device__ __noinline__ double philox_from_bits(uint64_t k53) {
 // radii are within 1e-6 (relative) of the exact ones, every other FP32
 // operation and conversion within 2^-24, the velocity difference carries an
 // absolute slack for its cancellation, and the bounds are widened by 2^-14
-// relative (and 1e-36 absolute).  Non-positive multiplicities (left by
-// multiple collections) are undecided.  [r_lo, r_hi] brackets the draw.
+// relative (and 1e-36 absolute); |du| + |dw| in place of the Euclidean norm
+// gives a looser upper bound that decides most skips alone.  Non-positive
+// multiplicities (left by multiple collections) are undecided.  [r_lo, r_hi]
+// brackets the draw.
 __device__ __forceinline__ int screen_pair(const CellArgs& a, bool use_E, float4 vi, int32_t ki,
                                            float4 vj, int32_t kj, float r_lo, float r_hi) {
   const float du = vi.z - vj.z, dw = vi.w - vj.w;
+  const float adu = fabsf(du), adw = fabsf(dw);
   const float slack = 0x1p-21f * (fabsf(vi.z) + fabsf(vj.z) + fabsf(vi.w) + fabsf(vj.w));
-  const float dvm = sqrtf(du * du + dw * dw);
   const float rs = vi.y + vj.y;
   float ef = a.E_const_f;
   if (use_E) {
@@ -327,11 +329,17 @@ __device__ __forceinline__ int screen_pair(const CellArgs& a, bool use_E, float4
     ef = a.Ef ? __ldg(a.Ef + ke) : d2f_flush(__ldg(a.E + ke));
   }
   const float core = ((fmaxf(vi.x, vj.x) * a.dtdv_f) * (float)(LC_PI * 1.0E-12)) * rs * rs * ef;
+  const bool sane = vi.x > 0.0f && vj.x > 0.0f && core >= 1e-30f;
+  // common case first: |du| + |dw| >= |(du, dw)| gives an upper bound without
+  // the square root, enough to skip the pair when the draw is above it
+  const float p_l1 = core * ((adu + adw) + slack) * (1.0f + 0x1p-14f) + 1e-36f;
+  if (sane && p_l1 < 1.0f && p_l1 < r_lo) return 0;
+  const float dvm = sqrtf(du * du + dw * dw);
   const float p_hi = core * (dvm + slack) * (1.0f + 0x1p-14f) + 1e-36f;
   const float p_lo = core * fmaxf(dvm - slack, 0.0f) * (1.0f - 0x1p-14f);
-  const bool sane = vi.x > 0.0f && vj.x > 0.0f && p_hi < 1.0f && core >= 1e-30f;
-  if (sane && p_hi < r_lo) return 0;
-  if (sane && p_lo > r_hi) return 1;
+  const bool ok = sane && p_hi < 1.0f;
+  if (ok && p_hi < r_lo) return 0;
+  if (ok && p_lo > r_hi) return 1;
   return 2;
 }
 // draw intervals: Philox bits (exact: r - r_lo < 2^-24) or an injected draw
