@@ -91,8 +91,8 @@ def _member_state(a):
 def make_members(args, rank):
     """The ensemble's states, generated on the host cores in parallel (spawned
     workers: no CUDA context is forked)."""
-    jobs = [(args.nx, args.nz, args.uneven[0], args.uneven[1], 5000 + 1000 * rank + m)
-            for m in range(args.members)]
+    jobs = [(args.nx, args.nz, args.uneven[0], args.uneven[1], sd)
+            for sd in rank_seeds(rank, args.members)[1]]
     workers = max(1, min(len(jobs), (os.cpu_count() or 1)))
     with ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn")) as ex:
         return list(ex.map(_member_state, jobs))
@@ -173,6 +173,23 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def aggregate_ranks(ms, ups, dist, device):
+    """Whole-job numbers of N replicas: the slowest rank's time and the sum of
+    all ranks' SIP updates (value = updates / time)."""
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    u = torch.tensor([ups], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
+def rank_seeds(rank, members):
+    """Philox keys and state seeds of a rank's ensemble: disjoint across ranks."""
+    return ([1 + 64 * rank + m for m in range(members)],
+            [5000 + 1000 * rank + m for m in range(members)])
 
 
 # ---------------------------------------------------------------------------
@@ -290,15 +307,11 @@ def run_ours(args):
         ms = sum(a.elapsed_time(b) for a, b in ev)
         ups = float(sum(int(x) for x in n_active))
         if dist:
-            t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-            u = torch.tensor([ups], dtype=torch.float64, device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dist.all_reduce(u, op=dist.ReduceOp.SUM)
-            ms, ups = float(t.item()), float(u.item())
+            ms, ups = aggregate_ranks(ms, ups, dist, "cuda")
         return ms, ups, launches, clocks
 
     # ---- headline: the batched mixed-precision ensemble ----
-    seeds = [1 + 64 * rank + m for m in range(args.members)]
+    seeds = rank_seeds(rank, args.members)[0]
     batch = BatchState(members, seeds, precision="mixed")   # copies the states to the GPU
     n_total = batch.n_total
     ms, ups, launches, clocks = timed(batch, True)
