@@ -329,6 +329,34 @@ int lacmo_radius_and_bin(const double* m, const double* rho, int64_t n, double R
                          double bin_factor_R_log, int64_t no_kernel_bins, double* R,
                          int64_t* bin, void* stream);
 
+/* ---- adjoint of the condensation sub-steps (k_adjoint.cu) ----
+ * The differentiated model: SIPs keep their cells and multiplicities (motion,
+ * advection and collisions are recorded events held fixed); each sub-step
+ * solves the implicit Euler condensation step of integration.py:728-836 to
+ * convergence for every SIP with cell >= 0, then updates Theta and r_v of the
+ * cells as integration.py:402-438 does, the ambient terms following from Theta
+ * and r_v.  Hygroscopicity kappa scales the ammonium-sulfate water activity,
+ * a_w = 1 + (kappa / 0.6)(a_w_AS(w_s) - 1); kappa = 0.6 is the reference.
+ * Arrays are device pointers: m_w, m_s, xi, cell [n]; Theta, r_v, rho_d,
+ * mass_dry_inv [C]; dTh, drv [C] optional per-sub-step increments (null =
+ * 0); dml [C] scratch.  lacmo_adj_forward advances n_sub sub-steps in place
+ * and, when tape_m ([n_sub + 1][n]) and tape_c ([n_sub][2][C]) are given,
+ * records the states for lacmo_adj_backward.  lacmo_adj_backward turns the
+ * adjoints of the final state (lam_m [n], lam_Th, lam_rv [C]) into those of
+ * the initial state, accumulating d/d m_s into grad_ms [n] and d/d kappa into
+ * grad_kappa [1]; lam_dml [C] is scratch. */
+int lacmo_adj_forward(int64_t n, int64_t C, double* m_w, const double* m_s, const double* xi,
+                      const int32_t* cell, double* Th, double* r_v, const double* rho_d,
+                      const double* mass_dry_inv, const double* dTh, const double* drv,
+                      double* dml, double dt_sub, double kappa, double p_ref, double V, int n_sub,
+                      double* tape_m, double* tape_c, void* stream);
+int lacmo_adj_backward(int64_t n, int64_t C, const double* m_s, const double* xi,
+                       const int32_t* cell, const double* rho_d, const double* mass_dry_inv,
+                       const double* dTh, const double* drv, double* dml, double dt_sub,
+                       double kappa, double p_ref, double V, int n_sub, const double* tape_m,
+                       const double* tape_c, double* lam_m, double* lam_Th, double* lam_rv,
+                       double* lam_dml, double* grad_ms, double* grad_kappa, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

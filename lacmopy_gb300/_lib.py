@@ -113,6 +113,10 @@ PROTOTYPES = {
     "lacmo_newton_full": (ctypes.c_int, [ctypes.c_int, i64, dbl, ctypes.c_int] + [vp] * 16 + [vp]),
     "lacmo_interpolate_velocity": (ctypes.c_int, [vp, vp, vp, i64, i64, i64, vp, vp]),
     "lacmo_radius_and_bin": (ctypes.c_int, [vp, vp, i64, dbl, dbl, i64, vp, vp, vp]),
+    "lacmo_adj_forward": (ctypes.c_int, [i64, i64] + [vp] * 11 + [dbl, dbl, dbl, dbl,
+                                                                   ctypes.c_int, vp, vp, vp]),
+    "lacmo_adj_backward": (ctypes.c_int, [i64, i64] + [vp] * 8 + [dbl, dbl, dbl, dbl,
+                                                                  ctypes.c_int] + [vp] * 9),
 }
 
 _lib = None

@@ -24,6 +24,7 @@ UNITS = {
     "k_particles.cu": [],
     "k_collision.cu": ["-fmad=false"],
     "k_static.cu": [],
+    "k_adjoint.cu": [],
 }
 
 

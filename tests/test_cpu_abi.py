@@ -31,9 +31,24 @@ def test_library_exports_every_declared_symbol():
     assert lib.lacmo_error_string(-3) == b"injected draw buffer too short"
 
 
+def _arity():
+    """Number of parameters of every function the header declares."""
+    txt = open(os.path.join(REPO, "include", "lacmo_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(lacmo_\w+)\s*\(([^;{]*?)\)\s*;", txt, flags=re.S):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
 def test_python_binding_covers_header():
     from lacmopy_gb300 import _lib
     assert set(_declared()) == set(_lib.PROTOTYPES)
+    arity = _arity()
+    wrong = {n: (len(args), arity[n]) for n, (_, args) in _lib.PROTOTYPES.items()
+             if n in arity and len(args) != arity[n]}
+    assert not wrong, wrong
 
 
 def test_workspace_size_and_argument_errors():
