@@ -13,6 +13,11 @@ spun-up 2-D state with the same Philox draws; per-output error statement.
 
     python -m lacmopy_gb300.reports golovin [--kappa K] [--t-end T] [--seeds S ...]
     python -m lacmopy_gb300.reports precision [--spcm A B] [--spinup N] [--horizons N ...]
+    python -m lacmopy_gb300.reports adjoint [--spcm A B]
+
+``adjoint``: gradients of the domain-mean liquid water path after 600 s of
+condensation sub-steps with respect to per-SIP solute mass and hygroscopicity
+(lacmopy_gb300.adjoint), timing, and a finite-difference check.
 """
 import argparse
 import json
@@ -128,9 +133,46 @@ def precision(spcm=(52, 76), nx=75, nz=75, spinup=60, horizons=(10, 60), seed=10
     return {"spinup_steps": spinup, "rows": rows}
 
 
+def adjoint(spcm=(52, 76), nx=75, nz=75, seconds=600, every_steps=60, seed=1001,
+            kappa=0.6, fd_h=1e-5):
+    """d(domain-mean LWP)/d m_s and d/d kappa through ``seconds`` of
+    condensation sub-steps (collisions and motion held fixed), checkpointed
+    every ``every_steps`` advection steps; timing and a central finite
+    difference of d/d kappa."""
+    import torch
+    from . import adjoint as adj, synthetic
+    st = synthetic.make_icmw_state(Nx=nx, Nz=nz, no_spcm=tuple(spcm), seed=seed,
+                                   kernel_type="Long_Bott")
+    model = adj.CondensationModel(st)
+    n_sub = int(round(seconds / model.dt_sub))
+    every = int(round(every_steps * 1.0 / model.dt_sub))
+    m_s = model.m_s0.clone().requires_grad_(True)
+    k = torch.tensor(kappa, dtype=torch.float64, device="cuda", requires_grad=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J = adj.liquid_water(model, m_s, k, n_sub=n_sub, checkpoint_every=every)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    J.backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    w = model.lwp_weights()
+
+    def J_of(kv):
+        m_w, _, _ = model.run(model.m_s0, kv, n_sub)
+        return float((w * m_w).sum())
+    fd = (J_of(kappa + fd_h) - J_of(kappa - fd_h)) / (2 * fd_h)
+    g = m_s.grad
+    return {"n_sips": model.n, "sub_steps": n_sub, "checkpoint_every_sub_steps": every,
+            "lwp": float(J.detach()), "dlwp_dkappa": float(k.grad), "dlwp_dkappa_fd": fd,
+            "fd_rel_err": abs(float(k.grad) - fd) / abs(fd),
+            "dlwp_dms_max_abs": float(g.abs().max()), "dlwp_dms_mean": float(g.mean()),
+            "forward_s": t1 - t0, "backward_s": t2 - t1}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["golovin", "precision"])
+    ap.add_argument("what", choices=["golovin", "precision", "adjoint"])
     ap.add_argument("--kappa", type=int, default=1000)
     ap.add_argument("--t-end", type=float, default=3600.0)
     ap.add_argument("--dt-save", type=float, default=600.0)
@@ -141,6 +183,8 @@ def main():
     a = ap.parse_args()
     if a.what == "golovin":
         r = golovin_box(a.kappa, a.t_end, 1.0, tuple(a.seeds), a.dt_save)
+    elif a.what == "adjoint":
+        r = adjoint(tuple(a.spcm))
     else:
         r = precision(tuple(a.spcm), spinup=a.spinup, horizons=tuple(a.horizons))
     print(json.dumps(r))
