@@ -85,6 +85,9 @@ typedef struct {
   int64_t no_kernel_bins;
   double R_kernel_low_log, bin_factor_R_log;
   int32_t precision;     /* LACMO_PRECISION_FP64 or LACMO_PRECISION_MIXED     */
+  int32_t thin_draws;    /* Philox draws only: 0 one draw per pair; 1 the
+                            thinned draws (the same iid uniforms, sampled per
+                            chunk of 32 pairs; lacmo_thin.h)                   */
 } lacmo_params_t;
 
 /* Arithmetic of lacmo_integrate_adv_step.  FP64: the reference's FP64 path

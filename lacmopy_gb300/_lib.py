@@ -46,7 +46,7 @@ class Params(ctypes.Structure):
                 ("solute", i32), ("init_profile_r_v", vp), ("init_profile_Theta", vp),
                 ("relaxation_time_profile", vp), ("E_col_grid", vp), ("E_col_const", dbl),
                 ("no_kernel_bins", i64), ("R_kernel_low_log", dbl), ("bin_factor_R_log", dbl),
-                ("precision", i32)]
+                ("precision", i32), ("thin_draws", i32)]
 
 
 PRECISION_FP64 = 0

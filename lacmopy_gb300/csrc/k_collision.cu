@@ -22,6 +22,7 @@
 #include "lacmo_crmath.h"
 #include "lacmo_internal.cuh"
 #include "lacmo_physics.cuh"
+#include "lacmo_thin.h"
 
 namespace lacmo {
 
@@ -107,6 +108,7 @@ struct CellArgs {
   const int32_t* cell_order;   // cells, largest first
   int32_t* cell_ctr;           // next cell_order entry to take
   float* gcopy;                // [6][n] FP32 copies by slot, for cells above CELL_SMEM
+  int thin;                    // thinned Philox draws (lacmo_thin.h)
 };
 
 // the parameters a collision step shares across members
@@ -121,6 +123,7 @@ struct CellCommon {
   int64_t n_draws;
   float dtdv_f, lo_f, inv_bl_f, E_const_f;
   const float* Ef;
+  int thin;
 };
 struct CK {
   MRef m;
@@ -140,6 +143,7 @@ __device__ __forceinline__ void make_cellargs(CellArgs& a, const Member& mb, con
   a.Ef = cc.Ef;
   a.cell_order = mb.w.cell_order; a.cell_ctr = mb.w.cell_ctr;
   a.gcopy = mb.w.gcopy;
+  a.thin = cc.thin;
 }
 
 // integer-unit conversions (GB300 runs FP64 conversions on its narrow FP64
@@ -355,6 +359,171 @@ __device__ __forceinline__ void injected_interval(double r, float& r_lo, float& 
   r_hi = in01 ? r_lo + 0x1p-24f : -1.0f;
 }
 
+// the exact data of a cell's SIPs, computed lazily from the step-start masses
+__device__ __forceinline__ void init_exact_scratch(const CellArgs& a, const CellSmem& S, int n,
+                                                   int lane) {
+  for (int q = lane; q < n; q += 32) {
+    const int32_t id = S.sid[q];
+    a.gR[id] = a.m_w[id] + a.m_s[id];
+    a.grho[id] = a.m_s[id];
+    a.gk[id] = -1;
+  }
+  __syncwarp();
+}
+
+// (i, j) moved forward by `adv` ranks in lexicographic order
+__device__ __forceinline__ void advance_pair(int n, int& i, int& j, int adv) {
+  j += adv;
+  while (j > n - 1 && i < n - 2) { j += i + 2 - n; ++i; }
+}
+
+// one pair with draw r: the screen on the FP32 copies, else the exact
+// evaluation; returns 0 (no change) or the outcome counters it adds
+__device__ __forceinline__ void decide_pair(const CellArgs& a, const CellSmem& S, bool use_E,
+                                            int i, int j, double r, float r_lo, float r_hi,
+                                            double Tc, int64_t& c0, int64_t& c1) {
+  const int sc = screen_pair(a, use_E, S.v[i], S.sk[i], S.v[j], S.sk[j], r_lo, r_hi);
+  if (sc == 0) return;
+  if (sc == 1) {
+    certain_collection(a, S, i, j, Tc, use_E);
+    c0 += 1;
+    return;
+  }
+  const int o = exact_pair(a, S, S.sid[i], S.sid[j], i, j, Tc, use_E, r);
+  c0 += o == 1;
+  c1 += o == 2;
+}
+
+// the thinned draws of lacmo_thin.h for one cell, warp-cooperative: each
+// part is bounded with one pair per lane; a warp maximum over the background
+// pairs gives q and one uniform (the sub-0 ones of 32 chunks computed ahead,
+// one per lane) decides their hit, whose first-hit draws are evaluated by all
+// lanes at once; individual pairs are screened in parallel with their own
+// draws; the walk then takes the events in rank order
+__device__ __noinline__ void thin_cell(const CellArgs& a, const CellSmem& S, int n, int P,
+                                       double Tc, bool use_E, uint64_t pc1, int lane,
+                                       int64_t& c0, int64_t& c1) {
+  constexpr int L = LACMO_THIN_L;
+  static_assert(LACMO_THIN_L == 32, "one pair of a part per lane");
+  int pos = 0, sub = 0;   // first unprocessed rank, part counter of its chunk
+  int bi = 0, bj = 1;     // the pair of rank pos
+  bool scratch = false;
+  int ubase = -1;         // chunk of lane 0's precomputed sub-0 uniform
+  double upre = 0.0;
+  const unsigned below = (1u << lane) - 1u;
+  while (pos < P) {
+    const int chunk = pos / L;
+    const int e_end = (chunk + 1) * L < P ? (chunk + 1) * L : P;
+    const int m = e_end - pos;
+    int i = bi, j = bj;
+    const bool mine = lane < m;
+    if (mine) advance_pair(n, i, j, lane);
+    float pb = -1.0f;
+    float4 vi, vj;
+    int32_t ki = 0, kj = 0;
+    if (mine) {
+      vi = S.v[i]; vj = S.v[j]; ki = S.sk[i]; kj = S.sk[j];
+      const float ef = use_E ? (a.Ef ? __ldg(a.Ef + (int64_t)ki * a.nb + kj)
+                                     : d2f_flush(__ldg(a.E + (int64_t)ki * a.nb + kj)))
+                             : a.E_const_f;
+      pb = lt_pair_bound(vi.x, vi.y, vi.z, vi.w, vj.x, vj.y, vj.z, vj.w, ef, a.dtdv_f);
+    }
+    const bool bg = mine && pb >= 0.0f && pb < LACMO_THIN_TAU;
+    const unsigned bgmask = __ballot_sync(0xffffffffu, bg);
+    const int m_bg = __popc(bgmask);
+    // background hit: lane h (or none)
+    int h = 32;
+    int e = 0;
+    uint32_t jd = 0;
+    if (m_bg > 0) {
+      float qmax = bg ? pb : 0.0f;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) qmax = fmaxf(qmax, __shfl_xor_sync(0xffffffffu, qmax, off));
+      e = lt_exponent(qmax);
+      double u;
+      if (sub == 0) {
+        if (ubase < 0 || chunk < ubase || chunk >= ubase + 32) {
+          ubase = chunk;
+          upre = lt_uniform(a.seed, (uint64_t)(chunk + lane), 0u, 0u, pc1);
+        }
+        u = __shfl_sync(0xffffffffu, upre, chunk - ubase);
+      } else {
+        u = lt_uniform(a.seed, (uint64_t)chunk, (uint32_t)sub, 0u, pc1);
+      }
+      if (u < __ldg(&LACMO_THIN_H[e - LACMO_THIN_E_MIN][m_bg - 1])) {
+        bool succ = false;
+        if (lane < m_bg - 1) {
+          const double v = lt_uniform(a.seed, (uint64_t)chunk, (uint32_t)sub, (uint32_t)(1 + lane), pc1);
+          succ = v < __ldg(&LACMO_THIN_P[e - LACMO_THIN_E_MIN][m_bg - lane - 1]);
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, succ);
+        const int g = bal ? __ffs(bal) - 1 : m_bg - 1;
+        jd = g < m_bg - 1 ? (uint32_t)(g + 2) : (uint32_t)m_bg;
+        // the lane holding the g-th background pair
+        h = __ffs(__ballot_sync(0xffffffffu, bg && __popc(bgmask & below) == g)) - 1;
+      }
+    }
+    // individual pairs: their own draws, screened
+    uint64_t k53 = 0;
+    int sc = 0;
+    if (mine && !bg && lane < h) {
+      k53 = philox_bits53(a.seed, (uint64_t)(pos + lane), pc1);
+      float r_lo, r_hi;
+      philox_interval(k53, r_lo, r_hi);
+      sc = screen_pair(a, use_E, vi, ki, vj, kj, r_lo, r_hi);
+    }
+    unsigned cand = __ballot_sync(0xffffffffu, sc != 0);
+    // the walk: candidates before the hit in rank order, then the hit
+    int stop = -1;
+    while (stop < 0) {
+      const int t = cand ? __ffs(cand) - 1 : 32;
+      if (t >= h && h < 32) {
+        if (!scratch) { init_exact_scratch(a, S, n, lane); scratch = true; }
+        if (lane == h) {
+          const double r = ldexp(lt_uniform(a.seed, (uint64_t)chunk, (uint32_t)sub, jd, pc1), -e);
+          // a float interval around r: truncation and the next float up
+          // (below the normal range: [0, 2^-126])
+          const bool normal = r >= 0x1p-126;
+          const float r_lo = normal ? d2f_down_pos(r) : 0.0f;
+          const float r_hi = normal ? __uint_as_float(__float_as_uint(r_lo) + 1u) : 0x1p-126f;
+          decide_pair(a, S, use_E, i, j, r, r_lo, r_hi, Tc, c0, c1);
+        }
+        stop = h;
+        break;
+      }
+      if (t == 32) break;   // no event in the part
+      if (!scratch) { init_exact_scratch(a, S, n, lane); scratch = true; }
+      int collided = 0;
+      if (lane == t) {
+        if (sc == 1) {
+          certain_collection(a, S, i, j, Tc, use_E);
+          c0 += 1;
+          collided = 1;
+        } else {
+          const int o = exact_pair(a, S, S.sid[i], S.sid[j], i, j, Tc, use_E,
+                                   philox_from_bits(k53));
+          c0 += o == 1;
+          c1 += o == 2;
+          collided = o != 0;
+        }
+      }
+      collided = __shfl_sync(0xffffffffu, collided, t);
+      if (collided) { stop = t; break; }
+      cand &= cand - 1;   // no change: the screens of the later pairs still hold
+    }
+    __threadfence_block();
+    __syncwarp();
+    if (stop < 0) {
+      advance_pair(n, bi, bj, m);
+      pos = e_end; sub = 0;
+    } else {
+      advance_pair(n, bi, bj, stop + 1);
+      pos += stop + 1;
+      sub = pos < e_end ? sub + 1 : 0;
+    }
+  }
+}
+
 // One warp per cell.  Shared memory holds FP32 copies of xi, R, u, w and the
 // kernel bin (24 B per SIP with the SIP ID); the pairs are screened in
 // parallel in lexicographic order and only the events of the sequential
@@ -431,7 +600,7 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
                                   (float)LC_PAR_SOL_DENS_NACL_3 * wsf * wsf +
                                   (float)LC_PAR_SOL_DENS_NACL_4 * wsf * Tf +
                                   (float)LC_PAR_SOL_DENS_NACL_5 * Tf * Tf;
-      const float Rf = cbrtf(c43 * mpf / rho);
+      const float Rf = lt_cbrtf(c43 * mpf / rho);
       int32_t kb = 0;
       if (use_E) {
         const float v = (__logf(Rf) - a.lo_f) * a.inv_bl_f + 0.5f;
@@ -448,6 +617,12 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
       S.sid[q] = id;
     }
     __syncwarp();
+    const int P = (int)((int64_t)n * (n - 1) / 2);
+    if (a.thin) {
+      thin_cell(a, S, n, P, Tc, use_E, pc1, lane, c0, c1);
+      __syncwarp();
+      continue;
+    }
     // Speculative sequential order.  From rank pos on, the lanes screen the
     // pairs in parallel with the current state: lane l takes the couples
     // (p0 + 2l + 64t, p0 + 2l + 64t + 1), p0 = pos rounded down to even, in
@@ -458,7 +633,6 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
     // evaluation), then screening resumes at p* + 1.  Most cells have no
     // event at all.  A cell with many events finishes with the anti-diagonal
     // schedule from its current position.
-    const int P = (int)((int64_t)n * (n - 1) / 2);
     const int event_limit = 16 + P / 64;
     int pos = 0;           // first rank not processed yet
     int bi = 0, bj = 1;    // the pair of rank pos & ~1
@@ -819,6 +993,7 @@ cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lac
   cc.sol = p.solute; cc.draws = d.draws; cc.n_draws = d.n_draws;
   cc.dtdv_f = (float)cc.dtdv; cc.lo_f = (float)cc.lo; cc.inv_bl_f = (float)(1.0 / cc.bl);
   cc.E_const_f = (float)cc.E_const;
+  cc.thin = (p.thin_draws != 0 && d.draws == nullptr) ? 1 : 0;
   cc.Ef = nullptr;
   float* Ef = B.one.w.Ef;   // member 0's slot serves the whole batch
   if (p.E_col_grid && Ef && p.no_kernel_bins <= LACMO_MAX_KERNEL_BINS) {

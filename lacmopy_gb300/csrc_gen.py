@@ -1,13 +1,20 @@
-"""Generate csrc/lacmo_constants.h from lacmopy_gb300.constants.
+"""Generate csrc/lacmo_constants.h from lacmopy_gb300.constants, and
+csrc/lacmo_thin_tables.h (the hit probabilities of the thinned collision
+draws, computed in exact rational arithmetic).
 
-``python -m lacmopy_gb300.csrc_gen`` rewrites the header (hexadecimal float
-literals, so the CUDA kernels see the reference's exact constants).
+``python -m lacmopy_gb300.csrc_gen`` rewrites both headers (hexadecimal float
+literals, so the CUDA kernels and the oracle see identical values).
 """
 import os
+from fractions import Fraction
 
 from .constants import named_doubles
 
-HEADER = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "lacmo_constants.h")
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc")
+HEADER = os.path.join(HERE, "lacmo_constants.h")
+THIN_HEADER = os.path.join(HERE, "lacmo_thin_tables.h")
+# thinning bounds q = 2^-e, e = THIN_E_MIN .. THIN_E_MAX; chunks of up to THIN_L pairs
+THIN_E_MIN, THIN_E_MAX, THIN_L = 2, 127, 32
 
 
 def render_constants():
@@ -20,6 +27,46 @@ def render_constants():
     return "\n".join(lines) + "\n"
 
 
+def thin_tables():
+    """H[e][m] = 1 - (1 - 2^-e)^m, the probability that at least one of m
+    independent uniforms falls below q = 2^-e, and P[e][r] = q / H[e][r], the
+    probability that the first of r remaining pairs is a hit given that one
+    of them is; each exact, rounded once to double."""
+    H, P = [], []
+    for e in range(THIN_E_MIN, THIN_E_MAX + 1):
+        q = Fraction(1, 2 ** e)
+        hr = [float(1 - (1 - q) ** m) for m in range(1, THIN_L + 1)]
+        pr = [float(q / (1 - (1 - q) ** r)) for r in range(1, THIN_L + 1)]
+        H.append(hr)
+        P.append(pr)
+    return H, P
+
+
+def render_thin_tables():
+    H, P = thin_tables()
+    ne = THIN_E_MAX - THIN_E_MIN + 1
+    lines = ["/* Generated by lacmopy_gb300/csrc_gen.py (exact rational arithmetic). */",
+             "/* Thinned collision draws: q = 2^-e, e = LACMO_THIN_E_MIN ..        */",
+             "/* LACMO_THIN_E_MAX; chunks of up to LACMO_THIN_L pairs.             */",
+             "/* LACMO_THIN_H[e - E_MIN][m - 1] = 1 - (1 - q)^m                    */",
+             "/* LACMO_THIN_P[e - E_MIN][r - 1] = q / (1 - (1 - q)^r)              */",
+             "#pragma once", "",
+             f"#define LACMO_THIN_E_MIN {THIN_E_MIN}",
+             f"#define LACMO_THIN_E_MAX {THIN_E_MAX}",
+             f"#define LACMO_THIN_L {THIN_L}", "",
+             "#ifndef LACMO_THIN_QUAL",
+             "#define LACMO_THIN_QUAL static const",
+             "#endif"]
+    for name, T in (("LACMO_THIN_H", H), ("LACMO_THIN_P", P)):
+        lines.append(f"LACMO_THIN_QUAL double {name}[{ne}][{THIN_L}] = {{")
+        for row in T:
+            lines.append("  {" + ", ".join(v.hex() for v in row) + "},")
+        lines.append("};")
+    return "\n".join(lines) + "\n"
+
+
 if __name__ == "__main__":
     with open(HEADER, "w") as f:
         f.write(render_constants())
+    with open(THIN_HEADER, "w") as f:
+        f.write(render_thin_tables())

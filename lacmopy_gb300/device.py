@@ -52,7 +52,7 @@ class DeviceState:
                  "grid_mass_flux_air_dry")
 
     def __init__(self, st, device="cuda", draws="philox", seed=1001, precision="fp64",
-                 workspace=True):
+                 workspace=True, thin=False):
         self.lib = _lib.load()
         self.device = device
         g = st["grid_no_cells"]
@@ -96,6 +96,7 @@ class DeviceState:
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', got {precision!r}")
         self.precision = precision
+        self.thin = bool(thin)
         self.set_params(st)
         self.draw_mode = draws if isinstance(draws, str) else "buffer"
         self.seed = int(seed)
@@ -139,7 +140,7 @@ class DeviceState:
             solute_code(st["solute_type"]), self.prof_rv.data_ptr(), self.prof_th.data_ptr(),
             self.t_relax.data_ptr(), self.E.data_ptr() if self.E is not None else None, E_const,
             nb, lo, bl, _lib.PRECISION_MIXED if getattr(self, "precision", "fp64") == "mixed"
-            else _lib.PRECISION_FP64)
+            else _lib.PRECISION_FP64, int(getattr(self, "thin", False)))
 
     def prepare(self):
         _lib.check(self.lib.lacmo_prepare(ctypes.byref(self.sips), ctypes.byref(self.grid),
@@ -334,12 +335,12 @@ class BatchState:
     keyed by each member's seed, so member m evolves exactly like a
     ``DeviceState(states[m], draws="philox", seed=seeds[m])`` on its own."""
 
-    def __init__(self, states, seeds, device="cuda", precision="mixed"):
+    def __init__(self, states, seeds, device="cuda", precision="mixed", thin=False):
         if len(states) != len(seeds) or not states:
             raise ValueError("one seed per member state is required")
         self.lib = _lib.load()
         self.members = [DeviceState(st, device=device, draws="philox", seed=int(sd),
-                                    precision=precision, workspace=False)
+                                    precision=precision, workspace=False, thin=thin)
                         for st, sd in zip(states, seeds)]
         self.M = len(self.members)
         self.params = self.members[0].params

@@ -31,6 +31,7 @@
 #endif
 
 #include "../lacmopy_gb300/csrc/lacmo_constants.h"
+#include "../lacmopy_gb300/csrc/lacmo_thin.h"
 #ifdef ORC_CRMATH
 #include "../lacmopy_gb300/csrc/lacmo_crmath.h"
 #define COL_POW13(x) lacmo_cr_pow(x, LC_ONE_THIRD)
@@ -519,6 +520,178 @@ static void collide_cell_2d(double* xis, double* m_w, double* m_s, double* radii
   }
 }
 
+/* One pair (i, j) with draw r (collision/all_or_nothing.py:553-633), as in
+   collide_cell_2d; when xf is given the FP32 copies (xi, R) of the changed
+   SIPs are refreshed the way the GPU refreshes its shared copies. */
+static void process_pair_2d(int64_t i, int64_t j, double r, double* xis, double* m_w,
+                            double* m_s, double* radii, const double* v0, const double* v1,
+                            const double* rho, double dt_over_dV, const double* E,
+                            double E_const, int64_t nb, double lo, double bl, int64_t* no_cols,
+                            int64_t* kbuf, float* xf, float* Rf) {
+  int64_t imin, imax;
+  if (xis[i] <= xis[j]) { imin = i; imax = j; } else { imin = j; imax = i; }
+  double xi_min = xis[imin], xi_max = xis[imax];
+  double m_w_min = m_w[imin], m_w_max = m_w[imax];
+  double m_s_min = m_s[imin], m_s_max = m_s[imax];
+  double s = radii[i] + radii[j];
+  double e = E ? E[kbuf[i] * nb + kbuf[j]] : E_const;
+  double dv = sqrt(SQ(v0[i] - v0[j]) + SQ(v1[i] - v1[j]));
+  double p_crit = xi_max * dt_over_dV * (LC_PI * s * s * e * dv * 1.0E-12);
+  if (p_crit > 1.0) {
+    double xi_col = p_crit * xi_min;
+    m_w[imin] = m_w_min + p_crit * m_w_max;
+    m_s[imin] = m_s_min + p_crit * m_s_max;
+    radii[imin] = radius_from_mass_col((m_w[imin] + m_s[imin]), rho[imin]);
+    xis[imax] -= xi_col;
+    if (E) kbuf[imin] = kernel_index(radii[imin], lo, bl, nb);
+    no_cols[1] += 1;
+    if (xf) { xf[imax] = (float)xis[imax]; Rf[imin] = (float)radii[imin]; }
+  } else if (p_crit > r) {
+    no_cols[0] += 1;
+    double xi_rel_dev = (xi_max - xi_min) / xi_max;
+    if (xi_rel_dev < 1.0E-5) {
+      double xi_ges = xi_min + xi_max;
+      m_w[imin] = 2.0 * (xi_min * m_w_min + xi_max * m_w_max) / xi_ges;
+      m_s[imin] = 2.0 * (xi_min * m_s_min + xi_max * m_s_max) / xi_ges;
+      m_w[imax] = m_w[imin];
+      m_s[imax] = m_s[imin];
+      radii[imin] = radius_from_mass_col((m_w[imin] + m_s[imin]), rho[imin]);
+      radii[imax] = radii[imin];
+      xis[imax] = 0.5 * 0.7 * xi_ges;
+      xis[imin] = 0.5 * xi_ges - xis[imax];
+      if (E) { kbuf[imin] = kernel_index(radii[imin], lo, bl, nb); kbuf[imax] = kbuf[imin]; }
+      if (xf) {
+        xf[imin] = (float)xis[imin]; xf[imax] = (float)xis[imax];
+        Rf[imin] = (float)radii[imin]; Rf[imax] = Rf[imin];
+      }
+    } else {
+      m_w[imin] += m_w_max;
+      m_s[imin] += m_s_max;
+      radii[imin] = radius_from_mass_col((m_w[imin] + m_s[imin]), rho[imin]);
+      xis[imax] -= xi_min;
+      if (E) kbuf[imin] = kernel_index(radii[imin], lo, bl, nb);
+      if (xf) { xf[imax] = (float)xis[imax]; Rf[imin] = (float)radii[imin]; }
+    }
+  }
+}
+
+/* The thinned Philox draws of lacmopy_gb300/csrc/lacmo_thin.h for one cell:
+   the sequential definition the GPU kernel parallelises.  FP32 copies follow
+   the GPU: xi, u, w rounded from the doubles; R from the FP32 mass and
+   density at the cell temperature Tc; refreshed from the exact values after
+   each change. */
+static void collide_cell_2d_thin(double* xis, double* m_w, double* m_s, double* radii,
+                                 const double* v0, const double* v1, const double* rho, int64_t n,
+                                 double dt_over_dV, const double* E, double E_const, int64_t nb,
+                                 double lo, double bl, int64_t* no_cols, int64_t* kbuf,
+                                 uint64_t seed, uint64_t pc1, double Tc, int sol, float* xf,
+                                 float* Rf, float* uf, float* wf) {
+  if (E) for (int64_t i = 0; i < n; ++i) kbuf[i] = kernel_index(radii[i], lo, bl, nb);
+  const float Tf = (float)Tc;
+  const float rhow_f = (float)LC_PAR_WATER_DENS_0 +
+                       (float)LC_PAR_WATER_DENS_1 * ((Tf - (float)LC_PAR_WATER_DENS_2) *
+                                                      (Tf - (float)LC_PAR_WATER_DENS_2));
+  const float c43 = (float)LC_FOUR_PI_OVER_THREE_INV;
+  for (int64_t q = 0; q < n; ++q) {
+    const float mwf = (float)m_w[q], msf = (float)m_s[q];
+    const float mpf = mwf + msf;
+    const float wsf = msf / mpf;
+    const float rh = (sol == SOL_AS)
+                         ? rhow_f * ((((float)LC_PAR_RHO_AS_0 * wsf + (float)LC_PAR_RHO_AS_1) *
+                                          wsf + (float)LC_PAR_RHO_AS_2) * wsf +
+                                     (float)LC_PAR_RHO_AS_3)
+                         : (float)LC_PAR_SOL_DENS_NACL_0 + (float)LC_PAR_SOL_DENS_NACL_1 * wsf +
+                               (float)LC_PAR_SOL_DENS_NACL_2 * Tf +
+                               (float)LC_PAR_SOL_DENS_NACL_3 * wsf * wsf +
+                               (float)LC_PAR_SOL_DENS_NACL_4 * wsf * Tf +
+                               (float)LC_PAR_SOL_DENS_NACL_5 * Tf * Tf;
+    Rf[q] = lt_cbrtf(c43 * mpf / rh);
+    xf[q] = (float)xis[q];
+    uf[q] = (float)v0[q];
+    wf[q] = (float)v1[q];
+  }
+  const float dtdv_f = (float)dt_over_dV;
+  const float Ec_f = (float)E_const;
+  const int64_t P = n * (n - 1) / 2;
+  const int64_t L = LACMO_THIN_L;
+  int64_t pos = 0, bi = 0, bj = 1;
+  uint32_t sub = 0;
+  float pb[LACMO_THIN_L];
+  int64_t pi[LACMO_THIN_L], pj[LACMO_THIN_L];
+  while (pos < P) {
+    const int64_t chunk = pos / L;
+    const int64_t e_end = (chunk + 1) * L < P ? (chunk + 1) * L : P;
+    const int m = (int)(e_end - pos);
+    /* bounds and classes of the part's pairs */
+    int m_bg = 0;
+    float qmax = 0.0f;
+    {
+      int64_t ii = bi, jj = bj;
+      for (int t = 0; t < m; ++t) {
+        pi[t] = ii; pj[t] = jj;
+        const float ef = E ? (float)E[kbuf[ii] * nb + kbuf[jj]] : Ec_f;
+        pb[t] = lt_pair_bound(xf[ii], Rf[ii], uf[ii], wf[ii], xf[jj], Rf[jj], uf[jj], wf[jj], ef,
+                              dtdv_f);
+        if (pb[t] >= 0.0f && pb[t] < LACMO_THIN_TAU) {
+          ++m_bg;
+          qmax = qmax > pb[t] ? qmax : pb[t];
+        }
+        if (++jj > n - 1) { ++ii; jj = ii + 1; }
+      }
+    }
+    /* the background hit, if any: its index among the background pairs */
+    int h = -1, e = 0;
+    double r_bg = 0.0;
+    if (m_bg > 0) {
+      e = lt_exponent(qmax);
+      const double u = lt_uniform(seed, (uint64_t)chunk, sub, 0u, pc1);
+      if (u < LACMO_THIN_H[e - LACMO_THIN_E_MIN][m_bg - 1]) {
+        uint32_t jd = 1;
+        int g = 0;
+        for (; g < m_bg - 1; ++g) {
+          const double v = lt_uniform(seed, (uint64_t)chunk, sub, jd++, pc1);
+          if (v < LACMO_THIN_P[e - LACMO_THIN_E_MIN][m_bg - g - 1]) break;
+        }
+        r_bg = ldexp(lt_uniform(seed, (uint64_t)chunk, sub, jd, pc1), -e);
+        int seen = 0;
+        for (int t = 0; t < m; ++t) {
+          if (pb[t] >= 0.0f && pb[t] < LACMO_THIN_TAU) {
+            if (seen == g) { h = t; break; }
+            ++seen;
+          }
+        }
+      }
+    }
+    /* the walk in rank order */
+    int stop = -1;
+    for (int t = 0; t < m; ++t) {
+      if (t == h) {
+        process_pair_2d(pi[t], pj[t], r_bg, xis, m_w, m_s, radii, v0, v1, rho, dt_over_dV, E,
+                        E_const, nb, lo, bl, no_cols, kbuf, xf, Rf);
+        stop = t;
+        break;
+      }
+      if (!(pb[t] >= 0.0f && pb[t] < LACMO_THIN_TAU)) {
+        const int64_t before = no_cols[0] + no_cols[1];
+        const double r = philox_uniform(seed, (uint64_t)(pos + t), pc1);
+        process_pair_2d(pi[t], pj[t], r, xis, m_w, m_s, radii, v0, v1, rho, dt_over_dV, E,
+                        E_const, nb, lo, bl, no_cols, kbuf, xf, Rf);
+        if (no_cols[0] + no_cols[1] != before) { stop = t; break; }
+      }
+    }
+    if (stop < 0) {
+      pos = e_end; sub = 0;
+      bi = pi[m - 1]; bj = pj[m - 1];
+      if (++bj > n - 1) { ++bi; bj = bi + 1; }
+    } else {
+      pos = pos + stop + 1;
+      sub = pos < e_end ? sub + 1 : 0;
+      bi = pi[stop]; bj = pj[stop];
+      if (++bj > n - 1) { ++bi; bj = bi + 1; }
+    }
+  }
+}
+
 /* collision/all_or_nothing.py:754-846: every cell, x-outer / z-inner, SIPs of
    a cell in ascending ID; the radius uses the cell temperature and the
    solute's density.  Draws are consumed in that order from rnd[*rnd_pos..].
@@ -527,7 +700,7 @@ static int collision_all_cells(double* xis, double* m_w, double* m_s,
     const double* vel, const double* T, const int64_t* cells, int64_t N, int64_t Nx, int64_t Nz,
     double dt_over_dV, const double* E, double E_const, int64_t nb, double lo, double bl,
     int64_t* no_cols, int sol, const double* rnd, int64_t rnd_len, int64_t* rnd_pos,
-    uint64_t seed, int64_t* col_step) {
+    uint64_t seed, int64_t* col_step, int thin) {
   int64_t C = Nx * Nz;
   int64_t* start = (int64_t*)calloc(C + 1, sizeof(int64_t));
   int64_t* order = (int64_t*)malloc(sizeof(int64_t) * (N > 0 ? N : 1));
@@ -559,6 +732,7 @@ static int collision_all_cells(double* xis, double* m_w, double* m_s,
     int64_t cap = 0;
     double *xb = NULL, *wb = NULL, *sb = NULL, *Rb = NULL, *v0 = NULL, *v1 = NULL, *rb = NULL;
     int64_t* kb = NULL;
+    float *fx = NULL, *fR = NULL, *fu = NULL, *fw = NULL;
 #pragma omp for schedule(dynamic, 16)
     for (int64_t c = 0; c < C; ++c) {
       int64_t n = start[c + 1] - start[c];
@@ -568,6 +742,8 @@ static int collision_all_cells(double* xis, double* m_w, double* m_s,
         xb = realloc(xb, 8 * n); wb = realloc(wb, 8 * n); sb = realloc(sb, 8 * n);
         Rb = realloc(Rb, 8 * n); v0 = realloc(v0, 8 * n); v1 = realloc(v1, 8 * n);
         rb = realloc(rb, 8 * n); kb = realloc(kb, 8 * n);
+        fx = realloc(fx, 4 * n); fR = realloc(fR, 4 * n); fu = realloc(fu, 4 * n);
+        fw = realloc(fw, 4 * n);
       }
       const int64_t* ids = order + start[c];
       double Tc = T[c];
@@ -582,8 +758,12 @@ static int collision_all_cells(double* xis, double* m_w, double* m_s,
         Rb[q] = radius_from_mass_col(m_p, r);
       }
       int64_t cnt[2] = {0, 0};
-      collide_cell_2d(xb, wb, sb, Rb, v0, v1, rb, n, dt_over_dV, E, E_const, nb, lo, bl, cnt,
-                      rnd ? rnd + draw0[c] : NULL, kb, seed, (cstep << 32) | (uint64_t)c);
+      if (thin && !rnd)
+        collide_cell_2d_thin(xb, wb, sb, Rb, v0, v1, rb, n, dt_over_dV, E, E_const, nb, lo, bl,
+                             cnt, kb, seed, (cstep << 32) | (uint64_t)c, Tc, sol, fx, fR, fu, fw);
+      else
+        collide_cell_2d(xb, wb, sb, Rb, v0, v1, rb, n, dt_over_dV, E, E_const, nb, lo, bl, cnt,
+                        rnd ? rnd + draw0[c] : NULL, kb, seed, (cstep << 32) | (uint64_t)c);
       nc0 += cnt[0]; nc1 += cnt[1];
       for (int64_t q = 0; q < n; ++q) {
         int64_t id = ids[q];
@@ -591,6 +771,7 @@ static int collision_all_cells(double* xis, double* m_w, double* m_s,
       }
     }
     free(xb); free(wb); free(sb); free(Rb); free(v0); free(v1); free(rb); free(kb);
+    free(fx); free(fR); free(fu); free(fw);
   }
   no_cols[0] += nc0; no_cols[1] += nc1;
   if (rnd) *rnd_pos = draw0[C];
@@ -604,16 +785,16 @@ ORC_EXPORT int orc_collision_step_all_cells_2d(double* xis, double* m_w, double*
     double dt_over_dV, const double* E, double E_const, int64_t nb, double lo, double bl,
     int64_t* no_cols, int sol, const double* rnd, int64_t rnd_len, int64_t* rnd_pos) {
   return collision_all_cells(xis, m_w, m_s, vel, T, cells, N, Nx, Nz, dt_over_dV, E, E_const, nb,
-                             lo, bl, no_cols, sol, rnd, rnd_len, rnd_pos, 0, NULL);
+                             lo, bl, no_cols, sol, rnd, rnd_len, rnd_pos, 0, NULL, 0);
 }
 
 /* the same with Philox draws (key seed, collision-step counter *col_step) */
 ORC_EXPORT int orc_collision_step_all_cells_2d_philox(double* xis, double* m_w, double* m_s,
     const double* vel, const double* T, const int64_t* cells, int64_t N, int64_t Nx, int64_t Nz,
     double dt_over_dV, const double* E, double E_const, int64_t nb, double lo, double bl,
-    int64_t* no_cols, int sol, uint64_t seed, int64_t* col_step) {
+    int64_t* no_cols, int sol, uint64_t seed, int64_t* col_step, int thin) {
   return collision_all_cells(xis, m_w, m_s, vel, T, cells, N, Nx, Nz, dt_over_dV, E, E_const, nb,
-                             lo, bl, no_cols, sol, NULL, 0, NULL, seed, col_step);
+                             lo, bl, no_cols, sol, NULL, 0, NULL, seed, col_step, thin);
 }
 
 /* total number of pair draws the next all-cells step consumes */
@@ -925,12 +1106,14 @@ typedef struct {
   int64_t N;
   uint64_t seed;
   int64_t* col_step;
+  int thin;
 } orc_adv_t;
 
 static int collide_all(orc_adv_t* a) {
   return collision_all_cells(a->xi, a->m_w, a->m_s, a->vel, a->gsf, a->cells, a->N, a->Nx, a->Nz,
                              a->dt_col_over_dV, a->E, a->E_const, a->nb, a->lo, a->bl, a->no_cols,
-                             a->sol, a->rnd, a->rnd_len, a->rnd_pos, a->seed, a->col_step);
+                             a->sol, a->rnd, a->rnd_len, a->rnd_pos, a->seed, a->col_step,
+                             a->thin);
 }
 
 /* integration.py:1095-1294 */
@@ -1009,12 +1192,12 @@ ORC_EXPORT int orc_integrate_adv_step(double* gsf, double* gmp, const double* gv
     int act_relaxation, const double* prof_r_v, const double* prof_Theta, const double* t_relax,
     int no_iter, double g_set, const double* E, double E_const, int64_t nb, double lo, double bl,
     int64_t* no_cols, const double* rnd, int64_t rnd_len, int64_t* rnd_pos, int64_t N,
-    uint64_t seed, int64_t* col_step) {
+    uint64_t seed, int64_t* col_step, int thin) {
   orc_adv_t a = {gsf, gmp, gv, flux, p_ref, p_ref_inv, Nx, Nz, ranges, steps, V, pos, vel, cells,
                  rel_pos, m_w, m_s, xi, sol, water_removed, active, T_p, delta_m_l, dt, dt_sub,
                  dt_sub_half, dt_col_over_dV, scale_dt_cond, no_col_per_adv, act_collisions,
                  act_relaxation, prof_r_v, prof_Theta, t_relax, no_iter, g_set, E, E_const, nb, lo,
-                 bl, no_cols, rnd, rnd_len, rnd_pos, N, seed, col_step};
+                 bl, no_cols, rnd, rnd_len, rnd_pos, N, seed, col_step, thin};
   return adv_step(&a);
 }
 

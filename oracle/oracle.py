@@ -73,10 +73,10 @@ def _lib(variant):
         D, D, D, D, dbl, dbl, i64, i64, D, D, dbl, D, D, I64, D, D, D, D, cint, D, U8, D, D,
         dbl, dbl, dbl, dbl, cint, cint, cint, cint, D, D, D, cint, dbl, ctypes.c_void_p, dbl,
         i64, dbl, dbl, I64, ctypes.c_void_p, i64, ctypes.c_void_p, i64, ctypes.c_uint64,
-        ctypes.c_void_p]
+        ctypes.c_void_p, cint]
     lib.orc_collision_step_all_cells_2d_philox.argtypes = [
         D, D, D, D, D, I64, i64, i64, i64, dbl, ctypes.c_void_p, dbl, i64, dbl, dbl, I64, cint,
-        ctypes.c_uint64, I64]
+        ctypes.c_uint64, I64, cint]
     lib.orc_collision_step_all_cells_2d_philox.restype = cint
     U64 = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
     lib.orc_philox_uniform.argtypes = [ctypes.c_uint64, U64, U64, i64, D]
@@ -266,7 +266,7 @@ class Oracle:
             act_collisions, act_relaxation, init_profile_r_v, init_profile_Theta,
             relaxation_time_profile, no_iter_impl_mass, g_set, E_col_grid, no_kernel_bins,
             R_kernel_low_log, bin_factor_R_log, no_cols, draws, draw_pos=None, seed=0,
-            col_step=None):
+            col_step=None, thin=False):
         """``draws``: uniform buffer consumed from ``draw_pos``, or None for
         Philox draws keyed by ``seed`` and the counter ``col_step`` (int64[1])."""
         E, Ec = _E(E_col_grid)
@@ -290,7 +290,7 @@ class Oracle:
             float(R_kernel_low_log or 0.0), float(bin_factor_R_log or 1.0), _c(no_cols, np.int64),
             None if draws is None else _c(draws).ctypes.data, 0 if draws is None else len(draws),
             draw_pos.ctypes.data, len(xi), int(seed),
-            None if col_step is None else _c(col_step, np.int64).ctypes.data)
+            None if col_step is None else _c(col_step, np.int64).ctypes.data, int(bool(thin)))
         if rc != 0:
             raise ValueError("not enough draws for the advection step")
         return draw_pos
@@ -298,14 +298,14 @@ class Oracle:
     def collision_step_all_cells_philox(self, xis, m_w, m_s, vel, grid_temperature, cells,
                                         no_cells, dt_over_dV, E_col_grid, no_kernel_bins,
                                         R_kernel_low_log, bin_factor_R_log, no_cols, solute_type,
-                                        seed, col_step):
+                                        seed, col_step, thin=False):
         E, Ec = _E(E_col_grid)
         self.lib.orc_collision_step_all_cells_2d_philox(
             _c(xis), _c(m_w), _c(m_s), _c(vel), np.ascontiguousarray(grid_temperature, dtype=np.float64),
             _c(cells, np.int64), len(xis), int(no_cells[0]), int(no_cells[1]), float(dt_over_dV),
             None if E is None else E.ctypes.data, Ec, int(no_kernel_bins or 0),
             float(R_kernel_low_log or 0.0), float(bin_factor_R_log or 1.0), _c(no_cols, np.int64),
-            _sol(solute_type), int(seed), _c(col_step, np.int64))
+            _sol(solute_type), int(seed), _c(col_step, np.int64), int(bool(thin)))
 
     def philox_uniform(self, key, k, c1):
         """Uniforms of pair ranks ``k`` (block k >> 1, half k & 1) under

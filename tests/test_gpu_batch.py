@@ -32,17 +32,17 @@ def _copy(st):
     return {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in st.items()}
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision,thin", [("fp64", False), ("mixed", False), ("mixed", True)])
 @pytest.mark.parametrize("graph", [False, True])
-def test_batch_equals_single_members(precision, graph):
+def test_batch_equals_single_members(precision, thin, graph):
     from lacmopy_gb300 import BatchState, DeviceState
     sts = _members(3)
     seeds = [11, 12, 13]
     assert len({st["xi"].size for st in sts}) == 3   # uneven member sizes
-    b = BatchState([_copy(st) for st in sts], seeds, precision=precision)
+    b = BatchState([_copy(st) for st in sts], seeds, precision=precision, thin=thin)
     b.adv_step(3, graph=graph)
     for m, st in enumerate(sts):
-        d = DeviceState(_copy(st), draws="philox", seed=seeds[m], precision=precision)
+        d = DeviceState(_copy(st), draws="philox", seed=seeds[m], precision=precision, thin=thin)
         d.adv_step(3)
         A, B = d.snapshot(), b.snapshot(m)
         assert np.array_equal(A["cells"], B["cells"])

@@ -237,6 +237,33 @@ def test_philox_draws_match_oracle(oracle_cr):
     assert np.array_equal(out["m_s"], ms)
 
 
+@pytest.mark.parametrize("boost", [1.0, 40.0])
+def test_thinned_philox_draws_match_oracle(oracle_cr, boost):
+    """Thinned Philox draws: GPU == the oracle's sequential thinning bit for
+    bit over two consecutive collision steps (the FP32 bounds, the chunk
+    draws and every decision agree)."""
+    from lacmopy_gb300 import DeviceState
+    st = _full_state(13, nx=40, nz=40, kernel="Hall_Bott", drizzle_fraction=0.1, r_tot=12.5E-3)
+    st["dt_col_over_dV"] = st["dt_col_over_dV"] * boost
+    ds = DeviceState(st, draws="philox", seed=777, thin=True)
+    ds.collision_step()
+    ds.collision_step()
+    out = ds.snapshot()
+    xi, mw, ms = st["xi"].copy(), st["m_w"].copy(), st["m_s"].copy()
+    nc = np.zeros(2, np.int64)
+    cs = np.zeros(1, np.int64)
+    for _ in range(2):
+        oracle_cr.collision_step_all_cells_philox(
+            xi, mw, ms, st["vel"], st["grid_scalar_fields"][0], st["cells"], st["grid_no_cells"],
+            st["dt_col_over_dV"], st["E_col_grid"], st["no_kernel_bins"], st["R_kernel_low_log"],
+            st["bin_factor_R_log"], nc, "AS", 777, cs, thin=True)
+    assert nc.sum() > 0
+    assert np.array_equal(out["no_cols"], nc)
+    assert np.array_equal(out["xi"], xi)
+    assert np.array_equal(out["m_w"], mw)
+    assert np.array_equal(out["m_s"], ms)
+
+
 def test_adv_step_philox_vs_oracle(oracle_cr):
     from lacmopy_gb300 import DeviceState
     st = _full_state(17, nx=20, nz=20, spcm=(13, 19), r_tot=12.5E-3, drizzle_fraction=0.15)
