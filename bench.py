@@ -7,8 +7,10 @@ drawn uniformly in [32, 256] per cell and member (~52M SIPs), Hall/Bott
 collision efficiencies, mixed precision, Philox collision draws, one advection
 step dt = 1 s per step (10 condensation sub-steps with the 3-iteration
 implicit Newton, 2 all-or-nothing collision steps), each kernel launch covering
-all members, the step replayed from a CUDA graph.  The "FP64 plain" side is
-the single 75 x 75 x 64-SIPs/cell state with the Long/Bott table in FP64;
+all members, the step replayed from a CUDA graph; thinned Philox draws (an
+exact sampler of the per-pair uniforms; the per-pair draws are reported under
+"modes").  The "FP64 plain" side is the single 75 x 75 x 64-SIPs/cell state
+with the Long/Bott table in FP64 and one Philox uniform per pair;
 both sides and the mixed single state are reported under "modes".  Seeded
 synthetic states with the case's shapes and distributions.
 
@@ -64,6 +66,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-single", action="store_true", help="skip the single-state modes")
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one")
+    ap.add_argument("--draws", default="thinned", choices=["thinned", "philox"],
+                    help="collision draws of the headline: thinned Philox draws (an exact "
+                         "sampler of the per-pair uniforms) or one Philox uniform per pair")
+    ap.add_argument("--no-draws-compare", action="store_true",
+                    help="skip the headline ensemble with the other draw mode")
     return ap.parse_args()
 
 
@@ -74,7 +81,10 @@ def workload_config(args, n_sips):
             "sips_per_cell": f"uniform in [{args.uneven[0]}, {args.uneven[1]}] per cell and member",
             "n_sips": int(n_sips), "kernel": "Hall_Bott", "precision_mode": "mixed",
             "dt_s": 1.0, "cond_substeps": 10, "collision_steps": 2, "newton_iterations": 3,
-            "draws": "philox4x32-10 (device), keyed per member",
+            "draws": ("philox4x32-10 (device), keyed per member, " +
+                      ("thinned draws: one uniform per low-probability segment of pairs, an "
+                       "exact sampler of the per-pair uniforms" if args.draws == "thinned"
+                       else "one uniform per pair")),
             "cuda_graph": not args.no_graph,
             "l2": "inputs larger than L2 (state ~8 GB); L2 also flushed between timed steps "
                   "(512 MiB device memset)",
@@ -312,7 +322,7 @@ def run_ours(args):
 
     # ---- headline: the batched mixed-precision ensemble ----
     seeds = rank_seeds(rank, args.members)[0]
-    batch = BatchState(members, seeds, precision="mixed")   # copies the states to the GPU
+    batch = BatchState(members, seeds, precision="mixed", draws=args.draws)   # copies to the GPU
     n_total = batch.n_total
     ms, ups, launches, clocks = timed(batch, True)
     value = ups / (ms / 1000.0)
@@ -347,6 +357,14 @@ def run_ours(args):
                 "bytes_per_sip": BYTES_PARTICLE_SUBSTEP}
     del batch
     torch.cuda.empty_cache()
+    if not args.no_draws_compare:
+        other = "philox" if args.draws == "thinned" else "thinned"
+        batch = BatchState(members, seeds, precision="mixed", draws=other)
+        ms_o, ups_o, _, _ = timed(batch, False)
+        modes[f"batched_mixed_{other}_draws"] = {"value": ups_o / (ms_o / 1000.0),
+                                                  "ms_per_step": ms_o / args.steps}
+        del batch
+        torch.cuda.empty_cache()
 
     # ---- the FP64 plain path and the mixed single state (75 x 75 x 64) ----
     if single is not None:
@@ -382,14 +400,14 @@ def run_ours(args):
                        ("pos", "vel", "rel_pos", "m_w", "m_s", "xi", "T_p", "water_removed",
                         "cells", "grid_scalar_fields", "grid_mat_prop", "delta_m_l",
                         "no_cols")) + n
-        I.integrate_adv_step_np(*[sts[0][k] for k in keys], draws="philox", seed=7)  # warm-up
+        I.integrate_adv_step_np(*[sts[0][k] for k in keys], draws=args.draws, seed=7)  # warm-up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ups_e = 0
         for _ in range(args.e2e_steps):
             for m, se in enumerate(sts):
                 ups_e += int(np.count_nonzero(se["active_ids"]))
-                I.integrate_adv_step_np(*[se[k] for k in keys], draws="philox", seed=7 + m)
+                I.integrate_adv_step_np(*[se[k] for k in keys], draws=args.draws, seed=7 + m)
         torch.cuda.synchronize()
         te = time.perf_counter() - t0
         e2e = {"value": ups_e / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

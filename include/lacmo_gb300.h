@@ -86,8 +86,10 @@ typedef struct {
   double R_kernel_low_log, bin_factor_R_log;
   int32_t precision;     /* LACMO_PRECISION_FP64 or LACMO_PRECISION_MIXED     */
   int32_t thin_draws;    /* Philox draws only: 0 one draw per pair; 1 the
-                            thinned draws (the same iid uniforms, sampled per
-                            chunk of 32 pairs; lacmo_thin.h)                   */
+                            thinned draws (the same iid uniforms, one draw per
+                            low-probability segment of up to 32 pairs;
+                            lacmo_thin.h; needs E_col_grid with at most
+                            LACMO_MAX_KERNEL_BINS bins, else per pair)         */
 } lacmo_params_t;
 
 /* Arithmetic of lacmo_integrate_adv_step.  FP64: the reference's FP64 path
@@ -265,7 +267,7 @@ int lacmo_collision_step_cells(const lacmo_sips_t* sips, const lacmo_grid_t* gri
  * memory pool or under a fixed memory budget, plugin hosts that forbid
  * cudaMalloc after start-up).  It does the work of lacmo_collision_step_cells
  * from the SIP cell indices alone (binning included), with its scratch in a
- * fixed array inside the library (about 27 MB of device memory, held by every
+ * fixed array inside the library (about 28 MB of device memory, held by every
  * GPU that loads the library until the process exits) instead of a
  * workspace.  The caller still passes all inputs and outputs: xi, m_w, m_s
  * are updated in place, vel is [2][n], grid_T is the [nx][nz] temperature,

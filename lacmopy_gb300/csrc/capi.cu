@@ -41,9 +41,10 @@ static WsPlan ws_plan(int64_t n, int64_t nx, int64_t nz) {
       4 * N,           // colk
       64,              // scalars
       4 * 2 * (size_t)((nx + 1) * (nz + 1)),  // gvf
-      4 * (size_t)LACMO_MAX_KERNEL_BINS * LACMO_MAX_KERNEL_BINS,  // Ef
+      4 * (size_t)LACMO_MAX_KERNEL_BINS * (LACMO_MAX_KERNEL_BINS + 1),  // Ef, row maxima
       4 * C,           // cell_order
       24 * N,          // gcopy
+      32 * (N / 32 + C + 1),  // gstats
   };
   WsPlan p;
   size_t o = 0;
@@ -89,6 +90,7 @@ bool ws_carve(void* base, size_t bytes, int64_t n, int64_t nx, int64_t nz, Ws* w
   w->cell_order = (int32_t*)(b + p.off[19]);
   w->cell_ctr = (int32_t*)(sc + 40);
   w->gcopy = (float*)(b + p.off[20]);
+  w->gstats = (float*)(b + p.off[21]);
   return true;
 }
 

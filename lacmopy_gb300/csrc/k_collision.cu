@@ -108,6 +108,8 @@ struct CellArgs {
   const int32_t* cell_order;   // cells, largest first
   int32_t* cell_ctr;           // next cell_order entry to take
   float* gcopy;                // [6][n] FP32 copies by slot, for cells above CELL_SMEM
+  float4* gstats;              // block statistics of cells above CELL_SMEM (thinned draws)
+  const float* erow;           // largest FP32 efficiency of each table row (thinned draws)
   int thin;                    // thinned Philox draws (lacmo_thin.h)
 };
 
@@ -123,6 +125,7 @@ struct CellCommon {
   int64_t n_draws;
   float dtdv_f, lo_f, inv_bl_f, E_const_f;
   const float* Ef;
+  const float* erow;
   int thin;
 };
 struct CK {
@@ -143,6 +146,8 @@ __device__ __forceinline__ void make_cellargs(CellArgs& a, const Member& mb, con
   a.Ef = cc.Ef;
   a.cell_order = mb.w.cell_order; a.cell_ctr = mb.w.cell_ctr;
   a.gcopy = mb.w.gcopy;
+  a.gstats = (float4*)mb.w.gstats;
+  a.erow = cc.erow;
   a.thin = cc.thin;
 }
 
@@ -213,6 +218,7 @@ __device__ __forceinline__ void ensure_exact(const CellArgs& a, int32_t id, doub
 struct CellSmem {
   float4* v;
   int32_t *sk, *sid;
+  float4* st;   // thinned draws: statistics of block b at st[2b], st[2b + 1]
 };
 
 // One ordinary collection (p_crit <= 1 and p_crit > r) of the pair imin/imax
@@ -394,143 +400,193 @@ __device__ __forceinline__ void decide_pair(const CellArgs& a, const CellSmem& S
   c1 += o == 2;
 }
 
-// the thinned draws of lacmo_thin.h for one cell, warp-cooperative: each
-// part is bounded with one pair per lane; a warp maximum over the background
-// pairs gives q and one uniform (the sub-0 ones of 32 chunks computed ahead,
-// one per lane) decides their hit, whose first-hit draws are evaluated by all
-// lanes at once; individual pairs are screened in parallel with their own
-// draws; the walk then takes the events in rank order
-__device__ __noinline__ void thin_cell(const CellArgs& a, const CellSmem& S, int n, int P,
-                                       double Tc, bool use_E, uint64_t pc1, int lane,
-                                       int64_t& c0, int64_t& c1) {
-  constexpr int L = LACMO_THIN_L;
-  static_assert(LACMO_THIN_L == 32, "one pair of a part per lane");
-  int pos = 0, sub = 0;   // first unprocessed rank, part counter of its chunk
-  int bi = 0, bj = 1;     // the pair of rank pos
+// order-preserving keys of non-NaN floats (for warp min/max reductions)
+__device__ __forceinline__ uint32_t ord_key(float f) {
+  const uint32_t b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float ord_val(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// statistics (lt_block_stats) of block b, slots [32 b, min(32 b + 32, n)),
+// from the FP32 copies, warp-cooperative: st[2b] = (xmax, Rmax, umin, umax),
+// st[2b + 1] = (wmin, wmax, ok, 0)
+__device__ __forceinline__ void block_stats(const CellSmem& S, int n, int b, int lane) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int q = (b << 5) + lane;
+  const bool in = q < n;
+  const float4 v = in ? S.v[q] : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+  const bool bad = in && !(v.x > 0.0f && v.y == v.y && v.z == v.z && v.w == v.w);
+  const int ok = __ballot_sync(FULL, bad) == 0u;
+  const uint32_t xk = __reduce_max_sync(FULL, in ? ord_key(v.x) : 0u);
+  const uint32_t Rk = __reduce_max_sync(FULL, in ? ord_key(v.y) : 0u);
+  const uint32_t ulo = __reduce_min_sync(FULL, in ? ord_key(v.z) : 0xffffffffu);
+  const uint32_t uhi = __reduce_max_sync(FULL, in ? ord_key(v.z) : 0u);
+  const uint32_t wlo = __reduce_min_sync(FULL, in ? ord_key(v.w) : 0xffffffffu);
+  const uint32_t whi = __reduce_max_sync(FULL, in ? ord_key(v.w) : 0u);
+  if (lane == 0) {
+    S.st[2 * b] = make_float4(ord_val(xk), ord_val(Rk), ord_val(ulo), ord_val(uhi));
+    S.st[2 * b + 1] = make_float4(ord_val(wlo), ord_val(whi), __int_as_float(ok), 0.0f);
+  }
+}
+
+// segment (i, b) moved forward by `adv` segments (row i holds the segments
+// b = (i + 1) / 32 .. B - 1); past the cell's last segment b >= B
+__device__ __forceinline__ void advance_seg(int n, int B, int& i, int& b, int adv) {
+  b += adv;
+  while (b > B - 1 && i < n - 2) {
+    ++i;
+    b += ((i + 1) >> 5) - B;
+  }
+}
+
+// The thinned draws of lacmo_thin.h for one cell, warp-cooperative.  A round
+// takes 32 consecutive segments, one per lane (lane 0 the current part of the
+// current segment): each lane bounds its segment from SIP i and the block
+// statistics and, when the bound is below LACMO_THIN_TAU, draws the uniform
+// that decides whether the segment holds a draw below q.  Segments with
+// neither such a hit nor per-pair draws are done; the first one with either
+// is then processed by the warp: per-pair draws screened in parallel, or the
+// hit's first-hit draws evaluated by all lanes at once and the hit pair by
+// one lane.  The statistics of the blocks it may have changed are refreshed,
+// and the next round starts after it.
+__device__ __forceinline__ int2 thin_cell(const CellArgs& a, const CellSmem S, int n, double Tc,
+                                       bool use_E, uint64_t pc1, int lane) {
+  static_assert(LACMO_THIN_L == 32, "one block of slots per warp");
+  int64_t c0 = 0, c1 = 0;   // this lane's outcome counts
+  constexpr unsigned FULL = 0xffffffffu;
+  const int B = (n + 31) >> 5;
+  for (int b = 0; b < B; ++b) block_stats(S, n, b, lane);
+  __syncwarp();
+  int si = 0, sb = 0, sj = 1, ssub = 0;   // current segment, its part start and counter
   bool scratch = false;
-  int ubase = -1;         // chunk of lane 0's precomputed sub-0 uniform
-  double upre = 0.0;
-  const unsigned below = (1u << lane) - 1u;
-  while (pos < P) {
-    const int chunk = pos / L;
-    const int e_end = (chunk + 1) * L < P ? (chunk + 1) * L : P;
-    const int m = e_end - pos;
-    int i = bi, j = bj;
-    const bool mine = lane < m;
-    if (mine) advance_pair(n, i, j, lane);
-    float pb = -1.0f;
-    float4 vi, vj;
-    int32_t ki = 0, kj = 0;
-    if (mine) {
-      vi = S.v[i]; vj = S.v[j]; ki = S.sk[i]; kj = S.sk[j];
-      const float ef = use_E ? (a.Ef ? __ldg(a.Ef + (int64_t)ki * a.nb + kj)
-                                     : d2f_flush(__ldg(a.E + (int64_t)ki * a.nb + kj)))
-                             : a.E_const_f;
-      pb = lt_pair_bound(vi.x, vi.y, vi.z, vi.w, vj.x, vj.y, vj.z, vj.w, ef, a.dtdv_f);
-    }
-    const bool bg = mine && pb >= 0.0f && pb < LACMO_THIN_TAU;
-    const unsigned bgmask = __ballot_sync(0xffffffffu, bg);
-    const int m_bg = __popc(bgmask);
-    // background hit: lane h (or none)
-    int h = 32;
+  for (;;) {
+    int i = si, b = sb;
+    if (lane) advance_seg(n, B, i, b, lane);
+    const bool valid = b < B;
+    const int blo = b << 5;
+    const int jfirst = blo > i + 1 ? blo : i + 1;
+    const int j = lane ? jfirst : sj;
+    const int jend = blo + 32 < n ? blo + 32 : n;
+    const uint32_t sub = lane ? 0u : (uint32_t)ssub;
+    bool indiv = false, hit = false;
     int e = 0;
-    uint32_t jd = 0;
-    if (m_bg > 0) {
-      float qmax = bg ? pb : 0.0f;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) qmax = fmaxf(qmax, __shfl_xor_sync(0xffffffffu, qmax, off));
-      e = lt_exponent(qmax);
-      double u;
-      if (sub == 0) {
-        if (ubase < 0 || chunk < ubase || chunk >= ubase + 32) {
-          ubase = chunk;
-          upre = lt_uniform(a.seed, (uint64_t)(chunk + lane), 0u, 0u, pc1);
-        }
-        u = __shfl_sync(0xffffffffu, upre, chunk - ubase);
-      } else {
-        u = lt_uniform(a.seed, (uint64_t)chunk, (uint32_t)sub, 0u, pc1);
-      }
-      if (u < __ldg(&LACMO_THIN_H[e - LACMO_THIN_E_MIN][m_bg - 1])) {
-        bool succ = false;
-        if (lane < m_bg - 1) {
-          const double v = lt_uniform(a.seed, (uint64_t)chunk, (uint32_t)sub, (uint32_t)(1 + lane), pc1);
-          succ = v < __ldg(&LACMO_THIN_P[e - LACMO_THIN_E_MIN][m_bg - lane - 1]);
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, succ);
-        const int g = bal ? __ffs(bal) - 1 : m_bg - 1;
-        jd = g < m_bg - 1 ? (uint32_t)(g + 2) : (uint32_t)m_bg;
-        // the lane holding the g-th background pair
-        h = __ffs(__ballot_sync(0xffffffffu, bg && __popc(bgmask & below) == g)) - 1;
+    if (valid) {
+      const float4 vi = S.v[i];
+      const float4 s0 = S.st[2 * b], s1 = S.st[2 * b + 1];
+      const lt_block_t st{s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, __float_as_int(s1.z)};
+      const float er = use_E ? __ldg(a.erow + S.sk[i]) : a.E_const_f;
+      const float Q = lt_segment_bound(vi.x, vi.y, vi.z, vi.w, &st, er, a.dtdv_f);
+      indiv = !(Q >= 0.0f && Q < LACMO_THIN_TAU);
+      if (!indiv) {
+        e = lt_exponent(Q);
+        const uint64_t u = lt_bits53(a.seed, (uint64_t)pair_rank(i, jfirst, n), sub, 0u, pc1);
+        hit = u < __ldg(&LACMO_THIN_HT[e - LACMO_THIN_E_MIN][jend - j - 1]);
       }
     }
-    // individual pairs: their own draws, screened
-    uint64_t k53 = 0;
-    int sc = 0;
-    if (mine && !bg && lane < h) {
-      k53 = philox_bits53(a.seed, (uint64_t)(pos + lane), pc1);
-      float r_lo, r_hi;
-      philox_interval(k53, r_lo, r_hi);
-      sc = screen_pair(a, use_E, vi, ki, vj, kj, r_lo, r_hi);
+    const unsigned ev = __ballot_sync(FULL, valid && (indiv || hit));
+    if (!ev) {
+      if (__ballot_sync(FULL, valid) != FULL) break;   // the cell's last segment is done
+      advance_seg(n, B, si, sb, 32);
+      if (sb >= B) break;
+      sj = (sb << 5) > si + 1 ? (sb << 5) : si + 1;
+      ssub = 0;
+      continue;
     }
-    unsigned cand = __ballot_sync(0xffffffffu, sc != 0);
-    // the walk: candidates before the hit in rank order, then the hit
-    int stop = -1;
-    while (stop < 0) {
-      const int t = cand ? __ffs(cand) - 1 : 32;
-      if (t >= h && h < 32) {
-        if (!scratch) { init_exact_scratch(a, S, n, lane); scratch = true; }
-        if (lane == h) {
-          const double r = ldexp(lt_uniform(a.seed, (uint64_t)chunk, (uint32_t)sub, jd, pc1), -e);
-          // a float interval around r: truncation and the next float up
-          // (below the normal range: [0, 2^-126])
-          const bool normal = r >= 0x1p-126;
-          const float r_lo = normal ? d2f_down_pos(r) : 0.0f;
-          const float r_hi = normal ? __uint_as_float(__float_as_uint(r_lo) + 1u) : 0x1p-126f;
-          decide_pair(a, S, use_E, i, j, r, r_lo, r_hi, Tc, c0, c1);
+    // the first segment with an event
+    const int L = __ffs(ev) - 1;
+    const int ei = __shfl_sync(FULL, i, L), eb = __shfl_sync(FULL, b, L);
+    const int ej = __shfl_sync(FULL, j, L), eend = __shfl_sync(FULL, jend, L);
+    const int ejf = __shfl_sync(FULL, jfirst, L), ee = __shfl_sync(FULL, e, L);
+    const uint32_t esub = __shfl_sync(FULL, sub, L);
+    const bool eind = __shfl_sync(FULL, (int)indiv, L) != 0;
+    if (!scratch) { init_exact_scratch(a, S, n, lane); scratch = true; }
+    int next_j = eend;
+    if (eind) {
+      // per-pair draws of the rest of the segment, screened in parallel
+      int jj = ej;
+      while (jj < eend) {
+        const int q = jj + lane;
+        int sc = 0;
+        uint64_t k53 = 0;
+        if (q < eend) {
+          k53 = philox_bits53(a.seed, (uint64_t)pair_rank(ei, q, n), pc1);
+          float r_lo, r_hi;
+          philox_interval(k53, r_lo, r_hi);
+          sc = screen_pair(a, use_E, S.v[ei], S.sk[ei], S.v[q], S.sk[q], r_lo, r_hi);
         }
-        stop = h;
-        break;
-      }
-      if (t == 32) break;   // no event in the part
-      if (!scratch) { init_exact_scratch(a, S, n, lane); scratch = true; }
-      int collided = 0;
-      if (lane == t) {
-        if (sc == 1) {
-          certain_collection(a, S, i, j, Tc, use_E);
-          c0 += 1;
-          collided = 1;
-        } else {
-          const int o = exact_pair(a, S, S.sid[i], S.sid[j], i, j, Tc, use_E,
-                                   philox_from_bits(k53));
-          c0 += o == 1;
-          c1 += o == 2;
-          collided = o != 0;
+        const unsigned cand = __ballot_sync(FULL, sc != 0);
+        if (!cand) break;
+        const int t = __ffs(cand) - 1;
+        if (lane == t) {
+          if (sc == 1) {
+            certain_collection(a, S, ei, q, Tc, use_E);
+            c0 += 1;
+          } else {
+            const int o = exact_pair(a, S, S.sid[ei], S.sid[q], ei, q, Tc, use_E,
+                                     philox_from_bits(k53));
+            c0 += o == 1;
+            c1 += o == 2;
+          }
         }
+        __threadfence_block();
+        __syncwarp();
+        jj += t + 1;   // the later pairs are screened again with the new state
       }
-      collided = __shfl_sync(0xffffffffu, collided, t);
-      if (collided) { stop = t; break; }
-      cand &= cand - 1;   // no change: the screens of the later pairs still hold
-    }
-    __threadfence_block();
-    __syncwarp();
-    if (stop < 0) {
-      advance_pair(n, bi, bj, m);
-      pos = e_end; sub = 0;
     } else {
-      advance_pair(n, bi, bj, stop + 1);
-      pos += stop + 1;
-      sub = pos < e_end ? sub + 1 : 0;
+      // the hit: first-hit draws of all lanes, then the pair with r = q u
+      const int m = eend - ej;
+      const uint64_t chunk = (uint64_t)pair_rank(ei, ejf, n);
+      bool succ = false;
+      if (lane < m - 1)
+        succ = lt_bits53(a.seed, chunk, esub, (uint32_t)(1 + lane), pc1) <
+               __ldg(&LACMO_THIN_PT[ee - LACMO_THIN_E_MIN][m - lane - 1]);
+      const unsigned bal = __ballot_sync(FULL, succ);
+      const int g = bal ? __ffs(bal) - 1 : m - 1;
+      const uint32_t jd = g < m - 1 ? (uint32_t)(g + 2) : (uint32_t)m;
+      if (lane == 0) {
+        const double r = ldexp((double)lt_bits53(a.seed, chunk, esub, jd, pc1) *
+                                   (1.0 / 9007199254740992.0), -ee);
+        // a float interval around r: truncation and the next float up
+        // (below the normal range: [0, 2^-126])
+        const bool normal = r >= 0x1p-126;
+        const float r_lo = normal ? d2f_down_pos(r) : 0.0f;
+        const float r_hi = normal ? __uint_as_float(__float_as_uint(r_lo) + 1u) : 0x1p-126f;
+        decide_pair(a, S, use_E, ei, ej + g, r, r_lo, r_hi, Tc, c0, c1);
+      }
+      __threadfence_block();
+      __syncwarp();
+      next_j = ej + g + 1;
+    }
+    // the statistics of the blocks the event may have changed
+    block_stats(S, n, ei >> 5, lane);
+    if ((ei >> 5) != eb) block_stats(S, n, eb, lane);
+    __syncwarp();
+    si = ei; sb = eb;
+    if (!eind && next_j < eend) {
+      sj = next_j;
+      ssub = (int)esub + 1;
+    } else {
+      advance_seg(n, B, si, sb, 1);
+      if (sb >= B) break;
+      sj = (sb << 5) > si + 1 ? (sb << 5) : si + 1;
+      ssub = 0;
     }
   }
+  return make_int2((int)c0, (int)c1);
 }
 
 // One warp per cell.  Shared memory holds FP32 copies of xi, R, u, w and the
 // kernel bin (24 B per SIP with the SIP ID); the pairs are screened in
 // parallel in lexicographic order and only the events of the sequential
 // order (collections and undecided pairs) are processed one at a time.
-constexpr size_t CELL_WARP_BYTES = (size_t)CELL_SMEM * (4 * 4 + 4 + 4);
+constexpr size_t CELL_WARP_BYTES = (size_t)CELL_SMEM * (4 * 4 + 4 + 4) + (CELL_SMEM / 32) * 32;
 
-__global__ void __launch_bounds__(CELL_WARPS * 32, 3)
+// THIN: the thinned draws (registers for 2 blocks per SM), else per-pair
+// draws (3 blocks per SM)
+template <bool THIN>
+__global__ void __launch_bounds__(CELL_WARPS * 32, THIN ? 2 : 3)
     k_collide_cells(const __grid_constant__ CK x) {
   // the member's arguments, once per block (all warps of a block belong to
   // the same member); shared memory keeps them addressable without a copy
@@ -576,10 +632,12 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
       S.v = (float4*)a.gcopy + b;
       S.sk = (int32_t*)((float4*)a.gcopy + a.n) + b;
       S.sid = S.sk + a.n;
+      S.st = a.gstats + 2 * ((int64_t)(b >> 5) + c);
     } else {
       S.v = (float4*)wslice;
       S.sk = (int32_t*)(S.v + CELL_SMEM);
       S.sid = S.sk + CELL_SMEM;
+      S.st = (float4*)(S.sid + CELL_SMEM);
     }
     const float Tf = d2f_rn(Tc);
     const float rhow_f = (float)LC_PAR_WATER_DENS_0 +
@@ -618,8 +676,10 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, 3)
     }
     __syncwarp();
     const int P = (int)((int64_t)n * (n - 1) / 2);
-    if (a.thin) {
-      thin_cell(a, S, n, P, Tc, use_E, pc1, lane, c0, c1);
+    if constexpr (THIN) {
+      const int2 tc = thin_cell(a, S, n, Tc, use_E, pc1, lane);
+      c0 += tc.x;
+      c1 += tc.y;
       __syncwarp();
       continue;
     }
@@ -973,6 +1033,15 @@ __global__ void k_table_to_float(const double* __restrict__ E, float* __restrict
        k += (int64_t)gridDim.x * blockDim.x)
     Ef[k] = (float)E[k];
 }
+// largest FP32 efficiency of each row, in column order (the oracle's order)
+__global__ void k_table_rowmax(const double* __restrict__ E, float* __restrict__ erow, int64_t nb) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nb;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    float mx = (float)E[k * nb];
+    for (int64_t q = 1; q < nb; ++q) mx = lt_max(mx, (float)E[k * nb + q]);
+    erow[k] = mx;
+  }
+}
 
 cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d,
                                  cudaStream_t s) {
@@ -981,7 +1050,10 @@ cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lac
   if (e != cudaSuccess) return e;
   static std::atomic<uint64_t> attr_done{0};   // one bit per device
   if (dev < 64 && !(attr_done.load() & (1ull << dev))) {
-    e = cudaFuncSetAttribute(k_collide_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(k_collide_cells<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)CELL_SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_collide_cells<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)CELL_SMEM_BYTES);
     if (e != cudaSuccess) return e;
     attr_done.fetch_or(1ull << dev);
@@ -993,27 +1065,38 @@ cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lac
   cc.sol = p.solute; cc.draws = d.draws; cc.n_draws = d.n_draws;
   cc.dtdv_f = (float)cc.dtdv; cc.lo_f = (float)cc.lo; cc.inv_bl_f = (float)(1.0 / cc.bl);
   cc.E_const_f = (float)cc.E_const;
-  cc.thin = (p.thin_draws != 0 && d.draws == nullptr) ? 1 : 0;
   cc.Ef = nullptr;
+  cc.erow = nullptr;
   float* Ef = B.one.w.Ef;   // member 0's slot serves the whole batch
   if (p.E_col_grid && Ef && p.no_kernel_bins <= LACMO_MAX_KERNEL_BINS) {
     const int64_t m = p.no_kernel_bins * p.no_kernel_bins;
     k_table_to_float<<<nblk(m, 256), 256, 0, s>>>(p.E_col_grid, Ef, m); note_launches(1);
     cc.Ef = Ef;
+    if (p.thin_draws) {
+      float* erow = Ef + (int64_t)LACMO_MAX_KERNEL_BINS * LACMO_MAX_KERNEL_BINS;
+      k_table_rowmax<<<nblk(p.no_kernel_bins, 128), 128, 0, s>>>(p.E_col_grid, erow,
+                                                                 p.no_kernel_bins);
+      note_launches(1);
+      cc.erow = erow;
+    }
   }
+  // thinned draws need the row maxima of a tabulated efficiency
+  cc.thin = (p.thin_draws != 0 && d.draws == nullptr && (!p.E_col_grid || cc.erow)) ? 1 : 0;
   CK x{B.ref(), cc};
   // persistent blocks: as many as are resident at once, split over members
-  static std::atomic<int> resident[64];
-  int res = dev < 64 ? resident[dev].load() : 0;
+  static std::atomic<int> resident[2][64];
+  const int th = cc.thin ? 1 : 0;
+  int res = dev < 64 ? resident[th][dev].load() : 0;
   if (res <= 0) {
     int per_sm = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collide_cells, CELL_WARPS * 32,
-                                                      CELL_SMEM_BYTES);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, th ? k_collide_cells<true> : k_collide_cells<false>, CELL_WARPS * 32,
+        CELL_SMEM_BYTES);
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     res = per_sm * sms > 0 ? per_sm * sms : 1;
-    if (dev < 64) resident[dev].store(res);
+    if (dev < 64) resident[th][dev].store(res);
   }
   const int64_t C = B.nx * B.nz;
   int64_t bx = res / B.M;
@@ -1021,7 +1104,11 @@ cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lac
   if (bx > need) bx = need;
   if (bx < 1) bx = 1;
   dim3 grid((unsigned)bx, (unsigned)B.M);
-  k_collide_cells<<<grid, CELL_WARPS * 32, CELL_SMEM_BYTES, s>>>(x); note_launches(1);
+  if (th)
+    k_collide_cells<true><<<grid, CELL_WARPS * 32, CELL_SMEM_BYTES, s>>>(x);
+  else
+    k_collide_cells<false><<<grid, CELL_WARPS * 32, CELL_SMEM_BYTES, s>>>(x);
+  note_launches(1);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_col_advance<<<dim3(1, B.M), 1, 0, s>>>(B.ref(), d.draws ? 1 : 0); note_launches(1);

@@ -36,7 +36,10 @@ constexpr size_t st_off_colrho = a256(st_off_colR + 8 * STATIC_MAX_SIPS);
 constexpr size_t st_off_colk = a256(st_off_colrho + 8 * STATIC_MAX_SIPS);
 constexpr size_t st_off_order = a256(st_off_colk + 4 * STATIC_MAX_SIPS);
 constexpr size_t st_off_gcopy = a256(st_off_order + 4 * STATIC_MAX_CELLS);
-constexpr size_t st_off_scalars = a256(st_off_gcopy + 24 * STATIC_MAX_SIPS);
+constexpr size_t st_off_gstats = a256(st_off_gcopy + 24 * STATIC_MAX_SIPS);
+constexpr size_t st_off_Ef = a256(st_off_gstats + 32 * (STATIC_MAX_SIPS / 32 + STATIC_MAX_CELLS + 1));
+constexpr size_t st_off_scalars =
+    a256(st_off_Ef + 4 * (size_t)LACMO_MAX_KERNEL_BINS * (LACMO_MAX_KERNEL_BINS + 1));
 constexpr size_t STATIC_BYTES = st_off_scalars + 256;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[STATIC_BYTES];
@@ -106,6 +109,8 @@ extern "C" int lacmo_collision_step_cells_noalloc(double* xi, double* m_w, doubl
   w.colk = (int32_t*)(b + st_off_colk);
   w.cell_order = (int32_t*)(b + st_off_order);
   w.gcopy = (float*)(b + st_off_gcopy);
+  w.gstats = (float*)(b + st_off_gstats);
+  w.Ef = (float*)(b + st_off_Ef);
   char* sc = b + st_off_scalars;
   w.flags = (uint32_t*)sc;
   w.rm_count = (int32_t*)(sc + 4);

@@ -35,10 +35,12 @@ struct Ws {
   int64_t* total_pairs;
   unsigned long long* nfb;   // mixed precision: Newton repeats in FP64
   float* gvf;                // [2][nx+1][nz+1] FP32 copy of the wind (mixed precision)
-  float* Ef;                 // [LACMO_MAX_KERNEL_BINS^2] FP32 copy of the efficiency table
+  float* Ef;                 // [LACMO_MAX_KERNEL_BINS^2] FP32 copy of the efficiency table,
+                             // then [LACMO_MAX_KERNEL_BINS] row maxima
   int32_t* cell_order;       // [C]   cells by descending SIP count (collision work order)
   int32_t* cell_ctr;         // next entry of cell_order a collision warp takes
   float* gcopy;              // [6][n] collision FP32 copies of cells above the shared-memory size
+  float* gstats;             // [n/32 + C + 1][8] block statistics of those cells (thinned draws)
 };
 
 size_t ws_bytes(int64_t n, int64_t nx, int64_t nz);

@@ -4,27 +4,24 @@
  *
  * The reference draws one uniform r_k per pair k of a cell (lexicographic
  * order) and collects when p_crit(k) > r_k.  The thinned draws define the same
- * iid uniforms partly implicitly.  The pairs are grouped in chunks of
- * LACMO_THIN_L consecutive ranks; the still unprocessed part of a chunk
- * (ranks pos .. end-1, part counter `sub`) is handled as follows, with a
- * certified bound b_k >= p_crit(k) of each pair from the FP32 copies of the
- * current state (lt_pair_bound):
- *  - an "individual" pair (b_k >= LACMO_THIN_TAU, or no valid bound) keeps
- *    its own per-pair Philox draw;
- *  - the other ("background") pairs share q = 2^-e >= every background b_k
- *    and each "hits" when its draw falls below q: one uniform decides whether
- *    the m background pairs hold a hit (probability 1 - (1 - q)^m); if they
- *    do, the first hit h is drawn from its exact conditional distribution and
- *    its draw is r = q u (uniform below q).  A background pair before h has
- *    r_k >= q >= p_crit and is skipped.
- * The part is then walked in rank order: at the hit h the pair is evaluated
- * with r, and at an individual pair with its own draw; the walk stops after
- * h, or after an individual pair that collides, and the rest of the chunk
- * starts again as a new part (sub + 1) from the state after it; otherwise
- * the part ends with its chunk.
- * The probabilities come from exact rational tables (lacmo_thin_tables.h); the
- * bound uses only IEEE single-precision +, -, *, /, fabs and fmax (no
- * contraction), so device and host agree bit for bit.
+ * iid uniforms partly implicitly.  The SIP slots of a cell form blocks of
+ * LACMO_THIN_L; the pairs (i, j) of row i with j in block b form a segment,
+ * and the segments are taken in lexicographic order.  The still unprocessed
+ * part of a segment (pairs (i, j .. jend-1), part counter `sub`) is handled
+ * with a certified bound Q >= p_crit of all its pairs, computed from the FP32
+ * copies of SIP i and the statistics of block b (lt_segment_bound):
+ *  - if Q >= LACMO_THIN_TAU or there is no valid bound, every remaining pair
+ *    of the segment takes its own per-pair Philox draw, in order;
+ *  - otherwise, with q = 2^-e >= Q and m remaining pairs, one uniform decides
+ *    whether a draw falls below q (probability 1 - (1 - q)^m); if none does,
+ *    no pair collects and the segment is done; else the first such pair h is
+ *    drawn from its exact conditional distribution, its draw is r = q u
+ *    (uniform below q), the pair is evaluated with r, and the pairs after h
+ *    form a new part (sub + 1) bounded from the state after it.  Pairs before
+ *    h have r_k >= q > p_crit and are skipped.
+ * The probabilities come from exact rational tables (lacmo_thin_tables.h,
+ * compared as 53-bit integers); the bound uses only IEEE single-precision +,
+ * -, * and comparisons (no contraction), so device and host agree bit for bit.
  */
 #ifndef LACMO_THIN_H_
 #define LACMO_THIN_H_
@@ -37,8 +34,8 @@
 #endif
 #include "lacmo_thin_tables.h"
 
-/* pairs bounded at or above this keep their own draw */
-#define LACMO_THIN_TAU 0x1p-12f
+/* segments bounded at or above this take per-pair draws */
+#define LACMO_THIN_TAU 0x1p-8f
 
 #ifdef __CUDACC__
 #define LT_FN __host__ __device__ __forceinline__
@@ -48,6 +45,9 @@
 
 LT_FN uint32_t lt_f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
 LT_FN float lt_u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+LT_FN float lt_max(float a, float b) { return a > b ? a : b; }
+LT_FN float lt_min(float a, float b) { return a < b ? a : b; }
+LT_FN float lt_abs(float a) { return a < 0.0f ? -a : a; }
 
 /* cube root of x > 0 from IEEE operations only: a bit-pattern first guess
  * (within 4% relative) and three Newton steps y <- (2y + x/y^2)/3, which
@@ -60,19 +60,47 @@ LT_FN float lt_cbrtf(float x) {
   return y;
 }
 
-/* certified upper bound of p_crit of a pair from the FP32 copies (xi, R, u,
- * w) of its SIPs and the FP32 efficiency ef; returns a negative value when the
- * pair must use its own draw (a non-positive multiplicity, NaN) */
-LT_FN float lt_pair_bound(float xa, float Ra, float ua, float wa, float xb, float Rb, float ub,
-                          float wb, float ef, float dtdv_f) {
-  if (!(xa > 0.0f && xb > 0.0f)) return -1.0f;
-  const float du = ua - ub;
-  const float dw = wa - wb;
-  const float slack = 0x1p-21f * (((fabsf(ua) + fabsf(ub)) + fabsf(wa)) + fabsf(wb));
-  const float rs = Ra + Rb;
-  const float core = ((((xa > xb ? xa : xb) * dtdv_f) * 3.14159265e-12f) * rs) * rs * ef;
+/* statistics of one block of SIP slots from the FP32 copies (x = multiplicity,
+ * R = radius, u, w = velocity): maxima of x and R, ranges of u and w, and
+ * ok = every SIP has x > 0 and R, u, w not NaN (otherwise the values are
+ * not used) */
+typedef struct {
+  float xmax, Rmax, umin, umax, wmin, wmax;
+  int ok;
+} lt_block_t;
+
+LT_FN void lt_block_stats(const float* x, const float* R, const float* u, const float* w, int64_t lo,
+                          int64_t hi, lt_block_t* s) {
+  s->xmax = 0.0f; s->Rmax = 0.0f;
+  s->umin = s->wmin = lt_u2f(0x7f800000u); s->umax = s->wmax = lt_u2f(0xff800000u);
+  s->ok = 1;
+  for (int64_t q = lo; q < hi; ++q) {
+    if (!(x[q] > 0.0f) || !(R[q] == R[q] && u[q] == u[q] && w[q] == w[q])) s->ok = 0;
+    s->xmax = lt_max(s->xmax, x[q]); s->Rmax = lt_max(s->Rmax, R[q]);
+    s->umin = lt_min(s->umin, u[q]); s->umax = lt_max(s->umax, u[q]);
+    s->wmin = lt_min(s->wmin, w[q]); s->wmax = lt_max(s->wmax, w[q]);
+  }
+}
+
+/* certified upper bound of p_crit over the pairs (a, j), j in a block with
+ * statistics s, from the FP32 copies of SIP a, the largest FP32 efficiency
+ * er of row bin(a) and dt/dV: every factor is at least the pair's own (the
+ * operations are monotone), and the bound carries the slack of the FP32
+ * radii (1e-6 relative), velocities (2^-21 sum |u|, |w|) and roundings
+ * (2^-14 relative, 1e-36 absolute).  Returns a negative value when the
+ * segment must take per-pair draws (non-positive multiplicity, NaN). */
+LT_FN float lt_segment_bound(float xa, float Ra, float ua, float wa, const lt_block_t* s, float er,
+                             float dtdv_f) {
+  if (!s->ok || !(xa > 0.0f) || !(Ra == Ra && ua == ua && wa == wa)) return -1.0f;
+  const float du = lt_max(ua - s->umin, s->umax - ua);
+  const float dw = lt_max(wa - s->wmin, s->wmax - wa);
+  const float um = lt_max(lt_abs(s->umin), lt_abs(s->umax));
+  const float wm = lt_max(lt_abs(s->wmin), lt_abs(s->wmax));
+  const float slack = 0x1p-21f * (((lt_abs(ua) + um) + lt_abs(wa)) + wm);
+  const float rs = Ra + s->Rmax;
+  const float core = ((((lt_max(xa, s->xmax) * dtdv_f) * 3.14159265e-12f) * rs) * rs) * er;
   if (!(core >= 1e-30f)) return core == core ? 1e-27f : -1.0f;
-  const float pb = ((core * ((fabsf(du) + fabsf(dw)) + slack)) * (1.0f + 0x1p-14f)) + 1e-36f;
+  const float pb = ((core * ((du + dw) + slack)) * (1.0f + 0x1p-14f)) + 1e-36f;
   return pb == pb ? pb : -1.0f;
 }
 
@@ -86,9 +114,10 @@ LT_FN int lt_exponent(float qmax) {
   return e;
 }
 
-/* Philox4x32-10 block, words (x0, x1) as 53 bits: the j-th uniform of part
- * `sub` of chunk `chunk` under counter word c1 (collision step << 32 | cell) */
-LT_FN double lt_uniform(uint64_t key, uint64_t chunk, uint32_t sub, uint32_t j, uint64_t c1) {
+/* Philox4x32-10 block, words (x0, x1) as a 53-bit integer u53: the j-th
+ * uniform u = u53 2^-53 of part `sub` of chunk `chunk` under counter word c1
+ * (collision step << 32 | cell) */
+LT_FN uint64_t lt_bits53(uint64_t key, uint64_t chunk, uint32_t sub, uint32_t j, uint64_t c1) {
   const uint64_t c0 = (1ull << 62) | (chunk << 20) | ((uint64_t)sub << 8) | (uint64_t)j;
   uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
   uint32_t x0 = (uint32_t)c0, x1 = (uint32_t)(c0 >> 32), x2 = (uint32_t)c1, x3 = (uint32_t)(c1 >> 32);
@@ -99,8 +128,10 @@ LT_FN double lt_uniform(uint64_t key, uint64_t chunk, uint32_t sub, uint32_t j, 
     x0 = y0; x1 = y1; x2 = y2; x3 = y3;
     k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
   }
-  return (double)((uint64_t)(x0 >> 5) * 67108864ull + (uint64_t)(x1 >> 6)) *
-         (1.0 / 9007199254740992.0);
+  return (uint64_t)(x0 >> 5) * 67108864ull + (uint64_t)(x1 >> 6);
+}
+LT_FN double lt_uniform(uint64_t key, uint64_t chunk, uint32_t sub, uint32_t j, uint64_t c1) {
+  return (double)lt_bits53(key, chunk, sub, j, c1) * (1.0 / 9007199254740992.0);
 }
 
 #endif

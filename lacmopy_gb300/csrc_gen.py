@@ -62,7 +62,21 @@ def render_thin_tables():
         for row in T:
             lines.append("  {" + ", ".join(v.hex() for v in row) + "},")
         lines.append("};")
+    # the same decisions on the 53-bit integer u53 of a uniform u = u53 2^-53:
+    # u < X  <=>  u53 < ceil(X 2^53)
+    lines += ["/* LACMO_THIN_HT / _PT = ceil(2^53 LACMO_THIN_H / _P): u < H <=> u53 < HT */"]
+    for name, T in (("LACMO_THIN_HT", H), ("LACMO_THIN_PT", P)):
+        lines.append(f"LACMO_THIN_QUAL uint64_t {name}[{ne}][{THIN_L}] = {{")
+        for row in T:
+            lines.append("  {" + ", ".join(f"{threshold53(v)}ull" for v in row) + "},")
+        lines.append("};")
     return "\n".join(lines) + "\n"
+
+
+def threshold53(x):
+    """ceil(x 2^53) for a double x in [0, 1], exactly."""
+    f = Fraction(x) * 2 ** 53
+    return -((-f.numerator) // f.denominator)
 
 
 if __name__ == "__main__":

@@ -8,7 +8,11 @@ advection steps with ``adv_step`` and copies the state back into NumPy arrays
 with ``export_to``.
 
 Draw sources for the all-or-nothing collisions:
-* ``"philox"``: counter-based Philox4x32-10 on the device (performance mode);
+* ``"philox"``: counter-based Philox4x32-10 on the device, one uniform per
+  pair (performance mode);
+* ``"thinned"``: the same Philox generator with the thinned draws of
+  csrc/lacmo_thin.h: an exact sampler of the same iid per-pair uniforms that
+  draws one uniform per low-probability segment of pairs (fastest mode);
 * ``"numpy"``: each collision step draws ``np.random.rand(pairs)`` from NumPy's
   global generator on the host, exactly the count and order the reference
   consumes, and copies it to the device (parity mode);
@@ -96,6 +100,8 @@ class DeviceState:
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', got {precision!r}")
         self.precision = precision
+        if isinstance(draws, str) and draws == "thinned":
+            draws, thin = "philox", True
         self.thin = bool(thin)
         self.set_params(st)
         self.draw_mode = draws if isinstance(draws, str) else "buffer"
@@ -333,9 +339,15 @@ class BatchState:
     shape and parameters, own SIP counts and states) advanced together, each
     kernel launch covering every member.  Collision draws come from Philox
     keyed by each member's seed, so member m evolves exactly like a
-    ``DeviceState(states[m], draws="philox", seed=seeds[m])`` on its own."""
+    ``DeviceState(states[m], draws="thinned", seed=seeds[m])`` on its own
+    (``draws="philox"``: per-pair draws)."""
 
-    def __init__(self, states, seeds, device="cuda", precision="mixed", thin=False):
+    def __init__(self, states, seeds, device="cuda", precision="mixed", draws="thinned",
+                 thin=None):
+        if draws not in ("thinned", "philox"):
+            raise ValueError(f"batch draws must be 'thinned' or 'philox', got {draws!r}")
+        if thin is None:
+            thin = draws == "thinned"
         if len(states) != len(seeds) or not states:
             raise ValueError("one seed per member state is required")
         self.lib = _lib.load()

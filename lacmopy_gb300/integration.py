@@ -7,7 +7,8 @@ back in place; CUDA tensors stay on the device.  Extra keyword-only arguments
 select the collision draw source (see lacmopy_gb300.device):
 
     draws="numpy"   NumPy's global generator, the reference's count and order
-    draws="philox"  device Philox4x32-10 with ``seed``
+    draws="philox"  device Philox4x32-10 with ``seed``, one uniform per pair
+    draws="thinned" the same generator, thinned draws (csrc/lacmo_thin.h)
     draws=<array>   injected uniforms
 
 For repeated stepping keep the state on the device with

@@ -576,16 +576,17 @@ static void process_pair_2d(int64_t i, int64_t j, double r, double* xis, double*
 }
 
 /* The thinned Philox draws of lacmopy_gb300/csrc/lacmo_thin.h for one cell:
-   the sequential definition the GPU kernel parallelises.  FP32 copies follow
-   the GPU: xi, u, w rounded from the doubles; R from the FP32 mass and
-   density at the cell temperature Tc; refreshed from the exact values after
-   each change. */
+   the sequential definition the GPU kernel parallelises (segments of row i
+   over blocks of LACMO_THIN_L slots).  FP32 copies follow the GPU: xi, u, w
+   rounded from the doubles; R from the FP32 mass and density at the cell
+   temperature Tc; refreshed from the exact values after each change.  erow[k]
+   is the largest FP32 efficiency of row k of the table. */
 static void collide_cell_2d_thin(double* xis, double* m_w, double* m_s, double* radii,
                                  const double* v0, const double* v1, const double* rho, int64_t n,
                                  double dt_over_dV, const double* E, double E_const, int64_t nb,
                                  double lo, double bl, int64_t* no_cols, int64_t* kbuf,
                                  uint64_t seed, uint64_t pc1, double Tc, int sol, float* xf,
-                                 float* Rf, float* uf, float* wf) {
+                                 float* Rf, float* uf, float* wf, const float* erow) {
   if (E) for (int64_t i = 0; i < n; ++i) kbuf[i] = kernel_index(radii[i], lo, bl, nb);
   const float Tf = (float)Tc;
   const float rhow_f = (float)LC_PAR_WATER_DENS_0 +
@@ -612,82 +613,44 @@ static void collide_cell_2d_thin(double* xis, double* m_w, double* m_s, double* 
   }
   const float dtdv_f = (float)dt_over_dV;
   const float Ec_f = (float)E_const;
-  const int64_t P = n * (n - 1) / 2;
   const int64_t L = LACMO_THIN_L;
-  int64_t pos = 0, bi = 0, bj = 1;
-  uint32_t sub = 0;
-  float pb[LACMO_THIN_L];
-  int64_t pi[LACMO_THIN_L], pj[LACMO_THIN_L];
-  while (pos < P) {
-    const int64_t chunk = pos / L;
-    const int64_t e_end = (chunk + 1) * L < P ? (chunk + 1) * L : P;
-    const int m = (int)(e_end - pos);
-    /* bounds and classes of the part's pairs */
-    int m_bg = 0;
-    float qmax = 0.0f;
-    {
-      int64_t ii = bi, jj = bj;
-      for (int t = 0; t < m; ++t) {
-        pi[t] = ii; pj[t] = jj;
-        const float ef = E ? (float)E[kbuf[ii] * nb + kbuf[jj]] : Ec_f;
-        pb[t] = lt_pair_bound(xf[ii], Rf[ii], uf[ii], wf[ii], xf[jj], Rf[jj], uf[jj], wf[jj], ef,
-                              dtdv_f);
-        if (pb[t] >= 0.0f && pb[t] < LACMO_THIN_TAU) {
-          ++m_bg;
-          qmax = qmax > pb[t] ? qmax : pb[t];
+  const int64_t B = (n + L - 1) / L;
+  for (int64_t i = 0; i + 1 < n; ++i) {
+    for (int64_t b = (i + 1) / L; b < B; ++b) {
+      const int64_t blo = b * L, bhi = (b + 1) * L < n ? (b + 1) * L : n;
+      int64_t j = blo > i + 1 ? blo : i + 1;
+      const uint64_t chunk = (uint64_t)(i * n - i * (i + 1) / 2 + (j - i - 1));   /* rank of (i, j) */
+      uint32_t sub = 0;
+      while (j < bhi) {
+        lt_block_t st;
+        lt_block_stats(xf, Rf, uf, wf, blo, bhi, &st);
+        const float er = E ? erow[kbuf[i]] : Ec_f;
+        const float Q = lt_segment_bound(xf[i], Rf[i], uf[i], wf[i], &st, er, dtdv_f);
+        if (!(Q >= 0.0f && Q < LACMO_THIN_TAU)) {
+          /* per-pair draws for the rest of the segment */
+          for (; j < bhi; ++j) {
+            const int64_t rk = i * n - i * (i + 1) / 2 + (j - i - 1);
+            process_pair_2d(i, j, philox_uniform(seed, (uint64_t)rk, pc1), xis, m_w, m_s, radii,
+                            v0, v1, rho, dt_over_dV, E, E_const, nb, lo, bl, no_cols, kbuf, xf, Rf);
+          }
+          break;
         }
-        if (++jj > n - 1) { ++ii; jj = ii + 1; }
-      }
-    }
-    /* the background hit, if any: its index among the background pairs */
-    int h = -1, e = 0;
-    double r_bg = 0.0;
-    if (m_bg > 0) {
-      e = lt_exponent(qmax);
-      const double u = lt_uniform(seed, (uint64_t)chunk, sub, 0u, pc1);
-      if (u < LACMO_THIN_H[e - LACMO_THIN_E_MIN][m_bg - 1]) {
+        const int m = (int)(bhi - j);
+        const int e = lt_exponent(Q);
+        if (lt_bits53(seed, chunk, sub, 0u, pc1) >= LACMO_THIN_HT[e - LACMO_THIN_E_MIN][m - 1])
+          break;   /* no draw of the part falls below q */
         uint32_t jd = 1;
         int g = 0;
-        for (; g < m_bg - 1; ++g) {
-          const double v = lt_uniform(seed, (uint64_t)chunk, sub, jd++, pc1);
-          if (v < LACMO_THIN_P[e - LACMO_THIN_E_MIN][m_bg - g - 1]) break;
-        }
-        r_bg = ldexp(lt_uniform(seed, (uint64_t)chunk, sub, jd, pc1), -e);
-        int seen = 0;
-        for (int t = 0; t < m; ++t) {
-          if (pb[t] >= 0.0f && pb[t] < LACMO_THIN_TAU) {
-            if (seen == g) { h = t; break; }
-            ++seen;
-          }
-        }
+        for (; g < m - 1; ++g)
+          if (lt_bits53(seed, chunk, sub, jd++, pc1) < LACMO_THIN_PT[e - LACMO_THIN_E_MIN][m - g - 1])
+            break;
+        const double r = ldexp((double)lt_bits53(seed, chunk, sub, jd, pc1) *
+                                   (1.0 / 9007199254740992.0), -e);
+        process_pair_2d(i, j + g, r, xis, m_w, m_s, radii, v0, v1, rho, dt_over_dV, E, E_const, nb,
+                        lo, bl, no_cols, kbuf, xf, Rf);
+        j += g + 1;
+        ++sub;
       }
-    }
-    /* the walk in rank order */
-    int stop = -1;
-    for (int t = 0; t < m; ++t) {
-      if (t == h) {
-        process_pair_2d(pi[t], pj[t], r_bg, xis, m_w, m_s, radii, v0, v1, rho, dt_over_dV, E,
-                        E_const, nb, lo, bl, no_cols, kbuf, xf, Rf);
-        stop = t;
-        break;
-      }
-      if (!(pb[t] >= 0.0f && pb[t] < LACMO_THIN_TAU)) {
-        const int64_t before = no_cols[0] + no_cols[1];
-        const double r = philox_uniform(seed, (uint64_t)(pos + t), pc1);
-        process_pair_2d(pi[t], pj[t], r, xis, m_w, m_s, radii, v0, v1, rho, dt_over_dV, E,
-                        E_const, nb, lo, bl, no_cols, kbuf, xf, Rf);
-        if (no_cols[0] + no_cols[1] != before) { stop = t; break; }
-      }
-    }
-    if (stop < 0) {
-      pos = e_end; sub = 0;
-      bi = pi[m - 1]; bj = pj[m - 1];
-      if (++bj > n - 1) { ++bi; bj = bi + 1; }
-    } else {
-      pos = pos + stop + 1;
-      sub = pos < e_end ? sub + 1 : 0;
-      bi = pi[stop]; bj = pj[stop];
-      if (++bj > n - 1) { ++bi; bj = bi + 1; }
     }
   }
 }
@@ -717,6 +680,15 @@ static int collision_all_cells(double* xis, double* m_w, double* m_s,
   }
   if (rnd && draw0[C] > rnd_len) { free(start); free(order); free(draw0); return -1; }
   const uint64_t cstep = col_step ? (uint64_t)*col_step : 0;
+  float* erow = NULL;
+  if (thin && E) {
+    erow = (float*)malloc(sizeof(float) * (nb > 0 ? nb : 1));
+    for (int64_t k = 0; k < nb; ++k) {
+      float mx = (float)E[k * nb];
+      for (int64_t q = 1; q < nb; ++q) mx = lt_max(mx, (float)E[k * nb + q]);
+      erow[k] = mx;
+    }
+  }
   {
     int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (C > 0 ? C : 1));
     memcpy(fill, start, sizeof(int64_t) * C);
@@ -760,7 +732,8 @@ static int collision_all_cells(double* xis, double* m_w, double* m_s,
       int64_t cnt[2] = {0, 0};
       if (thin && !rnd)
         collide_cell_2d_thin(xb, wb, sb, Rb, v0, v1, rb, n, dt_over_dV, E, E_const, nb, lo, bl,
-                             cnt, kb, seed, (cstep << 32) | (uint64_t)c, Tc, sol, fx, fR, fu, fw);
+                             cnt, kb, seed, (cstep << 32) | (uint64_t)c, Tc, sol, fx, fR, fu, fw,
+                             erow);
       else
         collide_cell_2d(xb, wb, sb, Rb, v0, v1, rb, n, dt_over_dV, E, E_const, nb, lo, bl, cnt,
                         rnd ? rnd + draw0[c] : NULL, kb, seed, (cstep << 32) | (uint64_t)c);
@@ -776,7 +749,7 @@ static int collision_all_cells(double* xis, double* m_w, double* m_s,
   no_cols[0] += nc0; no_cols[1] += nc1;
   if (rnd) *rnd_pos = draw0[C];
   if (col_step) *col_step += 1;
-  free(start); free(order); free(draw0);
+  free(start); free(order); free(draw0); free(erow);
   return 0;
 }
 

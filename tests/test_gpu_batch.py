@@ -32,17 +32,18 @@ def _copy(st):
     return {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in st.items()}
 
 
-@pytest.mark.parametrize("precision,thin", [("fp64", False), ("mixed", False), ("mixed", True)])
+@pytest.mark.parametrize("precision,draws", [("fp64", "philox"), ("mixed", "philox"),
+                                             ("mixed", "thinned"), ("fp64", "thinned")])
 @pytest.mark.parametrize("graph", [False, True])
-def test_batch_equals_single_members(precision, thin, graph):
+def test_batch_equals_single_members(precision, draws, graph):
     from lacmopy_gb300 import BatchState, DeviceState
     sts = _members(3)
     seeds = [11, 12, 13]
     assert len({st["xi"].size for st in sts}) == 3   # uneven member sizes
-    b = BatchState([_copy(st) for st in sts], seeds, precision=precision, thin=thin)
+    b = BatchState([_copy(st) for st in sts], seeds, precision=precision, draws=draws)
     b.adv_step(3, graph=graph)
     for m, st in enumerate(sts):
-        d = DeviceState(_copy(st), draws="philox", seed=seeds[m], precision=precision, thin=thin)
+        d = DeviceState(_copy(st), draws=draws, seed=seeds[m], precision=precision)
         d.adv_step(3)
         A, B = d.snapshot(), b.snapshot(m)
         assert np.array_equal(A["cells"], B["cells"])

@@ -237,13 +237,31 @@ def test_philox_draws_match_oracle(oracle_cr):
     assert np.array_equal(out["m_s"], ms)
 
 
-@pytest.mark.parametrize("boost", [1.0, 40.0])
-def test_thinned_philox_draws_match_oracle(oracle_cr, boost):
+def _oversized(st):
+    """Move SIPs so that some cells hold more SIPs than shared memory does."""
+    cells = st["cells"].copy()
+    sel = np.flatnonzero((cells[0] == 0) & (cells[1] == 0))[::3]
+    cells[1, sel] = 1
+    st["cells"] = cells
+    assert np.bincount(cells[0] * st["grid_no_cells"][1] + cells[1]).max() > 256
+    return st
+
+
+@pytest.mark.parametrize("boost,big", [(1.0, False), (40.0, False), (400.0, False),
+                                       (200.0, True)])
+def test_thinned_philox_draws_match_oracle(oracle_cr, boost, big):
     """Thinned Philox draws: GPU == the oracle's sequential thinning bit for
-    bit over two consecutive collision steps (the FP32 bounds, the chunk
-    draws and every decision agree)."""
+    bit over two consecutive collision steps (the FP32 segment bounds, the
+    block statistics, the draws and every decision agree); with boosted
+    kernels many segments take per-pair draws, and oversized cells keep their
+    block statistics in global memory."""
     from lacmopy_gb300 import DeviceState
-    st = _full_state(13, nx=40, nz=40, kernel="Hall_Bott", drizzle_fraction=0.1, r_tot=12.5E-3)
+    if big:
+        st = _oversized(_full_state(21, nx=6, nz=5, spcm=(150, 180), kernel="Hall_Bott",
+                                    drizzle_fraction=0.3, r_tot=12.5E-3))
+    else:
+        st = _full_state(13, nx=40, nz=40, kernel="Hall_Bott", drizzle_fraction=0.1,
+                         r_tot=12.5E-3)
     st["dt_col_over_dV"] = st["dt_col_over_dV"] * boost
     ds = DeviceState(st, draws="philox", seed=777, thin=True)
     ds.collision_step()

@@ -33,3 +33,20 @@ def test_thinned_and_per_pair_draws_agree_in_distribution(oracle_nb, boost):
         assert d <= 4.5 * se + 1e-9 * abs(a[:, col].mean()), (col, d, se)
     # collisions move water between SIPs but conserve it
     np.testing.assert_allclose(b[:, 3], a[0, 3], rtol=1e-12)
+
+
+def test_integer_thresholds_take_the_same_decisions():
+    """The kernels compare 53-bit integers u53 < ceil(2^53 X) where the oracle
+    compares u = u53 2^-53 < X: the two agree for every u53."""
+    import re
+    from fractions import Fraction
+    from lacmopy_gb300.csrc_gen import thin_tables, threshold53
+    H, P = thin_tables()
+    txt = open(__import__("os").path.join(__import__("os").path.dirname(__file__), "..",
+                                          "lacmopy_gb300", "csrc", "lacmo_thin_tables.h")).read()
+    ht = [int(v) for v in re.findall(r"(\d+)ull", txt)]
+    flat = [x for row in H for x in row] + [x for row in P for x in row]
+    assert ht == [threshold53(x) for x in flat]
+    for x in flat:
+        t = threshold53(x)
+        assert Fraction(t - 1, 2 ** 53) < Fraction(x) <= Fraction(t, 2 ** 53)
