@@ -31,7 +31,7 @@ static WsPlan ws_plan(int64_t n, int64_t nx, int64_t nz) {
       8 * N,           // dmxi
       4 * N,           // rm_id
       8 * N,           // rm_val
-      8 * 6 * C + 4 * 12 * C,  // aux: 6 doubles + 12 floats per cell
+      8 * cell_records_offset((int64_t)C) + 16 * CELL_REC * C,  // aux: 6 doubles, records
       8 * C,           // dTh
       8 * C,           // drv
       8 * C,           // div
@@ -40,7 +40,7 @@ static WsPlan ws_plan(int64_t n, int64_t nx, int64_t nz) {
       8 * N,           // colrho
       4 * N,           // colk
       64,              // scalars
-      4 * 2 * (size_t)((nx + 1) * (nz + 1)),  // gvf
+      0,               // (unused)
       4 * (size_t)LACMO_MAX_KERNEL_BINS * (LACMO_MAX_KERNEL_BINS + 1),  // Ef, row maxima
       4 * C,           // cell_order
       24 * N,          // gcopy
@@ -85,7 +85,6 @@ bool ws_carve(void* base, size_t bytes, int64_t n, int64_t nx, int64_t nz, Ws* w
   w->col_step = (int64_t*)(sc + 16);
   w->total_pairs = (int64_t*)(sc + 24);
   w->nfb = (unsigned long long*)(sc + 32);
-  w->gvf = (float*)(b + p.off[17]);
   w->Ef = (float*)(b + p.off[18]);
   w->cell_order = (int32_t*)(b + p.off[19]);
   w->cell_ctr = (int32_t*)(sc + 40);

@@ -56,17 +56,16 @@ __global__ void k_cells_export(const int32_t* __restrict__ cell, const double* _
   }
 }
 
-// per-cell terms of the mass rate for the next sub-step; the FP32 table that
-// follows them in the workspace (12 floats per cell, cell-major, so a SIP
-// reads its cell's entry with three 16-byte loads) feeds the mixed-precision
-// kernel without double->float conversions there
+// per-cell terms of the mass rate for the next sub-step; their FP32 copies in
+// the cell records (cell_records) feed the mixed-precision kernel without
+// double->float conversions there
 __device__ __forceinline__ void write_aux(const double* gsf, const double* gmp, double* aux,
                                           int64_t c, int64_t C) {
   CellAmb a = make_cell_amb(gsf[c], gsf[C + c], gsf[6 * C + c], gsf[7 * C + c], gmp[2 * C + c],
                             gmp[c], gmp[C + c]);
   aux[c] = a.sigw; aux[C + c] = a.rhow; aux[2 * C + c] = a.lap0; aux[3 * C + c] = a.lbp0;
   aux[4 * C + c] = a.c1; aux[5 * C + c] = a.c2;
-  float4* af = (float4*)(aux + 6 * C) + 3 * c;
+  float4* af = cell_records(aux, C) + CELL_REC * c;
   af[0] = make_float4((float)a.T, (float)(a.S - 1.0), (float)a.sigw, (float)a.rhow);
   af[1] = make_float4((float)a.lap0, (float)a.lbp0, (float)a.c1, (float)a.c2);
   af[2] = make_float4((float)gmp[5 * C + c], (float)gmp[6 * C + c], 0.0f, 0.0f);
@@ -288,8 +287,7 @@ struct PArgs {
   double* acc;                  // [C] per-cell FP64 sums of dm * xi
   int hist;                     // count SIPs per new cell for a following binning
   unsigned long long* nfb;      // SIPs whose Newton fell back to FP64
-  const float4* auxf;           // [C][3] FP32 per-cell terms (see write_aux)
-  const float* gvf;             // [2][nx+1][nz+1] FP32 wind field
+  const float4* crec;           // [C][CELL_REC] FP32 cell records (cell_records)
   double inv_dx, inv_dz;
   float inv_dxf, inv_dzf, dt_subf, dtg_f, dt_posf;
   float x_minf, x_maxf, z_minf, z_capf;
@@ -323,7 +321,7 @@ __device__ __forceinline__ PArgs make_pargs(const Member& mb, const PCall& c) {
   a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
   a.rm_id = w.rm_id; a.rm_val = w.rm_val; a.flags = w.flags;
   a.acc = w.div; a.hist = c.hist; a.nfb = w.nfb;
-  a.auxf = (const float4*)(w.aux + 6 * g.nx * g.nz); a.gvf = w.gvf;
+  a.crec = cell_records(w.aux, g.nx * g.nz);
   a.inv_dx = mb.inv_dx; a.inv_dz = mb.inv_dz;
   a.inv_dxf = mb.inv_dxf; a.inv_dzf = mb.inv_dzf;
   a.dt_subf = c.dt_subf; a.dtg_f = c.dtg_f; a.dt_posf = c.dt_posf;
@@ -333,41 +331,52 @@ __device__ __forceinline__ PArgs make_pargs(const Member& mb, const PCall& c) {
 }
 
 
-struct GridVelF {
-  const float* gv;
-  int64_t nx, nz;
-  __device__ __forceinline__ float at(int c, int64_t i, int64_t j) const {
-    if (i < 0) i += nx + 1;
-    if (j < 0) j += nz + 1;
-    return __ldg(gv + ((int64_t)c * (nx + 1) + i) * (nz + 1) + j);
-  }
-  __device__ __forceinline__ float bilin(int c, int64_t i, int64_t j, float a, float b) const {
-    return a * (b * at(c, i + 1, j + 1) + (1 - b) * at(c, i + 1, j)) +
-           (1 - a) * (b * at(c, i, j + 1) + (1 - b) * at(c, i, j));
-  }
-  // grid.py:257-323 in FP32
-  __device__ __forceinline__ void interp(int64_t i, int64_t j, float wx, float wy, float& u,
-                                         float& v) const {
-    if ((j == 0 && wy <= 0.5f) || (j == nz - 1 && wy >= 0.5f)) {
-      u = wx * at(0, i + 1, j) + (1 - wx) * at(0, i, j);
-    } else if (wy > 0.5f) {
-      u = bilin(0, i, j, wx, wy - 0.5f);
-    } else {
-      u = bilin(0, i, j - 1, wx, wy + 0.5f);
-    }
-    if (wx > 0.5f) v = bilin(1, i, j, wx - 0.5f, wy);
-    else v = bilin(1, i - 1, j, wx + 0.5f, wy);
-  }
-};
-
-__global__ void k_to_float(const __grid_constant__ MRef mr) {
+// The wind corners the FP32 interpolation of grid.py:257-323 can read in cell
+// (i, j), in float4 3..5 of the cell's record: U[a][b] = u at (i + a,
+// j - 1 + b), a < 2, b < 3, and V[a][b] = w at (i - 1 + a, j + b), a < 3,
+// b < 2, as (U00 U01 U02 U10) (U11 U12 V00 V01) (V10 V11 V20 V21); indices
+// below zero wrap like the reference's (the periodic column i = -1 is column
+// nx; row j - 1 = -1 is never read).
+__global__ void k_wind_table(const __grid_constant__ MRef mr) {
   const Member& mb = mr.get();
   const double* in = mb.g.velocity;
-  float* out = mb.w.gvf;
-  const int64_t n = 2 * (mb.g.nx + 1) * (mb.g.nz + 1);
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
-       k += (int64_t)gridDim.x * blockDim.x)
-    out[k] = (float)in[k];
+  const int64_t nx = mb.g.nx, nz = mb.g.nz, C = nx * nz;
+  float4* rec = cell_records(mb.w.aux, C);
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = c / nz, j = c - i * nz;
+    auto at = [&](int comp, int64_t ii, int64_t jj) {
+      if (ii < 0) ii += nx + 1;
+      if (jj < 0) jj += nz + 1;
+      return (float)in[((int64_t)comp * (nx + 1) + ii) * (nz + 1) + jj];
+    };
+    float4* out = rec + CELL_REC * c;
+    out[3] = make_float4(at(0, i, j - 1), at(0, i, j), at(0, i, j + 1), at(0, i + 1, j - 1));
+    out[4] = make_float4(at(0, i + 1, j), at(0, i + 1, j + 1), at(1, i - 1, j), at(1, i - 1, j + 1));
+    out[5] = make_float4(at(1, i, j), at(1, i, j + 1), at(1, i + 1, j), at(1, i + 1, j + 1));
+  }
+}
+
+// grid.py:257-323 in FP32 from a cell's wind corners (k_wind_table); wx, wy
+// are the position in the cell in units of the cell size
+__device__ __forceinline__ void interp_wind(const float4 w0, const float4 w1, const float4 w2, int j,
+                                            int nz, float wx, float wy, float& u, float& v) {
+  if ((j == 0 && wy <= 0.5f) || (j == nz - 1 && wy >= 0.5f)) {
+    u = wx * w1.x + (1 - wx) * w0.y;
+  } else if (wy > 0.5f) {
+    const float b = wy - 0.5f;
+    u = wx * (b * w1.y + (1 - b) * w1.x) + (1 - wx) * (b * w0.z + (1 - b) * w0.y);
+  } else {
+    const float b = wy + 0.5f;
+    u = wx * (b * w1.x + (1 - b) * w0.w) + (1 - wx) * (b * w0.y + (1 - b) * w0.x);
+  }
+  if (wx > 0.5f) {
+    const float a = wx - 0.5f;
+    v = a * (wy * w2.w + (1 - wy) * w2.z) + (1 - a) * (wy * w2.y + (1 - wy) * w2.x);
+  } else {
+    const float a = wx + 0.5f;
+    v = a * (wy * w2.y + (1 - wy) * w2.x) + (1 - a) * (wy * w1.w + (1 - wy) * w1.z);
+  }
 }
 
 template <bool PHYS>
@@ -592,9 +601,9 @@ struct NewtonFP64 {
   int sol, no_iter;
   unsigned long long* nfb;
 };
-__device__ __noinline__ double mixed_newton_fp64(NewtonFP64 a, int32_t c, double mw, double ms,
-                                                 double T_p) {
+__device__ __noinline__ double mixed_newton_fp64(NewtonFP64 a, int32_t c, double mw, double ms) {
   const int64_t C = a.C;
+  const double T_p = __ldg(a.gsf + c);   // the cell temperature
   CellAmb amb;
   amb.T = T_p; amb.p = __ldg(a.gsf + C + c); amb.S = __ldg(a.gsf + 6 * C + c);
   amb.e_s = __ldg(a.gsf + 7 * C + c); amb.K = __ldg(a.gmp + c);
@@ -652,16 +661,16 @@ __device__ __forceinline__ void cp_async_wait0() {
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
-// The SIP state a sub-step reads, staged one SIP ahead: each thread copies its
-// next SIP's attributes into its own shared-memory slots while it works on
-// the current one (two stages, field-major so a warp's slots are contiguous).
+// The SIP state a sub-step reads is staged in shared memory one SIP ahead
+// (each thread copies its next SIP's attributes into its own slots, field-
+// major so a warp's slots are contiguous), the cell index two SIPs ahead, and
+// the next SIP's cell record (one 128-byte line) is prefetched into L1 as
+// soon as that index has landed.
 constexpr int PM_THREADS = 128;
 enum { PF_X, PF_Z, PF_U, PF_W, PF_MW, PF_MS, PF_XI, PF_N };
 template <bool PHYS>
-__device__ __forceinline__ void prefetch_sip(double (*st)[PM_THREADS], int32_t* sc,
-                                             const PArgs& a, int64_t k) {
+__device__ __forceinline__ void prefetch_sip(double (*st)[PM_THREADS], const PArgs& a, int64_t k) {
   const int t = threadIdx.x;
-  cp_async4(sc + t, a.cell + k);
   cp_async8(&st[PF_X][t], a.pos + k);
   cp_async8(&st[PF_Z][t], a.pos + a.n + k);
   cp_async8(&st[PF_U][t], a.vel + k);
@@ -671,6 +680,9 @@ __device__ __forceinline__ void prefetch_sip(double (*st)[PM_THREADS], int32_t* 
     cp_async8(&st[PF_MS][t], a.m_s + k);
     cp_async8(&st[PF_XI][t], a.xi + k);
   }
+}
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];\n" ::"l"(p));
 }
 
 template <bool PHYS>
@@ -683,26 +695,35 @@ __global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_
   const PArgs& a = s_a;
   const int C = (int)(a.nx * a.nz);
   const int nz = (int)a.nz;
-  const GridVelF gvf{a.gvf, a.nx, a.nz};
   __shared__ double s_pf[2][PF_N][PM_THREADS];
-  __shared__ int32_t s_pc[2][PM_THREADS];
+  __shared__ int32_t s_pc[3][PM_THREADS];
   const int t = threadIdx.x;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t k = blockIdx.x * (int64_t)blockDim.x + t;
-  int sg = 0;
-  if (k < a.n) prefetch_sip<PHYS>(s_pf[0], s_pc[0], a, k);
+  // the first SIP's state and the cell indices of the first two
+  if (k < a.n) {
+    cp_async4(&s_pc[0][t], a.cell + k);
+    prefetch_sip<PHYS>(s_pf[0], a, k);
+  }
+  if (k + stride < a.n) cp_async4(&s_pc[1][t], a.cell + k + stride);
   cp_async_commit();
-  for (; k < a.n; k += stride, sg ^= 1) {
-    if (k + stride < a.n) prefetch_sip<PHYS>(s_pf[sg ^ 1], s_pc[sg ^ 1], a, k + stride);
+  int sg = 0, c3 = 0;   // slots of SIP k: state sg, cell index c3
+  for (; k < a.n; k += stride, sg ^= 1, c3 = c3 == 2 ? 0 : c3 + 1) {
+    const int n3 = c3 == 2 ? 0 : c3 + 1, nn3 = n3 == 2 ? 0 : n3 + 1;
+    if (k + stride < a.n) prefetch_sip<PHYS>(s_pf[sg ^ 1], a, k + stride);
+    if (k + 2 * stride < a.n) cp_async4(&s_pc[nn3][t], a.cell + k + 2 * stride);
     cp_async_commit();
-    cp_async_wait1();   // this SIP's copies have landed
-    const int32_t c = s_pc[sg][t];
+    cp_async_wait1();   // this SIP's state and the next SIP's cell index have landed
+    if (PHYS && k + stride < a.n) {
+      const int32_t cn = s_pc[n3][t];
+      if (cn >= 0) prefetch_l1(a.crec + CELL_REC * (int64_t)cn);
+    }
+    const int32_t c = s_pc[c3][t];
     const bool active = c >= 0;
     const int i = active ? c / nz : -1 - c;
     const int j = active ? c - i * nz : -1;
     double x = s_pf[sg][PF_X][t], z = s_pf[sg][PF_Z][t];
-    const double T_p = __ldg(a.gsf + (int64_t)i * nz + (active ? j : nz - 1));
-    if (a.write_Tp) a.T_p[k] = T_p;
+    if (a.write_Tp) a.T_p[k] = __ldg(a.gsf + (int64_t)i * nz + (active ? j : nz - 1));
     if (!active) {
       mixed_inactive_rel(a.rel, a.n, a.dx, a.dz, k, i);
       continue;
@@ -716,7 +737,8 @@ __global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_
       const double ms = s_pf[sg][PF_MS][t];
       xik = s_pf[sg][PF_XI][t];
       CellAmbF af;
-      const float4 q0 = __ldg(a.auxf + 3 * c), q1 = __ldg(a.auxf + 3 * c + 1);
+      const float4* rec = a.crec + CELL_REC * (int64_t)c;
+      const float4 q0 = __ldg(rec), q1 = __ldg(rec + 1);
       af.T = q0.x; af.S_m1 = q0.y; af.sigw = q0.z; af.rhow = q0.w;
       af.lap0 = q1.x; af.lbp0 = q1.y; af.c1 = q1.z; af.c2 = q1.w;
       const float msf = d2f_int(ms), mwf = d2f_int(mw), xif = d2f_int(xik);
@@ -745,7 +767,7 @@ __global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_
       } else {
         dm = mixed_newton_fp64(NewtonFP64{a.gsf, a.gmp, a.aux, (int64_t)C, a.dt_sub, a.sol,
                                           a.no_iter, a.nfb},
-                               c, mw, ms, T_p);
+                               c, mw, ms);
         d = d2f_int(dm);
       }
       mw += dm;
@@ -760,8 +782,8 @@ __global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_
       const float rxf = (xf - a.x_minf) * a.inv_dxf - (float)i;
       const float rzf = (zf - a.z_minf) * a.inv_dzf - (float)j;
       float uf, wf;
-      gvf.interp(i, j, rxf, rzf, uf, wf);
-      const float2 q2 = __ldg((const float2*)(a.auxf + 3 * c + 2));
+      interp_wind(__ldg(rec + 3), __ldg(rec + 4), __ldg(rec + 5), j, nz, rxf, rzf, uf, wf);
+      const float2 q2 = __ldg((const float2*)(rec + 2));
       const float mu_f = q2.x, rho_f = q2.y;
       const float uo = d2f_int(s_pf[sg][PF_U][t]), wo = d2f_int(s_pf[sg][PF_W][t]);
       const float d0 = uf - uo, d1 = wf - wo;
@@ -864,7 +886,7 @@ __device__ __forceinline__ void grid_cell_update_mixed(double* gsf, double* gmp,
   const double c2 = LC_R_V * T / (D_v * e_s);
   aux[c] = sigw; aux[C + c] = rhow; aux[2 * C + c] = lap0; aux[3 * C + c] = lbp0;
   aux[4 * C + c] = c1; aux[5 * C + c] = c2;
-  float4* af = (float4*)(aux + 6 * C) + 3 * c;
+  float4* af = cell_records(aux, C) + CELL_REC * c;
   af[0] = make_float4((float)T, (float)(S - 1.0), (float)sigw, (float)rhow);
   af[1] = make_float4((float)lap0, (float)lbp0, (float)c1, (float)c2);
   af[2] = make_float4((float)mu, (float)rho_f, 0.0f, 0.0f);
@@ -1174,7 +1196,7 @@ cudaError_t launch_move_mixed(const Bt& B, double dt_pos, cudaStream_t s) {
   return cudaGetLastError();
 }
 cudaError_t launch_wind_float(const Bt& B, cudaStream_t s) {
-  k_to_float<<<grid2(2 * (B.nx + 1) * (B.nz + 1), 256, B.M), 256, 0, s>>>(B.ref()); note_launches(1);
+  k_wind_table<<<grid2(B.nx * B.nz, 256, B.M), 256, 0, s>>>(B.ref()); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_grid_acc(const Bt& B, cudaStream_t s) {

@@ -34,7 +34,6 @@ struct Ws {
   int64_t* col_step;   // collision-step counter (Philox)
   int64_t* total_pairs;
   unsigned long long* nfb;   // mixed precision: Newton repeats in FP64
-  float* gvf;                // [2][nx+1][nz+1] FP32 copy of the wind (mixed precision)
   float* Ef;                 // [LACMO_MAX_KERNEL_BINS^2] FP32 copy of the efficiency table,
                              // then [LACMO_MAX_KERNEL_BINS] row maxima
   int32_t* cell_order;       // [C]   cells by descending SIP count (collision work order)
@@ -42,6 +41,19 @@ struct Ws {
   float* gcopy;              // [6][n] collision FP32 copies of cells above the shared-memory size
   float* gstats;             // [n/32 + C + 1][8] block statistics of those cells (thinned draws)
 };
+
+// The FP32 per-cell records of the mixed-precision particle kernel, after the
+// six FP64 per-cell terms in the aux array: 8 float4 (one 128-byte line) per
+// cell, cell-major: [0..2] the Newton and drag terms (write_aux), [3..5] the
+// wind corners (k_wind_table).
+__host__ __device__ inline size_t cell_records_offset(int64_t C) {
+  return (size_t)((6 * C + 15) / 16) * 16;   // in doubles, 128-byte aligned
+}
+__host__ __device__ inline float4* cell_records(double* aux, int64_t C) {
+  return (float4*)(aux + cell_records_offset(C));
+}
+constexpr int CELL_REC = 8;   // float4 per cell record
+
 
 size_t ws_bytes(int64_t n, int64_t nx, int64_t nz);
 bool ws_carve(void* base, size_t bytes, int64_t n, int64_t nx, int64_t nz, Ws* ws);
