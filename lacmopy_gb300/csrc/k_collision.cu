@@ -462,9 +462,30 @@ __device__ __forceinline__ int2 thin_cell(const CellArgs& a, const CellSmem S, i
   int si = 0, sb = 0, sj = 1, ssub = 0;   // current segment, its part start and counter
   bool scratch = false;
   for (;;) {
-    int i = si, b = sb;
-    if (lane) advance_seg(n, B, i, b, lane);
-    const bool valid = b < B;
+    // lane l takes the l-th segment from (si, sb): the segments left in rows
+    // si, si + 1, ... (one row per lane) summed by a warp scan, then the row
+    // holding offset l found by a binary search over the sums
+    int cnt = 0;
+    {
+      const int r = si + lane;
+      if (r <= n - 2) cnt = B - (lane ? (r + 1) >> 5 : sb);
+    }
+    int csum = cnt;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int v = __shfl_up_sync(FULL, csum, off);
+      if (lane >= off) csum += v;
+    }
+    int rho = 0;   // first row k with csum_k > lane
+#pragma unroll
+    for (int step = 16; step; step >>= 1) {
+      const int ck = __shfl_sync(FULL, csum, rho + step - 1);
+      if (ck <= lane) rho += step;
+    }
+    const int before = __shfl_sync(FULL, csum, rho > 0 ? rho - 1 : 0);
+    const bool valid = lane < __shfl_sync(FULL, csum, 31);
+    const int i = si + rho;
+    const int b = (rho ? (i + 1) >> 5 : sb) + lane - (rho ? before : 0);
     const int blo = b << 5;
     const int jfirst = blo > i + 1 ? blo : i + 1;
     const int j = lane ? jfirst : sj;
@@ -488,7 +509,9 @@ __device__ __forceinline__ int2 thin_cell(const CellArgs& a, const CellSmem S, i
     const unsigned ev = __ballot_sync(FULL, valid && (indiv || hit));
     if (!ev) {
       if (__ballot_sync(FULL, valid) != FULL) break;   // the cell's last segment is done
-      advance_seg(n, B, si, sb, 32);
+      si = __shfl_sync(FULL, i, 31);
+      sb = __shfl_sync(FULL, b, 31);
+      advance_seg(n, B, si, sb, 1);
       if (sb >= B) break;
       sj = (sb << 5) > si + 1 ? (sb << 5) : si + 1;
       ssub = 0;

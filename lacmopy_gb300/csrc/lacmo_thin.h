@@ -121,6 +121,15 @@ LT_FN uint64_t lt_bits53(uint64_t key, uint64_t chunk, uint32_t sub, uint32_t j,
   const uint64_t c0 = (1ull << 62) | (chunk << 20) | ((uint64_t)sub << 8) | (uint64_t)j;
   uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
   uint32_t x0 = (uint32_t)c0, x1 = (uint32_t)(c0 >> 32), x2 = (uint32_t)c1, x3 = (uint32_t)(c1 >> 32);
+#ifdef __CUDA_ARCH__
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, x0), lo0 = 0xD2511F53u * x0;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, x2), lo1 = 0xCD9E8D57u * x2;
+    x0 = hi1 ^ x1 ^ k0; x1 = lo1; x2 = hi0 ^ x3 ^ k1; x3 = lo0;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+#else
   for (int r = 0; r < 10; ++r) {
     const uint64_t p0 = (uint64_t)0xD2511F53u * x0, p1 = (uint64_t)0xCD9E8D57u * x2;
     const uint32_t y0 = (uint32_t)(p1 >> 32) ^ x1 ^ k0, y1 = (uint32_t)p1;
@@ -128,6 +137,7 @@ LT_FN uint64_t lt_bits53(uint64_t key, uint64_t chunk, uint32_t sub, uint32_t j,
     x0 = y0; x1 = y1; x2 = y2; x3 = y3;
     k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
   }
+#endif
   return (uint64_t)(x0 >> 5) * 67108864ull + (uint64_t)(x1 >> 6);
 }
 LT_FN double lt_uniform(uint64_t key, uint64_t chunk, uint32_t sub, uint32_t j, uint64_t c1) {
