@@ -1061,6 +1061,7 @@ __global__ void k_table_rowmax(const double* __restrict__ E, float* __restrict__
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nb;
        k += (int64_t)gridDim.x * blockDim.x) {
     float mx = (float)E[k * nb];
+#pragma unroll 8
     for (int64_t q = 1; q < nb; ++q) mx = lt_max(mx, (float)E[k * nb + q]);
     erow[k] = mx;
   }

@@ -224,36 +224,70 @@ __global__ void k_scatter(const __grid_constant__ MRef mr) {
   }
 }
 
-// one warp per cell: order the cell's slots by ascending SIP ID
+// Bitonic sort of 32 * PER keys held by a warp, key[u] = element lane * PER + u,
+// ascending: compare-exchange stages of distance j >= PER between lanes
+// (shuffles), of smaller distance within a lane's registers.
+template <int PER>
+__device__ __forceinline__ void warp_bitonic(int32_t (&key)[PER], int lane) {
+  constexpr int N = 32 * PER;
+#pragma unroll
+  for (int k = 2; k <= N; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j >= PER) {
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+          const int e = lane * PER + u;
+          const int32_t other = __shfl_xor_sync(0xffffffffu, key[u], j / PER);
+          const bool take_min = ((e & k) == 0) == ((e & j) == 0);
+          key[u] = take_min ? min(key[u], other) : max(key[u], other);
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+          if (u & j) continue;
+          const bool up = ((lane * PER + u) & k) == 0;
+          const int32_t x = key[u], y = key[u ^ j];
+          key[u] = up ? min(x, y) : max(x, y);
+          key[u ^ j] = up ? max(x, y) : min(x, y);
+        }
+      }
+    }
+  }
+}
+// the L <= 32 * PER slots of one cell sorted by SIP ID in the warp's registers
+template <int PER>
+__device__ __forceinline__ void sort_cell_ids(int32_t* perm, int32_t b, int L, int lane) {
+  int32_t key[PER];
+#pragma unroll
+  for (int u = 0; u < PER; ++u) {
+    const int e = lane * PER + u;
+    key[u] = e < L ? perm[b + e] : 0x7fffffff;
+  }
+  warp_bitonic<PER>(key, lane);
+#pragma unroll
+  for (int u = 0; u < PER; ++u) {
+    const int e = lane * PER + u;
+    if (e < L) perm[b + e] = key[u];
+  }
+}
+
+// one warp per cell: order the cell's slots by ascending SIP ID (a bitonic
+// sort in registers up to 256 slots, else ranks by counting)
 constexpr int ORDER_SMEM = 256;
 __global__ void __launch_bounds__(256) k_order(const __grid_constant__ MRef mr) {
   const Member& mb = mr.get();
   const int32_t* __restrict__ start = mb.w.start;
   int32_t *perm = mb.w.perm, *scratch = mb.w.rank;
   const int64_t C = mb.g.nx * mb.g.nz;
-  __shared__ int32_t s_ids[8][ORDER_SMEM];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int64_t c = blockIdx.x * 8LL + wid; c < C; c += (int64_t)gridDim.x * 8) {
     const int32_t b = start[c], L = start[c + 1] - b;
     if (L <= 1) continue;
     if (L <= ORDER_SMEM) {
-      for (int q = lane; q < L; q += 32) s_ids[wid][q] = perm[b + q];
-      __syncwarp();
-      int32_t mine[ORDER_SMEM / 32];
-      int32_t r[ORDER_SMEM / 32];
-#pragma unroll
-      for (int u = 0; u < ORDER_SMEM / 32; ++u) { mine[u] = 0; r[u] = 0; }
-#pragma unroll
-      for (int u = 0; u < ORDER_SMEM / 32; ++u)
-        if (lane + 32 * u < L) mine[u] = s_ids[wid][lane + 32 * u];
-      for (int q = 0; q < L; ++q) {
-        int32_t v = s_ids[wid][q];
-#pragma unroll
-        for (int u = 0; u < ORDER_SMEM / 32; ++u) r[u] += (v < mine[u]);
-      }
-#pragma unroll
-      for (int u = 0; u < ORDER_SMEM / 32; ++u)
-        if (lane + 32 * u < L) perm[b + r[u]] = mine[u];
+      if (L <= 64) sort_cell_ids<2>(perm, b, L, lane);
+      else if (L <= 128) sort_cell_ids<4>(perm, b, L, lane);
+      else sort_cell_ids<8>(perm, b, L, lane);
       __syncwarp();
     } else {
       for (int q = lane; q < L; q += 32) scratch[b + q] = perm[b + q];
