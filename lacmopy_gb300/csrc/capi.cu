@@ -88,6 +88,8 @@ bool ws_carve(void* base, size_t bytes, int64_t n, int64_t nx, int64_t nz, Ws* w
   w->Ef = (float*)(b + p.off[18]);
   w->cell_order = (int32_t*)(b + p.off[19]);
   w->cell_ctr = (int32_t*)(sc + 40);
+  w->fb_count = (int32_t*)(sc + 44);
+  w->fb_done = (int32_t*)(sc + 48);
   w->gcopy = (float*)(b + p.off[20]);
   w->gstats = (float*)(b + p.off[21]);
   return true;

@@ -316,6 +316,10 @@ struct PArgs {
   double* dmxi;
   int32_t *counts, *rank, *rm_count, *rm_id;
   double* rm_val;
+  // mixed precision: SIPs whose Newton repeats in FP64 (k_newton_fallback),
+  // queued in scratch that mixed sub-steps leave unused
+  int32_t *fb_count, *fb_done, *fb_id, *fb_c;
+  double* fb_mw;
   uint32_t* flags;
   // mixed precision
   double* acc;                  // [C] per-cell FP64 sums of dm * xi
@@ -354,6 +358,8 @@ __device__ __forceinline__ PArgs make_pargs(const Member& mb, const PCall& c) {
   a.no_iter = c.no_iter; a.sol = c.sol; a.write_Tp = c.write_Tp;
   a.dmxi = w.dmxi; a.counts = w.counts; a.rank = w.rank; a.rm_count = w.rm_count;
   a.rm_id = w.rm_id; a.rm_val = w.rm_val; a.flags = w.flags;
+  a.fb_count = w.fb_count; a.fb_done = w.fb_done; a.fb_id = w.rm_id; a.fb_c = w.colk;
+  a.fb_mw = w.rm_val;
   a.acc = w.div; a.hist = c.hist; a.nfb = w.nfb;
   a.crec = cell_records(w.aux, g.nx * g.nz);
   a.inv_dx = mb.inv_dx; a.inv_dz = mb.inv_dz;
@@ -687,6 +693,22 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(
                    (unsigned)__cvta_generic_to_shared(smem)), "l"(gmem));
 }
+// the same with an L2 eviction-priority policy (createpolicy): the SIP state
+// streams through once per sub-step, evict-first, so that the per-cell
+// records the kernel gathers stay in L2
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ void cp_async8_ef(void* smem, const void* gmem, uint64_t pol) {
+  asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;\n" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(smem)), "l"(gmem), "l"(pol));
+}
+__device__ __forceinline__ void cp_async4_ef(void* smem, const void* gmem, uint64_t pol) {
+  asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 4, %2;\n" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(smem)), "l"(gmem), "l"(pol));
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n"); }
 __device__ __forceinline__ void cp_async_wait1() {
   asm volatile("cp.async.wait_group 1;\n" ::: "memory");
@@ -703,16 +725,17 @@ __device__ __forceinline__ void cp_async_wait0() {
 constexpr int PM_THREADS = 128;
 enum { PF_X, PF_Z, PF_U, PF_W, PF_MW, PF_MS, PF_XI, PF_N };
 template <bool PHYS>
-__device__ __forceinline__ void prefetch_sip(double (*st)[PM_THREADS], const PArgs& a, int64_t k) {
+__device__ __forceinline__ void prefetch_sip(double (*st)[PM_THREADS], const PArgs& a, int64_t k,
+                                             uint64_t pol) {
   const int t = threadIdx.x;
-  cp_async8(&st[PF_X][t], a.pos + k);
-  cp_async8(&st[PF_Z][t], a.pos + a.n + k);
-  cp_async8(&st[PF_U][t], a.vel + k);
-  cp_async8(&st[PF_W][t], a.vel + a.n + k);
+  cp_async8_ef(&st[PF_X][t], a.pos + k, pol);
+  cp_async8_ef(&st[PF_Z][t], a.pos + a.n + k, pol);
+  cp_async8_ef(&st[PF_U][t], a.vel + k, pol);
+  cp_async8_ef(&st[PF_W][t], a.vel + a.n + k, pol);
   if (PHYS) {
-    cp_async8(&st[PF_MW][t], a.m_w + k);
-    cp_async8(&st[PF_MS][t], a.m_s + k);
-    cp_async8(&st[PF_XI][t], a.xi + k);
+    cp_async8_ef(&st[PF_MW][t], a.m_w + k, pol);
+    cp_async8_ef(&st[PF_MS][t], a.m_s + k, pol);
+    cp_async8_ef(&st[PF_XI][t], a.xi + k, pol);
   }
 }
 __device__ __forceinline__ void prefetch_l1(const void* p) {
@@ -735,17 +758,18 @@ __global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t k = blockIdx.x * (int64_t)blockDim.x + t;
   // the first SIP's state and the cell indices of the first two
+  const uint64_t pol = l2_evict_first_policy();
   if (k < a.n) {
-    cp_async4(&s_pc[0][t], a.cell + k);
-    prefetch_sip<PHYS>(s_pf[0], a, k);
+    cp_async4_ef(&s_pc[0][t], a.cell + k, pol);
+    prefetch_sip<PHYS>(s_pf[0], a, k, pol);
   }
-  if (k + stride < a.n) cp_async4(&s_pc[1][t], a.cell + k + stride);
+  if (k + stride < a.n) cp_async4_ef(&s_pc[1][t], a.cell + k + stride, pol);
   cp_async_commit();
   int sg = 0, c3 = 0;   // slots of SIP k: state sg, cell index c3
   for (; k < a.n; k += stride, sg ^= 1, c3 = c3 == 2 ? 0 : c3 + 1) {
     const int n3 = c3 == 2 ? 0 : c3 + 1, nn3 = n3 == 2 ? 0 : n3 + 1;
-    if (k + stride < a.n) prefetch_sip<PHYS>(s_pf[sg ^ 1], a, k + stride);
-    if (k + 2 * stride < a.n) cp_async4(&s_pc[nn3][t], a.cell + k + 2 * stride);
+    if (k + stride < a.n) prefetch_sip<PHYS>(s_pf[sg ^ 1], a, k + stride, pol);
+    if (k + 2 * stride < a.n) cp_async4_ef(&s_pc[nn3][t], a.cell + k + 2 * stride, pol);
     cp_async_commit();
     cp_async_wait1();   // this SIP's state and the next SIP's cell index have landed
     if (PHYS && k + stride < a.n) {
@@ -765,6 +789,9 @@ __global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_
     double mw = 0.0;
     double xik = 0.0;
     float un, wn2;
+    int fb_slot = -1;           // queue slot of a SIP whose Newton repeats in FP64
+    double mw_in = 0.0, ms_k = 0.0;
+    float xif_k = 0.0f;
     const float xf = d2f_int(x), zf = d2f_int(z);
     if (PHYS) {
       mw = s_pf[sg][PF_MW][t];
@@ -795,18 +822,23 @@ __global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_
       float d;
       const bool ok = newton_mixed_f(a.sol, a.dt_subf, a.no_iter, mwf, msf, wsf, R, af.T, rho, sig,
                                      af, d_effl, &d);
-      double dm;
+      const double dm = f2d_int(d);
       if (ok) {
-        dm = f2d_int(d);
+        // per-cell FP64 sum of dm * xi (executed by L2)
+        atomicAdd(a.acc + c, f2d_int(d * xif));
       } else {
-        dm = mixed_newton_fp64(NewtonFP64{a.gsf, a.gmp, a.aux, (int64_t)C, a.dt_sub, a.sol,
-                                          a.no_iter, a.nfb},
-                               c, mw, ms);
-        d = d2f_int(dm);
+        // near the critical radius the Newton repeats in FP64, in full warps
+        // in k_newton_fallback: queue the SIP with its mass before the
+        // sub-step; drag and motion go on with the FP32 increment
+        fb_slot = atomicAdd(a.fb_count, 1);
+        a.fb_id[fb_slot] = (int32_t)k;
+        a.fb_c[fb_slot] = c;
+        a.fb_mw[fb_slot] = mw;
       }
+      mw_in = mw;
+      ms_k = ms;
+      xif_k = xif;
       mw += dm;
-      // per-cell FP64 sum of dm * xi (executed by L2)
-      atomicAdd(a.acc + c, f2d_int(d * xif));
       // drag (integration.py:699-718) in FP32 with the ammonium-sulfate radius
       const float mpn = (mwf + d) + msf;
       const float wn = msf * f_rcp(mpn);
@@ -850,6 +882,16 @@ __global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_
     bool removed = false;
     if (!(znf > a.z_minf + 1e-3f) && mixed_below(z, a.z_min)) {
       if (!PHYS) { xik = a.xi[k]; mw = a.m_w[k]; }
+      if (PHYS && fb_slot >= 0) {
+        // a queued SIP leaving the domain: its FP64 Newton here, for the
+        // water it takes along
+        const double dm = mixed_newton_fp64(NewtonFP64{a.gsf, a.gmp, a.aux, (int64_t)C, a.dt_sub,
+                                                       a.sol, a.no_iter, a.nfb},
+                                            c, mw_in, ms_k);
+        mw = mw_in + dm;
+        atomicAdd(a.acc + c, f2d_int(d2f_int(dm) * xif_k));
+        a.fb_id[fb_slot] = -1;
+      }
       z = mixed_remove(GroundGeo{a.rel, a.water_removed, a.n, a.x_min, a.z_min, a.dx, a.dz}, k,
                        i, j, x0, z0, xik, mw);
       u = 0.0; w = 0.0;
@@ -869,12 +911,43 @@ __global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_
       newc = (int32_t)(ci * nz + cj);
       if (a.hist) a.rank[k] = atomicAdd(a.counts + newc, 1);
     }
-    a.pos[k] = x; a.pos[a.n + k] = z;
-    if (PHYS || removed) { a.vel[k] = u; a.vel[a.n + k] = w; }
-    if (PHYS) a.m_w[k] = mw;
-    a.cell[k] = newc;
+    // streaming stores (evict first)
+    __stcs(a.pos + k, x); __stcs(a.pos + a.n + k, z);
+    if (PHYS || removed) { __stcs(a.vel + k, u); __stcs(a.vel + a.n + k, w); }
+    if (PHYS) __stcs(a.m_w + k, mw);
+    __stcs(a.cell + k, newc);
   }
   cp_async_wait0();
+}
+
+// The FP64 Newton of the SIPs a mixed sub-step queued (near the critical
+// radius), one SIP per thread: the mass and the per-cell sum as the inline
+// FP64 path gives them; the last block empties the queue.
+__global__ void __launch_bounds__(128) k_newton_fallback(const __grid_constant__ PK x) {
+  __shared__ PArgs s_a;
+  if (threadIdx.x == 0) s_a = make_pargs(x.m.get(), x.c);
+  __syncthreads();
+  const PArgs& a = s_a;
+  const int cnt = *(volatile int32_t*)a.fb_count;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x) {
+    const int32_t k = a.fb_id[q];
+    if (k < 0) continue;   // handled where it left the domain
+    const int32_t c = a.fb_c[q];
+    const double mw0 = a.fb_mw[q];
+    const double dm = mixed_newton_fp64(NewtonFP64{a.gsf, a.gmp, a.aux, a.nx * a.nz, a.dt_sub,
+                                                   a.sol, a.no_iter, a.nfb},
+                                        c, mw0, a.m_s[k]);
+    a.m_w[k] = mw0 + dm;
+    atomicAdd(a.acc + c, f2d_int(d2f_int(dm) * d2f_int(a.xi[k])));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(a.fb_done, 1) == (int)gridDim.x - 1) {
+      *a.fb_count = 0;
+      *a.fb_done = 0;
+    }
+  }
 }
 
 // Mixed precision: the grid update of one cell (integration.py:402-484,
@@ -1218,6 +1291,7 @@ cudaError_t launch_particles_mixed(const Bt& B, const lacmo_params_t& p, double 
   cudaError_t e = mixed_grid<true>(B, &grid);
   if (e != cudaSuccess) return e;
   k_particles_mixed<true><<<grid, PM_THREADS, 0, s>>>(x); note_launches(1);
+  k_newton_fallback<<<dim3(16, B.M), 128, 0, s>>>(x); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_move_mixed(const Bt& B, double dt_pos, cudaStream_t s) {

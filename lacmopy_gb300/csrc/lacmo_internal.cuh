@@ -38,6 +38,7 @@ struct Ws {
                              // then [LACMO_MAX_KERNEL_BINS] row maxima
   int32_t* cell_order;       // [C]   cells by descending SIP count (collision work order)
   int32_t* cell_ctr;         // next entry of cell_order a collision warp takes
+  int32_t *fb_count, *fb_done;   // mixed precision: FP64 Newton queue length, blocks done
   float* gcopy;              // [6][n] collision FP32 copies of cells above the shared-memory size
   float* gstats;             // [n/32 + C + 1][8] block statistics of those cells (thinned draws)
 };
