@@ -104,6 +104,7 @@ struct CellArgs {
   double *gR, *grho;   // per SIP: exact radius and density, or the step-start m_p, m_s
   int32_t* gk;         // per SIP: exact kernel bin, or -1 while gR/grho hold m_p, m_s
   float dtdv_f, lo_f, inv_bl_f, E_const_f;   // FP32 copies for the screen
+  float bin_margin;    // distance from a bin edge below which the FP32 bin is not trusted
   const float* Ef;     // FP32 efficiency table, or null (then E is read and rounded)
   const int32_t* cell_order;   // cells, largest first
   int32_t* cell_ctr;           // next cell_order entry to take
@@ -123,7 +124,7 @@ struct CellCommon {
   int sol;
   const double* draws;
   int64_t n_draws;
-  float dtdv_f, lo_f, inv_bl_f, E_const_f;
+  float dtdv_f, lo_f, inv_bl_f, E_const_f, bin_margin;
   const float* Ef;
   const float* erow;
   int thin;
@@ -143,6 +144,7 @@ __device__ __forceinline__ void make_cellargs(CellArgs& a, const Member& mb, con
   a.no_cols = mb.sp.no_cols; a.flags = mb.w.flags;
   a.gR = mb.w.colR; a.grho = mb.w.colrho; a.gk = mb.w.colk;
   a.dtdv_f = cc.dtdv_f; a.lo_f = cc.lo_f; a.inv_bl_f = cc.inv_bl_f; a.E_const_f = cc.E_const_f;
+  a.bin_margin = cc.bin_margin;
   a.Ef = cc.Ef;
   a.cell_order = mb.w.cell_order; a.cell_ctr = mb.w.cell_ctr;
   a.gcopy = mb.w.gcopy;
@@ -686,7 +688,8 @@ __global__ void __launch_bounds__(CELL_WARPS * 32, THIN ? 2 : 3)
       if (use_E) {
         const float v = (__logf(Rf) - a.lo_f) * a.inv_bl_f + 0.5f;
         const float fl = floorf(v);
-        if (v - fl > 2e-3f && (fl + 1.0f) - v > 2e-3f && v > -1e6f && v < 1e6f && Rf > 0.f) {
+        if (v - fl > a.bin_margin && (fl + 1.0f) - v > a.bin_margin && v > -1e6f && v < 1e6f &&
+            Rf > 0.f) {
           kb = __float2int_rz(fl);
           kb = kb < 0 ? 0 : (kb > a.nb - 1 ? (int32_t)a.nb - 1 : kb);
         } else {
@@ -1067,6 +1070,24 @@ __global__ void k_table_rowmax(const double* __restrict__ E, float* __restrict__
   }
 }
 
+// Bound on the error of the FP32 bin position v = (__logf(Rf) - lo_f) *
+// inv_bl_f + 0.5 against the exact (log R - lo) / bl + 0.5, doubled: Rf is
+// within 1e-6 of R (relative), so log Rf within 1e-6; __logf within 2^-21.41
+// absolute on [0.5, 2] and 3 ulp elsewhere (taken as 4 ulp of the largest
+// |log R| a bin edge can have); lo_f and the subtraction round within one ulp
+// of that value together; inv_bl_f, the product and the + 0.5 each within
+// 2^-24 of v <= nb + 1.  Bins closer than this to an edge are taken from the
+// exact FP64 path.
+static float fp32_bin_margin(double lo, double bl, int64_t nb) {
+  if (!(bl > 0.0) || nb <= 0) return 0.5f;
+  const double lmax = fmax(fabs(lo), fabs(lo + (double)(nb + 1) * bl)) + 1.0;
+  const double ulp = ldexp(1.0, (int)floor(log2(lmax)) - 23);
+  const double log_err = fmax(ldexp(1.0, -21) , 4.0 * ulp);
+  const double v_err = (1e-6 + log_err + ulp) / bl + 3.0 * (double)(nb + 1) * ldexp(1.0, -24);
+  const double m = 2.0 * v_err;
+  return (float)(m < 0.5 ? m : 0.5);
+}
+
 cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d,
                                  cudaStream_t s) {
   int dev = 0;
@@ -1088,6 +1109,7 @@ cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lac
   cc.nb = p.no_kernel_bins; cc.lo = p.R_kernel_low_log; cc.bl = p.bin_factor_R_log;
   cc.sol = p.solute; cc.draws = d.draws; cc.n_draws = d.n_draws;
   cc.dtdv_f = (float)cc.dtdv; cc.lo_f = (float)cc.lo; cc.inv_bl_f = (float)(1.0 / cc.bl);
+  cc.bin_margin = fp32_bin_margin(cc.lo, cc.bl, cc.nb);
   cc.E_const_f = (float)cc.E_const;
   cc.Ef = nullptr;
   cc.erow = nullptr;

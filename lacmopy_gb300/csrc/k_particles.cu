@@ -372,7 +372,8 @@ __device__ __forceinline__ PArgs make_pargs(const Member& mb, const PCall& c) {
 
 
 // The wind corners the FP32 interpolation of grid.py:257-323 can read in cell
-// (i, j), in float4 3..5 of the cell's record: U[a][b] = u at (i + a,
+// (i, j), in float4 3..5 of the cell's record (float4 6 holds i, j and
+// whether j is the bottom or top row): U[a][b] = u at (i + a,
 // j - 1 + b), a < 2, b < 3, and V[a][b] = w at (i - 1 + a, j + b), a < 3,
 // b < 2, as (U00 U01 U02 U10) (U11 U12 V00 V01) (V10 V11 V20 V21); indices
 // below zero wrap like the reference's (the periodic column i = -1 is column
@@ -394,14 +395,17 @@ __global__ void k_wind_table(const __grid_constant__ MRef mr) {
     out[3] = make_float4(at(0, i, j - 1), at(0, i, j), at(0, i, j + 1), at(0, i + 1, j - 1));
     out[4] = make_float4(at(0, i + 1, j), at(0, i + 1, j + 1), at(1, i - 1, j), at(1, i - 1, j + 1));
     out[5] = make_float4(at(1, i, j), at(1, i, j + 1), at(1, i + 1, j), at(1, i + 1, j + 1));
+    out[6] = make_float4((float)i, (float)j, j == 0 ? 1.0f : 0.0f, j == nz - 1 ? 1.0f : 0.0f);
   }
 }
 
 // grid.py:257-323 in FP32 from a cell's wind corners (k_wind_table); wx, wy
-// are the position in the cell in units of the cell size
-__device__ __forceinline__ void interp_wind(const float4 w0, const float4 w1, const float4 w2, int j,
-                                            int nz, float wx, float wy, float& u, float& v) {
-  if ((j == 0 && wy <= 0.5f) || (j == nz - 1 && wy >= 0.5f)) {
+// are the position in the cell in units of the cell size, jlo / jhi mark the
+// bottom and top rows of cells
+__device__ __forceinline__ void interp_wind(const float4 w0, const float4 w1, const float4 w2,
+                                            bool jlo, bool jhi, float wx, float wy, float& u,
+                                            float& v) {
+  if ((jlo && wy <= 0.5f) || (jhi && wy >= 0.5f)) {
     u = wx * w1.x + (1 - wx) * w0.y;
   } else if (wy > 0.5f) {
     const float b = wy - 0.5f;
@@ -778,14 +782,14 @@ __global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_
     }
     const int32_t c = s_pc[c3][t];
     const bool active = c >= 0;
-    const int i = active ? c / nz : -1 - c;
-    const int j = active ? c - i * nz : -1;
     double x = s_pf[sg][PF_X][t], z = s_pf[sg][PF_Z][t];
-    if (a.write_Tp) a.T_p[k] = __ldg(a.gsf + (int64_t)i * nz + (active ? j : nz - 1));
     if (!active) {
+      const int i = -1 - c;
+      if (a.write_Tp) a.T_p[k] = __ldg(a.gsf + (int64_t)i * nz + nz - 1);
       mixed_inactive_rel(a.rel, a.n, a.dx, a.dz, k, i);
       continue;
     }
+    if (a.write_Tp) a.T_p[k] = __ldg(a.gsf + c);
     double mw = 0.0;
     double xik = 0.0;
     float un, wn2;
@@ -845,10 +849,12 @@ __global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_
       rho = af.rhow * ((((float)LC_PAR_RHO_AS_0 * wn + (float)LC_PAR_RHO_AS_1) * wn +
                         (float)LC_PAR_RHO_AS_2) * wn + (float)LC_PAR_RHO_AS_3);
       R = f_cbrt((float)LC_FOUR_PI_OVER_THREE_INV * mpn * f_rcp(rho));
-      const float rxf = (xf - a.x_minf) * a.inv_dxf - (float)i;
-      const float rzf = (zf - a.z_minf) * a.inv_dzf - (float)j;
+      const float4 cij = __ldg(rec + 6);   // (i, j, j == 0, j == nz - 1)
+      const float rxf = (xf - a.x_minf) * a.inv_dxf - cij.x;
+      const float rzf = (zf - a.z_minf) * a.inv_dzf - cij.y;
       float uf, wf;
-      interp_wind(__ldg(rec + 3), __ldg(rec + 4), __ldg(rec + 5), j, nz, rxf, rzf, uf, wf);
+      interp_wind(__ldg(rec + 3), __ldg(rec + 4), __ldg(rec + 5), cij.z != 0.0f, cij.w != 0.0f,
+                  rxf, rzf, uf, wf);
       const float2 q2 = __ldg((const float2*)(rec + 2));
       const float mu_f = q2.x, rho_f = q2.y;
       const float uo = d2f_int(s_pf[sg][PF_U][t]), wo = d2f_int(s_pf[sg][PF_W][t]);
@@ -881,6 +887,7 @@ __global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_
     int32_t newc;
     bool removed = false;
     if (!(znf > a.z_minf + 1e-3f) && mixed_below(z, a.z_min)) {
+      const int i = c / nz, j = c - i * nz;
       if (!PHYS) { xik = a.xi[k]; mw = a.m_w[k]; }
       if (PHYS && fb_slot >= 0) {
         // a queued SIP leaving the domain: its FP64 Newton here, for the
@@ -1230,6 +1237,8 @@ static PCall pcall(const lacmo_params_t& p, double dt_sub, double dt_pos, bool w
 }
 cudaError_t launch_cell_aux(const Bt& B, cudaStream_t s) {
   k_cell_aux<<<grid2(B.nx * B.nz, 32, B.M), 32, 0, s>>>(B.ref()); note_launches(1);
+  // the wind part of the cell records too, for sub-steps run before a full step
+  k_wind_table<<<grid2(B.nx * B.nz, 256, B.M), 256, 0, s>>>(B.ref()); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_histogram(const Bt& B, cudaStream_t s) {
@@ -1291,7 +1300,7 @@ cudaError_t launch_particles_mixed(const Bt& B, const lacmo_params_t& p, double 
   cudaError_t e = mixed_grid<true>(B, &grid);
   if (e != cudaSuccess) return e;
   k_particles_mixed<true><<<grid, PM_THREADS, 0, s>>>(x); note_launches(1);
-  k_newton_fallback<<<dim3(16, B.M), 128, 0, s>>>(x); note_launches(1);
+  k_newton_fallback<<<dim3(64, B.M), 128, 0, s>>>(x); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_move_mixed(const Bt& B, double dt_pos, cudaStream_t s) {
