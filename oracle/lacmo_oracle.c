@@ -348,6 +348,18 @@ static double philox_uniform(uint64_t key, uint64_t k, uint64_t c1) {
   uint64_t a = (k & 1) ? (x2 >> 5) : (x0 >> 5), b = (k & 1) ? (x3 >> 6) : (x1 >> 6);
   return (double)(a * 67108864ull + b) * (1.0 / 9007199254740992.0);
 }
+/* the segment bound of lacmopy_gb300/csrc/lacmo_thin.h for SIP a against the
+   block of slots [lo, hi) of the FP32 copies (certification tests) */
+ORC_EXPORT float orc_segment_bound(const float* x, const float* R, const float* u, const float* w,
+                                   int64_t a, int64_t lo, int64_t hi, float er, float dtdv_f) {
+  lt_block_t st;
+  lt_block_stats(x, R, u, w, lo, hi, &st);
+  return lt_segment_bound(x[a], R[a], u[a], w[a], &st, er, dtdv_f);
+}
+/* the FP32 cube root of lacmo_thin.h (accuracy tests) */
+ORC_EXPORT void orc_lt_cbrtf(const float* x, int64_t n, float* out) {
+  for (int64_t k = 0; k < n; ++k) out[k] = lt_cbrtf(x[k]);
+}
 /* the raw Philox4x32-10 block, for known-answer tests */
 ORC_EXPORT void orc_philox_block(uint64_t key, uint64_t c0, uint64_t c1, uint32_t* out) {
   uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);

@@ -40,6 +40,9 @@ def build(quiet=True):
         print(out.stdout)
 
 
+F32 = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+
+
 def _lib(variant):
     if variant in _cache:
         return _cache[variant]
@@ -80,6 +83,9 @@ def _lib(variant):
     lib.orc_collision_step_all_cells_2d_philox.restype = cint
     U64 = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
     lib.orc_philox_uniform.argtypes = [ctypes.c_uint64, U64, U64, i64, D]
+    lib.orc_segment_bound.argtypes = [F32] * 4 + [i64, i64, i64, ctypes.c_float, ctypes.c_float]
+    lib.orc_segment_bound.restype = ctypes.c_float
+    lib.orc_lt_cbrtf.argtypes = [F32, i64, F32]
     lib.orc_philox_block.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
                                      np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")]
     lib.orc_integrate_adv_step.restype = cint
@@ -314,6 +320,19 @@ class Oracle:
         c1 = np.ascontiguousarray(c1, dtype=np.uint64)
         out = np.empty(k.size)
         self.lib.orc_philox_uniform(int(key), k, c1, k.size, out)
+        return out
+
+    def segment_bound(self, x, R, u, w, a, lo, hi, er, dtdv):
+        """lt_segment_bound of SIP a against the block [lo, hi) of the FP32
+        copies x, R, u, w (lacmopy_gb300/csrc/lacmo_thin.h)."""
+        f = lambda v: np.ascontiguousarray(v, dtype=np.float32)
+        return float(self.lib.orc_segment_bound(f(x), f(R), f(u), f(w), int(a), int(lo), int(hi),
+                                                float(er), float(dtdv)))
+
+    def lt_cbrtf(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.empty_like(x)
+        self.lib.orc_lt_cbrtf(x, x.size, out)
         return out
 
     def philox_block(self, key, c0, c1):

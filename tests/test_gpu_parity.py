@@ -247,14 +247,16 @@ def _oversized(st):
     return st
 
 
-@pytest.mark.parametrize("boost,big", [(1.0, False), (40.0, False), (400.0, False),
-                                       (200.0, True)])
-def test_thinned_philox_draws_match_oracle(oracle_cr, boost, big):
+@pytest.mark.parametrize("boost,big,const_E", [(1.0, False, False), (40.0, False, False),
+                                               (400.0, False, False), (200.0, True, False),
+                                               (40.0, False, True)])
+def test_thinned_philox_draws_match_oracle(oracle_cr, boost, big, const_E):
     """Thinned Philox draws: GPU == the oracle's sequential thinning bit for
     bit over two consecutive collision steps (the FP32 segment bounds, the
     block statistics, the draws and every decision agree); with boosted
     kernels many segments take per-pair draws, and oversized cells keep their
-    block statistics in global memory."""
+    block statistics in global memory; a constant efficiency replaces the
+    table's row maxima."""
     from lacmopy_gb300 import DeviceState
     if big:
         st = _oversized(_full_state(21, nx=6, nz=5, spcm=(150, 180), kernel="Hall_Bott",
@@ -263,7 +265,9 @@ def test_thinned_philox_draws_match_oracle(oracle_cr, boost, big):
         st = _full_state(13, nx=40, nz=40, kernel="Hall_Bott", drizzle_fraction=0.1,
                          r_tot=12.5E-3)
     st["dt_col_over_dV"] = st["dt_col_over_dV"] * boost
-    ds = DeviceState(st, draws="philox", seed=777, thin=True)
+    if const_E:   # constant collection efficiency: the row maximum is the constant
+        st["E_col_grid"] = 0.5
+    ds = DeviceState(st, draws="thinned", seed=777)
     ds.collision_step()
     ds.collision_step()
     out = ds.snapshot()
