@@ -529,35 +529,48 @@ __device__ __forceinline__ int2 thin_cell(const CellArgs& a, const CellSmem S, i
     if (!scratch) { init_exact_scratch(a, S, n, lane); scratch = true; }
     int next_j = eend;
     if (eind) {
-      // per-pair draws of the rest of the segment, screened in parallel
-      int jj = ej;
-      while (jj < eend) {
-        const int q = jj + lane;
+      // per-pair draws of the rest of the segment (pair ej + lane per lane,
+      // drawn once), screened in parallel; the candidates are processed in
+      // order, and the rest is screened again only after a state change
+      const int q = ej + lane;
+      const bool mine = q < eend;
+      uint64_t k53 = 0;
+      float r_lo = 0.0f, r_hi = 0.0f;
+      if (mine) {
+        k53 = philox_bits53(a.seed, (uint64_t)pair_rank(ei, q, n), pc1);
+        philox_interval(k53, r_lo, r_hi);
+      }
+      unsigned todo = __ballot_sync(FULL, mine);   // pairs not processed yet
+      while (todo) {
         int sc = 0;
-        uint64_t k53 = 0;
-        if (q < eend) {
-          k53 = philox_bits53(a.seed, (uint64_t)pair_rank(ei, q, n), pc1);
-          float r_lo, r_hi;
-          philox_interval(k53, r_lo, r_hi);
+        if ((todo >> lane) & 1u)
           sc = screen_pair(a, use_E, S.v[ei], S.sk[ei], S.v[q], S.sk[q], r_lo, r_hi);
-        }
-        const unsigned cand = __ballot_sync(FULL, sc != 0);
-        if (!cand) break;
-        const int t = __ffs(cand) - 1;
-        if (lane == t) {
-          if (sc == 1) {
-            certain_collection(a, S, ei, q, Tc, use_E);
-            c0 += 1;
-          } else {
-            const int o = exact_pair(a, S, S.sid[ei], S.sid[q], ei, q, Tc, use_E,
-                                     philox_from_bits(k53));
-            c0 += o == 1;
-            c1 += o == 2;
+        unsigned cand = __ballot_sync(FULL, sc != 0);
+        bool changed = false;
+        while (cand) {
+          const int t = __ffs(cand) - 1;
+          int col = 0;
+          if (lane == t) {
+            if (sc == 1) {
+              certain_collection(a, S, ei, q, Tc, use_E);
+              c0 += 1;
+              col = 1;
+            } else {
+              const int o = exact_pair(a, S, S.sid[ei], S.sid[q], ei, q, Tc, use_E,
+                                       philox_from_bits(k53));
+              c0 += o == 1;
+              c1 += o == 2;
+              col = o != 0;
+            }
           }
+          col = __shfl_sync(FULL, col, t);
+          __threadfence_block();
+          __syncwarp();
+          todo &= ~((2u << t) - 1u);   // pairs up to t are done
+          if (col) { changed = true; break; }
+          cand &= cand - 1u;   // no change: the later screens still hold
         }
-        __threadfence_block();
-        __syncwarp();
-        jj += t + 1;   // the later pairs are screened again with the new state
+        if (!changed) break;
       }
     } else {
       // the hit: first-hit draws of all lanes, then the pair with r = q u
