@@ -400,20 +400,23 @@ def run_ours(args):
                        ("pos", "vel", "rel_pos", "m_w", "m_s", "xi", "T_p", "water_removed",
                         "cells", "grid_scalar_fields", "grid_mat_prop", "delta_m_l",
                         "no_cols")) + n
-        I.integrate_adv_step_np(*[sts[0][k] for k in keys], draws=args.draws, seed=7)  # warm-up
+        I.integrate_adv_step_np(*[sts[0][k] for k in keys], draws=args.draws, seed=7,
+                                precision="mixed")  # warm-up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ups_e = 0
         for _ in range(args.e2e_steps):
             for m, se in enumerate(sts):
                 ups_e += int(np.count_nonzero(se["active_ids"]))
-                I.integrate_adv_step_np(*[se[k] for k in keys], draws=args.draws, seed=7 + m)
+                I.integrate_adv_step_np(*[se[k] for k in keys], draws=args.draws, seed=7 + m,
+                                        precision="mixed")
         torch.cuda.synchronize()
         te = time.perf_counter() - t0
         e2e = {"value": ups_e / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h),
                "api": "lacmopy_gb300.integration.integrate_adv_step_np (reference argument "
-                      "list) per member, NumPy host state copied in and out every call",
+                      "list, precision=\"mixed\") per member, NumPy host state copied in and "
+                      "out every call",
                "sample": f"{len(sts)} members x {args.e2e_steps} steps of the workload"}
 
     cpu = None

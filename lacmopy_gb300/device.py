@@ -37,6 +37,17 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
+def _copy_to_host(dst, t):
+    """Device tensor -> the caller's NumPy array in place: straight into its
+    (already resident) pages when dtype and layout allow, else through a
+    temporary."""
+    if (isinstance(dst, np.ndarray) and dst.flags.c_contiguous and dst.flags.writeable
+            and dst.size == t.numel() and torch.from_numpy(dst[:0]).dtype == t.dtype):
+        torch.from_numpy(dst).view(-1).copy_(t.reshape(-1))
+    else:
+        np.copyto(dst, t.cpu().numpy().reshape(np.shape(dst)))
+
+
 def to_device(a, dtype=F64, device="cuda"):
     """NumPy array / scalar / tensor -> contiguous CUDA tensor of ``dtype``."""
     if isinstance(a, torch.Tensor):
@@ -315,9 +326,13 @@ class DeviceState:
                  ("no_cols", self.no_cols), ("cells", cells)]
         for k, t in pairs:
             if k in st and st[k] is not None:
-                np.copyto(st[k], t.cpu().numpy().reshape(np.shape(st[k])))
-        if "active_ids" in st:
-            np.copyto(st["active_ids"], act.cpu().numpy().astype(bool))
+                _copy_to_host(st[k], t)
+        if "active_ids" in st and st["active_ids"] is not None:
+            dst = st["active_ids"]
+            if isinstance(dst, np.ndarray) and dst.dtype == np.bool_ and dst.flags.c_contiguous:
+                _copy_to_host(dst.view(np.uint8), act)   # 0/1 bytes are valid booleans
+            else:
+                np.copyto(dst, act.cpu().numpy().astype(bool))
         return st
 
     def snapshot(self):

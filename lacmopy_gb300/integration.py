@@ -41,8 +41,10 @@ def integrate_adv_step_np(grid_scalar_fields, grid_mat_prop, grid_velocity,
                           act_collisions, act_relaxation, init_profile_r_v, init_profile_Theta,
                           relaxation_time_profile, no_iter_impl_mass, g_set, E_col_grid,
                           no_kernel_bins, R_kernel_low_log, bin_factor_R_log, no_cols, *,
-                          draws="numpy", seed=1001):
-    """One advection step dt on the GPU (integration.py:1298-1611), in place."""
+                          draws="numpy", seed=1001, precision="fp64"):
+    """One advection step dt on the GPU (integration.py:1298-1611), in place.
+    ``precision="mixed"`` runs the mixed-precision sub-steps
+    (lacmopy_gb300.device)."""
     st = dict(zip(_STATE_KEYS, (
         grid_scalar_fields, grid_mat_prop, grid_velocity, grid_mass_flux_air_dry, p_ref,
         p_ref_inv, grid_no_cells, grid_ranges, grid_steps, grid_volume_cell, pos, vel, cells,
@@ -51,7 +53,7 @@ def integrate_adv_step_np(grid_scalar_fields, grid_mat_prop, grid_velocity,
         act_relaxation, init_profile_r_v, init_profile_Theta, relaxation_time_profile,
         no_iter_impl_mass, g_set, E_col_grid, no_kernel_bins, R_kernel_low_log,
         bin_factor_R_log, no_cols)))
-    ds = DeviceState(st, draws=draws, seed=seed)
+    ds = DeviceState(st, draws=draws, seed=seed, precision=precision)
     ds.adv_step(1)
     ds.export_to(st)
 
