@@ -621,10 +621,13 @@ __device__ __forceinline__ int2 thin_cell(const CellArgs& a, const CellSmem S, i
 // order (collections and undecided pairs) are processed one at a time.
 constexpr size_t CELL_WARP_BYTES = (size_t)CELL_SMEM * (4 * 4 + 4 + 4) + (CELL_SMEM / 32) * 32;
 
-// THIN: the thinned draws (registers for 2 blocks per SM), else per-pair
-// draws (3 blocks per SM)
+// THIN: the thinned draws, else per-pair draws; 3 blocks per SM either way
+// (the thinned rounds gain more from the warps than they lose to spills)
+#ifndef LACMO_COL_BLOCKS
+#define LACMO_COL_BLOCKS 3
+#endif
 template <bool THIN>
-__global__ void __launch_bounds__(CELL_WARPS * 32, THIN ? 2 : 3)
+__global__ void __launch_bounds__(CELL_WARPS * 32, LACMO_COL_BLOCKS)
     k_collide_cells(const __grid_constant__ CK x) {
   // the member's arguments, once per block (all warps of a block belong to
   // the same member); shared memory keeps them addressable without a copy
