@@ -747,7 +747,10 @@ __device__ __forceinline__ void prefetch_l1(const void* p) {
 }
 
 template <bool PHYS>
-__global__ void __launch_bounds__(PM_THREADS, 6) k_particles_mixed(const __grid_constant__ PK x) {
+#ifndef LACMO_PM_BLOCKS
+#define LACMO_PM_BLOCKS 8   // resident blocks per SM (register budget 64)
+#endif
+__global__ void __launch_bounds__(PM_THREADS, LACMO_PM_BLOCKS) k_particles_mixed(const __grid_constant__ PK x) {
   // the member's arguments, once per block in shared memory: threads read
   // them on use instead of holding some 60 registers of pointers and sizes
   __shared__ PArgs s_a;
