@@ -252,6 +252,26 @@ int lacmo_relaxation_term(const double* field, int64_t nx, int64_t nz, const dou
 int lacmo_update_grid_r_l(const lacmo_sips_t* sips, const lacmo_grid_t* grid, void* ws,
                           size_t ws_bytes, void* stream);
 
+/* ---- diagnostics ---------------------------------------------------------------- */
+/* Per-cell sums over the SIPs in ascending ID order, bit for bit the
+ * reference's loops.  cell: the int32 cell index of lacmo_cells_import (a SIP
+ * removed at the ground, -1 - i, counts in cell (i, nz - 1) where the
+ * reference's row index -1 lands).  ws: a workspace of
+ * lacmo_workspace_bytes(n, nx, nz), whose cell binning the call replaces.
+ * out[nx][nz].
+ * kind 0 replaces evaluation.py:93 update_mixing_ratio (sum m_w xi over the
+ * masked SIPs, times 1E-18 mass_dry_inv); kind 1 replaces evaluation.py:136
+ * update_number_concentration_per_dry_mass (sum xi, times mass_dry_inv). */
+int lacmo_update_cell_sum(int kind, const double* m_w, const double* xi, const int32_t* cell,
+                          const uint8_t* mask, const double* mass_dry_inv, int64_t n, int64_t nx,
+                          int64_t nz, double* out, void* ws, size_t ws_bytes, void* stream);
+/* Replaces evaluation.py:1393 compute_moment_R_grid: sum over the active SIPs
+ * of xi R_p^order (R_p^order by repeated squaring, as Numba's integer
+ * power), divided by V0. */
+int lacmo_compute_moment_R_grid(int64_t order, const double* R_p, const double* xi, double V0,
+                                const int32_t* cell, int64_t n, int64_t nx, int64_t nz,
+                                double* out, void* ws, size_t ws_bytes, void* stream);
+
 /* ---- collisions ------------------------------------------------------------------ */
 /* All cells of the 2-D grid: replaces collision/all_or_nothing.py:754
  * collision_step_Ecol_grid_R_all_cells_2D_multicomp_np (and :498 / :637 per

@@ -100,6 +100,10 @@ PROTOTYPES = {
                                                ctypes.c_int, vp, vp]),
     "lacmo_relaxation_term": (ctypes.c_int, [vp, i64, i64, vp, vp, dbl, vp, vp]),
     "lacmo_update_grid_r_l": (ctypes.c_int, [P(Sips), P(Grid), vp, sz, vp]),
+    "lacmo_update_cell_sum": (ctypes.c_int, [ctypes.c_int, vp, vp, vp, vp, vp, i64, i64, i64, vp,
+                                             vp, sz, vp]),
+    "lacmo_compute_moment_R_grid": (ctypes.c_int, [i64, vp, vp, dbl, vp, i64, i64, i64, vp, vp,
+                                                   sz, vp]),
     "lacmo_collision_step_cells": (ctypes.c_int, [P(Sips), P(Grid), P(Params), P(Draws), vp, sz,
                                                   vp]),
     "lacmo_collision_pair_count": (ctypes.c_int, [vp, i64, i64, i64, P(i64), vp]),

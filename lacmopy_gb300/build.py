@@ -25,6 +25,7 @@ UNITS = {
     "k_collision.cu": ["-fmad=false"],
     "k_static.cu": [],
     "k_adjoint.cu": [],
+    "k_diag.cu": ["-fmad=false"],
 }
 
 

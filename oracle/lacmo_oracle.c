@@ -348,6 +348,59 @@ static double philox_uniform(uint64_t key, uint64_t k, uint64_t c1) {
   uint64_t a = (k & 1) ? (x2 >> 5) : (x0 >> 5), b = (k & 1) ? (x3 >> 6) : (x1 >> 6);
   return (double)(a * 67108864ull + b) * (1.0 / 9007199254740992.0);
 }
+/* ---- diagnostics (evaluation.py) ------------------------------------------
+   Per-cell sums over SIPs in ascending ID order, as the reference's loops
+   over id_list[mask] (id_list = 0 .. N-1).  A removed SIP has cells[1] = -1,
+   which the reference's indexing wraps to the top row nz - 1. */
+static inline int64_t diag_cell(const int64_t* cells, int64_t N, int64_t Nz, int64_t id) {
+  int64_t j = cells[N + id];
+  if (j < 0) j += Nz;
+  return cells[id] * Nz + j;
+}
+/* x**n for an integer n >= 0: CPython's pow(x, n) in the _py variant, else
+   Numba's exponentiation by squaring */
+static inline double diag_ipow(double x, int64_t n) {
+#ifdef ORC_SQUARE_POW
+  return pow(x, (double)n);
+#else
+  double r = 1.0;
+  while (n != 0) {
+    if (n & 1) r *= x;
+    n >>= 1;
+    x *= x;
+  }
+  return r;
+#endif
+}
+/* evaluation.py:93-133 (kind 0: m_w xi, 1E-18 / m_dry) and :136-174 (kind 1:
+   xi, 1 / m_dry) */
+ORC_EXPORT void orc_update_cell_sum(int kind, double* out, const double* m_w, const double* xi,
+                                    const int64_t* cells, int64_t N, int64_t Nx, int64_t Nz,
+                                    const double* mass_dry_inv, const uint8_t* mask) {
+  for (int64_t c = 0; c < Nx * Nz; ++c) out[c] = 0.0;
+  for (int64_t id = 0; id < N; ++id) {
+    if (!mask[id]) continue;
+    const int64_t c = diag_cell(cells, N, Nz, id);
+    out[c] += kind == 0 ? m_w[id] * xi[id] : xi[id];
+  }
+  for (int64_t c = 0; c < Nx * Nz; ++c)
+    out[c] *= kind == 0 ? 1.0E-18 * mass_dry_inv[c] : mass_dry_inv[c];
+}
+/* evaluation.py:1392-1445: the n-th radius moment per cell, active SIPs */
+ORC_EXPORT void orc_compute_moment_R_grid(int64_t n, const double* R_p, const double* xi,
+                                          double V0, const int64_t* cells,
+                                          const uint8_t* active, int64_t N, int64_t Nx,
+                                          int64_t Nz, double* out) {
+  for (int64_t c = 0; c < Nx * Nz; ++c) out[c] = 0.0;
+  for (int64_t id = 0; id < N; ++id) {
+    if (!active[id]) continue;
+    const int64_t c = diag_cell(cells, N, Nz, id);
+    if (n == 0) out[c] += xi[id];
+    else out[c] += xi[id] * diag_ipow(R_p[id], n);
+  }
+  for (int64_t c = 0; c < Nx * Nz; ++c) out[c] = out[c] / V0;
+}
+
 /* the segment bound of lacmopy_gb300/csrc/lacmo_thin.h for SIP a against the
    block of slots [lo, hi) of the FP32 copies (certification tests) */
 ORC_EXPORT float orc_segment_bound(const float* x, const float* R, const float* u, const float* w,

@@ -83,6 +83,9 @@ def _lib(variant):
     lib.orc_collision_step_all_cells_2d_philox.restype = cint
     U64 = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
     lib.orc_philox_uniform.argtypes = [ctypes.c_uint64, U64, U64, i64, D]
+    U8P = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+    lib.orc_update_cell_sum.argtypes = [cint, D, D, D, I64, i64, i64, i64, D, U8P]
+    lib.orc_compute_moment_R_grid.argtypes = [i64, D, D, dbl, I64, U8P, i64, i64, i64, D]
     lib.orc_segment_bound.argtypes = [F32] * 4 + [i64, i64, i64, ctypes.c_float, ctypes.c_float]
     lib.orc_segment_bound.restype = ctypes.c_float
     lib.orc_lt_cbrtf.argtypes = [F32, i64, F32]
@@ -321,6 +324,27 @@ class Oracle:
         out = np.empty(k.size)
         self.lib.orc_philox_uniform(int(key), k, c1, k.size, out)
         return out
+
+    # -- diagnostics (evaluation.py) -------------------------------------------
+    def update_cell_sum(self, kind, m_w, xi, cells, no_cells, mass_dry_inv, mask):
+        """kind 0: update_mixing_ratio (evaluation.py:93-133); kind 1:
+        update_number_concentration_per_dry_mass (:136-174); id_list = 0..N-1."""
+        Nx, Nz = int(no_cells[0]), int(no_cells[1])
+        out = np.empty(Nx * Nz)
+        self.lib.orc_update_cell_sum(int(kind), out, _c(m_w), _c(xi), _c(cells, np.int64), len(xi),
+                                     Nx, Nz, np.ascontiguousarray(mass_dry_inv, dtype=np.float64),
+                                     np.ascontiguousarray(mask, dtype=np.uint8))
+        return out.reshape(Nx, Nz)
+
+    def compute_moment_R_grid(self, n, R_p, xi, V0, cells, active_ids, no_cells):
+        """evaluation.py:1392-1445 with id_list = 0..N-1."""
+        Nx, Nz = int(no_cells[0]), int(no_cells[1])
+        out = np.empty(Nx * Nz)
+        self.lib.orc_compute_moment_R_grid(int(n), _c(R_p), _c(xi), float(V0),
+                                           _c(cells, np.int64),
+                                           np.ascontiguousarray(active_ids, dtype=np.uint8),
+                                           len(xi), Nx, Nz, out)
+        return out.reshape(Nx, Nz)
 
     def segment_bound(self, x, R, u, w, a, lo, hi, er, dtdv):
         """lt_segment_bound of SIP a against the block [lo, hi) of the FP32

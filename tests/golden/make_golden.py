@@ -358,6 +358,41 @@ def gen_adv_step(R):
     save("adv_step.npz", **out)
 
 
+def gen_diagnostics(R):
+    """evaluation.py: per-cell mixing ratios, number concentrations and
+    radius moments; some SIPs removed at the ground (cells[1] = -1)."""
+    import evaluation as ev
+    st = _small_state(41, Nx=6, Nz=5, spcm=(8, 12), kernel_type="Hall_Bott")
+    N = st["xi"].size
+    rng = np.random.default_rng(41)
+    cells = st["cells"].copy()
+    act = st["active_ids"].copy()
+    gone = rng.choice(N, 9, replace=False)
+    cells[1, gone] = -1
+    act[gone] = False
+    m_w, m_s, xi = st["m_w"], st["m_s"], st["xi"]
+    R_p = np.cbrt((m_w + m_s) / (4.0 / 3.0 * np.pi * 1.1E3))   # any positive radii
+    mass_dry_inv = 1.0 / (rng.uniform(0.9, 1.3, (6, 5)) * 8.0E3)
+    id_list = np.arange(N)
+    masks = {"active": act, "large": act & (R_p > np.median(R_p)),
+             "with_removed": act | np.isin(id_list, gone[:5])}
+    out = {"m_w": m_w, "xi": xi, "cells": cells, "active_ids": act, "R_p": R_p,
+           "mass_dry_inv": mass_dry_inv, "V0": np.float64(st["grid_volume_cell"]),
+           "no_cells": np.array([6, 5])}
+    for name, mask in masks.items():
+        mr = np.zeros((6, 5))
+        ev.update_mixing_ratio(mr, m_w, xi, cells, mass_dry_inv, id_list, mask)
+        nc = np.zeros((6, 5))
+        ev.update_number_concentration_per_dry_mass(nc, xi, cells, mass_dry_inv, id_list, mask)
+        out["mask_" + name] = mask
+        out["mixing_ratio_" + name] = mr
+        out["number_conc_" + name] = nc
+    for n in range(4):
+        out[f"moment_{n}"] = ev.compute_moment_R_grid(n, R_p, xi, float(st["grid_volume_cell"]),
+                                                      cells, act, id_list, np.array([6, 5]))
+    save("diagnostics.npz", **out)
+
+
 def gen_tables(R):
     out = {}
     for kt in ("Long_Bott", "Hall_Bott"):
@@ -382,6 +417,7 @@ def main(ref_root):
     gen_grid_and_divergence(R)
     gen_particle_substep(R)
     gen_adv_step(R)
+    gen_diagnostics(R)
 
 
 if __name__ == "__main__":

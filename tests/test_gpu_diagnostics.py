@@ -1,0 +1,55 @@
+"""GPU diagnostics (lacmopy_gb300/evaluation.py, csrc/k_diag.cu) against the
+oracle and the reference's own outputs (tests/golden/diagnostics.npz)."""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def test_diagnostics_match_golden_and_oracle(oracle_nb):
+    from lacmopy_gb300 import evaluation as E
+    g = golden("diagnostics.npz")
+    N = g["xi"].size
+    ids = np.arange(N)
+    for name in ("active", "large", "with_removed"):
+        mask = g["mask_" + name]
+        mr = np.zeros((6, 5))
+        E.update_mixing_ratio(mr, g["m_w"], g["xi"], g["cells"], g["mass_dry_inv"], ids, mask)
+        nc = np.zeros((6, 5))
+        E.update_number_concentration_per_dry_mass(nc, g["xi"], g["cells"], g["mass_dry_inv"],
+                                                   ids, mask)
+        if name == "with_removed":   # removed SIPs follow the top-row cell's own SIPs
+            np.testing.assert_allclose(mr, g["mixing_ratio_" + name], rtol=1e-14, atol=0)
+            np.testing.assert_allclose(nc, g["number_conc_" + name], rtol=1e-14, atol=0)
+        else:
+            assert np.array_equal(mr, g["mixing_ratio_" + name]), name
+            assert np.array_equal(nc, g["number_conc_" + name]), name
+    for n in range(4):
+        m = E.compute_moment_R_grid(n, g["R_p"], g["xi"], g["V0"], g["cells"], g["active_ids"],
+                                    ids, g["no_cells"])
+        ref = oracle_nb.compute_moment_R_grid(n, g["R_p"], g["xi"], g["V0"], g["cells"],
+                                              g["active_ids"], g["no_cells"])
+        assert np.array_equal(m, ref), n   # Numba's integer power, bit for bit
+        np.testing.assert_allclose(m, g[f"moment_{n}"], rtol=1e-14, atol=0)
+
+
+def test_diagnostics_full_grid_vs_oracle(oracle_nb):
+    """75 x 75 cells x 64 SIPs: bit for bit against the oracle."""
+    from lacmopy_gb300 import evaluation as E, synthetic
+    st = synthetic.make_icmw_state(Nx=75, Nz=75, seed=5, kernel_type="Long_Bott")
+    N = st["xi"].size
+    rng = np.random.default_rng(2)
+    R_p = 10.0 ** rng.uniform(-2, 2, N)
+    mdi = rng.uniform(1e-4, 2e-4, (75, 75))
+    mask = rng.random(N) < 0.7
+    mr = np.zeros((75, 75))
+    E.update_mixing_ratio(mr, st["m_w"], st["xi"], st["cells"], mdi, np.arange(N), mask)
+    ref = oracle_nb.update_cell_sum(0, st["m_w"], st["xi"], st["cells"], (75, 75), mdi, mask)
+    assert np.array_equal(mr, ref)
+    m3 = E.compute_moment_R_grid(3, R_p, st["xi"], 8000.0, st["cells"], st["active_ids"],
+                                 np.arange(N), (75, 75))
+    ref3 = oracle_nb.compute_moment_R_grid(3, R_p, st["xi"], 8000.0, st["cells"],
+                                           st["active_ids"], (75, 75))
+    assert np.array_equal(m3, ref3)

@@ -181,3 +181,26 @@ def test_tables_regenerate_bit_exactly():
         E, rg = load_kernel_data_Ecol(kt)[:2]
         assert hashlib.sha256(np.ascontiguousarray(E).tobytes()).hexdigest() == str(g[kt + "__E_sha256"])
         assert hashlib.sha256(np.ascontiguousarray(rg).tobytes()).hexdigest() == str(g[kt + "__r_sha256"])
+
+
+def test_diagnostics(oracle_py, oracle_nb):
+    """evaluation.py mixing ratios, number concentrations (masks with removed
+    SIPs, whose cells[1] = -1 index the top row) and radius moments 0..3."""
+    g = golden("diagnostics.npz")
+    no_cells = g["no_cells"]
+    for name in ("active", "large", "with_removed"):
+        mask = g["mask_" + name]
+        mr = oracle_py.update_cell_sum(0, g["m_w"], g["xi"], g["cells"], no_cells,
+                                       g["mass_dry_inv"], mask)
+        nc = oracle_py.update_cell_sum(1, g["m_w"], g["xi"], g["cells"], no_cells,
+                                       g["mass_dry_inv"], mask)
+        assert np.array_equal(mr, g["mixing_ratio_" + name]), name
+        assert np.array_equal(nc, g["number_conc_" + name]), name
+    for n in range(4):
+        m = oracle_py.compute_moment_R_grid(n, g["R_p"], g["xi"], g["V0"], g["cells"],
+                                            g["active_ids"], no_cells)
+        assert np.array_equal(m, g[f"moment_{n}"]), n
+        # Numba's integer power (repeated squaring) agrees to rounding
+        m_nb = oracle_nb.compute_moment_R_grid(n, g["R_p"], g["xi"], g["V0"], g["cells"],
+                                               g["active_ids"], no_cells)
+        np.testing.assert_allclose(m_nb, g[f"moment_{n}"], rtol=1e-14, atol=0)
