@@ -318,6 +318,15 @@ int lacmo_collision_pair_count(const void* ws, int64_t n, int64_t nx, int64_t nz
 int lacmo_collision_step_golovin(double* xis, double* masses, int64_t n, double dt_over_dV,
                                  int64_t* no_cols, const double* rnd, uint64_t seed,
                                  uint64_t step, void* stream);
+/* Box model, kernel K(m1, m2) tabulated on a logarithmic mass grid
+ * (kernel_grid[nb][nb]; bin int((log m - m_low_log) / bin_factor_m_log + 0.5)
+ * clamped): replaces collision/all_or_nothing.py:392
+ * collision_step_kernel_grid_m_np.  n <= LACMO_BOX_MAX_SIPS. */
+int lacmo_collision_step_kernel_grid_m(double* xis, double* masses, int64_t n, double dt_over_dV,
+                                       const double* kernel_grid, int64_t no_kernel_bins,
+                                       double m_kernel_low_log, double bin_factor_m_log,
+                                       int64_t* no_cols, const double* rnd, uint64_t seed,
+                                       uint64_t step, void* stream);
 /* Box model, E_col(R1, R2) table and 1-D velocities: replaces
  * collision/all_or_nothing.py:269 collision_step_Ecol_grid_R_np. */
 int lacmo_collision_step_ecol_grid_r_box(double* xis, double* masses, double* radii,

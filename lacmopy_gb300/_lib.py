@@ -110,6 +110,8 @@ PROTOTYPES = {
     "lacmo_collision_step_cells_noalloc": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, i64, i64, i64,
                                                           P(Params), P(Draws), u64, vp, vp]),
     "lacmo_collision_step_golovin": (ctypes.c_int, [vp, vp, i64, dbl, vp, vp, u64, u64, vp]),
+    "lacmo_collision_step_kernel_grid_m": (ctypes.c_int, [vp, vp, i64, dbl, vp, i64, dbl, dbl, vp,
+                                                          vp, u64, u64, vp]),
     "lacmo_collision_step_ecol_grid_r_box": (ctypes.c_int, [vp, vp, vp, vp, vp, i64, dbl, vp, i64,
                                                             dbl, dbl, vp, vp, u64, u64, vp]),
     "lacmo_update_velocity_beard": (ctypes.c_int, [vp, vp, i64, vp]),

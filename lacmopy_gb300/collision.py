@@ -47,6 +47,24 @@ def collision_step_Golovin_np(xis, masses, dt_over_dV, no_cols, *, draws="numpy"
         _writeback(dst, t)
 
 
+def collision_step_kernel_grid_m_np(xis, masses, dt_over_dV, kernel_grid, no_kernel_bins,
+                                    m_kernel_low_log, bin_factor_m_log, no_cols, *,
+                                    draws="numpy", seed=0, step=0):
+    """collision/all_or_nothing.py:392-491 (kernel K(m1, m2) on a logarithmic
+    mass grid, box model)."""
+    lib = _lib.load()
+    n = int(np.shape(xis)[0])
+    x, m, nc = to_device(xis), to_device(masses), to_device(no_cols, torch.int64)
+    K = to_device(kernel_grid)
+    r = _box_draws(draws, n)
+    _lib.check(lib.lacmo_collision_step_kernel_grid_m(
+        _ptr(x), _ptr(m), n, float(dt_over_dV), _ptr(K), int(no_kernel_bins),
+        float(m_kernel_low_log), float(bin_factor_m_log), _ptr(nc), _ptr(r), int(seed), int(step),
+        _stream()), "collision_step_kernel_grid_m")
+    for dst, t in ((xis, x), (masses, m), (no_cols, nc)):
+        _writeback(dst, t)
+
+
 def collision_step_Ecol_grid_R_np(xis, masses, radii, vel, mass_densities, dt_over_dV,
                                   E_col_grid, no_kernel_bins, R_kernel_low_log, bin_factor_R_log,
                                   no_cols, *, draws="numpy", seed=0, step=0):

@@ -634,6 +634,19 @@ int lacmo_collision_step_golovin(double* xis, double* masses, int64_t n, double 
   return LACMO_OK;
 }
 
+int lacmo_collision_step_kernel_grid_m(double* xis, double* masses, int64_t n, double dtdv,
+                                       const double* kernel_grid, int64_t nb, double m_low_log,
+                                       double bin_factor_m_log, int64_t* no_cols,
+                                       const double* rnd, uint64_t seed, uint64_t step,
+                                       void* stream) {
+  if (!xis || !masses || !kernel_grid || nb <= 0 || !no_cols || n < 0) return LACMO_ERR_ARG;
+  if (n > LACMO_BOX_MAX_SIPS) return LACMO_ERR_CAPACITY;
+  if (n < 2) return LACMO_OK;
+  LCHK(launch_kgrid_box(xis, masses, n, dtdv, kernel_grid, nb, m_low_log, bin_factor_m_log,
+                        no_cols, rnd, seed, step, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
 int lacmo_collision_step_ecol_grid_r_box(double* xis, double* masses, double* radii,
                                          const double* vel, const double* rho, int64_t n,
                                          double dtdv, const double* E, int64_t nb, double lo,

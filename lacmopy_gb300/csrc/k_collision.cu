@@ -936,6 +936,75 @@ __global__ void __launch_bounds__(BOX_THREADS) k_golovin(double* xis, double* ma
   }
 }
 
+// collision/all_or_nothing.py:392-491 (kernel K(m1, m2) tabulated on a
+// logarithmic mass grid): p_crit = xi_max K[k_i][k_j] dt/dV, the bins of
+// the collected SIP recomputed from its new mass
+__global__ void __launch_bounds__(BOX_THREADS) k_kgrid_box(double* xis, double* masses, int n,
+                                                           double dtdv, const double* K,
+                                                           int64_t nb, double lo, double bl,
+                                                           int64_t* no_cols, const double* rnd,
+                                                           uint64_t seed, uint64_t step) {
+  extern __shared__ double sm[];
+  double* X = sm;
+  double* M = sm + n;
+  int32_t* B = (int32_t*)(sm + 2 * n);
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    X[q] = xis[q]; M[q] = masses[q];
+    B[q] = col_bin(M[q], lo, bl, nb);
+  }
+  __syncthreads();
+  int64_t c0 = 0, c1 = 0;
+  for (int s = 1; s <= 2 * n - 3; ++s) {
+    const int ilo = s - (n - 1) > 0 ? s - (n - 1) : 0;
+    const int ihi = (s - 1) >> 1;
+    for (int i = ilo + threadIdx.x; i <= ihi; i += blockDim.x) {
+      const int j = s - i;
+      int imin, imax;
+      if (X[i] <= X[j]) { imin = i; imax = j; } else { imin = j; imax = i; }
+      const double xi_min = X[imin], xi_max = X[imax];
+      const double m_min = M[imin], m_max = M[imax];
+      const double p_crit = xi_max * K[(int64_t)B[i] * nb + B[j]] * dtdv;
+      if (p_crit > 1.0) {
+        c1 += 1;
+        const double xi_col = p_crit * xi_min;
+        M[imin] = (xi_min * m_min + xi_col * m_max) / xi_min;
+        X[imax] -= xi_col;
+        B[imin] = col_bin(M[imin], lo, bl, nb);
+      } else {
+        const int64_t rk = pair_rank(i, j, n);
+        const double r = rnd ? rnd[rk] : philox_uniform(seed, (uint64_t)rk, step);
+        if (p_crit > r) {
+          c0 += 1;
+          const double xi_rel_dev = (xi_max - xi_min) / xi_max;
+          if (xi_rel_dev < 1.0E-5) {
+            const double xi_ges = xi_min + xi_max;
+            M[imin] = 2.0 * (xi_min * m_min + xi_max * m_max) / xi_ges;
+            M[imax] = M[imin];
+            X[imax] = 0.5 * 0.7 * xi_ges;
+            X[imin] = 0.5 * xi_ges - X[imax];
+            B[imin] = col_bin(M[imin], lo, bl, nb);
+            B[imax] = B[imin];
+          } else {
+            M[imin] += m_max;
+            X[imax] -= xi_min;
+            B[imin] = col_bin(M[imin], lo, bl, nb);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < n; q += blockDim.x) { xis[q] = X[q]; masses[q] = M[q]; }
+  for (int off = 16; off > 0; off >>= 1) {
+    c0 += __shfl_down_sync(0xffffffffu, c0, off);
+    c1 += __shfl_down_sync(0xffffffffu, c1, off);
+  }
+  if ((threadIdx.x & 31) == 0 && (c0 | c1)) {
+    atomicAdd((unsigned long long*)no_cols, (unsigned long long)c0);
+    atomicAdd((unsigned long long*)(no_cols + 1), (unsigned long long)c1);
+  }
+}
+
 // collision/all_or_nothing.py:269-390 (E_col(R1, R2) table, 1-D velocities)
 __global__ void __launch_bounds__(BOX_THREADS) k_ecol_box(double* xis, double* masses,
                                                           double* radii, const double* vel,
@@ -1195,6 +1264,17 @@ cudaError_t launch_ecol_box(double* xis, double* m, double* R, const double* vel
   if (e != cudaSuccess) return e;
   k_ecol_box<<<1, BOX_THREADS, sh, s>>>(xis, m, R, vel, rho, (int)n, dtdv, E, nb, lo, bl, no_cols,
                                         rnd, seed, step); note_launches(1);
+  return cudaGetLastError();
+}
+cudaError_t launch_kgrid_box(double* xis, double* m, int64_t n, double dtdv, const double* K,
+                             int64_t nb, double lo, double bl, int64_t* no_cols, const double* rnd,
+                             uint64_t seed, uint64_t step, cudaStream_t s) {
+  size_t sh = (size_t)n * 20;
+  cudaError_t e = cudaFuncSetAttribute(k_kgrid_box, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(LACMO_BOX_MAX_SIPS * 20));
+  if (e != cudaSuccess) return e;
+  k_kgrid_box<<<1, BOX_THREADS, sh, s>>>(xis, m, (int)n, dtdv, K, nb, lo, bl, no_cols, rnd, seed,
+                                         step); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_beard(double* vel, const double* R, int64_t n, cudaStream_t s) {

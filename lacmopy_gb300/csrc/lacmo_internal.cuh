@@ -168,6 +168,9 @@ cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lac
                                  cudaStream_t s);
 cudaError_t launch_golovin(double* xis, double* m, int64_t n, double dtdv, int64_t* no_cols,
                            const double* rnd, uint64_t seed, uint64_t step, cudaStream_t s);
+cudaError_t launch_kgrid_box(double* xis, double* m, int64_t n, double dtdv, const double* K,
+                             int64_t nb, double lo, double bl, int64_t* no_cols, const double* rnd,
+                             uint64_t seed, uint64_t step, cudaStream_t s);
 cudaError_t launch_ecol_box(double* xis, double* m, double* R, const double* vel,
                             const double* rho, int64_t n, double dtdv, const double* E, int64_t nb,
                             double lo, double bl, int64_t* no_cols, const double* rnd,

@@ -446,6 +446,51 @@ ORC_EXPORT void orc_radius_from_mass_col(const double* m, const double* rho, int
 }
 
 /* collision/all_or_nothing.py:109-185: Golovin box step, all pairs i < j */
+/* collision/all_or_nothing.py:392-491: box model with the kernel K(m1, m2)
+   tabulated on a logarithmic mass grid; draws rnd[n(n-1)/2] in pair order */
+ORC_EXPORT void orc_collision_step_kernel_grid_m(double* xis, double* masses, int64_t n,
+                                                 double dt_over_dV, const double* K, int64_t nb,
+                                                 double lo, double bl, int64_t* no_cols,
+                                                 const double* rnd) {
+  int64_t* ind = (int64_t*)malloc(sizeof(int64_t) * (n > 0 ? n : 1));
+  for (int64_t q = 0; q < n; ++q) ind[q] = kernel_index(masses[q], lo, bl, nb);
+  int64_t cnt = 0;
+  for (int64_t i = 0; i < n - 1; ++i) {
+    for (int64_t j = i + 1; j < n; ++j) {
+      int64_t imin, imax;
+      if (xis[i] <= xis[j]) { imin = i; imax = j; } else { imin = j; imax = i; }
+      const double xi_min = xis[imin], xi_max = xis[imax];
+      const double m_min = masses[imin], m_max = masses[imax];
+      const double p_crit = xi_max * K[ind[i] * nb + ind[j]] * dt_over_dV;
+      if (p_crit > 1.0) {
+        const double xi_col = p_crit * xi_min;
+        masses[imin] = (xi_min * m_min + xi_col * m_max) / xi_min;
+        xis[imax] -= xi_col;
+        ind[imin] = kernel_index(masses[imin], lo, bl, nb);
+        no_cols[1] += 1;
+      } else if (p_crit > rnd[cnt]) {
+        no_cols[0] += 1;
+        const double xi_rel_dev = (xi_max - xi_min) / xi_max;
+        if (xi_rel_dev < 1.0E-5) {
+          const double xi_ges = xi_min + xi_max;
+          masses[imin] = 2.0 * (xi_min * m_min + xi_max * m_max) / xi_ges;
+          masses[imax] = masses[imin];
+          xis[imax] = 0.5 * 0.7 * xi_ges;
+          xis[imin] = 0.5 * xi_ges - xis[imax];
+          ind[imin] = kernel_index(masses[imin], lo, bl, nb);
+          ind[imax] = ind[imin];
+        } else {
+          masses[imin] += m_max;
+          xis[imax] -= xi_min;
+          ind[imin] = kernel_index(masses[imin], lo, bl, nb);
+        }
+      }
+      ++cnt;
+    }
+  }
+  free(ind);
+}
+
 ORC_EXPORT void orc_collision_step_Golovin(double* xis, double* masses, int64_t n,
                                            double dt_over_dV, int64_t* no_cols, const double* rnd) {
   int64_t cnt = 0;

@@ -59,6 +59,7 @@ def _lib(variant):
     lib.orc_kernel_index.argtypes = [D, i64, dbl, dbl, i64, I64]
     lib.orc_radius_from_mass_col.argtypes = [D, D, i64, D]
     lib.orc_collision_step_Golovin.argtypes = [D, D, i64, dbl, I64, D]
+    lib.orc_collision_step_kernel_grid_m.argtypes = [D, D, i64, dbl, D, i64, dbl, dbl, I64, D]
     lib.orc_collision_step_Ecol_grid_R.argtypes = [D, D, D, D, D, i64, dbl, D, i64, dbl, dbl, I64, D]
     lib.orc_collision_step_all_cells_2d.argtypes = [
         D, D, D, D, D, I64, i64, i64, i64, dbl, ctypes.c_void_p, dbl, i64, dbl, dbl, I64, cint,
@@ -183,6 +184,16 @@ class Oracle:
         assert len(draws) >= need
         self.lib.orc_collision_step_Golovin(_c(xis), _c(masses), n, float(dt_over_dV),
                                             _c(no_cols, np.int64), _c(draws))
+
+    def collision_step_kernel_grid_m_np(self, xis, masses, dt_over_dV, kernel_grid,
+                                        no_kernel_bins, m_kernel_low_log, bin_factor_m_log,
+                                        no_cols, draws):
+        n = len(xis)
+        assert len(draws) >= n * (n - 1) // 2
+        self.lib.orc_collision_step_kernel_grid_m(
+            _c(xis), _c(masses), n, float(dt_over_dV),
+            np.ascontiguousarray(kernel_grid, dtype=np.float64), int(no_kernel_bins),
+            float(m_kernel_low_log), float(bin_factor_m_log), _c(no_cols, np.int64), _c(draws))
 
     def update_velocity_Beard(self, vel, R):
         self.lib.orc_update_velocity_Beard(_c(vel), _c(R), len(vel))

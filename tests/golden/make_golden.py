@@ -393,6 +393,32 @@ def gen_diagnostics(R):
     save("diagnostics.npz", **out)
 
 
+def gen_kernel_grid_m(R):
+    """collision/all_or_nothing.py:392-491 on 200 SIPs with a tabulated
+    kernel on a logarithmic mass grid, three steps (multiple collections in
+    the last)."""
+    rng = np.random.default_rng(23)
+    n, nb = 200, 60
+    m_low_log, bf_log = np.log(1e-3), np.log(10.0) / 6.0
+    m_bins = np.exp(m_low_log + bf_log * np.arange(nb))
+    Kg = 1.5E-18 * (m_bins[:, None] + m_bins[None, :]) * rng.uniform(0.5, 1.5, (nb, nb))
+    xis0 = np.exp(rng.uniform(np.log(1e6), np.log(1e9), n))
+    xis0[::37] = xis0[1::37][: len(xis0[::37])]   # some equal multiplicities
+    m0 = np.exp(rng.uniform(np.log(1e-2), np.log(1e5), n))
+    out = {"xis0": xis0, "m0": m0, "K": Kg, "nb": np.int64(nb), "m_low_log": m_low_log,
+           "bf_log": bf_log}
+    xis, m = xis0.copy(), m0.copy()
+    no_cols = np.zeros(2, dtype=np.int64)
+    for step, dtdv in enumerate((50.0, 500.0, 3000.0)):
+        R.aon.collision_step_kernel_grid_m_np(xis, m, dtdv, Kg, nb, m_low_log, bf_log, no_cols)
+        out[f"draws_{step}"] = take_draws()
+        out[f"dtdv_{step}"] = np.float64(dtdv)
+        out[f"xis_{step}"] = xis.copy()
+        out[f"m_{step}"] = m.copy()
+        out[f"no_cols_{step}"] = no_cols.copy()
+    save("collision_kernel_grid_m.npz", **out)
+
+
 def gen_tables(R):
     out = {}
     for kt in ("Long_Bott", "Hall_Bott"):
@@ -418,6 +444,7 @@ def main(ref_root):
     gen_particle_substep(R)
     gen_adv_step(R)
     gen_diagnostics(R)
+    gen_kernel_grid_m(R)
 
 
 if __name__ == "__main__":

@@ -1,5 +1,6 @@
-"""GPU diagnostics (lacmopy_gb300/evaluation.py, csrc/k_diag.cu) against the
-oracle and the reference's own outputs (tests/golden/diagnostics.npz)."""
+"""GPU diagnostics (lacmopy_gb300/evaluation.py, csrc/k_diag.cu) and the
+kernel-grid-m box step against the oracle and the reference's own outputs
+(tests/golden/diagnostics.npz, collision_kernel_grid_m.npz)."""
 import numpy as np
 import pytest
 
@@ -53,3 +54,19 @@ def test_diagnostics_full_grid_vs_oracle(oracle_nb):
     ref3 = oracle_nb.compute_moment_R_grid(3, R_p, st["xi"], 8000.0, st["cells"],
                                            st["active_ids"], (75, 75))
     assert np.array_equal(m3, ref3)
+
+
+def test_kernel_grid_m_box_vs_golden():
+    """Box model with a tabulated K(m1, m2) (collision/all_or_nothing.py:
+    392-491): the reference's outputs with its own draws, bit for bit."""
+    from lacmopy_gb300 import collision as Cg
+    g = golden("collision_kernel_grid_m.npz")
+    xis, m = g["xis0"].copy(), g["m0"].copy()
+    no_cols = np.zeros(2, dtype=np.int64)
+    for step in range(3):
+        Cg.collision_step_kernel_grid_m_np(xis, m, g[f"dtdv_{step}"], g["K"], g["nb"],
+                                           g["m_low_log"], g["bf_log"], no_cols,
+                                           draws=g[f"draws_{step}"])
+        assert np.array_equal(no_cols, g[f"no_cols_{step}"]), step
+        assert np.array_equal(xis, g[f"xis_{step}"]), step
+        assert np.array_equal(m, g[f"m_{step}"]), step

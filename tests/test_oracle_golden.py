@@ -204,3 +204,18 @@ def test_diagnostics(oracle_py, oracle_nb):
         m_nb = oracle_nb.compute_moment_R_grid(n, g["R_p"], g["xi"], g["V0"], g["cells"],
                                                g["active_ids"], no_cells)
         np.testing.assert_allclose(m_nb, g[f"moment_{n}"], rtol=1e-14, atol=0)
+
+
+def test_kernel_grid_m(oracle_py):
+    """collision/all_or_nothing.py:392-491, three steps with the reference's
+    draws (ordinary, equal-multiplicity and multiple collections)."""
+    g = golden("collision_kernel_grid_m.npz")
+    xis, m = g["xis0"].copy(), g["m0"].copy()
+    no_cols = np.zeros(2, dtype=np.int64)
+    for step in range(3):
+        oracle_py.collision_step_kernel_grid_m_np(xis, m, g[f"dtdv_{step}"], g["K"], g["nb"],
+                                                  g["m_low_log"], g["bf_log"], no_cols,
+                                                  g[f"draws_{step}"])
+        assert np.array_equal(no_cols, g[f"no_cols_{step}"]), step
+        assert np.array_equal(xis, g[f"xis_{step}"]), step
+        assert np.array_equal(m, g[f"m_{step}"]), step
