@@ -379,12 +379,6 @@ __device__ __forceinline__ void init_exact_scratch(const CellArgs& a, const Cell
   __syncwarp();
 }
 
-// (i, j) moved forward by `adv` ranks in lexicographic order
-__device__ __forceinline__ void advance_pair(int n, int& i, int& j, int adv) {
-  j += adv;
-  while (j > n - 1 && i < n - 2) { j += i + 2 - n; ++i; }
-}
-
 // one pair with draw r: the screen on the FP32 copies, else the exact
 // evaluation; returns 0 (no change) or the outcome counters it adds
 __device__ __forceinline__ void decide_pair(const CellArgs& a, const CellSmem& S, bool use_E,

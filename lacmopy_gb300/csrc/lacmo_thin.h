@@ -140,8 +140,5 @@ LT_FN uint64_t lt_bits53(uint64_t key, uint64_t chunk, uint32_t sub, uint32_t j,
 #endif
   return (uint64_t)(x0 >> 5) * 67108864ull + (uint64_t)(x1 >> 6);
 }
-LT_FN double lt_uniform(uint64_t key, uint64_t chunk, uint32_t sub, uint32_t j, uint64_t c1) {
-  return (double)lt_bits53(key, chunk, sub, j, c1) * (1.0 / 9007199254740992.0);
-}
 
 #endif
