@@ -35,7 +35,7 @@
 #include "lacmo_thin_tables.h"
 
 /* segments bounded at or above this take per-pair draws */
-#define LACMO_THIN_TAU 0x1p-8f
+#define LACMO_THIN_TAU 0x1p-6f
 
 #ifdef __CUDACC__
 #define LT_FN __host__ __device__ __forceinline__
