@@ -50,3 +50,13 @@ def test_integer_thresholds_take_the_same_decisions():
     for x in flat:
         t = threshold53(x)
         assert Fraction(t - 1, 2 ** 53) < Fraction(x) <= Fraction(t, 2 ** 53)
+
+
+def test_rate_tables_are_probabilities():
+    """H[e][m] = 1 - (1 - q)^m grows with m and falls with e; P[e][r] =
+    q / H[e][r] is a probability, 1 for the last pair."""
+    from lacmopy_gb300.csrc_gen import thin_tables
+    H, P = thin_tables()
+    H, P = np.array(H), np.array(P)
+    assert np.all(np.diff(H, axis=1) > 0) and np.all(np.diff(H, axis=0) < 0)
+    assert np.all((P > 0) & (P <= 1)) and np.all(P[:, 0] == 1.0)
