@@ -41,6 +41,8 @@ extern "C" {
 #define LACMO_FLAG_CELL_CLAMPED 0x2u    /* x == x_max after the periodic wrap */
 #define LACMO_FLAG_NONFINITE 0x4u       /* NaN/inf met in a SIP mass         */
 #define LACMO_FLAG_CELL_TOO_BIG 0x8u    /* a cell above 65535 SIPs was not collided */
+#define LACMO_FLAG_CELL_RANGE 0x10u     /* a SIP's cell index >= nx*nz: left out of
+                                           the binning (not collided)           */
 
 #define LACMO_SOLUTE_AS 0
 #define LACMO_SOLUTE_NACL 1
@@ -129,6 +131,17 @@ int lacmo_workspace_reset(void* ws, size_t ws_bytes, int64_t n, int64_t nx, int6
  * (near-critical SIPs) since the workspace was reset (synchronises). */
 int lacmo_read_fallbacks(const void* ws, int64_t n, int64_t nx, int64_t nz, uint64_t* count,
                          void* stream);
+/* The Philox collision-step counter of a workspace: the counter word of the
+ * draws (collision step, cell) that the next collision step uses.  Each
+ * collision step advances it by one.  lacmo_workspace_reset sets it to 0; a
+ * caller that rebuilds a workspace for every call (like a drop-in step
+ * function called once per time step) carries it from one call to the next,
+ * so that each call draws fresh uniforms as the reference's np.random.rand
+ * does (collision/all_or_nothing.py:545).  _get synchronises the stream. */
+int lacmo_get_collision_step(const void* ws, int64_t n, int64_t nx, int64_t nz, int64_t* step,
+                             void* stream);
+int lacmo_set_collision_step(void* ws, int64_t n, int64_t nx, int64_t nz, int64_t step,
+                             void* stream);
 /* Copy the device-side flags to *flags (synchronises the stream). */
 int lacmo_read_flags(const void* ws, int64_t n, int64_t nx, int64_t nz, uint32_t* flags,
                      void* stream);
@@ -295,10 +308,17 @@ int lacmo_collision_step_cells(const lacmo_sips_t* sips, const lacmo_grid_t* gri
  * n <= LACMO_NOALLOC_MAX_SIPS and nx*nz <= LACMO_NOALLOC_MAX_CELLS, else
  * LACMO_ERR_CAPACITY.  Injected draws are read from the start of the buffer;
  * Philox draws use `step` as the collision-step counter.  The first call on a
- * device looks up the array's device address (once per device, with that
- * device current), so make that first call before any stream capture.  All
- * calls share the one array and each call clears what must start at zero:
- * calls whose work overlaps on the GPU race and must be serialised. */
+ * device loads the library's module there when it looks up the array's
+ * device address (every call looks it up, with the caller's device current),
+ * so make that first call before any stream capture.  All calls share the one
+ * array and each call clears what must start at zero: calls whose work
+ * overlaps on the GPU race and must be serialised.  SIPs whose cell index is
+ * >= nx*nz are left out of the step (LACMO_FLAG_CELL_RANGE).  The step's
+ * condition flags and pair count stay in the array until the next call:
+ * read them with lacmo_noalloc_status.  A step whose injected buffer holds
+ * fewer draws than the step's pair count is skipped as a whole (the state is
+ * unchanged, LACMO_FLAG_DRAWS_SHORT), and the pair count it reports sizes the
+ * buffer for the repeated call. */
 #define LACMO_NOALLOC_MAX_SIPS 524288
 #define LACMO_NOALLOC_MAX_CELLS 16384
 int lacmo_collision_step_cells_noalloc(double* xi, double* m_w, double* m_s, const double* vel,
@@ -306,6 +326,11 @@ int lacmo_collision_step_cells_noalloc(double* xi, double* m_w, double* m_s, con
                                        int64_t nx, int64_t nz, const lacmo_params_t* prm,
                                        const lacmo_draws_t* draws, uint64_t step,
                                        int64_t* no_cols, void* stream);
+/* Condition flags (LACMO_FLAG_*) and pair count of the last
+ * lacmo_collision_step_cells_noalloc call on the current device, read from
+ * the library's fixed array into host memory (synchronises the stream; either
+ * pointer may be null).  This reader has no counterpart in the reference. */
+int lacmo_noalloc_status(uint32_t* flags, int64_t* pairs, void* stream);
 /* Number of pair draws the next all-cells collision step consumes
  * (synchronises the stream; used to size an injected draw buffer). */
 int lacmo_collision_pair_count(const void* ws, int64_t n, int64_t nx, int64_t nz,

@@ -16,6 +16,9 @@ FLAG_DRAWS_SHORT = 0x1
 FLAG_CELL_CLAMPED = 0x2
 FLAG_NONFINITE = 0x4
 FLAG_CELL_TOO_BIG = 0x8
+FLAG_CELL_RANGE = 0x10
+NOALLOC_MAX_SIPS = 524288
+NOALLOC_MAX_CELLS = 16384
 BOX_MAX_SIPS = 8192
 ECOL_BOX_MAX_SIPS = 4096
 
@@ -68,6 +71,8 @@ PROTOTYPES = {
     "lacmo_workspace_bytes": (sz, [i64, i64, i64]),
     "lacmo_workspace_reset": (ctypes.c_int, [vp, sz, i64, i64, i64, vp]),
     "lacmo_read_flags": (ctypes.c_int, [vp, i64, i64, i64, P(ctypes.c_uint32), vp]),
+    "lacmo_get_collision_step": (ctypes.c_int, [vp, i64, i64, i64, P(i64), vp]),
+    "lacmo_set_collision_step": (ctypes.c_int, [vp, i64, i64, i64, i64, vp]),
     "lacmo_read_fallbacks": (ctypes.c_int, [vp, i64, i64, i64, P(ctypes.c_uint64), vp]),
     "lacmo_cells_import": (ctypes.c_int, [vp, vp, vp, i64, i64, i64, vp]),
     "lacmo_cells_export": (ctypes.c_int, [vp, vp, vp, vp, vp, i64, i64, i64, dbl, dbl, dbl, dbl,
@@ -109,6 +114,7 @@ PROTOTYPES = {
     "lacmo_collision_pair_count": (ctypes.c_int, [vp, i64, i64, i64, P(i64), vp]),
     "lacmo_collision_step_cells_noalloc": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, i64, i64, i64,
                                                           P(Params), P(Draws), u64, vp, vp]),
+    "lacmo_noalloc_status": (ctypes.c_int, [P(ctypes.c_uint32), P(i64), vp]),
     "lacmo_collision_step_golovin": (ctypes.c_int, [vp, vp, i64, dbl, vp, vp, u64, u64, vp]),
     "lacmo_collision_step_kernel_grid_m": (ctypes.c_int, [vp, vp, i64, dbl, vp, i64, dbl, dbl, vp,
                                                           vp, u64, u64, vp]),

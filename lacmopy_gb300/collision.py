@@ -95,8 +95,12 @@ def update_velocity_Beard(vel, R):
 def collision_step_Ecol_grid_R_all_cells_2D_multicomp_np(
         xis, m_w, m_s, vel, grid_temperature, cells, no_cells, dt_over_dV, E_col_grid,
         no_kernel_bins, R_kernel_low_log, bin_factor_R_log, no_cols, solute_type, *,
-        draws="numpy", seed=0):
-    """collision/all_or_nothing.py:754-846: one AON step in every grid cell."""
+        draws="numpy", seed=0, col_step=None):
+    """collision/all_or_nothing.py:754-846: one AON step in every grid cell.
+
+    With ``draws="philox"`` or ``"thinned"`` consecutive calls with the same
+    ``seed`` continue one stream of draws (lacmopy_gb300.integration);
+    ``col_step`` pins the collision-step counter."""
     Nx, Nz = int(no_cells[0]), int(no_cells[1])
     n = int(np.shape(xis)[0])
     cells_np = np.asarray(cells)
@@ -110,7 +114,12 @@ def collision_step_Ecol_grid_R_all_cells_2D_multicomp_np(
               solute_type=solute_type, no_cols=no_cols)
     mode = draws if isinstance(draws, str) else "philox"
     ds = DeviceState(st, draws=mode, seed=seed)
+    philox = isinstance(draws, str) and draws in ("philox", "thinned")
+    if philox:
+        ds.continue_philox(col_step)
     ds.collision_step(None if isinstance(draws, str) else draws)
+    if philox:
+        ds.record_philox()
     torch.cuda.current_stream().synchronize()
     for dst, t in ((xis, ds.xi), (m_w, ds.m_w), (m_s, ds.m_s), (no_cols, ds.no_cols)):
         _writeback(dst, t)
@@ -143,21 +152,32 @@ def simulate_collisions(SIP_quantities, kernel_quantities, kernel_name, kernel_m
     lib = _lib.load()
     if draws == "numpy":
         np.random.seed(seed)
-    if kernel_name == "Golovin":
+    # box_model.py:135-145 picks the step by kernel_name first, then loops by
+    # kernel_method (:160-194); the Golovin kernel runs with any method but the
+    # two tabulated ones
+    if kernel_name == "Golovin" and kernel_method not in ("Ecol_grid_R", "kernel_grid_m"):
+        method = "golovin"
         xis, masses = SIP_quantities
     elif kernel_method == "Ecol_grid_R":
+        method = "ecol"
         xis, masses, radii, vel, mass_densities = SIP_quantities
         E_col_grid, no_kernel_bins, R_kernel_low_log, bin_factor_R_log = kernel_quantities
+    elif kernel_method == "kernel_grid_m":
+        method = "kgrid"
+        xis, masses = SIP_quantities
+        kernel_grid, no_kernel_bins, m_kernel_low_log, bin_factor_m_log = kernel_quantities
     else:
-        raise NotImplementedError(f"kernel_method {kernel_method!r}")
+        raise ValueError(f"kernel_name {kernel_name!r} with kernel_method {kernel_method!r}")
     n = int(np.shape(xis)[0])
     no_steps = int(math.ceil(t_end / dt))
     no_saves = int(t_end / dt_save - 0.001) + 2
     dn_save = int(math.ceil(dt_save / dt))
     dt_over_dV = dt / dV
     x, m, nc = to_device(xis), to_device(masses), to_device(no_cols, torch.int64)
-    if kernel_name != "Golovin":
+    if method == "ecol":
         R, v, rho, E = (to_device(a) for a in (radii, vel, mass_densities, E_col_grid))
+    elif method == "kgrid":
+        K = to_device(kernel_grid)
     xis_vs_time = np.zeros((no_saves, n))
     masses_vs_time = np.zeros((no_saves, n))
     save_times = np.zeros(no_saves)
@@ -170,9 +190,15 @@ def simulate_collisions(SIP_quantities, kernel_quantities, kernel_name, kernel_m
             save_times[save_n] = step_n * dt
             save_n += 1
         r = _box_draws(draws, n)
-        if kernel_name == "Golovin":
+        if method == "golovin":
             _lib.check(lib.lacmo_collision_step_golovin(_ptr(x), _ptr(m), n, dt_over_dV, _ptr(nc),
                                                         _ptr(r), int(seed), step_n, s), "golovin")
+        elif method == "kgrid":
+            # no velocity update: the kernel table holds the whole K(m1, m2)
+            _lib.check(lib.lacmo_collision_step_kernel_grid_m(
+                _ptr(x), _ptr(m), n, dt_over_dV, _ptr(K), int(no_kernel_bins),
+                float(m_kernel_low_log), float(bin_factor_m_log), _ptr(nc), _ptr(r), int(seed),
+                step_n, s), "kernel_grid_m")
         else:
             _lib.check(lib.lacmo_collision_step_ecol_grid_r_box(
                 _ptr(x), _ptr(m), _ptr(R), _ptr(v), _ptr(rho), n, dt_over_dV, _ptr(E),
@@ -185,7 +211,7 @@ def simulate_collisions(SIP_quantities, kernel_quantities, kernel_name, kernel_m
     _writeback(xis, x)
     _writeback(masses, m)
     _writeback(no_cols, nc)
-    if kernel_name != "Golovin":
+    if method == "ecol":
         _writeback(radii, R)
         _writeback(vel, v)
     if save_dir is not None:

@@ -293,6 +293,23 @@ int lacmo_read_fallbacks(const void* ws, int64_t n, int64_t nx, int64_t nz, uint
   return LACMO_OK;
 }
 
+int lacmo_get_collision_step(const void* ws, int64_t n, int64_t nx, int64_t nz, int64_t* step,
+                             void* stream) {
+  Ws w;
+  if (!step || !ws_carve((void*)ws, ws_bytes(n, nx, nz), n, nx, nz, &w)) return LACMO_ERR_ARG;
+  LCHK(cudaMemcpyAsync(step, w.col_step, 8, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  LCHK(cudaStreamSynchronize((cudaStream_t)stream));
+  return LACMO_OK;
+}
+
+int lacmo_set_collision_step(void* ws, int64_t n, int64_t nx, int64_t nz, int64_t step,
+                             void* stream) {
+  Ws w;
+  if (step < 0 || !ws_carve(ws, ws_bytes(n, nx, nz), n, nx, nz, &w)) return LACMO_ERR_ARG;
+  LCHK(launch_set_i64(w.col_step, step, (cudaStream_t)stream));
+  return LACMO_OK;
+}
+
 int lacmo_read_flags(const void* ws, int64_t n, int64_t nx, int64_t nz, uint32_t* flags,
                      void* stream) {
   Ws w;

@@ -88,10 +88,13 @@ __global__ void k_histogram(const __grid_constant__ MRef mr) {
   const int32_t* __restrict__ cell = mb.sp.cell;
   const int64_t n = mb.sp.n;
   int32_t *counts = mb.w.counts, *rank = mb.w.rank;
+  const int64_t C = mb.g.nx * mb.g.nz;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x) {
     int32_t c = cell[k];
-    if (c >= 0) rank[k] = atomicAdd(counts + c, 1);
+    if (c < 0) continue;
+    if (c < C) rank[k] = atomicAdd(counts + c, 1);
+    else atomicOr(mb.w.flags, LACMO_FLAG_CELL_RANGE);   // left out of the binning
   }
 }
 
@@ -216,11 +219,11 @@ __global__ void k_scatter(const __grid_constant__ MRef mr) {
   const int32_t* __restrict__ rank = mb.w.rank;
   const int32_t* __restrict__ start = mb.w.start;
   int32_t* perm = mb.w.perm;
-  const int64_t n = mb.sp.n;
+  const int64_t n = mb.sp.n, C = mb.g.nx * mb.g.nz;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x) {
     int32_t c = cell[k];
-    if (c >= 0) perm[start[c] + rank[k]] = (int32_t)k;
+    if (c >= 0 && c < C) perm[start[c] + rank[k]] = (int32_t)k;
   }
 }
 
@@ -272,8 +275,22 @@ __device__ __forceinline__ void sort_cell_ids(int32_t* perm, int32_t b, int L, i
   }
 }
 
-// one warp per cell: order the cell's slots by ascending SIP ID (a bitonic
-// sort in registers up to 256 slots, else ranks by counting)
+// Number of keys of the sorted run a[0..len) that are below x (IDs are
+// unique, so keys of the other run never tie with x).
+__device__ __forceinline__ int32_t count_below(const int32_t* a, int32_t len, int32_t x) {
+  int32_t lo = 0, hi = len;
+  while (lo < hi) {
+    const int32_t mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// one warp per cell: order the cell's slots by ascending SIP ID.  Up to 256
+// slots: a bitonic sort in registers.  Larger cells: runs of 256 sorted in
+// registers, then merged pairwise, each key placed at its rank in the merged
+// run (its index in its own run plus a binary search in the other), ping-pong
+// between perm and the rank array (free after the scatter); O(L log L).
 constexpr int ORDER_SMEM = 256;
 __global__ void __launch_bounds__(256) k_order(const __grid_constant__ MRef mr) {
   const Member& mb = mr.get();
@@ -289,17 +306,30 @@ __global__ void __launch_bounds__(256) k_order(const __grid_constant__ MRef mr) 
       else if (L <= 128) sort_cell_ids<4>(perm, b, L, lane);
       else sort_cell_ids<8>(perm, b, L, lane);
       __syncwarp();
-    } else {
-      for (int q = lane; q < L; q += 32) scratch[b + q] = perm[b + q];
-      __syncwarp();
-      for (int q = lane; q < L; q += 32) {
-        int32_t v = scratch[b + q];
-        int32_t r = 0;
-        for (int p = 0; p < L; ++p) r += (scratch[b + p] < v);
-        perm[b + r] = v;
+      continue;
+    }
+    for (int32_t r0 = 0; r0 < L; r0 += ORDER_SMEM) {
+      const int32_t len = L - r0 < ORDER_SMEM ? L - r0 : ORDER_SMEM;
+      sort_cell_ids<8>(perm, b + r0, len, lane);
+    }
+    __syncwarp();
+    int32_t* src = perm + b;
+    int32_t* dst = scratch + b;
+    for (int32_t width = ORDER_SMEM; width < L; width <<= 1) {
+      for (int32_t lo = 0; lo < L; lo += 2 * width) {
+        const int32_t mid = lo + width < L ? lo + width : L;
+        const int32_t hi = lo + 2 * width < L ? lo + 2 * width : L;
+        const int32_t *A = src + lo, *Bv = src + mid;
+        const int32_t la = mid - lo, lb = hi - mid;
+        for (int32_t q = lane; q < la; q += 32) dst[lo + q + count_below(Bv, lb, A[q])] = A[q];
+        for (int32_t q = lane; q < lb; q += 32) dst[lo + q + count_below(A, la, Bv[q])] = Bv[q];
       }
       __syncwarp();
+      int32_t* t = src; src = dst; dst = t;
     }
+    if (src != perm + b)
+      for (int32_t q = lane; q < L; q += 32) perm[b + q] = src[q];
+    __syncwarp();
   }
 }
 
@@ -1244,6 +1274,12 @@ cudaError_t launch_cell_aux(const Bt& B, cudaStream_t s) {
   k_wind_table<<<grid2(B.nx * B.nz, 256, B.M), 256, 0, s>>>(B.ref()); note_launches(1);
   return cudaGetLastError();
 }
+__global__ void k_set_i64(int64_t* p, int64_t v) { *p = v; }
+cudaError_t launch_set_i64(int64_t* p, int64_t v, cudaStream_t s) {
+  k_set_i64<<<1, 1, 0, s>>>(p, v); note_launches(1);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_histogram(const Bt& B, cudaStream_t s) {
   k_histogram<<<grid2(B.n_max, 256, B.M), 256, 0, s>>>(B.ref()); note_launches(1);
   return cudaGetLastError();

@@ -15,8 +15,6 @@
 // must be serialised by the caller.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "lacmo_internal.cuh"
 
 namespace lacmo {
@@ -44,27 +42,15 @@ constexpr size_t STATIC_BYTES = st_off_scalars + 256;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[STATIC_BYTES];
 
-// the device address of the array, looked up once per device with that device
-// current (in host code the symbol name is only a host-side stand-in)
-static std::mutex g_mu;
-static void* g_addr[64];
-static bool g_have[64];
-
+// The device address of the array.  In host code the symbol name is only a
+// host-side stand-in, so the address is looked up with the caller's device
+// current.  The lookup runs on every call (it is not a stream operation):
+// a cached address would go stale after cudaDeviceReset or after the primary
+// context is released and created again, when the module is loaded anew.
+// The first lookup on a device loads the module there, which is why the
+// first call should come before any stream capture.
 static cudaError_t scratch_address(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_have[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_addr[dev] = p;
-    g_have[dev] = true;
-  }
-  *out = g_addr[dev];
-  return cudaSuccess;
+  return cudaGetSymbolAddress(out, g_noalloc_scratch);
 }
 
 // zero the cell counters and the scalars; set the collision-step counter
@@ -94,7 +80,10 @@ extern "C" int lacmo_collision_step_cells_noalloc(double* xi, double* m_w, doubl
     return LACMO_ERR_ARG;
   if (prm->solute != 0 && prm->solute != 1) return LACMO_ERR_ARG;
   if (prm->E_col_grid && prm->no_kernel_bins <= 0) return LACMO_ERR_ARG;
-  if (n > STATIC_MAX_SIPS || nx * nz > STATIC_MAX_CELLS) return LACMO_ERR_CAPACITY;
+  // nx and nz are bounded before they are multiplied (no int64 overflow)
+  if (n > STATIC_MAX_SIPS || nx > STATIC_MAX_CELLS || nz > STATIC_MAX_CELLS ||
+      nx * nz > STATIC_MAX_CELLS)
+    return LACMO_ERR_CAPACITY;
   void* base = nullptr;
   if (scratch_address(&base) != cudaSuccess) return LACMO_ERR_CUDA;
   char* b = (char*)base;
@@ -136,5 +125,22 @@ extern "C" int lacmo_collision_step_cells_noalloc(double* xi, double* m_w, doubl
   if (launch_histogram(B, s) != cudaSuccess) return LACMO_ERR_CUDA;
   if (launch_bin(B, s) != cudaSuccess) return LACMO_ERR_CUDA;
   if (launch_collide_cells(B, *prm, *draws, s) != cudaSuccess) return LACMO_ERR_CUDA;
+  return LACMO_OK;
+}
+
+extern "C" int lacmo_noalloc_status(uint32_t* flags, int64_t* pairs, void* stream) {
+  if (!flags && !pairs) return LACMO_ERR_ARG;
+  void* base = nullptr;
+  if (scratch_address(&base) != cudaSuccess) return LACMO_ERR_CUDA;
+  const char* sc = (const char*)base + st_off_scalars;
+  cudaStream_t s = (cudaStream_t)stream;
+  uint32_t f = 0;
+  int64_t p = 0;
+  if (cudaMemcpyAsync(&f, sc, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemcpyAsync(&p, sc + 24, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return LACMO_ERR_CUDA;
+  if (flags) *flags = f;
+  if (pairs) *pairs = p;
   return LACMO_OK;
 }

@@ -132,6 +132,8 @@ cudaError_t launch_cells_export(const int32_t* cell, const double* pos, double* 
                                 int64_t* cells, uint8_t* act, int64_t n, int64_t nx, int64_t nz,
                                 double x_min, double z_min, double dx, double dz, cudaStream_t s);
 cudaError_t launch_cell_aux(const Bt& B, cudaStream_t s);
+// *p = v, stream-ordered (one thread)
+cudaError_t launch_set_i64(int64_t* p, int64_t v, cudaStream_t s);
 cudaError_t launch_histogram(const Bt& B, cudaStream_t s);
 cudaError_t launch_bin(const Bt& B, cudaStream_t s);
 cudaError_t launch_particles(const Bt& B, const lacmo_params_t& p, double dt_sub,

@@ -28,6 +28,28 @@ from .constants import solute_code
 
 F64 = torch.float64
 
+# Philox collision-step counter per seed for the drop-in step functions.  They
+# build a fresh device state on every call; without this the counter would
+# restart at 0 on each call and every call with the same seed would replay the
+# same uniforms, where the reference draws fresh ones each call
+# (np.random.rand, collision/all_or_nothing.py:545).
+_philox_next = {}
+
+
+def philox_counter(seed):
+    """The collision-step counter the next drop-in call with ``seed`` starts
+    from (0 for a seed not used yet in this process)."""
+    return _philox_next.get(int(seed), 0)
+
+
+def reset_philox_counters(seed=None):
+    """Restart the drop-in functions' Philox stream of ``seed`` (of every seed
+    when None) at collision step 0."""
+    if seed is None:
+        _philox_next.clear()
+    else:
+        _philox_next.pop(int(seed), None)
+
 
 def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -290,6 +312,31 @@ class DeviceState:
         _lib.check(self.lib.lacmo_update_grid_r_l(ctypes.byref(self.sips), ctypes.byref(self.grid),
                                                   _ptr(self.ws), self.ws_bytes, _stream()),
                    "update_grid_r_l")
+
+    @property
+    def col_step(self):
+        """Philox collision-step counter: the step the next collision step
+        draws with (synchronises)."""
+        v = ctypes.c_int64(0)
+        _lib.check(self.lib.lacmo_get_collision_step(_ptr(self.ws), self.n, self.nx, self.nz,
+                                                     ctypes.byref(v), _stream()),
+                   "get_collision_step")
+        return int(v.value)
+
+    @col_step.setter
+    def col_step(self, step):
+        _lib.check(self.lib.lacmo_set_collision_step(_ptr(self.ws), self.n, self.nx, self.nz,
+                                                     int(step), _stream()), "set_collision_step")
+
+    def continue_philox(self, col_step=None):
+        """Start this state's Philox draws where the process's previous drop-in
+        call with the same seed stopped (or at ``col_step``)."""
+        self.col_step = philox_counter(self.seed) if col_step is None else int(col_step)
+
+    def record_philox(self):
+        """Remember where this state's Philox draws stopped, for the next
+        drop-in call with the same seed."""
+        _philox_next[self.seed] = self.col_step
 
     def fallbacks(self):
         """Mixed precision: SIP sub-steps whose Newton was repeated in FP64."""

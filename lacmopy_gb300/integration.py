@@ -11,6 +11,12 @@ select the collision draw source (see lacmopy_gb300.device):
     draws="thinned" the same generator, thinned draws (csrc/lacmo_thin.h)
     draws=<array>   injected uniforms
 
+With the Philox modes, consecutive calls with the same ``seed`` continue one
+stream of draws: each call starts at the collision-step counter where the
+previous call with that seed stopped (``lacmopy_gb300.device.philox_counter``),
+so every call draws fresh uniforms as the reference does.  ``col_step=k``
+pins the counter; ``lacmopy_gb300.device.reset_philox_counters`` restarts it.
+
 For repeated stepping keep the state on the device with
 ``lacmopy_gb300.DeviceState`` instead of calling these per step.
 """
@@ -41,10 +47,11 @@ def integrate_adv_step_np(grid_scalar_fields, grid_mat_prop, grid_velocity,
                           act_collisions, act_relaxation, init_profile_r_v, init_profile_Theta,
                           relaxation_time_profile, no_iter_impl_mass, g_set, E_col_grid,
                           no_kernel_bins, R_kernel_low_log, bin_factor_R_log, no_cols, *,
-                          draws="numpy", seed=1001, precision="fp64"):
+                          draws="numpy", seed=1001, precision="fp64", col_step=None):
     """One advection step dt on the GPU (integration.py:1298-1611), in place.
     ``precision="mixed"`` runs the mixed-precision sub-steps
-    (lacmopy_gb300.device)."""
+    (lacmopy_gb300.device); with Philox draws the call continues the seed's
+    stream of draws (module docstring)."""
     st = dict(zip(_STATE_KEYS, (
         grid_scalar_fields, grid_mat_prop, grid_velocity, grid_mass_flux_air_dry, p_ref,
         p_ref_inv, grid_no_cells, grid_ranges, grid_steps, grid_volume_cell, pos, vel, cells,
@@ -54,7 +61,12 @@ def integrate_adv_step_np(grid_scalar_fields, grid_mat_prop, grid_velocity,
         no_iter_impl_mass, g_set, E_col_grid, no_kernel_bins, R_kernel_low_log,
         bin_factor_R_log, no_cols)))
     ds = DeviceState(st, draws=draws, seed=seed, precision=precision)
+    philox = isinstance(draws, str) and draws in ("philox", "thinned")
+    if philox:
+        ds.continue_philox(col_step)
     ds.adv_step(1)
+    if philox:
+        ds.record_philox()
     ds.export_to(st)
 
 

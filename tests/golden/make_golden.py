@@ -7,8 +7,11 @@ ones the reference pulls from NumPy's global MT19937 stream; they are recorded
 by wrapping ``numpy.random.rand`` so kernels and the oracle can consume the
 identical sequence.
 
-Usage (from the repository root, in a container that has the reference):
-    python tests/golden/make_golden.py /root/reference
+Usage (from the repository root, in a container that has the reference; the
+path of the reference's source tree is required):
+    python tests/golden/make_golden.py <reference root> [fixture ...]
+With fixture names (the gen_* functions without the prefix) only those
+fixtures are regenerated.
 
 NumPy's SVML (AVX-512) dispatch is switched off before NumPy is imported so
 array pow/log/exp call scalar glibc libm like Numba-compiled code does.
@@ -431,21 +434,49 @@ def gen_tables(R):
     save("tables.npz", **out)
 
 
-def main(ref_root):
+def gen_box_model_kgrid(R):
+    """collision/box_model.py:44-205 simulate_collisions with
+    kernel_method='kernel_grid_m': 150 SIPs, 6 steps saved every 2 s, the
+    draws from NumPy's generator seeded with the run's seed."""
+    import tempfile
+    import collision.box_model as bm
+    rng = np.random.default_rng(29)
+    n, nb = 150, 60
+    m_low_log, bf_log = np.log(1e-3), np.log(10.0) / 6.0
+    m_bins = np.exp(m_low_log + bf_log * np.arange(nb))
+    Kg = 1.5E-18 * (m_bins[:, None] + m_bins[None, :]) * rng.uniform(0.5, 1.5, (nb, nb))
+    xis0 = np.exp(rng.uniform(np.log(1e6), np.log(1e9), n))
+    m0 = np.exp(rng.uniform(np.log(1e-2), np.log(1e5), n))
+    xis, m = xis0.copy(), m0.copy()
+    no_cols = np.zeros(2, dtype=np.int64)
+    seed, dV, dt, t_end, dt_save = 3711, 1.0E-3, 1.0, 6.0, 2.0
+    with tempfile.TemporaryDirectory() as d:
+        bm.simulate_collisions((xis, m), (Kg, nb, m_low_log, bf_log), "Long_Bott",
+                               "kernel_grid_m", dV, dt, t_end, dt_save, no_cols, seed,
+                               d + "/")
+        xt = np.load(d + f"/xis_vs_time_{seed}.npy")
+        mt = np.load(d + f"/masses_vs_time_{seed}.npy")
+        tt = np.load(d + f"/save_times_{seed}.npy")
+    take_draws()
+    save("box_model_kgrid.npz", xis0=xis0, m0=m0, K=Kg, nb=np.int64(nb), m_low_log=m_low_log,
+         bf_log=bf_log, seed=np.int64(seed), dV=dV, dt=dt, t_end=t_end, dt_save=dt_save,
+         xis_vs_time=xt, masses_vs_time=mt, save_times=tt, no_cols=no_cols, xis=xis, m=m)
+
+
+GENERATORS = [gen_tables, gen_mass_rate, gen_interp, gen_golovin, gen_ecol_box, gen_cells_2d,
+              gen_grid_and_divergence, gen_particle_substep, gen_adv_step, gen_diagnostics,
+              gen_kernel_grid_m, gen_box_model_kgrid]
+
+
+def main(ref_root, only=()):
     R = refstub.import_reference(ref_root)
     np.random.rand = _recording_rand
-    gen_tables(R)
-    gen_mass_rate(R)
-    gen_interp(R)
-    gen_golovin(R)
-    gen_ecol_box(R)
-    gen_cells_2d(R)
-    gen_grid_and_divergence(R)
-    gen_particle_substep(R)
-    gen_adv_step(R)
-    gen_diagnostics(R)
-    gen_kernel_grid_m(R)
+    for g in GENERATORS:
+        if not only or g.__name__[len("gen_"):] in only:
+            g(R)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <reference root> [fixture ...]")
+    main(os.path.abspath(sys.argv[1]), set(sys.argv[2:]))

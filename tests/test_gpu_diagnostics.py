@@ -70,3 +70,25 @@ def test_kernel_grid_m_box_vs_golden():
         assert np.array_equal(no_cols, g[f"no_cols_{step}"]), step
         assert np.array_equal(xis, g[f"xis_{step}"]), step
         assert np.array_equal(m, g[f"m_{step}"]), step
+
+
+def test_simulate_collisions_kernel_grid_m_vs_golden(tmp_path):
+    """The box-model time loop with kernel_method='kernel_grid_m'
+    (collision/box_model.py:44-205): saved snapshots, save times, counters and
+    the final state against the reference's run with the same seed (draws from
+    NumPy's generator seeded like the reference), bit for bit."""
+    from lacmopy_gb300 import collision as Cg
+    g = golden("box_model_kgrid.npz")
+    xis, m = g["xis0"].copy(), g["m0"].copy()
+    no_cols = np.zeros(2, dtype=np.int64)
+    seed = int(g["seed"])
+    xt, mt, tt = Cg.simulate_collisions(
+        (xis, m), (g["K"], int(g["nb"]), float(g["m_low_log"]), float(g["bf_log"])), "Long_Bott",
+        "kernel_grid_m", float(g["dV"]), float(g["dt"]), float(g["t_end"]), float(g["dt_save"]),
+        no_cols, seed, str(tmp_path) + "/")
+    assert np.array_equal(tt, g["save_times"])
+    assert np.array_equal(no_cols, g["no_cols"])
+    assert np.array_equal(xt, g["xis_vs_time"])
+    assert np.array_equal(mt, g["masses_vs_time"])
+    assert np.array_equal(xis, g["xis"]) and np.array_equal(m, g["m"])
+    assert np.array_equal(np.load(tmp_path / f"xis_vs_time_{seed}.npy"), g["xis_vs_time"])

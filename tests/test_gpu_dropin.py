@@ -1,0 +1,90 @@
+"""Drop-in step functions called once per time step with Philox draws.
+
+The reference draws fresh uniforms on every collision step
+(collision/all_or_nothing.py:545, np.random.rand).  The drop-in functions
+build a new device state on every call, so they carry the Philox
+collision-step counter of each seed from one call to the next: two
+consecutive ``integrate_adv_step_np`` calls equal two steps of one resident
+``DeviceState`` bit for bit, and two calls on identical inputs draw
+different uniforms.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from lacmopy_gb300 import build
+    build.build()
+
+
+def _state(seed=41):
+    from lacmopy_gb300 import synthetic
+    st = synthetic.make_icmw_state(Nx=20, Nz=18, no_spcm=(10, 14), seed=seed,
+                                   kernel_type="Hall_Bott", drizzle_fraction=0.3, r_tot=12.5E-3)
+    st["dt_col_over_dV"] = st["dt_col_over_dV"] * 60.0   # collisions in every step
+    return st
+
+
+@pytest.mark.parametrize("draws", ["philox", "thinned"])
+def test_consecutive_dropin_calls_continue_the_draws(draws):
+    from lacmopy_gb300 import DeviceState
+    from lacmopy_gb300 import integration as I
+    from lacmopy_gb300.device import philox_counter, reset_philox_counters
+    seed = 777
+    st = _state()
+    want_ds = DeviceState(copy.deepcopy(st), draws=draws, seed=seed)
+    want_ds.adv_step(2)
+    want = want_ds.snapshot()
+    assert want_ds.col_step == 4      # two collision steps per advection step
+
+    reset_philox_counters(seed)
+    got = copy.deepcopy(st)
+    for _ in range(2):
+        I.integrate_adv_step_np(*[got[k] for k in I._STATE_KEYS], draws=draws, seed=seed)
+    assert philox_counter(seed) == 4
+    assert want["no_cols"].sum() > 0
+    assert np.array_equal(got["no_cols"], want["no_cols"])
+    for k in ("xi", "m_w", "m_s", "pos", "vel"):
+        assert np.array_equal(got[k], want[k]), k
+    assert np.array_equal(got["cells"], want["cells"])
+
+    # a pinned counter reproduces the second call alone
+    again = copy.deepcopy(st)
+    I.integrate_adv_step_np(*[again[k] for k in I._STATE_KEYS], draws=draws, seed=seed,
+                            col_step=0)
+    I.integrate_adv_step_np(*[again[k] for k in I._STATE_KEYS], draws=draws, seed=seed,
+                            col_step=2)
+    for k in ("xi", "m_w", "m_s"):
+        assert np.array_equal(again[k], want[k]), k
+    reset_philox_counters(seed)
+
+
+@pytest.mark.parametrize("draws", ["philox", "thinned"])
+def test_repeated_collision_calls_draw_fresh_uniforms(draws):
+    """The all-cells collision drop-in on the same input twice: the second
+    call uses the next collision step's draws, so its outcome differs."""
+    from lacmopy_gb300 import collision as C
+    from lacmopy_gb300.device import reset_philox_counters
+    st = _state(seed=43)
+    seed = 5
+    reset_philox_counters(seed)
+    outs = []
+    for _ in range(2):
+        xi, mw, ms = st["xi"].copy(), st["m_w"].copy(), st["m_s"].copy()
+        nc = np.zeros(2, np.int64)
+        C.collision_step_Ecol_grid_R_all_cells_2D_multicomp_np(
+            xi, mw, ms, st["vel"], st["grid_scalar_fields"][0], st["cells"], st["grid_no_cells"],
+            st["dt_col_over_dV"], st["E_col_grid"], st["no_kernel_bins"], st["R_kernel_low_log"],
+            st["bin_factor_R_log"], nc, "AS", draws=draws, seed=seed)
+        outs.append((xi, mw, nc))
+    assert outs[0][2].sum() > 0 and outs[1][2].sum() > 0
+    assert not np.array_equal(outs[0][0], outs[1][0])
+    reset_philox_counters(seed)

@@ -219,3 +219,28 @@ def test_kernel_grid_m(oracle_py):
         assert np.array_equal(no_cols, g[f"no_cols_{step}"]), step
         assert np.array_equal(xis, g[f"xis_{step}"]), step
         assert np.array_equal(m, g[f"m_{step}"]), step
+
+
+def test_box_model_kernel_grid_m_loop(oracle_py):
+    """collision/box_model.py:44-205 with kernel_method='kernel_grid_m': the
+    oracle's step in the loop, with NumPy's generator seeded as the reference
+    seeds it, reproduces the reference's saved snapshots."""
+    import math
+    g = golden("box_model_kgrid.npz")
+    xis, m = g["xis0"].copy(), g["m0"].copy()
+    no_cols = np.zeros(2, dtype=np.int64)
+    rs = np.random.RandomState(int(g["seed"]))
+    n = xis.size
+    dt, t_end, dt_save = float(g["dt"]), float(g["t_end"]), float(g["dt_save"])
+    dtdv = dt / float(g["dV"])
+    no_steps, dn = int(math.ceil(t_end / dt)), int(math.ceil(dt_save / dt))
+    snaps = []
+    for step in range(no_steps):
+        if step % dn == 0:
+            snaps.append(xis.copy())
+        oracle_py.collision_step_kernel_grid_m_np(xis, m, dtdv, g["K"], g["nb"], g["m_low_log"],
+                                                  g["bf_log"], no_cols, rs.rand(n * (n - 1) // 2))
+    snaps.append(xis.copy())
+    assert np.array_equal(np.array(snaps), g["xis_vs_time"])
+    assert np.array_equal(no_cols, g["no_cols"])
+    assert np.array_equal(m, g["m"])
