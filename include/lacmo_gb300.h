@@ -43,6 +43,8 @@ extern "C" {
 #define LACMO_FLAG_CELL_TOO_BIG 0x8u    /* a cell above 65535 SIPs was not collided */
 #define LACMO_FLAG_CELL_RANGE 0x10u     /* a SIP's cell index >= nx*nz: left out of
                                            the binning (not collided)           */
+#define LACMO_FLAG_SYNC_TIMEOUT 0x20u   /* a kernel's bounded wait on its own
+                                           copies ran out; its work is incomplete */
 
 #define LACMO_SOLUTE_AS 0
 #define LACMO_SOLUTE_NACL 1

@@ -637,30 +637,36 @@ __global__ void __launch_bounds__(32) k_cell_update(const __grid_constant__ MRef
 // The Newton condensation and the drag update run in FP32 (lacmo_physics.cuh)
 // with the FP64 Newton for SIPs near the critical radius.  Per-cell sums and
 // water_removed are formed in arbitrary order.
-// Rare paths are out of line (__noinline__) so that the common path issues
-// no FP64 instruction, not even predicated off.
-__device__ __noinline__ float d2f_slow(double x) { return (float)x; }
-__device__ __noinline__ double f2d_slow(float f) { return (double)f; }
+// Conversions between FP64 and FP32 with integer operations: GB300 runs
+// FP64 arithmetic and double<->float conversions on a narrow pipe, and the
+// mixed kernel converts about a dozen values per SIP.  Branch-free (no call
+// on any path, so no register spills around one).
+//  d2f_int: for finite x within the FP32 range (positions, velocities,
+//    masses, multiplicities), the FP32 value rounded half away from zero on
+//    the magnitude (within 1 ulp of the correctly rounded value; the FP32
+//    copies only feed approximations with certified margins); below the FP32
+//    normal range a signed zero.  A NaN or huge x gives some finite value:
+//    the FP32 results then only feed increments that are added to the FP64
+//    state, which carries the NaN on.
+//  f2d_int: exact for normal floats and zero; FP32 subnormals give a signed
+//    zero, infinities and NaNs stay what they are.
 __device__ __forceinline__ float d2f_int(double x) {
-  const uint64_t b = (uint64_t)__double_as_longlong(x);
-  const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
-  if (e - 897u > 253u) return d2f_slow(x);   // zero, subnormal, huge, inf, nan
-  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
-  const uint64_t m = b & 0x000fffffffffffffull;
-  const uint32_t fm = (uint32_t)(m >> 29), rem = (uint32_t)m & 0x1fffffffu;
-  uint32_t fb = sign | ((e - 896u) << 23) | fm;
-  fb += (rem > 0x10000000u) || (rem == 0x10000000u && (fm & 1u));
-  return __int_as_float((int)fb);
+  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+  const uint32_t ax = hi & 0x7fffffffu, sign = hi & 0x80000000u;
+  // (ax << 3 | lo >> 29) holds the low 9 exponent bits over 23 mantissa bits
+  const uint32_t f = ((__funnelshift_l(lo, ax, 3) - (384u << 23)) + ((lo >> 28) & 1u)) | sign;
+  return __uint_as_float(ax < (897u << 20) ? sign : f);
 }
 __device__ __forceinline__ double f2d_int(float f) {
-  const uint32_t b = (uint32_t)__float_as_int(f);
-  const uint32_t e = (b >> 23) & 0xffu;
-  if (e - 1u > 253u) return f2d_slow(f);   // zero, subnormal, inf, nan
-  const uint64_t r = ((uint64_t)(b & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
-                     ((uint64_t)(b & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)r);
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t a = b & 0x7fffffffu, sign = b & 0x80000000u;
+  const uint32_t hi = ((a >> 3) + (896u << 20)) | sign | (a >= 0x7f800000u ? 0x7ff00000u : 0u);
+  const bool tiny = a < 0x00800000u;
+  return __hiloint2double((int)(tiny ? sign : hi), (int)(tiny ? 0u : b << 29));
 }
 
+// Rare FP64 paths stay out of line (__noinline__) so that the common path
+// issues no FP64 instruction, not even predicated off.
 // removed SIP: only the relative position keeps its per-call division
 __device__ __noinline__ void mixed_inactive_rel(double* rel, int64_t n, double dx, double dz,
                                                 int64_t k, int i) {
@@ -696,9 +702,17 @@ __device__ __noinline__ double mixed_newton_fp64(NewtonFP64 a, int32_t c, double
   return newton_full(a.sol, a.dt_sub, a.no_iter, mw, ms, w_s, R64, T_p, rho64, sig64, amb,
                      nullptr);
 }
-__device__ __noinline__ double mixed_wrap_x(double x, double x_max) { return py_mod(x, x_max); }
-__device__ __noinline__ double mixed_cap_z(double z, double z_cap) { return np_min(z, z_cap); }
-__device__ __noinline__ bool mixed_below(double z, double z_min) { return z <= z_min; }
+// the FP64 position update near or past a boundary: periodic x
+// (integration.py:577-583), capped z (:585-589), and whether the SIP reached
+// the ground (:606); bit 0 of the result: below z_min
+struct EdgeIn { double x, z, dx, dz, x_max, z_cap, z_min; int wrap, cap; };
+__device__ __noinline__ int mixed_edges(EdgeIn e, double* xo, double* zo) {
+  double x = e.x, z = e.z;
+  if (e.wrap) x = py_mod(x, e.x_max);
+  if (e.cap) z = np_min(z, e.z_cap);
+  *xo = x; *zo = z;
+  return z <= e.z_min ? 1 : 0;
+}
 __device__ __noinline__ int mixed_floor_div(double x, double d) { return (int)floor(x / d); }
 // SIP reaching the ground (integration.py:606-630)
 struct GroundGeo {
@@ -717,152 +731,240 @@ __device__ __noinline__ double mixed_remove(GroundGeo a, int64_t k, int i, int j
   return a.z_min - 0.01 * a.dz;
 }
 
-// per-thread asynchronous global->shared copies (cp.async, completion waited
-// per thread with cp.async.wait_group)
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(
-                   (unsigned)__cvta_generic_to_shared(smem)), "l"(gmem));
+// ---- bulk copies into shared memory (cp.async.bulk + mbarrier) ----
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
 }
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(
-                   (unsigned)__cvta_generic_to_shared(smem)), "l"(gmem));
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count));
 }
-// the same with an L2 eviction-priority policy (createpolicy): the SIP state
-// streams through once per sub-step, evict-first, so that the per-cell
-// records the kernel gathers stay in L2
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// global -> shared, completion counted in bytes on the mbarrier; the SIP
+// state streams through once per sub-step (L2 evict-first policy) so that
+// the per-cell records the kernel gathers stay in L2
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar, uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1], %2, [%3], %4;\n" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
+      : "memory");
+}
 __device__ __forceinline__ uint64_t l2_evict_first_policy() {
   uint64_t pol;
   asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(pol));
   return pol;
 }
-__device__ __forceinline__ void cp_async8_ef(void* smem, const void* gmem, uint64_t pol) {
-  asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;\n" ::"r"(
-                   (unsigned)__cvta_generic_to_shared(smem)), "l"(gmem), "l"(pol));
-}
-__device__ __forceinline__ void cp_async4_ef(void* smem, const void* gmem, uint64_t pol) {
-  asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 4, %2;\n" ::"r"(
-                   (unsigned)__cvta_generic_to_shared(smem)), "l"(gmem), "l"(pol));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n"); }
-__device__ __forceinline__ void cp_async_wait1() {
-  asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-}
-__device__ __forceinline__ void cp_async_wait0() {
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-}
-
-// The SIP state a sub-step reads is staged in shared memory one SIP ahead
-// (each thread copies its next SIP's attributes into its own slots, field-
-// major so a warp's slots are contiguous), the cell index two SIPs ahead, and
-// the next SIP's cell record (one 128-byte line) is prefetched into L1 as
-// soon as that index has landed.
-constexpr int PM_THREADS = 128;
-enum { PF_X, PF_Z, PF_U, PF_W, PF_MW, PF_MS, PF_XI, PF_N };
-template <bool PHYS>
-__device__ __forceinline__ void prefetch_sip(double (*st)[PM_THREADS], const PArgs& a, int64_t k,
-                                             uint64_t pol) {
-  const int t = threadIdx.x;
-  cp_async8_ef(&st[PF_X][t], a.pos + k, pol);
-  cp_async8_ef(&st[PF_Z][t], a.pos + a.n + k, pol);
-  cp_async8_ef(&st[PF_U][t], a.vel + k, pol);
-  cp_async8_ef(&st[PF_W][t], a.vel + a.n + k, pol);
-  if (PHYS) {
-    cp_async8_ef(&st[PF_MW][t], a.m_w + k, pol);
-    cp_async8_ef(&st[PF_MS][t], a.m_s + k, pol);
-    cp_async8_ef(&st[PF_XI][t], a.xi + k, pol);
-  }
-}
 __device__ __forceinline__ void prefetch_l1(const void* p) {
   asm volatile("prefetch.global.L1 [%0];\n" ::"l"(p));
 }
+// an mbarrier wait never spins without bound: after this many polls (each
+// try_wait suspends the thread for a while) the kernel gives up and raises
+// LACMO_FLAG_SYNC_TIMEOUT
+constexpr uint32_t MBAR_POLL_LIMIT = 1u << 22;
+
+// Tiles of PM_TILE consecutive SIPs move HBM -> shared memory as bulk copies,
+// one per attribute, issued by one thread two tiles ahead (three stages).
+// Each attribute's slot has room for a window that starts at the 16-byte
+// boundary below the tile's first element (the rows z and w start 8 bytes off
+// a boundary when n is odd).  When a tile's data lands, every thread
+// prefetches the cell record of its SIP in that tile into L1, one tile
+// before it is used.  Tiles a bulk copy cannot take (the last ones of a
+// member, or arrays not 16-byte aligned) are loaded by the threads.
+#ifndef LACMO_PM_THREADS
+#define LACMO_PM_THREADS 128
+#endif
+constexpr int PM_THREADS = LACMO_PM_THREADS;
+constexpr int PM_TILE = PM_THREADS;
+constexpr int PM_STAGES = 3;
+enum { PF_X, PF_Z, PF_U, PF_W, PF_MW, PF_MS, PF_XI, PF_N };
+struct PmStage {
+  double f[PF_N][PM_TILE + 2];
+  int32_t c[PM_TILE + 4];
+};
+
+template <bool PHYS>
+struct PmTiles {
+  // the rows z and w (second rows of pos and vel) start 8 bytes off a 16-byte
+  // boundary when n is odd: their slots then hold the window from 8 bytes
+  // below the tile's first element, and the data starts at slot index zoff
+  int zoff;
+  bool bulk;   // arrays aligned for bulk copies
+  __device__ __forceinline__ void init(const PArgs& a) {
+    uintptr_t al = (uintptr_t)a.pos | (uintptr_t)a.vel | (uintptr_t)a.cell;
+    if (PHYS) al |= (uintptr_t)a.m_w | (uintptr_t)a.m_s | (uintptr_t)a.xi;
+    bulk = al % 16 == 0;
+    zoff = bulk ? (int)(a.n & 1) : 0;
+  }
+  // tile k0 by bulk copy: aligned arrays, and every window inside its array
+  // (the window of a second row reaches 8 bytes past the tile's end)
+  __device__ __forceinline__ bool by_bulk(const PArgs& a, int64_t k0) const {
+    return bulk && k0 + PM_TILE + 2 <= a.n;
+  }
+  __device__ __forceinline__ void issue(const PArgs& a, int64_t k0, PmStage& s, uint64_t* bar,
+                                        uint64_t pol) const {
+    const uint32_t zb = PM_TILE * 8 + 16 * zoff;   // bytes of a second-row window
+    mbar_expect_tx(bar, PM_TILE * 4 + (PHYS ? 5 : 2) * PM_TILE * 8 + 2 * zb);
+    bulk_g2s(&s.f[PF_X][0], a.pos + k0, PM_TILE * 8, bar, pol);
+    bulk_g2s(&s.f[PF_Z][0], a.pos + a.n + k0 - zoff, zb, bar, pol);
+    bulk_g2s(&s.f[PF_U][0], a.vel + k0, PM_TILE * 8, bar, pol);
+    bulk_g2s(&s.f[PF_W][0], a.vel + a.n + k0 - zoff, zb, bar, pol);
+    if (PHYS) {
+      bulk_g2s(&s.f[PF_MW][0], a.m_w + k0, PM_TILE * 8, bar, pol);
+      bulk_g2s(&s.f[PF_MS][0], a.m_s + k0, PM_TILE * 8, bar, pol);
+      bulk_g2s(&s.f[PF_XI][0], a.xi + k0, PM_TILE * 8, bar, pol);
+    }
+    bulk_g2s(&s.c[0], a.cell + k0, PM_TILE * 4, bar, pol);
+  }
+  // the slot of thread t's SIP in the stage
+  __device__ __forceinline__ double get(const PmStage& s, int f, int t) const {
+    return s.f[f][(f == PF_Z || f == PF_W) ? zoff + t : t];
+  }
+  // the threads' own loads of a tile (same slots)
+  __device__ __forceinline__ void load(const PArgs& a, int64_t k, PmStage& s, int t) const {
+    if (k >= a.n) return;
+    s.f[PF_X][t] = __ldcs(a.pos + k);
+    s.f[PF_Z][zoff + t] = __ldcs(a.pos + a.n + k);
+    s.f[PF_U][t] = __ldcs(a.vel + k);
+    s.f[PF_W][zoff + t] = __ldcs(a.vel + a.n + k);
+    if (PHYS) {
+      s.f[PF_MW][t] = __ldcs(a.m_w + k);
+      s.f[PF_MS][t] = __ldcs(a.m_s + k);
+      s.f[PF_XI][t] = __ldcs(a.xi + k);
+    }
+    s.c[t] = __ldcs(a.cell + k);
+  }
+};
 
 template <bool PHYS>
 #ifndef LACMO_PM_BLOCKS
-#define LACMO_PM_BLOCKS 8   // resident blocks per SM (register budget 64)
+#define LACMO_PM_BLOCKS 6   // resident blocks per SM (register budget 80)
 #endif
 __global__ void __launch_bounds__(PM_THREADS, LACMO_PM_BLOCKS) k_particles_mixed(const __grid_constant__ PK x) {
   // the member's arguments, once per block in shared memory: threads read
   // them on use instead of holding some 60 registers of pointers and sizes
   __shared__ PArgs s_a;
-  if (threadIdx.x == 0) s_a = make_pargs(x.m.get(), x.c);
+  extern __shared__ __align__(128) unsigned char pm_smem[];
+  PmStage* st = (PmStage*)pm_smem;
+  __shared__ __align__(8) uint64_t s_bar[PM_STAGES];
+  const int t = threadIdx.x;
+  if (t == 0) {
+    s_a = make_pargs(x.m.get(), x.c);
+    for (int q = 0; q < PM_STAGES; ++q) mbar_init(&s_bar[q], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  }
   __syncthreads();
   const PArgs& a = s_a;
   const int C = (int)(a.nx * a.nz);
   const int nz = (int)a.nz;
-  __shared__ double s_pf[2][PF_N][PM_THREADS];
-  __shared__ int32_t s_pc[3][PM_THREADS];
-  const int t = threadIdx.x;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t k = blockIdx.x * (int64_t)blockDim.x + t;
-  // the first SIP's state and the cell indices of the first two
-  const uint64_t pol = l2_evict_first_policy();
-  if (k < a.n) {
-    cp_async4_ef(&s_pc[0][t], a.cell + k, pol);
-    prefetch_sip<PHYS>(s_pf[0], a, k, pol);
-  }
-  if (k + stride < a.n) cp_async4_ef(&s_pc[1][t], a.cell + k + stride, pol);
-  cp_async_commit();
-  int sg = 0, c3 = 0;   // slots of SIP k: state sg, cell index c3
-  for (; k < a.n; k += stride, sg ^= 1, c3 = c3 == 2 ? 0 : c3 + 1) {
-    const int n3 = c3 == 2 ? 0 : c3 + 1, nn3 = n3 == 2 ? 0 : n3 + 1;
-    if (k + stride < a.n) prefetch_sip<PHYS>(s_pf[sg ^ 1], a, k + stride, pol);
-    if (k + 2 * stride < a.n) cp_async4_ef(&s_pc[nn3][t], a.cell + k + 2 * stride, pol);
-    cp_async_commit();
-    cp_async_wait1();   // this SIP's state and the next SIP's cell index have landed
-    if (PHYS && k + stride < a.n) {
-      const int32_t cn = s_pc[n3][t];
-      if (cn >= 0) prefetch_l1(a.crec + CELL_REC * (int64_t)cn);
+  PmTiles<PHYS> tl;
+  tl.init(a);
+  // SIP indices fit in 32 bits (n < 2^31)
+  const int ntiles = (int)((a.n + PM_TILE - 1) / PM_TILE);
+  const int G = gridDim.x;
+  const int first = blockIdx.x;
+  const int my_tiles = first < ntiles ? (ntiles - first + G - 1) / G : 0;
+  // prologue: tiles 0 and 1 of this block in flight
+  if (t == 0) {
+    const uint64_t pol = l2_evict_first_policy();
+    for (int i = 0; i < 2 && i < my_tiles; ++i) {
+      const int k0 = (first + i * G) * PM_TILE;
+      if (tl.by_bulk(a, k0)) tl.issue(a, k0, st[i], &s_bar[i], pol);
     }
-    const int32_t c = s_pc[c3][t];
-    const bool active = c >= 0;
-    double x = s_pf[sg][PF_X][t], z = s_pf[sg][PF_Z][t];
-    if (!active) {
-      const int i = -1 - c;
-      if (a.write_Tp) a.T_p[k] = __ldg(a.gsf + (int64_t)i * nz + nz - 1);
-      mixed_inactive_rel(a.rel, a.n, a.dx, a.dz, k, i);
+  }
+  bool tout = false;   // an mbarrier wait of this thread ran out of polls
+  int i = 0;
+  for (; i < my_tiles; ++i) {
+    const int k0 = (first + i * G) * PM_TILE;
+    const int sg = i % PM_STAGES;
+    // every thread is done with tile i - 1's stage; all stop together when a
+    // wait ran out
+    if (i > 0 && __syncthreads_or(tout)) break;
+    if (t == 0 && i + 2 < my_tiles) {
+      const int k2 = (first + (i + 2) * G) * PM_TILE;
+      const int s2 = (i + 2) % PM_STAGES;
+      if (tl.by_bulk(a, k2)) {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        tl.issue(a, k2, st[s2], &s_bar[s2], l2_evict_first_policy());
+      }
+    }
+    // this tile's data (the first tile's, else waited for one tile ago), and
+    // the next tile's: its cell records go to L1 now
+    for (int w = (i == 0 ? 0 : 1); w <= 1; ++w) {
+      const int iw = i + w;
+      if (iw >= my_tiles) break;
+      const int kw = (first + iw * G) * PM_TILE;
+      if (!tl.by_bulk(a, kw)) continue;
+      const int sw = iw % PM_STAGES;
+      const uint32_t parity = (uint32_t)((iw / PM_STAGES) & 1);
+      uint32_t polls = 0;
+      while (!mbar_try_wait(&s_bar[sw], parity)) {
+        if (++polls >= MBAR_POLL_LIMIT) { tout = true; break; }
+      }
+      if (PHYS && w == 1 && !tout) {
+        const int32_t cn = st[sw].c[t];
+        if (cn >= 0) prefetch_l1(a.crec + CELL_REC * (int64_t)cn);
+      }
+    }
+    if (tout) continue;   // this tile's data cannot be trusted
+    PmStage& S = st[sg];
+    const int k = k0 + t;
+    if (!tl.by_bulk(a, k0)) tl.load(a, k, S, t);
+    if (k >= a.n) continue;
+    const int32_t c = S.c[t];
+    if (c < 0) {
+      const int i_ = -1 - c;
+      if (a.write_Tp) a.T_p[k] = __ldg(a.gsf + (int64_t)i_ * nz + nz - 1);
+      mixed_inactive_rel(a.rel, a.n, a.dx, a.dz, k, i_);
       continue;
     }
     if (a.write_Tp) a.T_p[k] = __ldg(a.gsf + c);
-    double mw = 0.0;
-    double xik = 0.0;
-    float un, wn2;
-    int fb_slot = -1;           // queue slot of a SIP whose Newton repeats in FP64
-    double mw_in = 0.0, ms_k = 0.0;
-    float xif_k = 0.0f;
-    const float xf = d2f_int(x), zf = d2f_int(z);
+    float un, wn2, d = 0.0f, xf, zf;
+    int fb_slot = -1;   // queue slot of a SIP whose Newton repeats in FP64
+    const float4* rec = a.crec + CELL_REC * (int64_t)c;
     if (PHYS) {
-      mw = s_pf[sg][PF_MW][t];
-      const double ms = s_pf[sg][PF_MS][t];
-      xik = s_pf[sg][PF_XI][t];
-      CellAmbF af;
-      const float4* rec = a.crec + CELL_REC * (int64_t)c;
       const float4 q0 = __ldg(rec), q1 = __ldg(rec + 1);
+      CellAmbF af;
       af.T = q0.x; af.S_m1 = q0.y; af.sigw = q0.z; af.rhow = q0.w;
       af.lap0 = q1.x; af.lbp0 = q1.y; af.c1 = q1.z; af.c2 = q1.w;
-      const float msf = d2f_int(ms), mwf = d2f_int(mw), xif = d2f_int(xik);
+      const float msf = d2f_int(tl.get(S, PF_MS, t)), mwf = d2f_int(tl.get(S, PF_MW, t));
       const float mpf = mwf + msf;
       const float wsf = msf * f_rcp(mpf);
-      float rho = (a.sol == SOL_AS)
-                      ? af.rhow * ((((float)LC_PAR_RHO_AS_0 * wsf + (float)LC_PAR_RHO_AS_1) * wsf +
-                                    (float)LC_PAR_RHO_AS_2) * wsf + (float)LC_PAR_RHO_AS_3)
-                      : (float)LC_PAR_SOL_DENS_NACL_0 + (float)LC_PAR_SOL_DENS_NACL_1 * wsf +
-                            (float)LC_PAR_SOL_DENS_NACL_2 * af.T +
-                            (float)LC_PAR_SOL_DENS_NACL_3 * wsf * wsf +
-                            (float)LC_PAR_SOL_DENS_NACL_4 * wsf * af.T +
-                            (float)LC_PAR_SOL_DENS_NACL_5 * af.T * af.T;
-      float R = f_cbrt((float)LC_FOUR_PI_OVER_THREE_INV * mpf * f_rcp(rho));
+      const float rho = (a.sol == SOL_AS)
+                            ? af.rhow * ((((float)LC_PAR_RHO_AS_0 * wsf + (float)LC_PAR_RHO_AS_1) *
+                                              wsf + (float)LC_PAR_RHO_AS_2) * wsf +
+                                         (float)LC_PAR_RHO_AS_3)
+                            : (float)LC_PAR_SOL_DENS_NACL_0 + (float)LC_PAR_SOL_DENS_NACL_1 * wsf +
+                                  (float)LC_PAR_SOL_DENS_NACL_2 * af.T +
+                                  (float)LC_PAR_SOL_DENS_NACL_3 * wsf * wsf +
+                                  (float)LC_PAR_SOL_DENS_NACL_4 * wsf * af.T +
+                                  (float)LC_PAR_SOL_DENS_NACL_5 * af.T * af.T;
+      const float R = f_cbrt((float)LC_FOUR_PI_OVER_THREE_INV * mpf * f_rcp(rho));
       const float sig = af.sigw * (1.0f + (a.sol == SOL_AS ? (float)LC_PAR_SIGMA_AS
                                                             : (float)LC_PAR_SIGMA_NACL) *
                                                wsf * f_rcp(1.f - wsf));
       // efflorescence floor m_s (1/0.78 - 1) as an increment, in FP32
       const float d_effl = msf * (float)(LC_W_S_MAX_AS_INV - 1.0) - mwf;
-      float d;
-      const bool ok = newton_mixed_f(a.sol, a.dt_subf, a.no_iter, mwf, msf, wsf, R, af.T, rho, sig,
-                                     af, d_effl, &d);
-      const double dm = f2d_int(d);
+      const bool ok = newton_mixed_f(a.sol, a.dt_subf, a.no_iter, mwf, msf, wsf, R, af.T, rho,
+                                     sig, af, d_effl, &d);
       if (ok) {
         // per-cell FP64 sum of dm * xi (executed by L2)
-        atomicAdd(a.acc + c, f2d_int(d * xif));
+        atomicAdd(a.acc + c, f2d_int(d * d2f_int(tl.get(S, PF_XI, t))));
       } else {
         // near the critical radius the Newton repeats in FP64, in full warps
         // in k_newton_fallback: queue the SIP with its mass before the
@@ -870,19 +972,17 @@ __global__ void __launch_bounds__(PM_THREADS, LACMO_PM_BLOCKS) k_particles_mixed
         fb_slot = atomicAdd(a.fb_count, 1);
         a.fb_id[fb_slot] = (int32_t)k;
         a.fb_c[fb_slot] = c;
-        a.fb_mw[fb_slot] = mw;
+        a.fb_mw[fb_slot] = tl.get(S, PF_MW, t);
       }
-      mw_in = mw;
-      ms_k = ms;
-      xif_k = xif;
-      mw += dm;
       // drag (integration.py:699-718) in FP32 with the ammonium-sulfate radius
       const float mpn = (mwf + d) + msf;
       const float wn = msf * f_rcp(mpn);
-      rho = af.rhow * ((((float)LC_PAR_RHO_AS_0 * wn + (float)LC_PAR_RHO_AS_1) * wn +
-                        (float)LC_PAR_RHO_AS_2) * wn + (float)LC_PAR_RHO_AS_3);
-      R = f_cbrt((float)LC_FOUR_PI_OVER_THREE_INV * mpn * f_rcp(rho));
+      const float rhon = af.rhow * ((((float)LC_PAR_RHO_AS_0 * wn + (float)LC_PAR_RHO_AS_1) * wn +
+                                     (float)LC_PAR_RHO_AS_2) * wn + (float)LC_PAR_RHO_AS_3);
+      const float Rn = f_cbrt((float)LC_FOUR_PI_OVER_THREE_INV * mpn * f_rcp(rhon));
       const float4 cij = __ldg(rec + 6);   // (i, j, j == 0, j == nz - 1)
+      xf = d2f_int(tl.get(S, PF_X, t));
+      zf = d2f_int(tl.get(S, PF_Z, t));
       const float rxf = (xf - a.x_minf) * a.inv_dxf - cij.x;
       const float rzf = (zf - a.z_minf) * a.inv_dzf - cij.y;
       float uf, wf;
@@ -890,12 +990,12 @@ __global__ void __launch_bounds__(PM_THREADS, LACMO_PM_BLOCKS) k_particles_mixed
                   rxf, rzf, uf, wf);
       const float2 q2 = __ldg((const float2*)(rec + 2));
       const float mu_f = q2.x, rho_f = q2.y;
-      const float uo = d2f_int(s_pf[sg][PF_U][t]), wo = d2f_int(s_pf[sg][PF_W][t]);
+      const float uo = d2f_int(tl.get(S, PF_U, t)), wo = d2f_int(tl.get(S, PF_W, t));
       const float d0 = uf - uo, d1 = wf - wo;
-      const float vel_dev = sqrtf(d0 * d0 + d1 * d1);
+      const float vel_dev = f_sqrt(d0 * d0 + d1 * d1);
       const float inv_mu = f_rcp(mu_f);
-      const float Re_p = 2.0E-6f * rho_f * R * vel_dev * inv_mu;
-      float k_dt = 4.5E12f * a.dt_subf * mu_f * f_rcp(rho * R * R);
+      const float Re_p = 2.0E-6f * rho_f * Rn * vel_dev * inv_mu;
+      float k_dt = 4.5E12f * a.dt_subf * mu_f * f_rcp(rhon * Rn * Rn);
       if (Re_p > 0.5f) {
         if (Re_p < 1000.0f) k_dt *= (1.f + 0.15f * f_pow(Re_p, 0.687f));
         else k_dt *= 0.0183333333333f * Re_p;
@@ -905,44 +1005,59 @@ __global__ void __launch_bounds__(PM_THREADS, LACMO_PM_BLOCKS) k_particles_mixed
       wn2 = (wo + k_dt * wf - a.dtg_f) * inv;
     } else {
       // the half-step move of integration.py:1474-1481: positions only
-      un = d2f_int(s_pf[sg][PF_U][t]);
-      wn2 = d2f_int(s_pf[sg][PF_W][t]);
+      un = d2f_int(tl.get(S, PF_U, t));
+      wn2 = d2f_int(tl.get(S, PF_W, t));
+      xf = d2f_int(tl.get(S, PF_X, t));
+      zf = d2f_int(tl.get(S, PF_Z, t));
     }
     // position (integration.py:552-630)
-    const double x0 = x, z0 = z;
-    x += f2d_int(a.dt_posf * un);
-    z += f2d_int(a.dt_posf * wn2);
-    const float xnf = xf + a.dt_posf * un, znf = zf + a.dt_posf * wn2;
+    const double x0 = tl.get(S, PF_X, t), z0 = tl.get(S, PF_Z, t);
+    const float xf0 = xf, zf0 = zf;
+    const float dxf = a.dt_posf * un, dzf = a.dt_posf * wn2;
+    double xn = x0 + f2d_int(dxf);
+    double zn = z0 + f2d_int(dzf);
+    const float xnf = xf0 + dxf, znf = zf0 + dzf;
     double u = f2d_int(un), w = f2d_int(wn2);
-    // periodic x / capped z: exact FP64 only when near or past a boundary
-    if (!(xnf > 1e-3f && xnf < a.x_maxf - 1e-3f)) x = mixed_wrap_x(x, a.x_max);
-    if (!(znf < a.z_capf - 1e-3f)) z = mixed_cap_z(z, a.z_cap);
+    // periodic x / capped z / ground: exact FP64 only when near or past a
+    // boundary
+    const int wrap = !(xnf > 1e-3f && xnf < a.x_maxf - 1e-3f);
+    const int cap = !(znf < a.z_capf - 1e-3f);
+    const int low = !(znf > a.z_minf + 1e-3f);
+    int edge = 0;
+    if (wrap | cap | low)
+      edge = mixed_edges(EdgeIn{xn, zn, a.dx, a.dz, a.x_max, a.z_cap, a.z_min, wrap, cap}, &xn,
+                         &zn);
     int32_t newc;
     bool removed = false;
-    if (!(znf > a.z_minf + 1e-3f) && mixed_below(z, a.z_min)) {
-      const int i = c / nz, j = c - i * nz;
-      if (!PHYS) { xik = a.xi[k]; mw = a.m_w[k]; }
+    if (low && (edge & 1)) {
+      const int i_ = c / nz, j_ = c - i_ * nz;
+      const double xik = PHYS ? tl.get(S, PF_XI, t) : a.xi[k];
+      double mw = PHYS ? tl.get(S, PF_MW, t) + f2d_int(d) : a.m_w[k];
       if (PHYS && fb_slot >= 0) {
         // a queued SIP leaving the domain: its FP64 Newton here, for the
         // water it takes along
+        const double mw0 = tl.get(S, PF_MW, t);
         const double dm = mixed_newton_fp64(NewtonFP64{a.gsf, a.gmp, a.aux, (int64_t)C, a.dt_sub,
                                                        a.sol, a.no_iter, a.nfb},
-                                            c, mw_in, ms_k);
-        mw = mw_in + dm;
-        atomicAdd(a.acc + c, f2d_int(d2f_int(dm) * xif_k));
+                                            c, mw0, tl.get(S, PF_MS, t));
+        mw = mw0 + dm;
+        atomicAdd(a.acc + c, f2d_int(d2f_int(dm) * d2f_int(xik)));
         a.fb_id[fb_slot] = -1;
       }
-      z = mixed_remove(GroundGeo{a.rel, a.water_removed, a.n, a.x_min, a.z_min, a.dx, a.dz}, k,
-                       i, j, x0, z0, xik, mw);
+      if (PHYS) __stcs(a.m_w + k, mw);
+      zn = mixed_remove(GroundGeo{a.rel, a.water_removed, a.n, a.x_min, a.z_min, a.dx, a.dz}, k,
+                        i_, j_, x0, z0, xik, mw);
       u = 0.0; w = 0.0;
       removed = true;
-      newc = (int32_t)(-1 - i);
+      newc = (int32_t)(-1 - i_);
     } else {
-      const float qx = d2f_int(x) * a.inv_dxf, qz = d2f_int(z) * a.inv_dzf;
+      // the new cell from the FP32 position, FP64 when within 1e-4 of an edge
+      const float px = wrap ? d2f_int(xn) : xnf, pz = cap ? d2f_int(zn) : znf;
+      const float qx = px * a.inv_dxf, qz = pz * a.inv_dzf;
       int ci = __float2int_rd(qx), cj = __float2int_rd(qz);
       const float fx = qx - floorf(qx), fz = qz - floorf(qz);
-      if (!(fx > 1e-4f && fx < 0.9999f)) ci = mixed_floor_div(x, a.dx);
-      if (!(fz > 1e-4f && fz < 0.9999f)) cj = mixed_floor_div(z, a.dz);
+      if (!(fx > 1e-4f && fx < 0.9999f)) ci = mixed_floor_div(xn, a.dx);
+      if (!(fz > 1e-4f && fz < 0.9999f)) cj = mixed_floor_div(zn, a.dz);
       if (ci >= a.nx || ci < 0 || cj >= nz || cj < 0) {
         atomicOr(a.flags, LACMO_FLAG_CELL_CLAMPED);
         ci = ci < 0 ? 0 : (ci >= a.nx ? (int)a.nx - 1 : ci);
@@ -950,15 +1065,28 @@ __global__ void __launch_bounds__(PM_THREADS, LACMO_PM_BLOCKS) k_particles_mixed
       }
       newc = (int32_t)(ci * nz + cj);
       if (a.hist) a.rank[k] = atomicAdd(a.counts + newc, 1);
+      if (PHYS) __stcs(a.m_w + k, tl.get(S, PF_MW, t) + f2d_int(d));
     }
     // streaming stores (evict first)
-    __stcs(a.pos + k, x); __stcs(a.pos + a.n + k, z);
+    __stcs(a.pos + k, xn); __stcs(a.pos + a.n + k, zn);
     if (PHYS || removed) { __stcs(a.vel + k, u); __stcs(a.vel + a.n + k, w); }
-    if (PHYS) __stcs(a.m_w + k, mw);
     __stcs(a.cell + k, newc);
   }
-  cp_async_wait0();
+  if (__syncthreads_or(tout)) {
+    // a wait ran out: flag it, and wait (again bounded) for the copies this
+    // block may still have in flight before the block's shared memory goes
+    if (t == 0) {
+      atomicOr(a.flags, LACMO_FLAG_SYNC_TIMEOUT);
+      for (int j = i; j < i + 2 && j < my_tiles; ++j) {
+        if (!tl.by_bulk(a, (first + j * G) * PM_TILE)) continue;
+        const int sj = (int)(j % PM_STAGES);
+        for (uint32_t p = 0; p < MBAR_POLL_LIMIT; ++p)
+          if (mbar_try_wait(&s_bar[sj], (uint32_t)((j / PM_STAGES) & 1))) break;
+      }
+    }
+  }
 }
+constexpr size_t PM_SMEM = (size_t)PM_STAGES * sizeof(PmStage);
 
 // The FP64 Newton of the SIPs a mixed sub-step queued (near the critical
 // radius), one SIP per thread: the mass and the per-cell sum as the inline
@@ -1315,7 +1443,7 @@ static cudaError_t mixed_grid(const Bt& B, dim3* grid) {
   if (res <= 0) {
     int per_sm = 0, sms = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_particles_mixed<PHYS>,
-                                                      PM_THREADS, 0);
+                                                      PM_THREADS, PM_SMEM);
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
@@ -1338,7 +1466,7 @@ cudaError_t launch_particles_mixed(const Bt& B, const lacmo_params_t& p, double 
   dim3 grid;
   cudaError_t e = mixed_grid<true>(B, &grid);
   if (e != cudaSuccess) return e;
-  k_particles_mixed<true><<<grid, PM_THREADS, 0, s>>>(x); note_launches(1);
+  k_particles_mixed<true><<<grid, PM_THREADS, PM_SMEM, s>>>(x); note_launches(1);
   k_newton_fallback<<<dim3(64, B.M), 128, 0, s>>>(x); note_launches(1);
   return cudaGetLastError();
 }
@@ -1348,7 +1476,7 @@ cudaError_t launch_move_mixed(const Bt& B, double dt_pos, cudaStream_t s) {
   dim3 grid;
   cudaError_t e = mixed_grid<false>(B, &grid);
   if (e != cudaSuccess) return e;
-  k_particles_mixed<false><<<grid, PM_THREADS, 0, s>>>(x); note_launches(1);
+  k_particles_mixed<false><<<grid, PM_THREADS, PM_SMEM, s>>>(x); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_wind_float(const Bt& B, cudaStream_t s) {

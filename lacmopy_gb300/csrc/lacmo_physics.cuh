@@ -179,24 +179,44 @@ LACMO_DEV double newton_full(int sol, double dt_sub, int no_iter, double m_w, do
 // Mixed precision: the same Fukuta-Walter mass rate, derivative and implicit
 // ---------------------------------------------------------------------------
 // FP32 building blocks of the mixed-precision path, on the hardware's special
-// function unit.  Each stays far inside the path's FP32 budget:
-//  f_div(a, b) = a * rcp.approx(b) (__fdividef): 2 ulp for 2^-126 < |b| < 2^126
-//    (all divisors here are masses, densities, radii and 1 - w terms);
-//  f_cbrt(x): 2^(log2(x)/3) from lg2/ex2 (relative error below 4e-6), then one
-//    Newton step on y^3 = x, which squares it: within a few ulp for x > 0;
+// function unit (the .approx.ftz forms of rcp, lg2, ex2 and rsqrt, written as
+// inline PTX so that no range fix-ups are issued; every argument here is a
+// normal float: masses, densities, radii, speeds and Reynolds numbers).  Each
+// stays far inside the path's FP32 budget:
+//  f_rcp(b): relative error below 2^-23;
+//  f_cbrt(x): 2^(log2(x)/3) (relative error near 1e-6), then one Newton step
+//    on y^3 = x, which squares it: within a few ulp for x > 0;
 //  f_expm1(e): Taylor series to e^8 for |e| <= 0.5 (truncation below 1e-8
-//    relative), expm1f beyond;
+//    relative); 2^(e log2 e) - 1 beyond, where there is no cancellation;
 //  f_pow(x, y) = 2^(y log2 x) for x > 0 (relative error near 1e-6 for the
-//    drag's Reynolds factor, whose exponent is 0.687).
-LACMO_DEV float f_div(float a, float b) { return __fdividef(a, b); }
-LACMO_DEV float f_rcp(float b) { return __fdividef(1.0f, b); }
+//    drag's Reynolds factor, whose exponent is 0.687);
+//  f_sqrt(v) = v rsqrt(v) for v > 0 (relative error below 2^-22), 0 else.
+LACMO_DEV float f_rcp(float b) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+  return r;
+}
+LACMO_DEV float f_div(float a, float b) { return a * f_rcp(b); }
+LACMO_DEV float f_lg2(float x) {
+  float r;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+LACMO_DEV float f_ex2(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+LACMO_DEV float f_sqrt(float v) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return v > 0.0f ? v * r : 0.0f;
+}
 LACMO_DEV float f_cbrt(float x) {
-  const float y = exp2f(__log2f(x) * (1.0f / 3.0f));
+  const float y = f_ex2(f_lg2(x) * (1.0f / 3.0f));
   return (2.0f / 3.0f) * y + (1.0f / 3.0f) * x * f_rcp(y * y);
 }
-static __device__ __noinline__ float f_expm1_wide(float e) { return expm1f(e); }
 LACMO_DEV float f_expm1(float e) {
-  if (!(fabsf(e) <= 0.5f)) return f_expm1_wide(e);
   float p = 2.4801587e-05f;                 // 1/8!
   p = p * e + 1.9841270e-04f;               // 1/7!
   p = p * e + 1.3888889e-03f;               // 1/6!
@@ -205,9 +225,9 @@ LACMO_DEV float f_expm1(float e) {
   p = p * e + 1.6666667e-01f;               // 1/3!
   p = p * e + 0.5f;
   p = p * e + 1.0f;
-  return p * e;
+  return fabsf(e) <= 0.5f ? p * e : f_ex2(e * 1.4426950408889634f) - 1.0f;
 }
-LACMO_DEV float f_pow(float x, float y) { return exp2f(y * __log2f(x)); }
+LACMO_DEV float f_pow(float x, float y) { return f_ex2(y * f_lg2(x)); }
 
 // Newton in FP32.  The residual f2 = S_amb - S_eq is formed from the two
 // deviations from saturation, S_amb - 1 (exact in FP64, rounded once) and
