@@ -9,10 +9,13 @@ step dt = 1 s per step (10 condensation sub-steps with the 3-iteration
 implicit Newton, 2 all-or-nothing collision steps), each kernel launch covering
 all members, the step replayed from a CUDA graph; thinned Philox draws (an
 exact sampler of the per-pair uniforms; the per-pair draws are reported under
-"modes").  The "FP64 plain" side is the single 75 x 75 x 64-SIPs/cell state
-with the Long/Bott table in FP64 and one Philox uniform per pair;
-both sides and the mixed single state are reported under "modes".  Seeded
-synthetic states with the case's shapes and distributions.
+"modes").  The headline times fresh states; "modes" also holds the same
+ensemble timed after --developed-steps untimed steps, when the cloud rains
+and collisions multiply.  The "FP64 plain" side is the single
+75 x 75 x 64-SIPs/cell state with the Long/Bott table in FP64, timed with one
+Philox uniform per pair and with thinned draws, so that both ratios compare
+like with like; both sides and the mixed single state are reported under
+"modes".  Seeded synthetic states with the case's shapes and distributions.
 
 Metric: SIP-updates/s = active SIPs advanced one dt per second (whole job).
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -71,24 +74,59 @@ def parse():
                          "sampler of the per-pair uniforms) or one Philox uniform per pair")
     ap.add_argument("--no-draws-compare", action="store_true",
                     help="skip the headline ensemble with the other draw mode")
+    ap.add_argument("--developed-steps", type=int, default=600,
+                    help="untimed steps that advance the headline ensemble to a developed "
+                         "(raining) state before the developed-regime timing; 0 skips it")
+    ap.add_argument("--cpu-1thread-steps", type=int, default=1,
+                    help="steps of the single-thread CPU sample (0 skips it)")
     return ap.parse_args()
 
 
-def workload_config(args, n_sips):
+def workload_config(args):
+    """The workload both arms time (the same dict in both JSON lines)."""
     return {"workload": f"icmw2012_case1_{args.nx}x{args.nz}_ensemble{args.members}_"
-                        f"uneven{args.uneven[0]}-{args.uneven[1]}spc_hall_bott_mixed",
+                        f"uneven{args.uneven[0]}-{args.uneven[1]}spc_hall_bott",
             "members": args.members, "nx": args.nx, "nz": args.nz,
             "sips_per_cell": f"uniform in [{args.uneven[0]}, {args.uneven[1]}] per cell and member",
-            "n_sips": int(n_sips), "kernel": "Hall_Bott", "precision_mode": "mixed",
-            "dt_s": 1.0, "cond_substeps": 10, "collision_steps": 2, "newton_iterations": 3,
+            "kernel": "Hall_Bott", "dt_s": 1.0, "cond_substeps": 10, "collision_steps": 2,
+            "newton_iterations": 3, "regime": "fresh seeded states, advection steps "
+                                              f"{args.warmup + 1}-{args.warmup + args.steps}",
+            "l2": "inputs larger than L2 (state ~8 GB); L2 also flushed between timed steps "
+                  "(512 MiB device memset)",
+            "parallelism": "replicas"}
+
+
+def impl_details(args):
+    """How our arm computes the workload (kept out of the shared config)."""
+    return {"precision_mode": "mixed",
             "draws": ("philox4x32-10 (device), keyed per member, " +
                       ("thinned draws: one uniform per low-probability segment of pairs, an "
                        "exact sampler of the per-pair uniforms" if args.draws == "thinned"
                        else "one uniform per pair")),
-            "cuda_graph": not args.no_graph,
-            "l2": "inputs larger than L2 (state ~8 GB); L2 also flushed between timed steps "
-                  "(512 MiB device memset)",
-            "parallelism": "replicas"}
+            "cuda_graph": not args.no_graph}
+
+
+def cpu_model():
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for ln in r.stdout.splitlines():
+            if ln.split(":")[0].strip() in ("Model name", "Vendor ID"):
+                name = ln.split(":", 1)[1].strip()
+                if name and ln.startswith("Model name"):
+                    return name
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def numba_probe():
+    """Whether the reference's own Numba path can run here."""
+    try:
+        import numba  # noqa: F401
+        return f"numba {numba.__version__} importable"
+    except Exception as e:
+        return f"numba not importable ({type(e).__name__}: {e})"
 
 
 def _member_state(a):
@@ -238,27 +276,31 @@ def run_reference(args):
     if rank != 0:
         return
     from lacmopy_gb300 import synthetic
-    # a bounded sample of the ensemble workload: one member, the oracle's
-    # restatement of the reference algorithm on all host cores
-    st = synthetic.make_icmw_state(Nx=args.nx, Nz=args.nz, seed=5000, kernel_type="Hall_Bott",
-                                   uneven=tuple(args.uneven))
+    # The reference's own path is Numba-compiled Python; without numba it
+    # cannot run as shipped, and the C restatement of the reference algorithm
+    # (oracle/, FP64, glibc libm, OpenMP over SIPs and cells) runs in its place.
+    probe = numba_probe()
+    # each step is a bounded sample of the workload: one member (the first
+    # member's state) advanced one step, on all host threads
+    st = synthetic.make_icmw_state(Nx=args.nx, Nz=args.nz, seed=rank_seeds(0, 1)[1][0],
+                                   kernel_type="Hall_Bott", uneven=tuple(args.uneven))
     threads = os.cpu_count() or 1
-    steps = max(1, min(args.steps, 2))
     if args.warmup > 0:
-        cpu_port_rate([st], 1, threads)
-    rate, secs = cpu_port_rate([st], steps, threads)
-    n_total_est = int(st["xi"].size) * args.members
+        cpu_port_rate([st], args.warmup, threads)
+    rate, secs = cpu_port_rate([st], args.steps, threads)
     line = {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": steps, "warmup": args.warmup,
-            "ms_per_step": 1000.0 * secs / steps, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload_config(args, n_total_est), "impl": "reference",
+            "config": workload_config(args), "impl": "reference",
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{steps} advection steps of one ensemble member "
-                                       f"({st['xi'].size} SIPs) of the workload; the reference's "
-                                       "Numba path is unavailable on this box (numba not "
-                                       "installed), so the C restatement of the reference "
-                                       "algorithm (FP64, OpenMP over SIPs and cells) runs"},
+                             "cpu": cpu_model(), "numba_probe": probe,
+                             "sample": f"each step: one member ({st['xi'].size} SIPs) of the "
+                                       f"{args.members}-member workload advanced one advection "
+                                       "step; the reference's Numba path is unavailable (" +
+                                       probe + "), so the C restatement of the reference "
+                                       "algorithm (FP64, OpenMP over SIPs and cells, one draw "
+                                       "per pair) runs"},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -357,6 +399,7 @@ def run_ours(args):
                 "bytes_per_sip": BYTES_PARTICLE_SUBSTEP}
     del batch
     torch.cuda.empty_cache()
+    modes[f"batched_mixed_{args.draws}_draws"] = {"value": value, "ms_per_step": ms / args.steps}
     if not args.no_draws_compare:
         other = "philox" if args.draws == "thinned" else "thinned"
         batch = BatchState(members, seeds, precision="mixed", draws=other)
@@ -366,20 +409,50 @@ def run_ours(args):
         del batch
         torch.cuda.empty_cache()
 
+    # ---- the developed regime: the same ensemble advanced (untimed) until
+    # the cloud rains, then timed the same way ----
+    if args.developed_steps > 0:
+        batch = BatchState(members, seeds, precision="mixed", draws=args.draws)
+        t0 = time.perf_counter()
+        for _ in range(args.developed_steps):
+            batch.adv_step(1, graph=graph)
+        torch.cuda.synchronize()
+        spin_s = time.perf_counter() - t0
+        cols = sum(int(m.no_cols.sum()) for m in batch.members)
+        ms_d, ups_d, _, _ = timed(batch, False)
+        cols_d = sum(int(m.no_cols.sum()) for m in batch.members) - cols
+        modes["batched_mixed_developed"] = {
+            "value": ups_d / (ms_d / 1000.0), "ms_per_step": ms_d / args.steps,
+            "regime": f"after {args.developed_steps} untimed advection steps "
+                      f"({args.developed_steps} s of model time, {spin_s:.0f} s of wall time) "
+                      f"of the headline ensemble, then {args.warmup} warm-up and "
+                      f"{args.steps} timed steps",
+            "collisions_per_step": cols_d / (args.warmup + args.steps),
+            "over_fresh": (ups_d / (ms_d / 1000.0)) / value}
+        del batch
+        torch.cuda.empty_cache()
+
     # ---- the FP64 plain path and the mixed single state (75 x 75 x 64) ----
     if single is not None:
-        for prec, key in (("fp64", "fp64_plain"), ("mixed", "mixed_single")):
-            ds = DeviceState(copy.deepcopy(single), draws="philox", seed=1001 + rank,
+        for prec, dr, key in (("fp64", "philox", "fp64_plain"),
+                              ("fp64", "thinned", "fp64_plain_thinned"),
+                              ("mixed", "philox", "mixed_single")):
+            ds = DeviceState(copy.deepcopy(single), draws=dr, seed=1001 + rank,
                              precision=prec)
             ms2, ups2, _, _ = timed(ds, False)
             modes[key] = {"value": ups2 / (ms2 / 1000.0), "ms_per_step": ms2 / args.steps,
-                          "n_sips": int(single["xi"].size),
+                          "n_sips": int(single["xi"].size), "draws": dr,
                           "workload": f"icmw2012_case1_{args.nx}x{args.nz}_{sum(args.spcm)}spc_"
                                       f"long_bott_{prec}"}
             del ds
-        modes["batched_mixed_over_fp64_plain"] = value / modes["fp64_plain"]["value"]
-        modes["mixed_single_over_fp64_plain"] = (modes["mixed_single"]["value"]
-                                                 / modes["fp64_plain"]["value"])
+        fp = modes["fp64_plain"]["value"]
+        fpt = modes["fp64_plain_thinned"]["value"]
+        modes["batched_mixed_over_fp64_plain"] = value / fp
+        modes["ratio_thinned_over_thinned"] = modes["batched_mixed_thinned_draws"]["value"] / fpt
+        if "batched_mixed_philox_draws" in modes:
+            modes["ratio_per_pair_over_per_pair"] = (
+                modes["batched_mixed_philox_draws"]["value"] / fp)
+        modes["mixed_single_over_fp64_plain"] = modes["mixed_single"]["value"] / fp
 
     # ---- end to end through the reference-facing drop-in API: each member's
     # NumPy state copied in and out by integrate_adv_step_np every step ----
@@ -423,10 +496,18 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         rate, secs = cpu_port_rate(members[:1], args.cpu_steps, threads)
+        probe = numba_probe()
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "cpu": cpu_model(), "numba_probe": probe,
                "sample": f"{args.cpu_steps} advection step(s) of one ensemble member "
                          f"({members[0]['xi'].size} SIPs), {secs:.1f} s; C restatement of "
-                         "the reference algorithm in FP64, OpenMP on all host cores"}
+                         "the reference algorithm in FP64, OpenMP on all host cores (the "
+                         "reference's Numba path is unavailable: " + probe + ")"}
+        if args.cpu_1thread_steps > 0:
+            rate1, secs1 = cpu_port_rate(members[:1], args.cpu_1thread_steps, 1)
+            cpu["single_thread"] = {"value": rate1, "unit": UNIT, "cores": 1,
+                                    "sample": f"{args.cpu_1thread_steps} advection step(s) of "
+                                              f"the same member, {secs1:.1f} s, one thread"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -434,7 +515,8 @@ def run_ours(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "mixed f32/f64 (f32 Newton, drag and pair screen; f64 state, "
                          "per-cell sums, near-critical Newton and collision updates)",
-                "data": "synthetic", "config": workload_config(args, n_total),
+                "data": "synthetic", "config": workload_config(args),
+                "impl_details": dict(impl_details(args), n_sips=int(n_total)),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": int(launches), "modes": modes,
                 "hbm_frac_whole_step": value * BYTES_PER_SIP_UPDATE / 1e9 / peak}
