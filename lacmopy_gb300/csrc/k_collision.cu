@@ -189,26 +189,39 @@ __device__ __forceinline__ float d2f_down_pos(double r) {  // r in [0, 1)
   return __int_as_float((int)(((e - 896u) << 23) | (uint32_t)((b >> 29) & 0x7fffffu)));
 }
 
-// exact per-SIP collision data (collision/all_or_nothing.py:812-826): the
-// density at the step-start masses and cell temperature, the correctly-rounded
-// radius and its kernel bin; computed on first need, then kept in gR/grho/gk
-__device__ __noinline__ void compute_exact(const CellArgs& a, int32_t id, double Tc, bool use_E) {
-  const double m_p = a.gR[id], ms = a.grho[id];
+// Exact per-SIP collision data (collision/all_or_nothing.py:812-826), kept
+// in gR / grho / gk and computed on first need.  The density belongs to the
+// step-start masses and the cell temperature (the reference keeps it for the
+// whole step); the radius and its kernel bin follow from the current masses
+// and that density, which the reference recomputes after every collection
+// (all_or_nothing.py:596-633).  A radius only matters when an exact
+// evaluation reads it, so after a collection it is recomputed lazily:
+//   gk = GK_NONE:  nothing computed; gR, grho hold the step-start m_p, m_s
+//   gk = GK_STALE: grho holds the density; gR, gk are out of date
+//   gk >= 0:       gR, gk are the exact radius and bin of the current masses
+constexpr int32_t GK_NONE = -1, GK_STALE = -2;
+__device__ __forceinline__ double density_of(const CellArgs& a, double m_p, double ms, double Tc) {
   const double w_s = ms / m_p;
-  const double rho = (a.sol == SOL_AS) ? density_water(Tc) * poly_rho_AS(w_s)
-                                       : density_NaCl_solution(w_s, Tc);
-  const double R = col_radius(m_p, rho);
+  return (a.sol == SOL_AS) ? density_water(Tc) * poly_rho_AS(w_s)
+                           : density_NaCl_solution(w_s, Tc);
+}
+__device__ __noinline__ void compute_density(const CellArgs& a, int32_t id, double Tc) {
+  a.grho[id] = density_of(a, a.gR[id], a.grho[id], Tc);
+  a.gk[id] = GK_STALE;
+}
+__device__ __forceinline__ void ensure_density(const CellArgs& a, int32_t id, double Tc) {
+  if (a.gk[id] == GK_NONE) compute_density(a, id, Tc);
+}
+__device__ __noinline__ void compute_exact(const CellArgs& a, int32_t id, double Tc, bool use_E) {
+  if (a.gk[id] == GK_NONE) a.grho[id] = density_of(a, a.gR[id], a.grho[id], Tc);
+  const double R = col_radius(a.m_w[id] + a.m_s[id], a.grho[id]);
   a.gR[id] = R;
-  a.grho[id] = rho;
   a.gk[id] = use_E ? col_bin(R, a.lo, a.bl, a.nb) : 0;
 }
 // the exact kernel bin of SIP id from its current masses, stored nowhere
 __device__ __noinline__ int32_t exact_bin_of(const CellArgs& a, int32_t id, double Tc) {
   const double m_p = a.m_w[id] + a.m_s[id];
-  const double w_s = a.m_s[id] / m_p;
-  const double rho = (a.sol == SOL_AS) ? density_water(Tc) * poly_rho_AS(w_s)
-                                       : density_NaCl_solution(w_s, Tc);
-  return col_bin(col_radius(m_p, rho), a.lo, a.bl, a.nb);
+  return col_bin(col_radius(m_p, density_of(a, m_p, a.m_s[id], Tc)), a.lo, a.bl, a.nb);
 }
 __device__ __forceinline__ void ensure_exact(const CellArgs& a, int32_t id, double Tc, bool use_E) {
   if (a.gk[id] < 0) compute_exact(a, id, Tc, use_E);
@@ -223,10 +236,37 @@ struct CellSmem {
   float4* st;   // thinned draws: statistics of block b at st[2b], st[2b + 1]
 };
 
+// SIP id's masses changed in a collection: its exact radius and bin become
+// stale, and its FP32 copies at slot l follow now from the FP32 masses and
+// the step-start density (the radius within the screen's 1e-6, as at the
+// cell's load; a bin near an edge is computed exactly, as there).
+__device__ __noinline__ void masses_changed(const CellArgs& a, const CellSmem* S, int32_t id,
+                                            int l, double Tc, bool use_E) {
+  a.gk[id] = GK_STALE;
+  if (!S) return;
+  const float Rf = lt_cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * d2f_rn(a.m_w[id] + a.m_s[id]) /
+                            d2f_rn(a.grho[id]));
+  int32_t kb = 0;
+  if (use_E) {
+    const float v = (__logf(Rf) - a.lo_f) * a.inv_bl_f + 0.5f;
+    const float fl = floorf(v);
+    if (v - fl > a.bin_margin && (fl + 1.0f) - v > a.bin_margin && v > -1e6f && v < 1e6f &&
+        Rf > 0.f) {
+      kb = __float2int_rz(fl);
+      kb = kb < 0 ? 0 : (kb > a.nb - 1 ? (int32_t)a.nb - 1 : kb);
+    } else {
+      compute_exact(a, id, Tc, use_E);
+      kb = a.gk[id];
+    }
+  }
+  S->v[l].y = Rf;
+  S->sk[l] = kb;
+}
+
 // One ordinary collection (p_crit <= 1 and p_crit > r) of the pair imin/imax
-// (collision/all_or_nothing.py:607-633) on the global arrays; the exact
-// radius of imin (and of imax for equal multiplicities) must be available.
-// S (may be null) receives the FP32 copies at local slots lmin/lmax.
+// (collision/all_or_nothing.py:607-633) on the global arrays; the density of
+// imin must be known.  S (may be null) receives the FP32 copies at local
+// slots lmin/lmax.
 __device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* S, int32_t imin,
                                              int32_t imax, int lmin, int lmax, double Tc,
                                              bool use_E) {
@@ -237,7 +277,9 @@ __device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* 
   const double m_s_min = MS[imin], m_s_max = MS[imax];
   const double xi_rel_dev = (xi_max - xi_min) / xi_max;
   if (xi_rel_dev < 1.0E-5) {
-    ensure_exact(a, imax, Tc, use_E);
+    // both radii follow from imin's density (all_or_nothing.py:615-624):
+    // computed now, not left stale
+    ensure_density(a, imax, Tc);
     const double xi_ges = xi_min + xi_max;
     MW[imin] = 2.0 * (xi_min * m_w_min + xi_max * m_w_max) / xi_ges;
     MS[imin] = 2.0 * (xi_min * m_s_min + xi_max * m_s_max) / xi_ges;
@@ -247,7 +289,8 @@ __device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* 
     RR[imax] = RR[imin];
     XI[imax] = 0.5 * 0.7 * xi_ges;
     XI[imin] = 0.5 * xi_ges - XI[imax];
-    if (use_E) { a.gk[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb); a.gk[imax] = a.gk[imin]; }
+    a.gk[imin] = use_E ? col_bin(RR[imin], a.lo, a.bl, a.nb) : 0;
+    a.gk[imax] = a.gk[imin];
     if (S) {
       S->v[lmin].x = d2f_rn(XI[imin]); S->v[lmax].x = d2f_rn(XI[imax]);
       S->v[lmin].y = d2f_rn(RR[imin]); S->v[lmax].y = S->v[lmin].y;
@@ -256,13 +299,9 @@ __device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* 
   } else {
     MW[imin] += m_w_max;
     MS[imin] += m_s_max;
-    RR[imin] = col_radius((MW[imin] + MS[imin]), RHO[imin]);
     XI[imax] -= xi_min;
-    if (use_E) a.gk[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
-    if (S) {
-      S->v[lmax].x = d2f_rn(XI[imax]); S->v[lmin].y = d2f_rn(RR[imin]);
-      S->sk[lmin] = a.gk[imin];
-    }
+    masses_changed(a, S, imin, lmin, Tc, use_E);
+    if (S) S->v[lmax].x = d2f_rn(XI[imax]);
   }
 }
 
@@ -291,13 +330,9 @@ __device__ __noinline__ int exact_pair(const CellArgs& a, CellSmem Sm, int32_t i
     const double xi_col = p_crit * xi_min;
     MW[imin] = MW[imin] + p_crit * MW[imax];
     MS[imin] = MS[imin] + p_crit * MS[imax];
-    RR[imin] = col_radius((MW[imin] + MS[imin]), a.grho[imin]);
     XI[imax] -= xi_col;
-    if (use_E) a.gk[imin] = col_bin(RR[imin], a.lo, a.bl, a.nb);
-    if (S) {
-      S->v[lmax].x = d2f_rn(XI[imax]); S->v[lmin].y = d2f_rn(RR[imin]);
-      S->sk[lmin] = a.gk[imin];
-    }
+    masses_changed(a, S, imin, lmin, Tc, use_E);
+    if (S) S->v[lmax].x = d2f_rn(XI[imax]);
     return 2;
   }
   if (!(p_crit > r)) return 0;
@@ -311,7 +346,7 @@ __device__ __noinline__ void certain_collection(const CellArgs& a, CellSmem S, i
   const int32_t ii = S.sid[i], jj = S.sid[j];
   const bool lo_i = a.xi[ii] <= a.xi[jj];
   const int32_t imin = lo_i ? ii : jj, imax = lo_i ? jj : ii;
-  ensure_exact(a, imin, Tc, use_E);
+  ensure_density(a, imin, Tc);
   collect_once(a, &S, imin, imax, lo_i ? i : j, lo_i ? j : i, Tc, use_E);
 }
 
