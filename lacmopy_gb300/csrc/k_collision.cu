@@ -34,7 +34,7 @@ namespace lacmo {
 // correctly-rounded result unless y + t lies within 2^-85 |y| of a rounding
 // midpoint; then (or for non-normal x) the full routine decides.  The margin
 // is wider than the full routine's own uncertainty, so both always agree.
-__device__ __forceinline__ double cr_pow13(double x) {
+__device__ __forceinline__ double cr_pow13_dd(double x) {
   if (!(x >= 0x1p-1000 && x <= 0x1p1000)) return lacmo_cr_pow(x, LC_ONE_THIRD);
   const double y = cbrt(x);
   const lacmo_dd y2 = lacmo_two_prod(y, y);
@@ -50,6 +50,49 @@ __device__ __forceinline__ double cr_pow13(double x) {
   double half_ulp = lacmo_as_f64((uint64_t)(ex - 53) << 52);
   if (e < 0.0 && (b & 0x000fffffffffffffULL) == 0) half_ulp *= 0.5;
   if (fabs(fabs(e) - half_ulp) <= 0x1p-85 * s) return lacmo_cr_pow(x, LC_ONE_THIRD);
+  return s;
+}
+
+// The same value with most of the FP64 work moved to FP32 (GB300's FP64 pipe
+// is narrow, and the collision events run on single lanes).  For x in
+// [2^-40, 2^40] (every radius from 1 nm to 1 cm in micrometres):
+//  - y: the FP32 cube root (a few ulp) refined by two Newton steps
+//    y += (x - y^3) / (3 y^2), the residual in FP64 and the quotient in FP32:
+//    the error goes 2^-21 -> 2^-43 -> within about an ulp (FP64 rounding of
+//    the residual);
+//  - t = r / (3 y^2) - y d ln x with r = x - y^3 in double-double as above,
+//    both terms in FP32: |r / (3 y^2)| < 2^-50 y and |y d ln x| < 2^-46 y,
+//    each within 2^-22 relative, their sum within 2^-24 of the larger, and the
+//    neglected (d ln x)^2 / 2 below 2^-92: t is within 2^-67 y of its value;
+//  - a flushed FP32 residual (|r| < 2^-126) changes t by less than
+//    2^-126 / (3 x) <= 2^-86 y.
+// s = y + t is then the correctly-rounded result unless it lies within
+// 2^-62 s of a rounding midpoint (about one call in 500), where cr_pow13_dd
+// decides.
+__device__ __forceinline__ double cr_pow13(double x) {
+  if (!(x >= 0x1p-40 && x <= 0x1p40)) return cr_pow13_dd(x);
+  const float xf = d2f_int(x);
+  double y = f2d_int(f_cbrt(xf));
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const float yf = d2f_int(y);
+    const double r0 = x - (y * y) * y;
+    y = y + f2d_int(d2f_int(r0) * f_rcp(3.0f * yf * yf));
+  }
+  const lacmo_dd y2 = lacmo_two_prod(y, y);
+  const lacmo_dd y3 = lacmo_dd_mul_d(y2, y);
+  const double r = (x - y3.hi) - y3.lo;
+  const float yf = d2f_int(y);
+  const float tf = d2f_int(r) * f_rcp(3.0f * yf * yf) -
+                   yf * (0x1.555556p-56f * (f_lg2(xf) * 0.693147181f));
+  const double t = f2d_int(tf);
+  const double s = y + t;
+  const double e = (y - s) + t;
+  const uint64_t b = lacmo_as_u64(s);
+  const int64_t ex = (int64_t)((b >> 52) & 0x7ff);
+  double half_ulp = lacmo_as_f64((uint64_t)(ex - 53) << 52);
+  if (e < 0.0 && (b & 0x000fffffffffffffULL) == 0) half_ulp *= 0.5;
+  if (fabs(fabs(e) - half_ulp) <= 0x1p-62 * s) return cr_pow13_dd(x);
   return s;
 }
 
@@ -70,6 +113,23 @@ __device__ __forceinline__ int32_t col_bin(double R, double lo, double bl, int64
   if (ind < 0) ind = 0;
   else if (ind > nb - 1) ind = nb - 1;
   return (int32_t)ind;
+}
+// The same bin from an FP32 bin position first: lo_f, inv_bl_f are lo and 1/bl
+// rounded to FP32 and margin bounds the error of the FP32 position (it is
+// derived for radii within 1e-6; R is rounded to within 2^-24 here).  A
+// position farther than margin from every bin edge gives the bin of the exact
+// position; closer ones take col_bin.
+__device__ __forceinline__ int32_t col_bin_f(double R, double lo, double bl, int64_t nb,
+                                             float lo_f, float inv_bl_f, float margin) {
+  const float Rf = d2f_int(R);
+  const float v = (f_lg2(Rf) * 0.693147181f - lo_f) * inv_bl_f + 0.5f;
+  const float fl = floorf(v);
+  if (v - fl > margin && (fl + 1.0f) - v > margin && v > -1e6f && v < 1e6f && Rf > 1e-30f &&
+      Rf < 1e30f) {
+    int32_t kb = __float2int_rz(fl);
+    return kb < 0 ? 0 : (kb > nb - 1 ? (int32_t)nb - 1 : kb);
+  }
+  return col_bin(R, lo, bl, nb);
 }
 __device__ __forceinline__ int64_t pair_rank(int64_t i, int64_t j, int64_t n) {
   return i * n - i * (i + 1) / 2 + (j - i - 1);
@@ -216,7 +276,7 @@ __device__ __noinline__ void compute_exact(const CellArgs& a, int32_t id, double
   if (a.gk[id] == GK_NONE) a.grho[id] = density_of(a, a.gR[id], a.grho[id], Tc);
   const double R = col_radius(a.m_w[id] + a.m_s[id], a.grho[id]);
   a.gR[id] = R;
-  a.gk[id] = use_E ? col_bin(R, a.lo, a.bl, a.nb) : 0;
+  a.gk[id] = use_E ? col_bin_f(R, a.lo, a.bl, a.nb, a.lo_f, a.inv_bl_f, a.bin_margin) : 0;
 }
 // the exact kernel bin of SIP id from its current masses, stored nowhere
 __device__ __noinline__ int32_t exact_bin_of(const CellArgs& a, int32_t id, double Tc) {
@@ -289,7 +349,8 @@ __device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* 
     RR[imax] = RR[imin];
     XI[imax] = 0.5 * 0.7 * xi_ges;
     XI[imin] = 0.5 * xi_ges - XI[imax];
-    a.gk[imin] = use_E ? col_bin(RR[imin], a.lo, a.bl, a.nb) : 0;
+    a.gk[imin] = use_E ? col_bin_f(RR[imin], a.lo, a.bl, a.nb, a.lo_f, a.inv_bl_f, a.bin_margin)
+                       : 0;
     a.gk[imax] = a.gk[imin];
     if (S) {
       S->v[lmin].x = d2f_rn(XI[imin]); S->v[lmax].x = d2f_rn(XI[imax]);

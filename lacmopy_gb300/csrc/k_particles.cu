@@ -637,34 +637,6 @@ __global__ void __launch_bounds__(32) k_cell_update(const __grid_constant__ MRef
 // The Newton condensation and the drag update run in FP32 (lacmo_physics.cuh)
 // with the FP64 Newton for SIPs near the critical radius.  Per-cell sums and
 // water_removed are formed in arbitrary order.
-// Conversions between FP64 and FP32 with integer operations: GB300 runs
-// FP64 arithmetic and double<->float conversions on a narrow pipe, and the
-// mixed kernel converts about a dozen values per SIP.  Branch-free (no call
-// on any path, so no register spills around one).
-//  d2f_int: for finite x within the FP32 range (positions, velocities,
-//    masses, multiplicities), the FP32 value rounded half away from zero on
-//    the magnitude (within 1 ulp of the correctly rounded value; the FP32
-//    copies only feed approximations with certified margins); below the FP32
-//    normal range a signed zero.  A NaN or huge x gives some finite value:
-//    the FP32 results then only feed increments that are added to the FP64
-//    state, which carries the NaN on.
-//  f2d_int: exact for normal floats and zero; FP32 subnormals give a signed
-//    zero, infinities and NaNs stay what they are.
-__device__ __forceinline__ float d2f_int(double x) {
-  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
-  const uint32_t ax = hi & 0x7fffffffu, sign = hi & 0x80000000u;
-  // (ax << 3 | lo >> 29) holds the low 9 exponent bits over 23 mantissa bits
-  const uint32_t f = ((__funnelshift_l(lo, ax, 3) - (384u << 23)) + ((lo >> 28) & 1u)) | sign;
-  return __uint_as_float(ax < (897u << 20) ? sign : f);
-}
-__device__ __forceinline__ double f2d_int(float f) {
-  const uint32_t b = __float_as_uint(f);
-  const uint32_t a = b & 0x7fffffffu, sign = b & 0x80000000u;
-  const uint32_t hi = ((a >> 3) + (896u << 20)) | sign | (a >= 0x7f800000u ? 0x7ff00000u : 0u);
-  const bool tiny = a < 0x00800000u;
-  return __hiloint2double((int)(tiny ? sign : hi), (int)(tiny ? 0u : b << 29));
-}
-
 // Rare FP64 paths stay out of line (__noinline__) so that the common path
 // issues no FP64 instruction, not even predicated off.
 // removed SIP: only the relative position keeps its per-call division
