@@ -29,21 +29,28 @@ MAT_PROP_NAMES = ("thermal_conductivity", "diffusion_constant",
                   "specific_heat_capacity", "viscosity", "mass_density_fluid")
 
 
+# elementwise libm pow (the reference's material functions are scalar
+# functions vectorized over the grid, so each power is one scalar pow call;
+# NumPy's array power may take a vectorized routine that rounds differently)
+_pow = np.vectorize(math.pow, otypes=[np.float64])
+
+
 def _sigma_w(T):
     tau = 1 - T / 647.096
-    return 0.2358 * tau ** 1.256 * (1 - 0.625 * tau)
+    return 0.2358 * _pow(tau, 1.256) * (1 - 0.625 * tau)
 
 
 def material_properties(gsf):
-    """Material-property grids from the scalar fields (integration.py:359-400)."""
+    """Material-property grids from the scalar fields (grid.py:713-727,
+    material_properties.py:224-544, atmosphere.py)."""
     T, p, r_v, rho_d = gsf[0], gsf[1], gsf[4], gsf[3]
     mp = np.empty((7,) + T.shape)
     mp[0] = 4.1868E-3 * (5.69 + 0.017 * (T - 273.15))
-    mp[1] = 4.01218E-5 * T ** 1.94 / p
+    mp[1] = 4.01218E-5 * _pow(T, 1.94) / p
     mp[2] = 1.0E3 * (2500.82 - 2.358 * (T - 273.0))
     mp[3] = _sigma_w(T)
     mp[4] = c.specific_heat_capacity_air_dry_NTP * (1 + 0.897 * r_v)
-    mp[5] = 1.458E-6 * T ** 1.5 / (T + 110.4)
+    mp[5] = 1.458E-6 * _pow(T, 1.5) / (T + 110.4)
     mp[6] = rho_d * (1.0 + r_v)
     return mp
 

@@ -463,9 +463,95 @@ def gen_box_model_kgrid(R):
          xis_vs_time=xt, masses_vs_time=mt, save_times=tt, no_cols=no_cols, xis=xis, m=m)
 
 
+def gen_file_formats(R):
+    """file_handling.py: the full-state files (save_grid_and_particles_full)
+    and the frame files (save_grid_scalar_fields, dump_particle_data_all,
+    dump_particle_data, dump_particle_tracer_data_block,
+    save_sim_paras_to_file) the reference writes for a small seeded state,
+    byte for byte, and what its load_grid_and_particles_full returns."""
+    import tempfile
+    st = _small_state(71, Nx=6, Nz=5, spcm=(4, 6))
+    st["active_ids"][::17] = False
+    st["cells"][1, ~st["active_ids"]] = -1
+    steps = np.asarray(st["grid_steps"])
+    dy = float(st["grid_volume_cell"]) / (steps[0] * steps[1])
+    grid = R.grid.Grid(np.array(st["grid_ranges"]), steps, dy)
+    gsf, gmp = st["grid_scalar_fields"], st["grid_mat_prop"]
+    names = ("temperature", "pressure", "potential_temperature", "mass_density_air_dry",
+             "mixing_ratio_water_vapor", "mixing_ratio_water_liquid", "saturation",
+             "saturation_pressure", "mass_dry_inv", "rho_dry_inv")
+    for k, nm in enumerate(names):
+        setattr(grid, nm, gsf[k].copy())
+    grid.velocity = st["grid_velocity"].copy()
+    grid.mass_flux_air_dry = st["grid_mass_flux_air_dry"].copy()
+    t = 600
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        path = d + "/"
+        R.fh.save_grid_and_particles_full(t, grid, st["pos"], st["cells"], st["vel"], st["m_w"],
+                                          st["m_s"], st["xi"], st["active_ids"], path)
+        loaded = R.fh.load_grid_and_particles_full(t, path)
+        R.fh.save_grid_scalar_fields(t, gsf, path, __import__("datetime").datetime.now())
+        R.fh.dump_particle_data_all(t, st["pos"], st["vel"], st["cells"], st["m_w"], st["m_s"],
+                                    st["xi"], st["active_ids"], path)
+        tr = np.arange(3, st["xi"].size, 40)
+        R.fh.dump_particle_data(t, st["pos"][:, tr], st["vel"][:, tr], st["m_w"][tr],
+                                st["m_s"][tr], st["xi"][tr], gsf[0], gsf[4], path)
+        tb = np.array([t + 60, t + 80])
+        R.fh.dump_particle_tracer_data_block(
+            tb, np.stack([np.array([st["pos"][:, tr], st["vel"][:, tr]])] * 2),
+            np.stack([np.array([st["m_w"][tr], st["m_s"][tr], st["T_p"][tr]])] * 2),
+            np.stack([st["xi"][tr]] * 2), np.array([0.5, 0.75]), path)
+        R.fh.save_sim_paras_to_file([1.0, 0.1, 3, 6001], "dt dt_sub no_iter_impl_mass rnd_seed_sim",
+                                    t, path)
+        for fn in sorted(os.listdir(d)):
+            out["file__" + fn] = np.frombuffer(open(path + fn, "rb").read(), dtype=np.uint8)
+    g = loaded[0]
+    for nm in ("pressure", "temperature", "potential_temperature", "mass_density_air_dry",
+               "mixing_ratio_water_vapor", "mixing_ratio_water_liquid", "saturation",
+               "saturation_pressure", "mass_dry_inv", "rho_dry_inv", "thermal_conductivity",
+               "diffusion_constant", "heat_of_vaporization", "surface_tension",
+               "specific_heat_capacity", "viscosity", "mass_density_fluid", "velocity",
+               "mass_flux_air_dry", "ranges", "steps", "no_cells"):
+        out["grid__" + nm] = np.asarray(getattr(g, nm))
+    out["grid__step_y"] = np.float64(g.step_y)
+    out["grid__volume_cell"] = np.float64(g.volume_cell)
+    for nm, a in zip(("pos", "cells", "vel", "m_w", "m_s", "xi", "active_ids"), loaded[1:]):
+        out["in__" + nm] = np.asarray(st[nm])
+        out["loaded__" + nm] = np.asarray(a)
+    for k, nm in enumerate(names):
+        out["in__gsf_" + nm] = gsf[k]
+    out["in__grid_mat_prop"] = gmp
+    out["in__T_p"] = st["T_p"]
+    out["in__grid_ranges"] = np.asarray(st["grid_ranges"])
+    out["in__grid_steps"] = steps
+    out["in__dy"] = np.float64(dy)
+    out["in__trace_ids"] = tr
+    out["t"] = np.int64(t)
+    save("file_formats.npz", **out)
+
+
+def gen_kernel_generators(R):
+    """collision/kernel.py:793-942: kernel grids K(R1, R2) with Beard
+    velocities for the Long and Hall efficiencies on two radius grids."""
+    out = {}
+    for kt, fn in (("Long_Bott", R.ker.generate_kernel_grid_Long_Bott_np),
+                   ("Hall_Bott", R.ker.generate_kernel_grid_Hall_Bott_np)):
+        for args in ((0.6, 2000.0, 10, 1000.0), (1.0, 4000.0, 20, 1000.0)):
+            K, v, m, rg = fn(*args)
+            tag = f"{kt}_{args[2]}"
+            out[tag + "__args"] = np.array(args, dtype=np.float64)
+            out[tag + "__K"] = K
+            out[tag + "__vel"] = v
+            out[tag + "__mass"] = m
+            out[tag + "__radius"] = rg
+    save("kernel_generators.npz", **out)
+
+
 GENERATORS = [gen_tables, gen_mass_rate, gen_interp, gen_golovin, gen_ecol_box, gen_cells_2d,
               gen_grid_and_divergence, gen_particle_substep, gen_adv_step, gen_diagnostics,
-              gen_kernel_grid_m, gen_box_model_kgrid]
+              gen_kernel_grid_m, gen_box_model_kgrid, gen_file_formats,
+              gen_kernel_generators]
 
 
 def main(ref_root, only=()):

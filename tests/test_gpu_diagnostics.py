@@ -92,3 +92,32 @@ def test_simulate_collisions_kernel_grid_m_vs_golden(tmp_path):
     assert np.array_equal(mt, g["masses_vs_time"])
     assert np.array_equal(xis, g["xis"]) and np.array_equal(m, g["m"])
     assert np.array_equal(np.load(tmp_path / f"xis_vs_time_{seed}.npy"), g["xis_vs_time"])
+
+
+def test_kernel_grid_m_box_with_generated_table(oracle_py, tmp_path):
+    """The box model with a kernel table made by the generator
+    (collision/kernel.py:793-867) and its mass-grid binning: the GPU loop
+    equals the oracle's step in a loop with the same seeded draws."""
+    import math
+    from lacmopy_gb300 import collision as Cg
+    from lacmopy_gb300 import tables
+    K, vel, mass, rg = tables.generate_kernel_grid_Long_Bott_np(0.6, 3000.0, 10, 1000.0)
+    nb, m_lo, bf = tables.kernel_grid_m_parameters(mass)
+    rng = np.random.default_rng(8)
+    n = 300
+    xis0 = np.exp(rng.uniform(np.log(1e6), np.log(1e9), n))
+    m0 = np.exp(rng.uniform(np.log(1e1), np.log(1e7), n))
+    seed, dV, dt, t_end, dt_save = 4242, 1.0, 1.0, 4.0, 2.0
+    xis, m = xis0.copy(), m0.copy()
+    nc = np.zeros(2, np.int64)
+    Cg.simulate_collisions((xis, m), (K, nb, m_lo, bf), "Long_Bott", "kernel_grid_m", dV, dt,
+                           t_end, dt_save, nc, seed, str(tmp_path) + "/")
+    rs = np.random.RandomState(seed)
+    xo, mo = xis0.copy(), m0.copy()
+    nco = np.zeros(2, np.int64)
+    for _ in range(int(math.ceil(t_end / dt))):
+        oracle_py.collision_step_kernel_grid_m_np(xo, mo, dt / dV, K, nb, m_lo, bf, nco,
+                                                  rs.rand(n * (n - 1) // 2))
+    assert nco.sum() > 0
+    assert np.array_equal(nc, nco)
+    assert np.array_equal(xis, xo) and np.array_equal(m, mo)
