@@ -14,10 +14,10 @@
  *                      Numba compiles it.  Used to pin the oracle bit-for-bit
  *                      against the golden fixtures made by the reference.
  *   ORC_CRMATH       : the collision path's radius pow(x, 1/3) and kernel-bin
- *                      log use the correctly-rounded routines of
- *                      lacmopy_gb300/csrc/lacmo_crmath.h (the same source the
- *                      GPU kernels compile), instead of glibc libm.  Collision
- *                      outputs of the GPU equal this variant bit for bit.
+ *                      log are correctly rounded (the oracle's own binary128
+ *                      evaluation, rounded once), instead of glibc libm.
+ *                      Collision outputs of the GPU, whose math is correctly
+ *                      rounded, equal this variant bit for bit.
  * Sums that the reference accumulates sequentially in SIP-ID order
  * (delta_m_l per cell, water_removed) are accumulated in that order here too,
  * also when OpenMP runs the per-SIP work in parallel.
@@ -31,11 +31,47 @@
 #endif
 
 #include "../lacmopy_gb300/csrc/lacmo_constants.h"
-#include "../lacmopy_gb300/csrc/lacmo_thin.h"
+
 #ifdef ORC_CRMATH
-#include "../lacmopy_gb300/csrc/lacmo_crmath.h"
-#define COL_POW13(x) lacmo_cr_pow(x, LC_ONE_THIRD)
-#define COL_LOG(x) lacmo_cr_log(x)
+/* Correctly rounded log and pow for the collision path, the oracle's own:
+   evaluated in IEEE binary128 (113-bit significand; __float128 with
+   libquadmath on x86-64, long double on AArch64 Linux) and rounded once to
+   double.  The binary128 result is within a few of its ulps (2^-112
+   relative) of the exact value, so the rounding is the correct one unless the
+   exact value lies within about 2^-100 of a midpoint of two doubles, which
+   *hard reports. */
+#include <float.h>
+#if defined(__x86_64__)
+#include <quadmath.h>
+typedef __float128 orc_quad;
+#define ORC_QLOG(x) logq(x)
+#define ORC_QPOW(x, y) powq(x, y)
+#define ORC_QFABS(x) fabsq(x)
+#elif defined(__aarch64__) && LDBL_MANT_DIG == 113
+typedef long double orc_quad;
+#define ORC_QLOG(x) logl(x)
+#define ORC_QPOW(x, y) powl(x, y)
+#define ORC_QFABS(x) fabsl(x)
+#else
+#error "the correctly rounded oracle variant needs binary128 arithmetic"
+#endif
+static double orc_round_quad(orc_quad v, int* hard) {
+  const double d = (double)v;
+  if (hard) *hard = 0;
+  if (hard && isfinite(d) && d != 0.0) {
+    const double up = nextafter(d, INFINITY), dn = nextafter(d, -INFINITY);
+    const orc_quad mid_up = ((orc_quad)d + (orc_quad)up) / 2, mid_dn = ((orc_quad)d + (orc_quad)dn) / 2;
+    const orc_quad tol = ORC_QFABS(v) * (orc_quad)0x1p-100;
+    if (ORC_QFABS(v - mid_up) <= tol || ORC_QFABS(v - mid_dn) <= tol) *hard = 1;
+  }
+  return d;
+}
+static double orc_cr_log(double x, int* hard) { return orc_round_quad(ORC_QLOG((orc_quad)x), hard); }
+static double orc_cr_pow(double x, double y, int* hard) {
+  return orc_round_quad(ORC_QPOW((orc_quad)x, (orc_quad)y), hard);
+}
+#define COL_POW13(x) orc_cr_pow(x, LC_ONE_THIRD, NULL)
+#define COL_LOG(x) orc_cr_log(x, NULL)
 #else
 #define COL_POW13(x) pow(x, LC_ONE_THIRD)
 #define COL_LOG(x) log(x)
@@ -348,6 +384,211 @@ static double philox_uniform(uint64_t key, uint64_t k, uint64_t c1) {
   uint64_t a = (k & 1) ? (x2 >> 5) : (x0 >> 5), b = (k & 1) ? (x3 >> 6) : (x1 >> 6);
   return (double)(a * 67108864ull + b) * (1.0 / 9007199254740992.0);
 }
+
+/* ---- thinned Philox draws (the draw definition of the GPU collision step,
+   restated here from its description) ----
+   The SIP slots of a cell form blocks of ORC_THIN_L; the pairs (i, j) of row
+   i with j in block b form a segment, taken in lexicographic order.  The
+   unprocessed part of a segment (pairs (i, j .. jend-1), part counter sub)
+   is bounded by Q >= p_crit of all its pairs from FP32 copies of SIP i and
+   the block's statistics.  Q >= ORC_THIN_TAU or no valid bound: per-pair
+   draws for the rest of the segment.  Otherwise q = 2^-e >= Q, m remaining
+   pairs: one uniform decides whether some draw of the part falls below q
+   (probability H(e, m) = 1 - (1 - q)^m); if none does the segment is done;
+   else the first such pair h is drawn from its conditional law (pair g of r
+   remaining is first with probability P(e, r) = q / H(e, r)), its draw is
+   q u, and the pairs after h form part sub + 1.  The bound uses IEEE single
+   +, -, * and comparisons only, in a fixed order.  Uniforms: Philox4x32-10
+   of key = seed, counter (2^62 | chunk << 20 | sub << 8 | j, c1), the 53
+   bits (x0 >> 5) 2^26 + (x1 >> 6). */
+#define ORC_THIN_L 32
+#define ORC_THIN_E_MIN 2
+#define ORC_THIN_E_MAX 127
+#define ORC_THIN_NE (ORC_THIN_E_MAX - ORC_THIN_E_MIN + 1)
+#define ORC_THIN_TAU 0x1p-6f
+
+static uint32_t th_bits(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+static float th_float(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+static float th_max(float a, float b) { return a > b ? a : b; }
+static float th_min(float a, float b) { return a < b ? a : b; }
+static float th_abs(float a) { return a < 0.0f ? -a : a; }
+
+/* FP32 cube root: exponent-thirding first guess, three Newton steps */
+static float th_cbrtf(float x) {
+  float y = th_float(th_bits(x) / 3u + 0x2a5137a0u);
+  for (int it = 0; it < 3; ++it) y = (y + y + x / (y * y)) / 3.0f;
+  return y;
+}
+
+typedef struct {
+  float xmax, Rmax, umin, umax, wmin, wmax;
+  int ok;
+} th_block_t;
+
+static void th_block_stats(const float* x, const float* R, const float* u, const float* w,
+                           int64_t lo, int64_t hi, th_block_t* s) {
+  s->xmax = 0.0f;
+  s->Rmax = 0.0f;
+  s->umin = INFINITY; s->wmin = INFINITY;
+  s->umax = -INFINITY; s->wmax = -INFINITY;
+  s->ok = 1;
+  for (int64_t q = lo; q < hi; ++q) {
+    if (!(x[q] > 0.0f) || isnan(R[q]) || isnan(u[q]) || isnan(w[q])) s->ok = 0;
+    s->xmax = th_max(s->xmax, x[q]);
+    s->Rmax = th_max(s->Rmax, R[q]);
+    s->umin = th_min(s->umin, u[q]);
+    s->umax = th_max(s->umax, u[q]);
+    s->wmin = th_min(s->wmin, w[q]);
+    s->wmax = th_max(s->wmax, w[q]);
+  }
+}
+
+/* Q >= p_crit of SIP a against every SIP of the block: the largest
+   multiplicity, the sum of radii squared, the largest velocity difference and
+   the row's largest efficiency, each at least the pair's own, with slack for
+   the FP32 copies (velocities 2^-21 sum |u|, |w|; roundings 2^-14 relative,
+   1e-36 absolute); negative: no valid bound */
+static float th_bound(float xa, float Ra, float ua, float wa, const th_block_t* s, float er,
+                      float dtdv) {
+  if (!s->ok || !(xa > 0.0f) || isnan(Ra) || isnan(ua) || isnan(wa)) return -1.0f;
+  const float du = th_max(ua - s->umin, s->umax - ua);
+  const float dw = th_max(wa - s->wmin, s->wmax - wa);
+  const float um = th_max(th_abs(s->umin), th_abs(s->umax));
+  const float wm = th_max(th_abs(s->wmin), th_abs(s->wmax));
+  const float slack = 0x1p-21f * (((th_abs(ua) + um) + th_abs(wa)) + wm);
+  const float rs = Ra + s->Rmax;
+  const float core = ((((th_max(xa, s->xmax) * dtdv) * 3.14159265e-12f) * rs) * rs) * er;
+  if (!(core >= 1e-30f)) return isnan(core) ? -1.0f : 1e-27f;
+  const float pb = ((core * ((du + dw) + slack)) * (1.0f + 0x1p-14f)) + 1e-36f;
+  return isnan(pb) ? -1.0f : pb;
+}
+
+/* e of the smallest q = 2^-e >= Q, clamped to the table */
+static int th_exponent(float Q) {
+  int E;
+  const float f = frexpf(Q, &E);   /* Q = f 2^E, f in [0.5, 1) */
+  int e = (f == 0.5f) ? 1 - E : -E;
+  if (e < ORC_THIN_E_MIN) e = ORC_THIN_E_MIN;
+  if (e > ORC_THIN_E_MAX) e = ORC_THIN_E_MAX;
+  return e;
+}
+
+static void philox_block(uint64_t key, uint64_t c0, uint64_t c1, uint32_t* out);
+static uint64_t th_u53(uint64_t key, uint64_t chunk, uint32_t sub, uint32_t j, uint64_t c1) {
+  uint32_t x[4];
+  philox_block(key, (1ull << 62) | (chunk << 20) | ((uint64_t)sub << 8) | (uint64_t)j, c1, x);
+  return ((uint64_t)(x[0] >> 5) << 26) + (uint64_t)(x[1] >> 6);
+}
+
+/* H(e, m), P(e, r) rounded to nearest double from their exact rational
+   values, and the 53-bit thresholds ceil(2^53 H), ceil(2^53 P): u < H <=>
+   u53 < ceil(2^53 H) for u = u53 2^-53.  Computed once with a small
+   fixed-size big-integer type. */
+#define BN_LIMBS 144   /* 4608 bits >= 127 * 32 + 2 * 64 */
+typedef struct { uint32_t w[BN_LIMBS]; int n; } bn_t;   /* n: limbs in use */
+static void bn_set(bn_t* a, uint64_t v) {
+  memset(a->w, 0, sizeof a->w);
+  a->w[0] = (uint32_t)v; a->w[1] = (uint32_t)(v >> 32);
+  a->n = 2;
+}
+static void bn_norm(bn_t* a) { while (a->n > 1 && a->w[a->n - 1] == 0) --a->n; }
+static void bn_shl(bn_t* a, int s) {
+  const int L = s / 32, b = s % 32;
+  int n = a->n + L + 1;
+  if (n > BN_LIMBS) n = BN_LIMBS;
+  for (int i = n - 1; i >= 0; --i) {
+    uint64_t v = 0;
+    if (i - L >= 0) v = (uint64_t)a->w[i - L] << b;
+    if (b && i - L - 1 >= 0) v |= a->w[i - L - 1] >> (32 - b);
+    a->w[i] = (uint32_t)v;
+  }
+  a->n = n;
+  bn_norm(a);
+}
+static void bn_sub(bn_t* a, const bn_t* b) {   /* a -= b, a >= b */
+  int64_t br = 0;
+  for (int i = 0; i < a->n; ++i) {
+    int64_t v = (int64_t)a->w[i] - (i < b->n ? (int64_t)b->w[i] : 0) - br;
+    br = v < 0;
+    a->w[i] = (uint32_t)(v + (br << 32));
+  }
+  bn_norm(a);
+}
+static void bn_mul_u64(bn_t* r, const bn_t* a, uint64_t m) {   /* r = a m */
+  const uint64_t ml = (uint32_t)m, mh = m >> 32;
+  memset(r->w, 0, sizeof r->w);
+  uint64_t carry = 0;
+  int n = a->n + 2 < BN_LIMBS ? a->n + 2 : BN_LIMBS;
+  for (int i = 0; i < n; ++i) {   /* low half */
+    uint64_t v = (i < a->n ? (uint64_t)a->w[i] * ml : 0) + carry;
+    r->w[i] = (uint32_t)v; carry = v >> 32;
+  }
+  carry = 0;
+  for (int i = 0; i + 1 < n; ++i) {   /* high half, one limb up */
+    uint64_t v = (i < a->n ? (uint64_t)a->w[i] * mh : 0) + r->w[i + 1] + carry;
+    r->w[i + 1] = (uint32_t)v; carry = v >> 32;
+  }
+  r->n = n;
+  bn_norm(r);
+}
+static int bn_cmp(const bn_t* a, const bn_t* b) {
+  const int n = a->n > b->n ? a->n : b->n;
+  for (int i = n - 1; i >= 0; --i) {
+    const uint32_t x = i < a->n ? a->w[i] : 0, y = i < b->n ? b->w[i] : 0;
+    if (x != y) return x < y ? -1 : 1;
+  }
+  return 0;
+}
+static int bn_bitlen(const bn_t* a) {
+  for (int i = a->n - 1; i >= 0; --i)
+    if (a->w[i]) { int b = 32; while (!(a->w[i] >> (b - 1))) --b; return 32 * i + b; }
+  return 0;
+}
+/* the double nearest num / den (ties to even), 0 < num / den <= 1 */
+static double bn_ratio(const bn_t* num, const bn_t* den) {
+  const int s = 63 - (bn_bitlen(num) - bn_bitlen(den));   /* quotient in [2^62, 2^64) */
+  bn_t ns = *num, t;
+  bn_shl(&ns, s);
+  uint64_t lo = 1ull << 61, hi = ~0ull;   /* largest Q with Q den <= ns */
+  while (lo < hi) {
+    const uint64_t mid = lo + ((hi - lo) >> 1) + ((hi - lo) & 1);
+    bn_mul_u64(&t, den, mid);
+    if (bn_cmp(&t, &ns) <= 0) lo = mid; else hi = mid - 1;
+  }
+  bn_mul_u64(&t, den, lo);
+  const int exact = bn_cmp(&t, &ns) == 0;
+  int bl = 64;
+  while (!(lo >> (bl - 1))) --bl;
+  const int sh = bl - 53;
+  uint64_t M = lo >> sh;
+  const uint64_t rem = lo & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+  if (rem > half || (rem == half && (!exact || (M & 1)))) ++M;
+  return ldexp((double)M, sh - s);
+}
+static double th_H[ORC_THIN_NE][ORC_THIN_L], th_P[ORC_THIN_NE][ORC_THIN_L];
+static uint64_t th_HT[ORC_THIN_NE][ORC_THIN_L], th_PT[ORC_THIN_NE][ORC_THIN_L];
+__attribute__((constructor)) static void th_tables(void) {
+  for (int e = ORC_THIN_E_MIN; e <= ORC_THIN_E_MAX; ++e) {
+    bn_t A, t, den, num, n2;
+    bn_set(&A, 1);   /* (2^e - 1)^m */
+    for (int m = 1; m <= ORC_THIN_L; ++m) {
+      t = A;
+      bn_shl(&A, e);
+      bn_sub(&A, &t);
+      bn_set(&den, 1);
+      bn_shl(&den, e * m);
+      num = den;
+      bn_sub(&num, &A);   /* 2^(em) H = 2^(em) - (2^e - 1)^m */
+      bn_set(&n2, 1);
+      bn_shl(&n2, e * (m - 1));   /* P = q / H = 2^(e(m-1)) / (2^(em) H) */
+      const int k = e - ORC_THIN_E_MIN;
+      th_H[k][m - 1] = bn_ratio(&num, &den);
+      th_P[k][m - 1] = bn_ratio(&n2, &num);
+      th_HT[k][m - 1] = (uint64_t)ceil(ldexp(th_H[k][m - 1], 53));
+      th_PT[k][m - 1] = (uint64_t)ceil(ldexp(th_P[k][m - 1], 53));
+    }
+  }
+}
 /* ---- diagnostics (evaluation.py) ------------------------------------------
    Per-cell sums over SIPs in ascending ID order, as the reference's loops
    over id_list[mask] (id_list = 0 .. N-1).  A removed SIP has cells[1] = -1,
@@ -401,20 +642,25 @@ ORC_EXPORT void orc_compute_moment_R_grid(int64_t n, const double* R_p, const do
   for (int64_t c = 0; c < Nx * Nz; ++c) out[c] = out[c] / V0;
 }
 
-/* the segment bound of lacmopy_gb300/csrc/lacmo_thin.h for SIP a against the
-   block of slots [lo, hi) of the FP32 copies (certification tests) */
+/* the segment bound of the thinned draws for SIP a against the block of
+   slots [lo, hi) of the FP32 copies (certification tests) */
 ORC_EXPORT float orc_segment_bound(const float* x, const float* R, const float* u, const float* w,
                                    int64_t a, int64_t lo, int64_t hi, float er, float dtdv_f) {
-  lt_block_t st;
-  lt_block_stats(x, R, u, w, lo, hi, &st);
-  return lt_segment_bound(x[a], R[a], u[a], w[a], &st, er, dtdv_f);
+  th_block_t st;
+  th_block_stats(x, R, u, w, lo, hi, &st);
+  return th_bound(x[a], R[a], u[a], w[a], &st, er, dtdv_f);
 }
-/* the FP32 cube root of lacmo_thin.h (accuracy tests) */
+/* the FP32 cube root of the thinned draws (accuracy tests) */
 ORC_EXPORT void orc_lt_cbrtf(const float* x, int64_t n, float* out) {
-  for (int64_t k = 0; k < n; ++k) out[k] = lt_cbrtf(x[k]);
+  for (int64_t k = 0; k < n; ++k) out[k] = th_cbrtf(x[k]);
+}
+/* the thinned draws' probability tables and thresholds [126][32] each */
+ORC_EXPORT void orc_thin_tables(double* H, double* P, uint64_t* HT, uint64_t* PT) {
+  memcpy(H, th_H, sizeof th_H); memcpy(P, th_P, sizeof th_P);
+  memcpy(HT, th_HT, sizeof th_HT); memcpy(PT, th_PT, sizeof th_PT);
 }
 /* the raw Philox4x32-10 block, for known-answer tests */
-ORC_EXPORT void orc_philox_block(uint64_t key, uint64_t c0, uint64_t c1, uint32_t* out) {
+static void philox_block(uint64_t key, uint64_t c0, uint64_t c1, uint32_t* out) {
   uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
   uint32_t x0 = (uint32_t)c0, x1 = (uint32_t)(c0 >> 32), x2 = (uint32_t)c1, x3 = (uint32_t)(c1 >> 32);
   for (int r = 0; r < 10; ++r) {
@@ -425,6 +671,9 @@ ORC_EXPORT void orc_philox_block(uint64_t key, uint64_t c0, uint64_t c1, uint32_
     k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
   }
   out[0] = x0; out[1] = x1; out[2] = x2; out[3] = x3;
+}
+ORC_EXPORT void orc_philox_block(uint64_t key, uint64_t c0, uint64_t c1, uint32_t* out) {
+  philox_block(key, c0, c1, out);
 }
 ORC_EXPORT void orc_philox_uniform(uint64_t key, const uint64_t* c0, const uint64_t* c1, int64_t n,
                                    double* out) {
@@ -685,9 +934,8 @@ static void process_pair_2d(int64_t i, int64_t j, double r, double* xis, double*
   }
 }
 
-/* The thinned Philox draws of lacmopy_gb300/csrc/lacmo_thin.h for one cell:
-   the sequential definition the GPU kernel parallelises (segments of row i
-   over blocks of LACMO_THIN_L slots).  FP32 copies follow the GPU: xi, u, w
+/* The thinned Philox draws for one cell: the sequential definition the GPU
+   kernel parallelises (segments of row i over blocks of ORC_THIN_L slots).  FP32 copies follow the GPU: xi, u, w
    rounded from the doubles; R from the FP32 mass and density at the cell
    temperature Tc; refreshed from the exact values after each change.  erow[k]
    is the largest FP32 efficiency of row k of the table. */
@@ -716,14 +964,14 @@ static void collide_cell_2d_thin(double* xis, double* m_w, double* m_s, double* 
                                (float)LC_PAR_SOL_DENS_NACL_3 * wsf * wsf +
                                (float)LC_PAR_SOL_DENS_NACL_4 * wsf * Tf +
                                (float)LC_PAR_SOL_DENS_NACL_5 * Tf * Tf;
-    Rf[q] = lt_cbrtf(c43 * mpf / rh);
+    Rf[q] = th_cbrtf(c43 * mpf / rh);
     xf[q] = (float)xis[q];
     uf[q] = (float)v0[q];
     wf[q] = (float)v1[q];
   }
   const float dtdv_f = (float)dt_over_dV;
   const float Ec_f = (float)E_const;
-  const int64_t L = LACMO_THIN_L;
+  const int64_t L = ORC_THIN_L;
   const int64_t B = (n + L - 1) / L;
   for (int64_t i = 0; i + 1 < n; ++i) {
     for (int64_t b = (i + 1) / L; b < B; ++b) {
@@ -732,11 +980,11 @@ static void collide_cell_2d_thin(double* xis, double* m_w, double* m_s, double* 
       const uint64_t chunk = (uint64_t)(i * n - i * (i + 1) / 2 + (j - i - 1));   /* rank of (i, j) */
       uint32_t sub = 0;
       while (j < bhi) {
-        lt_block_t st;
-        lt_block_stats(xf, Rf, uf, wf, blo, bhi, &st);
+        th_block_t st;
+        th_block_stats(xf, Rf, uf, wf, blo, bhi, &st);
         const float er = E ? erow[kbuf[i]] : Ec_f;
-        const float Q = lt_segment_bound(xf[i], Rf[i], uf[i], wf[i], &st, er, dtdv_f);
-        if (!(Q >= 0.0f && Q < LACMO_THIN_TAU)) {
+        const float Q = th_bound(xf[i], Rf[i], uf[i], wf[i], &st, er, dtdv_f);
+        if (!(Q >= 0.0f && Q < ORC_THIN_TAU)) {
           /* per-pair draws for the rest of the segment */
           for (; j < bhi; ++j) {
             const int64_t rk = i * n - i * (i + 1) / 2 + (j - i - 1);
@@ -746,15 +994,15 @@ static void collide_cell_2d_thin(double* xis, double* m_w, double* m_s, double* 
           break;
         }
         const int m = (int)(bhi - j);
-        const int e = lt_exponent(Q);
-        if (lt_bits53(seed, chunk, sub, 0u, pc1) >= LACMO_THIN_HT[e - LACMO_THIN_E_MIN][m - 1])
+        const int e = th_exponent(Q);
+        if (th_u53(seed, chunk, sub, 0u, pc1) >= th_HT[e - ORC_THIN_E_MIN][m - 1])
           break;   /* no draw of the part falls below q */
         uint32_t jd = 1;
         int g = 0;
         for (; g < m - 1; ++g)
-          if (lt_bits53(seed, chunk, sub, jd++, pc1) < LACMO_THIN_PT[e - LACMO_THIN_E_MIN][m - g - 1])
+          if (th_u53(seed, chunk, sub, jd++, pc1) < th_PT[e - ORC_THIN_E_MIN][m - g - 1])
             break;
-        const double r = ldexp((double)lt_bits53(seed, chunk, sub, jd, pc1) *
+        const double r = ldexp((double)th_u53(seed, chunk, sub, jd, pc1) *
                                    (1.0 / 9007199254740992.0), -e);
         process_pair_2d(i, j + g, r, xis, m_w, m_s, radii, v0, v1, rho, dt_over_dV, E, E_const, nb,
                         lo, bl, no_cols, kbuf, xf, Rf);
@@ -795,7 +1043,7 @@ static int collision_all_cells(double* xis, double* m_w, double* m_s,
     erow = (float*)malloc(sizeof(float) * (nb > 0 ? nb : 1));
     for (int64_t k = 0; k < nb; ++k) {
       float mx = (float)E[k * nb];
-      for (int64_t q = 1; q < nb; ++q) mx = lt_max(mx, (float)E[k * nb + q]);
+      for (int64_t q = 1; q < nb; ++q) mx = th_max(mx, (float)E[k * nb + q]);
       erow[k] = mx;
     }
   }
@@ -1300,11 +1548,11 @@ ORC_EXPORT int orc_get_threads(void) {
 }
 
 #ifdef ORC_CRMATH
-/* host builds of the correctly-rounded routines, for their own tests */
+/* the correctly rounded routines, for their own tests */
 ORC_EXPORT void orc_cr_pow_array(const double* x, const double* y, int64_t n, double* out, int* hard) {
-  for (int64_t i = 0; i < n; ++i) out[i] = lacmo_cr_pow_checked(x[i], y[i], &hard[i]);
+  for (int64_t i = 0; i < n; ++i) out[i] = orc_cr_pow(x[i], y[i], &hard[i]);
 }
 ORC_EXPORT void orc_cr_log_array(const double* x, int64_t n, double* out, int* hard) {
-  for (int64_t i = 0; i < n; ++i) out[i] = lacmo_cr_log_checked(x[i], &hard[i]);
+  for (int64_t i = 0; i < n; ++i) out[i] = orc_cr_log(x[i], &hard[i]);
 }
 #endif

@@ -1,7 +1,8 @@
-"""The thinned Philox draws (lacmopy_gb300/csrc/lacmo_thin.h) sample the same
-all-or-nothing process as one uniform per pair: over independent seeds the
-collision counts, the number of multiple collections, the conserved water
-mass and the multiplicity sum agree within sampling error (oracle, CPU)."""
+"""The thinned Philox draws (lacmopy_gb300/csrc/lacmo_thin.h, restated in the
+oracle) sample the same all-or-nothing process as one uniform per pair: over
+independent seeds the collision counts, the number of multiple collections,
+the conserved water mass and the multiplicity sum agree within sampling error
+(oracle, CPU); the oracle's own probability tables equal the kernels'."""
 import numpy as np
 import pytest
 
@@ -60,3 +61,22 @@ def test_rate_tables_are_probabilities():
     H, P = np.array(H), np.array(P)
     assert np.all(np.diff(H, axis=1) > 0) and np.all(np.diff(H, axis=0) < 0)
     assert np.all((P > 0) & (P <= 1)) and np.all(P[:, 0] == 1.0)
+
+
+def test_oracle_tables_equal_the_kernel_tables(oracle_nb):
+    """The oracle computes its probability tables and thresholds itself (big
+    integers, rounded once); they equal the kernels' generated header."""
+    import ctypes
+    import re
+    H, P = (np.zeros((126, 32)) for _ in range(2))
+    HT, PT = (np.zeros((126, 32), dtype=np.uint64) for _ in range(2))
+    lib = oracle_nb.lib
+    lib.orc_thin_tables.argtypes = [ctypes.c_void_p] * 4
+    lib.orc_thin_tables(H.ctypes.data, P.ctypes.data, HT.ctypes.data, PT.ctypes.data)
+    from lacmopy_gb300.csrc_gen import thin_tables
+    Hk, Pk = thin_tables()
+    assert np.array_equal(H, np.array(Hk)) and np.array_equal(P, np.array(Pk))
+    txt = open(__import__("os").path.join(__import__("os").path.dirname(__file__), "..",
+                                          "lacmopy_gb300", "csrc", "lacmo_thin_tables.h")).read()
+    ht = np.array([int(v) for v in re.findall(r"(\d+)ull", txt)], dtype=np.uint64)
+    assert np.array_equal(np.concatenate([HT.ravel(), PT.ravel()]), ht)
