@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--developed-steps", type=int, default=600,
                     help="untimed steps that advance the headline ensemble to a developed "
                          "(raining) state before the developed-regime timing; 0 skips it")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the default launch shapes (no autotuning)")
     ap.add_argument("--cpu-1thread-steps", type=int, default=1,
                     help="steps of the single-thread CPU sample (0 skips it)")
     return ap.parse_args()
@@ -364,7 +366,12 @@ def run_ours(args):
 
     # ---- headline: the batched mixed-precision ensemble ----
     seeds = rank_seeds(rank, args.members)[0]
-    batch = BatchState(members, seeds, precision="mixed", draws=args.draws)   # copies to the GPU
+    t_tune = time.perf_counter()
+    batch = BatchState(members, seeds, precision="mixed", draws=args.draws,   # copies to the GPU
+                       tune=not args.no_tune)
+    tune_s = time.perf_counter() - t_tune
+    from lacmopy_gb300 import autotune
+    shapes = autotune.current()
     n_total = batch.n_total
     ms, ups, launches, clocks = timed(batch, True)
     value = ups / (ms / 1000.0)
@@ -516,7 +523,11 @@ def run_ours(args):
                 "dtype": "mixed f32/f64 (f32 Newton, drag and pair screen; f64 state, "
                          "per-cell sums, near-critical Newton and collision updates)",
                 "data": "synthetic", "config": workload_config(args),
-                "impl_details": dict(impl_details(args), n_sips=int(n_total)),
+                "impl_details": dict(impl_details(args), n_sips=int(n_total),
+                                     launch_shapes=shapes,
+                                     autotune=("off" if args.no_tune else
+                                               f"timed on a throw-away batch of the members "
+                                               f"({tune_s:.1f} s incl. the batch upload)")),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": int(launches), "modes": modes,
                 "hbm_frac_whole_step": value * BYTES_PER_SIP_UPDATE / 1e9 / peak}

@@ -148,6 +148,21 @@ int lacmo_set_collision_step(void* ws, int64_t n, int64_t nx, int64_t nz, int64_
 int lacmo_read_flags(const void* ws, int64_t n, int64_t nx, int64_t nz, uint32_t* flags,
                      void* stream);
 
+/* ---- launch shapes (autotuning) ----------------------------------------------
+ * Knobs of the launch shapes of the hot kernels, process-wide: each knob takes
+ * one of a fixed list of options (lacmo_tune_options writes them, the default
+ * first, and returns their count); kernels read the knobs when they are
+ * launched, so a CUDA graph keeps the shapes it was captured with.  The
+ * results do not depend on the knobs (FP64 bit for bit), only the speed.
+ * The reference runs on the CPU and has no counterpart; its per-seed process
+ * launch (run_lacmo.sh) is what a batch replaces. */
+#define LACMO_TUNE_PARTICLE_BLOCKS 0   /* mixed particle kernel, blocks per SM */
+#define LACMO_TUNE_COLLISION_BLOCKS 1  /* collision kernels, blocks per SM     */
+#define LACMO_TUNE_ORDER_CTAS 2        /* cell ordering, blocks per SM         */
+int lacmo_tune_options(int knob, int* values, int max_values);
+int lacmo_tune_set(int knob, int value);   /* LACMO_ERR_ARG for a value not listed */
+int lacmo_tune_get(int knob);
+
 /* ---- layout conversion ------------------------------------------------------ */
 /* cells[2][n] int64 + active_ids[n] (uint8) -> cell[n] (file_handling.py
  * state layout; integration.py:509-550 cell convention). */
@@ -287,6 +302,55 @@ int lacmo_compute_moment_R_grid(int64_t order, const double* R_p, const double* 
                                 const int32_t* cell, int64_t n, int64_t nx, int64_t nz,
                                 double* out, void* ws, size_t ws_bytes, void* stream);
 
+/* Replaces microphysics.py:208-266 compute_R_p_w_s_rho_p (AS or NaCl): radius
+ * (um), solute mass fraction and density (kg/m^3) per SIP; w_s and rho_p may
+ * be null. */
+int lacmo_compute_R_p_w_s_rho_p(int solute, int64_t n, const double* m_w, const double* m_s,
+                                const double* T_p, double* R_p, double* w_s, double* rho_p,
+                                void* stream);
+/* Replaces microphysics.py:83-100 compute_radius_from_mass for one density
+ * (e.g. dry radii from solute masses). */
+int lacmo_radius_from_mass(int64_t n, const double* m, double rho, double* R, void* stream);
+/* Weighted histogram with numpy.histogram's bins (evaluation.py:1172-1390
+ * size spectra): edges [nbins + 1] ascending, bins [e_b, e_b+1) with the last
+ * one closed; w null counts 1 per value; out [nbins] is overwritten. */
+int lacmo_histogram_weighted(const double* x, const double* w, int64_t n, const double* edges,
+                             int64_t nbins, double* out, void* stream);
+
+/* ---- initialisation (init.py:439-1236) ------------------------------------------
+ * SinSIP mass ensembles (generation_SIP_ensemble.py:147-384) of n_seg
+ * (level, cell, mode) segments at once: segment s of mode seg_mode[s] takes
+ * its bins' uniforms from rnd + rnd_off[s] (l_max draws, then l_max more
+ * with the weak threshold, weak != 0), mode_par = [mu_m_log][sigma_m_log]
+ * [bin factor][m_low] (n_modes each) then sqrt(2 pi); the kept bins go to the
+ * front of masses / weights [n_seg][lmax_cap], their number to count[n_seg]. */
+int lacmo_sinsip_generate(const double* rnd, const int64_t* rnd_off, const int32_t* seg_mode,
+                          int64_t n_seg, int n_modes, const double* mode_par,
+                          const int32_t* l_max, double eta, int weak, int64_t lmax_cap,
+                          double* masses, double* weights, int32_t* count, void* stream);
+/* The kept bins of every segment concatenated from off[s] (exclusive sums of
+ * count), multiplicities = weights * seg_scale[s] (real particles per cell). */
+int lacmo_sinsip_gather(const double* masses, const double* weights, const int32_t* count,
+                        const int64_t* off, int64_t n_seg, int64_t lmax_cap,
+                        const double* seg_scale, double* m_out, double* xi_out, void* stream);
+/* Replaces microphysics.py:686-785 compute_initial_mass_fraction_solute_m_s
+ * (AS or NaCl, scipy fminbound / brentq per SIP): the solute mass fraction in
+ * equilibrium with S_amb at T_amb, the activation maximum where S_amb is
+ * above it, w_s_max where S_amb is below the efflorescence saturation. */
+int lacmo_init_mass_fraction(int solute, int64_t n, const double* m_s, double S_amb,
+                             double T_amb, double volume_to_radius, double w_s_max,
+                             double solubility, double* w_s, void* stream);
+/* One saturation-adjustment iteration of a level (init.py:887-960): the
+ * implicit Newton condensation step dt (no_iter evaluations) of every SIP at
+ * the level's T and p and its cell's capped S and e_s; the SIPs of cell c are
+ * off[c] .. off[c + 1] - 1; m_w is updated; dml_cell / mwxi_cell [cells]
+ * receive the cell sums of dm * xi and m_w * xi (1e-18 kg). */
+int lacmo_saturation_adjust_level(int solute, int64_t cells, const int64_t* off, double* m_w,
+                                  const double* m_s, const double* xi, const double* S_cap,
+                                  const double* e_s, double T, double p, double L_v, double K,
+                                  double D_v, double dt, int no_iter, double* dml_cell,
+                                  double* mwxi_cell, void* stream);
+
 /* ---- collisions ------------------------------------------------------------------ */
 /* All cells of the 2-D grid: replaces collision/all_or_nothing.py:754
  * collision_step_Ecol_grid_R_all_cells_2D_multicomp_np (and :498 / :637 per
@@ -391,32 +455,64 @@ int lacmo_radius_and_bin(const double* m, const double* rho, int64_t n, double R
                          int64_t* bin, void* stream);
 
 /* ---- adjoint of the condensation sub-steps (k_adjoint.cu) ----
- * The differentiated model: SIPs keep their cells and multiplicities (motion,
- * advection and collisions are recorded events held fixed); each sub-step
- * solves the implicit Euler condensation step of integration.py:728-836 to
- * convergence for every SIP with cell >= 0, then updates Theta and r_v of the
- * cells as integration.py:402-438 does, the ambient terms following from Theta
- * and r_v.  Hygroscopicity kappa scales the ammonium-sulfate water activity,
- * a_w = 1 + (kappa / 0.6)(a_w_AS(w_s) - 1); kappa = 0.6 is the reference.
- * Arrays are device pointers: m_w, m_s, xi, cell [n]; Theta, r_v, rho_d,
- * mass_dry_inv [C]; dTh, drv [C] optional per-sub-step increments (null =
- * 0); dml [C] scratch.  lacmo_adj_forward advances n_sub sub-steps in place
- * and, when tape_m ([n_sub + 1][n]) and tape_c ([n_sub][2][C]) are given,
- * records the states for lacmo_adj_backward.  lacmo_adj_backward turns the
- * adjoints of the final state (lam_m [n], lam_Th, lam_rv [C]) into those of
- * the initial state, accumulating d/d m_s into grad_ms [n] and d/d kappa into
- * grad_kappa [1]; lam_dml [C] is scratch. */
+ * The differentiated model: the SIPs' cells per sub-step and their
+ * multiplicities are recorded events (SIP motion, ground removal and cell
+ * re-indexing of integration.py:509-719 enter only through the piecewise
+ * constant cell index, whose derivative is zero); each sub-step runs the
+ * condensation step of integration.py:840-940 for every SIP with cell >= 0,
+ * then updates Theta and r_v of the cells as integration.py:402-438 does, the
+ * ambient terms following from Theta and r_v.  Hygroscopicity kappa scales the
+ * ammonium-sulfate water activity, a_w = 1 + (kappa / 0.6)(a_w_AS(w_s) - 1);
+ * kappa = 0.6 is the reference.
+ * Arrays are device pointers: m_w, m_s, xi [n]; cell [n_sub][n] with row
+ * stride cell_stride (0: the same cells every sub-step); Theta, r_v, rho_d,
+ * mass_dry_inv [C]; dTh, drv [C] the increments every sub-step adds (null =
+ * 0); dml [C] scratch.  no_iter > 0: the condensation step is the time step's
+ * own map of no_iter damped Newton evaluations (integration.py:786-836),
+ * differentiated exactly; no_iter = 0: the implicit Euler step solved to
+ * convergence, differentiated through the implicit-function theorem.
+ * lacmo_adj_forward advances n_sub sub-steps in place and, when tape_m
+ * ([n_sub + 1][n]) and tape_c ([n_sub][2][C]) are given, records the states
+ * for lacmo_adj_backward.  lacmo_adj_backward turns the adjoints of the final
+ * state (lam_m [n], lam_Th, lam_rv [C]) into those of the initial state,
+ * accumulating d/d m_s into grad_ms [n], d/d kappa into grad_kappa [1] and,
+ * when lam_inc ([2][C]) is given, the adjoints of (dTh, drv) into lam_inc;
+ * lam_dml [C] is scratch. */
 int lacmo_adj_forward(int64_t n, int64_t C, double* m_w, const double* m_s, const double* xi,
-                      const int32_t* cell, double* Th, double* r_v, const double* rho_d,
-                      const double* mass_dry_inv, const double* dTh, const double* drv,
-                      double* dml, double dt_sub, double kappa, double p_ref, double V, int n_sub,
-                      double* tape_m, double* tape_c, void* stream);
+                      const int32_t* cell, int64_t cell_stride, double* Th, double* r_v,
+                      const double* rho_d, const double* mass_dry_inv, const double* dTh,
+                      const double* drv, double* dml, double dt_sub, double kappa, double p_ref,
+                      double V, int n_sub, int no_iter, double* tape_m, double* tape_c,
+                      void* stream);
 int lacmo_adj_backward(int64_t n, int64_t C, const double* m_s, const double* xi,
-                       const int32_t* cell, const double* rho_d, const double* mass_dry_inv,
-                       const double* dTh, const double* drv, double* dml, double dt_sub,
-                       double kappa, double p_ref, double V, int n_sub, const double* tape_m,
-                       const double* tape_c, double* lam_m, double* lam_Th, double* lam_rv,
-                       double* lam_dml, double* grad_ms, double* grad_kappa, void* stream);
+                       const int32_t* cell, int64_t cell_stride, const double* rho_d,
+                       const double* mass_dry_inv, const double* dTh, const double* drv,
+                       double* dml, double dt_sub, double kappa, double p_ref, double V,
+                       int n_sub, int no_iter, const double* tape_m, const double* tape_c,
+                       double* lam_m, double* lam_Th, double* lam_rv, double* lam_dml,
+                       double* grad_ms, double* grad_kappa, double* lam_inc, void* stream);
+/* The increments a half advection step adds every sub-step (integration.py:
+ * 1483-1508 for second = 0; 1536-1561 for second = 1, where inc_Th, inc_rv
+ * hold the first half's increments on entry): the upwind divergence of the
+ * Hundsdorfer et al. (1995) scheme of Theta and r_v with the mass flux
+ * ([2][nx+1][nz+1], x periodic, z solid) times rho_dry_inv, and, when t_relax
+ * [nz] is given, the relaxation to the profiles prof_Th, prof_rv [nz].
+ * lacmo_adj_increments_vjp adds factor * J^T lam_inc ([2][C]) to lam_Th,
+ * lam_rv, J the Jacobian of the first-half increments at (Theta, r_v), and
+ * factor * lam_inc . (advective increments) / flux_scale to grad_s [1], the
+ * derivative by a common factor of the mass flux when flux is flux_scale
+ * times the unscaled one. */
+int lacmo_adj_increments(const double* Th, const double* r_v, const double* rho_dry_inv,
+                         const double* flux, int64_t nx, int64_t nz, double dx, double dz,
+                         double dt_sub, const double* prof_Th, const double* prof_rv,
+                         const double* t_relax, int second, double* inc_Th, double* inc_rv,
+                         void* stream);
+int lacmo_adj_increments_vjp(const double* Th, const double* r_v, const double* rho_dry_inv,
+                             const double* flux, int64_t nx, int64_t nz, double dx, double dz,
+                             double dt_sub, const double* prof_Th, const double* prof_rv,
+                             const double* t_relax, double factor, double flux_scale,
+                             const double* lam_inc, double* lam_Th, double* lam_rv,
+                             double* grad_s, void* stream);
 
 #ifdef __cplusplus
 }

@@ -52,6 +52,9 @@ class Params(ctypes.Structure):
                 ("precision", i32), ("thin_draws", i32)]
 
 
+TUNE_PARTICLE_BLOCKS = 0
+TUNE_COLLISION_BLOCKS = 1
+TUNE_ORDER_CTAS = 2
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
@@ -65,6 +68,9 @@ P = ctypes.POINTER
 PROTOTYPES = {
     "lacmo_abi_version": (ctypes.c_int, []),
     "lacmo_kernel_launches": (ctypes.c_uint64, []),
+    "lacmo_tune_options": (ctypes.c_int, [ctypes.c_int, P(ctypes.c_int), ctypes.c_int]),
+    "lacmo_tune_set": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "lacmo_tune_get": (ctypes.c_int, [ctypes.c_int]),
     "lacmo_particles_only": (ctypes.c_int, [P(Sips), P(Grid), P(Params), dbl, dbl, vp, sz, vp]),
     "lacmo_bin": (ctypes.c_int, [P(Sips), P(Grid), vp, sz, vp]),
     "lacmo_error_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -109,6 +115,18 @@ PROTOTYPES = {
                                              vp, sz, vp]),
     "lacmo_compute_moment_R_grid": (ctypes.c_int, [i64, vp, vp, dbl, vp, i64, i64, i64, vp, vp,
                                                    sz, vp]),
+    "lacmo_compute_R_p_w_s_rho_p": (ctypes.c_int, [ctypes.c_int, i64, vp, vp, vp, vp, vp, vp,
+                                                   vp]),
+    "lacmo_radius_from_mass": (ctypes.c_int, [i64, vp, dbl, vp, vp]),
+    "lacmo_histogram_weighted": (ctypes.c_int, [vp, vp, i64, vp, i64, vp, vp]),
+    "lacmo_sinsip_generate": (ctypes.c_int, [vp, vp, vp, i64, ctypes.c_int, vp, vp, dbl,
+                                             ctypes.c_int, i64, vp, vp, vp, vp]),
+    "lacmo_sinsip_gather": (ctypes.c_int, [vp, vp, vp, vp, i64, i64, vp, vp, vp, vp]),
+    "lacmo_init_mass_fraction": (ctypes.c_int, [ctypes.c_int, i64, vp, dbl, dbl, dbl, dbl, dbl,
+                                                vp, vp]),
+    "lacmo_saturation_adjust_level": (ctypes.c_int, [ctypes.c_int, i64, vp, vp, vp, vp, vp, vp,
+                                                     dbl, dbl, dbl, dbl, dbl, dbl, ctypes.c_int,
+                                                     vp, vp, vp]),
     "lacmo_collision_step_cells": (ctypes.c_int, [P(Sips), P(Grid), P(Params), P(Draws), vp, sz,
                                                   vp]),
     "lacmo_collision_pair_count": (ctypes.c_int, [vp, i64, i64, i64, P(i64), vp]),
@@ -125,10 +143,14 @@ PROTOTYPES = {
     "lacmo_newton_full": (ctypes.c_int, [ctypes.c_int, i64, dbl, ctypes.c_int] + [vp] * 16 + [vp]),
     "lacmo_interpolate_velocity": (ctypes.c_int, [vp, vp, vp, i64, i64, i64, vp, vp]),
     "lacmo_radius_and_bin": (ctypes.c_int, [vp, vp, i64, dbl, dbl, i64, vp, vp, vp]),
-    "lacmo_adj_forward": (ctypes.c_int, [i64, i64] + [vp] * 11 + [dbl, dbl, dbl, dbl,
-                                                                   ctypes.c_int, vp, vp, vp]),
-    "lacmo_adj_backward": (ctypes.c_int, [i64, i64] + [vp] * 8 + [dbl, dbl, dbl, dbl,
-                                                                  ctypes.c_int] + [vp] * 9),
+    "lacmo_adj_forward": (ctypes.c_int, [i64, i64, vp, vp, vp, vp, i64] + [vp] * 7 + [
+        dbl, dbl, dbl, dbl, ctypes.c_int, ctypes.c_int, vp, vp, vp]),
+    "lacmo_adj_backward": (ctypes.c_int, [i64, i64, vp, vp, vp, i64] + [vp] * 5 + [
+        dbl, dbl, dbl, dbl, ctypes.c_int, ctypes.c_int] + [vp] * 10),
+    "lacmo_adj_increments": (ctypes.c_int, [vp] * 4 + [i64, i64, dbl, dbl, dbl] + [vp] * 3 + [
+        ctypes.c_int, vp, vp, vp]),
+    "lacmo_adj_increments_vjp": (ctypes.c_int, [vp] * 4 + [i64, i64, dbl, dbl, dbl] + [vp] * 3 + [
+        dbl, dbl] + [vp] * 5),
 }
 
 _lib = None

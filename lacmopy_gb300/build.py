@@ -26,6 +26,7 @@ UNITS = {
     "k_static.cu": [],
     "k_adjoint.cu": [],
     "k_diag.cu": ["-fmad=false"],
+    "k_init.cu": ["-fmad=false"],
 }
 
 

@@ -13,6 +13,16 @@ namespace lacmo {
 static std::atomic<uint64_t> g_launches{0};
 void note_launches(int k) { g_launches.fetch_add((uint64_t)k, std::memory_order_relaxed); }
 
+// Launch-shape knobs (process-wide): the options each knob may take, the
+// first listed is the default.
+static const int k_tune_options[TUNE_KNOBS][4] = {
+    {6, 5, 8, 0},    // mixed particle kernel: resident blocks per SM (register budget)
+    {3, 2, 4, 0},    // collision kernels: resident blocks per SM
+    {16, 8, 4, 0},   // cell ordering: blocks per SM
+};
+static std::atomic<int> g_tune[TUNE_KNOBS] = {{6}, {3}, {16}};
+int tune_value(int knob) { return g_tune[knob].load(std::memory_order_relaxed); }
+
 static inline size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct WsPlan {
@@ -239,6 +249,31 @@ using namespace lacmo;
 extern "C" {
 
 int lacmo_abi_version(void) { return LACMO_ABI_VERSION; }
+
+int lacmo_tune_options(int knob, int* values, int max_values) {
+  if (knob < 0 || knob >= TUNE_KNOBS) return LACMO_ERR_ARG;
+  int n = 0;
+  while (n < 4 && k_tune_options[knob][n] > 0) {
+    if (values && n < max_values) values[n] = k_tune_options[knob][n];
+    ++n;
+  }
+  return n;
+}
+
+int lacmo_tune_set(int knob, int value) {
+  if (knob < 0 || knob >= TUNE_KNOBS) return LACMO_ERR_ARG;
+  for (int q = 0; q < 4 && k_tune_options[knob][q] > 0; ++q)
+    if (k_tune_options[knob][q] == value) {
+      g_tune[knob].store(value, std::memory_order_relaxed);
+      return LACMO_OK;
+    }
+  return LACMO_ERR_ARG;
+}
+
+int lacmo_tune_get(int knob) {
+  if (knob < 0 || knob >= TUNE_KNOBS) return LACMO_ERR_ARG;
+  return tune_value(knob);
+}
 
 uint64_t lacmo_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 

@@ -1,26 +1,31 @@
 // Hand-written adjoint of the condensation sub-steps with their cell heat and
-// vapour feedback (integration.py:840-940 with the Newton of :728-836 and the
-// grid update of :402-484), for gradients of liquid water with respect to
-// per-SIP solute mass and hygroscopicity.
+// vapour feedback and the grid advection of Theta and r_v (integration.py:
+// 840-940 with the Newton of :728-836, the grid update of :402-484 and the
+// advective increments of :80-287, 1483-1508, 1536-1561), for gradients of
+// liquid water and surface rain with respect to per-SIP solute mass,
+// hygroscopicity and the strength of the prescribed mass flux.
 //
-// Differentiated model ("condensation model"): SIPs keep their cells and
-// multiplicities (positions, advection and collisions are recorded events held
-// fixed); every sub-step of length dt_sub solves the implicit Euler step
-// m - m_w - dt_sub gamma(m) = 0 of each SIP to convergence (the damped Newton
-// of the reference, iterated until the step falls below 1e-15 relative),
-// floored at the efflorescence mass, and then updates Theta and r_v of each
-// cell from the condensed mass, with all ambient terms (T, p, S, e_s, K, D_v,
-// L_v, sigma_w, rho_w) functions of the cell's Theta and r_v.
+// Differentiated model: the SIPs' cells per sub-step and their multiplicities
+// are recorded events (positions, ground removal and collisions are held
+// fixed; SIP motion reaches condensation only through the piecewise constant
+// cell index); every sub-step runs the condensation step of each SIP, either
+// the time step's own map of no_iter damped Newton evaluations (the product's
+// map, differentiated exactly with forward-mode duals through every
+// evaluation, second derivatives included) or the implicit Euler step solved
+// to convergence (implicit-function theorem), and then updates Theta and r_v
+// of each cell from the condensed mass and the half step's advective (+
+// relaxation) increments, with all ambient terms (T, p, S, e_s, K, D_v, L_v,
+// sigma_w, rho_w) functions of the cell's Theta and r_v.  The reference sets a
+// SIP's temperature to its cell's at the start of every sub-step
+// (integration.py:1059-1060), so T_p is the ambient T here.
 // Hygroscopicity: the ammonium-sulfate water activity a_w(w_s) (material_
 // properties.py:429-436) becomes 1 + (kappa / 0.6) (a_w(w_s) - 1), so kappa =
 // 0.6 reproduces the reference.
 //
-// Reverse sweep per sub-step: the implicit-function theorem through the root,
-// dm/dx = dt (dgamma/dx) / (1 - dt dgamma/dm) for x = m_w, m_s, kappa, Theta,
-// r_v (dm/dm_w = 1 / (1 - dt dgamma/dm)), or dm/dm_s = 1/0.78 - 1 on the
-// floor; the local partials come from forward-mode dual numbers through the
-// same formulas; the cell update's Jacobian likewise.  Sums over a cell's
-// SIPs use atomics (FP64).
+// Reverse sweep per sub-step: the local partials come from forward-mode dual
+// numbers through the same formulas; the cell update's Jacobian likewise; the
+// increments' Jacobian from duals through the limited face fluxes.  Sums over
+// a cell's SIPs use atomics (FP64).
 #include <cuda_runtime.h>
 
 #include "lacmo_internal.cuh"
@@ -124,6 +129,15 @@ __device__ __forceinline__ double dcbrt(double a) { return cbrt(a); }
 __device__ __forceinline__ double val(double a) { return a; }
 template <int N>
 __device__ __forceinline__ double val(const Dual<N>& a) { return a.v; }
+// a constant of scalar type S
+template <class S>
+struct Const {
+  static __device__ __forceinline__ S of(double v) { return v; }
+};
+template <int N>
+struct Const<Dual<N>> {
+  static __device__ __forceinline__ Dual<N> of(double v) { return cst<N>(v); }
+};
 
 // ---- cell ambient from Theta and r_v (integration.py:402-484, 359-400) ----
 struct GridConst {
@@ -158,9 +172,9 @@ __device__ __forceinline__ Amb<S> ambient(const S& Th, const S& r_v, double rho_
 
 // ---- mass rate of an ammonium-sulfate SIP (microphysics.py:1359-1469) with
 // the kappa scaling; gamma in fg/s and (for S = double) dgamma/dm_w ----
-template <class S>
-__device__ __forceinline__ S mass_rate(double m, const S& m_s, const S& ks, const Amb<S>& a,
-                                       double* dg_out) {
+template <class S, class M>
+__device__ __forceinline__ S mass_rate(const M& m, const S& m_s, const S& ks, const Amb<S>& a,
+                                       S* dg_out) {
   const S m_p = m + m_s;
   const S w_s = m_s / m_p;
   S pr = LC_PAR_RHO_AS_0 * w_s + LC_PAR_RHO_AS_1;
@@ -194,46 +208,67 @@ __device__ __forceinline__ S mass_rate(double m, const S& m_s, const S& ks, cons
   const S f3 = 1.0 / (l_a * S_eq * a.c1 + l_b * a.c2);
   const S f1f3 = LC_FOUR_PI * R_p * R_p * f3;
   const S f2 = a.Sat - S_eq;
-  if (dg_out) {
-    const double dSeq = val(da_w_dm) * val(kel) +
-                        val(S_eq) * val(eps_k) *
-                            (val(dsigma_dm) / val(sigma_p) - val(drho_dm_over_rho) -
-                             val(dR_dm_over_R));
-    const double dg1 = (dSeq * val(l_a) + val(S_eq) * val(dR_dm)) * val(a.c1) +
-                       val(dR_dm) * val(a.c2);
-    *dg_out = 1.0E-12 * val(f1f3) *
-              (val(f2) * (2.0 * val(dR_dm_over_R) - val(f3) * dg1) - dSeq);
+  if (dg_out) {   // dgamma/dm_w in the arithmetic of S (second derivatives for duals)
+    const S dSeq = da_w_dm * kel + S_eq * eps_k * (dsigma_dm / sigma_p - drho_dm_over_rho -
+                                                   dR_dm_over_R);
+    const S dg1 = (dSeq * l_a + S_eq * dR_dm) * a.c1 + dR_dm * a.c2;
+    *dg_out = 1.0E-12 * f1f3 * (f2 * (2.0 * dR_dm_over_R - f3 * dg1) - dSeq);
   }
   return 1.0E6 * f1f3 * f2;
 }
 
 // the implicit Euler step solved to convergence; returns the new mass and
 // whether it sits on the efflorescence floor
+// (no_iter > 0: exactly no_iter evaluations, the map of integration.py:728-836
+// the time step uses; 0: to convergence)
 __device__ __forceinline__ double solve_step(double m_w, double m_s, double ks,
-                                             const Amb<double>& a, double dt, bool* floored) {
+                                             const Amb<double>& a, double dt, int no_iter,
+                                             bool* floored) {
   const double m_eff = m_s * (LC_W_S_MAX_AS_INV - 1.0);
   double dg;
   double g = mass_rate<double>(m_w, m_s, ks, a, &dg);
   double x = dt * dg;
   double m = m_w + dt * g * ((x < 0.9) ? 1.0 / (1.0 - x) : 10.0);
   if (!(m >= m_eff)) m = m_eff;
-  for (int it = 0; it < 40; ++it) {
+  const int iters = no_iter > 0 ? no_iter - 1 : 40;
+  for (int it = 0; it < iters; ++it) {
     g = mass_rate<double>(m, m_s, ks, a, &dg);
     x = dt * dg;
     double mn = m + (dt * g + m_w - m) * ((x < 0.9) ? 1.0 / (1.0 - x) : 10.0);
     if (!(mn >= m_eff)) mn = m_eff;
     const double step = fabs(mn - m);
     m = mn;
-    if (step <= 1e-15 * fabs(m)) break;
+    if (no_iter == 0 && step <= 1e-15 * fabs(m)) break;
   }
   *floored = !(m > m_eff);
   return m;
 }
 
-// cell update (integration.py:402-438): Theta and r_v after the sub-step
+// the time step's own map (integration.py:786-836): no_iter evaluations of the
+// damped Newton, each floored at the efflorescence mass, in the arithmetic of
+// S (duals: the exact derivative of the map, branches taken as evaluated)
 template <class S>
+__device__ __forceinline__ S newton_map(const S& m_w, const S& m_s, const S& ks, const Amb<S>& a,
+                                        double dt, int no_iter) {
+  const S m_eff = m_s * (LC_W_S_MAX_AS_INV - 1.0);
+  S dg;
+  S g = mass_rate<S>(m_w, m_s, ks, a, &dg);
+  S x = dt * dg;
+  S m = m_w + dt * g * ((val(x) < 0.9) ? 1.0 / (1.0 - x) : Const<S>::of(10.0));
+  if (!(val(m) >= val(m_eff))) m = m_eff;
+  for (int it = 0; it < no_iter - 1; ++it) {
+    g = mass_rate<S>(m, m_s, ks, a, &dg);
+    x = dt * dg;
+    m = m + (dt * g + m_w - m) * ((val(x) < 0.9) ? 1.0 / (1.0 - x) : Const<S>::of(10.0));
+    if (!(val(m) >= val(m_eff))) m = m_eff;
+  }
+  return m;
+}
+
+// cell update (integration.py:402-438): Theta and r_v after the sub-step
+template <class S, class F>
 __device__ __forceinline__ void cell_update(const S& Th, const S& r_v, const S& dml, double rho_d,
-                                            double mdi, double dTh, double drv,
+                                            double mdi, const F& dTh, const F& drv,
                                             const GridConst& g, S* Th_out, S* rv_out) {
   const Amb<S> a = ambient<S>(Th, r_v, rho_d, g);   // L_v before the update
   const S Th1 = Th + dTh;
@@ -248,7 +283,7 @@ struct Args {
   double* m_w;          // [n] in/out
   const double* m_s;    // [n]
   const double* xi;     // [n]
-  const int32_t* cell;  // [n] (negative: not condensing)
+  const int32_t* cell;  // [n] this sub-step's cells (negative: not condensing)
   double* Th;           // [C] in/out
   double* r_v;          // [C] in/out
   const double* rho_d;  // [C]
@@ -258,6 +293,7 @@ struct Args {
   double* dml;          // [C] scratch
   double dt, ks;
   GridConst g;
+  int no_iter;          // 0: implicit step to convergence, else the step's map
 };
 
 __global__ void k_fwd_sips(Args a, double* tape_m) {
@@ -269,7 +305,7 @@ __global__ void k_fwd_sips(Args a, double* tape_m) {
     if (c < 0) continue;
     const Amb<double> am = ambient<double>(a.Th[c], a.r_v[c], a.rho_d[c], a.g);
     bool fl;
-    const double m = solve_step(mw, a.m_s[k], a.ks, am, a.dt, &fl);
+    const double m = solve_step(mw, a.m_s[k], a.ks, am, a.dt, a.no_iter, &fl);
     a.m_w[k] = m;
     atomicAdd(a.dml + c, (m - mw) * a.xi[k]);
   }
@@ -283,8 +319,8 @@ __global__ void k_fwd_cells(Args a, double* tape_c) {
     const double dml = a.dml[c] * 1.0E-18;
     a.dml[c] = 0.0;
     double Th2, rv2;
-    cell_update<double>(Th, rv, dml, a.rho_d[c], a.mdi[c], a.dTh ? a.dTh[c] : 0.0,
-                        a.drv ? a.drv[c] : 0.0, a.g, &Th2, &rv2);
+    cell_update<double, double>(Th, rv, dml, a.rho_d[c], a.mdi[c], a.dTh ? a.dTh[c] : 0.0,
+                                a.drv ? a.drv[c] : 0.0, a.g, &Th2, &rv2);
     a.Th[c] = Th2;
     a.r_v[c] = rv2;
   }
@@ -294,20 +330,27 @@ __global__ void k_fwd_cells(Args a, double* tape_c) {
 // state after the sub-step), tape_m (m_w before), tape_c (Theta, r_v before),
 // m_after [n] (m_w after).  Out: the same adjoints for the state before;
 // grad_ms [n] and grad_ks [1] accumulate.
+// lam_inc (optional, [2][C]) accumulates the adjoints of the increments
+// (dTh, drv), which every sub-step of a half step shares
 __global__ void k_bwd_cells(Args a, const double* tape_c, const double* m_before,
                             const double* m_after, double* lam_Th, double* lam_rv,
-                            double* lam_dml) {
+                            double* lam_dml, double* lam_inc) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < a.C;
        c += (int64_t)gridDim.x * blockDim.x) {
     const double Th = tape_c[c], rv = tape_c[a.C + c];
     const double dml = a.dml[c] * 1.0E-18;   // recomputed forward sum of this sub-step
-    Dual<3> Th2, rv2;
-    cell_update<Dual<3>>(var<3>(Th, 0), var<3>(rv, 1), var<3>(dml, 2), a.rho_d[c], a.mdi[c],
-                         a.dTh ? a.dTh[c] : 0.0, a.drv ? a.drv[c] : 0.0, a.g, &Th2, &rv2);
+    const double fT = a.dTh ? a.dTh[c] : 0.0, fr = a.drv ? a.drv[c] : 0.0;
+    Dual<5> Th2, rv2;
+    cell_update<Dual<5>, Dual<5>>(var<5>(Th, 0), var<5>(rv, 1), var<5>(dml, 2), a.rho_d[c],
+                                  a.mdi[c], var<5>(fT, 3), var<5>(fr, 4), a.g, &Th2, &rv2);
     const double lT = lam_Th[c], lr = lam_rv[c];
     lam_Th[c] = lT * Th2.d[0] + lr * rv2.d[0];
     lam_rv[c] = lT * Th2.d[1] + lr * rv2.d[1];
     lam_dml[c] = (lT * Th2.d[2] + lr * rv2.d[2]) * 1.0E-18;   // per fg of dm*xi
+    if (lam_inc) {
+      lam_inc[c] += lT * Th2.d[3] + lr * rv2.d[3];
+      lam_inc[a.C + c] += lT * Th2.d[4] + lr * rv2.d[4];
+    }
     a.dml[c] = 0.0;
   }
 }
@@ -334,6 +377,18 @@ __global__ void k_bwd_sips(Args a, const double* tape_c, const double* m_before,
     const double ms = a.m_s[k];
     // total adjoint of the new mass: the state after, and the cell sum
     const double lm = lam_m[k] + lam_dml[c] * xi;
+    if (a.no_iter > 0) {   // the time step's map, differentiated exactly
+      const double Th = tape_c[c], rv = tape_c[a.C + c];
+      const Amb<Dual<5>> am = ambient<Dual<5>>(var<5>(Th, 3), var<5>(rv, 4), a.rho_d[c], a.g);
+      const Dual<5> mn = newton_map<Dual<5>>(var<5>(m_before[k], 0), var<5>(ms, 1),
+                                             var<5>(a.ks, 2), am, a.dt, a.no_iter);
+      grad_ms[k] += lm * mn.d[1];
+      gk += lm * mn.d[2] * (1.0 / 0.6);
+      atomicAdd(lam_Th_pre + c, lm * mn.d[3]);
+      atomicAdd(lam_rv_pre + c, lm * mn.d[4]);
+      lam_m[k] = lm * mn.d[0] - lam_dml[c] * xi;
+      continue;
+    }
     const double m_eff = ms * (LC_W_S_MAX_AS_INV - 1.0);
     if (!(m > m_eff)) {
       grad_ms[k] += lm * (LC_W_S_MAX_AS_INV - 1.0);
@@ -359,6 +414,149 @@ __global__ void k_bwd_sips(Args a, const double* tape_c, const double* m_before,
   if (gk != 0.0) atomicAdd(grad_ks, gk);
 }
 
+// ---- advective increments of Theta and r_v (integration.py:80-287 with the
+// sub-step increments of :1483-1508 and :1536-1561) in the arithmetic of S ----
+__device__ __forceinline__ double dfmin(double x, double y) { return fmin(x, y); }
+template <int N>
+__device__ __forceinline__ Dual<N> dfmin(const Dual<N>& x, const Dual<N>& y) {
+  if (isnan(x.v)) return y;   // C fmin: a NaN operand is ignored
+  if (isnan(y.v)) return x;
+  return (y.v < x.v) ? y : x;
+}
+__device__ __forceinline__ double dmax0(double z) { return np_max(0.0, z); }
+template <int N>
+__device__ __forceinline__ Dual<N> dmax0(const Dual<N>& z) {   // np.maximum(0, z)
+  return (0.0 >= z.v) ? cst<N>(0.0) : z;
+}
+// integration.py:113-148 limiter of the Hundsdorfer et al. (1995) scheme
+template <class S>
+__device__ __forceinline__ S limiter_of(const S& a0, const S& a1, const S& a2) {
+  const S r = (fabs(val(a1) - val(a2)) > 1.0E-8 * fabs(val(a0) - val(a1)))
+                  ? (a0 - a1) / (a1 - a2)
+                  : (a0 - a1) * 1.0E8 * np_sign(val(a1) - val(a2));
+  const S K = (1.0 + 2.0 * r) * LC_ONE_THIRD;
+  return dmax0(dfmin(2.0 * r, dfmin(K, Const<S>::of(2.0))));
+}
+// flux through the face left of stencil value a0 (integration.py:204-228)
+template <class S>
+__device__ __forceinline__ S face_flux_of(double u, const S& am2, const S& am1, const S& a0,
+                                          const S& ap1) {
+  if (u >= 0.0) return u * (am1 + 0.5 * limiter_of(a0, am1, am2) * (am1 - am2));
+  return u * (a0 + 0.5 * limiter_of(am1, a0, ap1) * (a0 - ap1));
+}
+__device__ __forceinline__ int64_t wrap_idx(int64_t i, int64_t N, int bc) {
+  if (bc == 0) { i %= N; return i < 0 ? i + N : i; }
+  return i < 0 ? 0 : (i > N - 1 ? N - 1 : i);
+}
+// the four face fluxes of cell (i, j) (x: periodic, z: solid walls) and the
+// flat indices of their stencils
+struct Stencil {
+  double u[4];
+  int64_t idx[4][4];
+  bool zero[4];
+};
+__device__ __forceinline__ Stencil stencil_of(const double* flux, int64_t nx, int64_t nz,
+                                              int64_t i, int64_t j) {
+  Stencil st;
+  for (int s = 0; s < 2; ++s) {
+    const int64_t fi = i + s, fj = j + s;
+    st.u[s] = flux[fi * (nz + 1) + j];
+    st.zero[s] = false;
+    st.u[2 + s] = flux[(nx + 1) * (nz + 1) + i * (nz + 1) + fj];
+    st.zero[2 + s] = (fj == 0 || fj == nz);
+    for (int t = 0; t < 4; ++t) {
+      st.idx[s][t] = wrap_idx(fi - 2 + t, nx, 0) * nz + j;
+      st.idx[2 + s][t] = i * nz + wrap_idx(fj - 2 + t, nz, 1);
+    }
+  }
+  return st;
+}
+
+struct IncArgs {
+  const double* f[2];     // Theta, r_v [C]
+  const double* rdi;      // rho_dry_inv [C]
+  const double* flux;     // mass flux at the faces [2][nx+1][nz+1]
+  const double* trel;     // relaxation time [nz] or null (no relaxation)
+  const double* prof[2];  // initial profiles of Theta and r_v [nz]
+  int64_t nx, nz;
+  double dx, dz, dt;
+};
+
+// increments of a half step: second = 0: inc = -dt div rdi + relax;
+// second = 1: inc = -2 dt div rdi - inc_prev + 2 relax (inc holds inc_prev)
+__global__ void k_increments(IncArgs a, int second, double* inc_Th, double* inc_rv) {
+  const int64_t C = a.nx * a.nz;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 2 * C;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int fld = t < C ? 0 : 1;
+    const int64_t c = t - fld * C, i = c / a.nz, j = c - i * a.nz;
+    const double* f = a.f[fld];
+    const Stencil st = stencil_of(a.flux, a.nx, a.nz, i, j);
+    double F[4];
+    for (int q = 0; q < 4; ++q)
+      F[q] = st.zero[q] ? 0.0
+                        : face_flux_of<double>(st.u[q], f[st.idx[q][0]], f[st.idx[q][1]],
+                                               f[st.idx[q][2]], f[st.idx[q][3]]);
+    const double div = (F[1] - F[0]) / a.dx + (F[3] - F[2]) / a.dz;
+    double relax = 0.0;
+    if (a.trel) {   // integration.py:325-354, column sum in x order
+      double sum = f[j];
+      for (int64_t ii = 1; ii < a.nx; ++ii) sum += f[ii * a.nz + j];
+      relax = a.dt * (a.prof[fld][j] - sum / (double)a.nx) / a.trel[j];
+    }
+    double* out = fld == 0 ? inc_Th : inc_rv;
+    double v;
+    if (!second) {
+      v = -a.dt * div * a.rdi[c];
+      if (a.trel) v += relax;
+    } else {
+      v = -2.0 * a.dt * div * a.rdi[c] - out[c];
+      if (a.trel) v += 2. * relax;
+    }
+    out[c] = v;
+  }
+}
+
+// vector-Jacobian product of factor * (advective + relaxation increment):
+// lam_f += factor J^T lam_inc for both fields; grad_s += factor lam_inc .
+// (advective increment) / flux_scale, the derivative by a common factor s of
+// the mass flux (the flux passed is s times the unscaled one)
+__global__ void k_increments_vjp(IncArgs a, double factor, double flux_scale,
+                                 const double* lam_inc, double* lam_Th, double* lam_rv,
+                                 double* grad_s) {
+  const int64_t C = a.nx * a.nz;
+  double gs = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 2 * C;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int fld = t < C ? 0 : 1;
+    const int64_t c = t - fld * C, i = c / a.nz, j = c - i * a.nz;
+    const double* f = a.f[fld];
+    double* lam_f = fld == 0 ? lam_Th : lam_rv;
+    const double li = lam_inc[fld * C + c];
+    if (li == 0.0) continue;
+    const Stencil st = stencil_of(a.flux, a.nx, a.nz, i, j);
+    const double ld = factor * li * (-a.dt * a.rdi[c]);   // adjoint of div(c)
+    double div = 0.0;
+    for (int q = 0; q < 4; ++q) {
+      if (st.zero[q]) continue;
+      const Dual<4> F = face_flux_of<Dual<4>>(st.u[q], var<4>(f[st.idx[q][0]], 0),
+                                              var<4>(f[st.idx[q][1]], 1),
+                                              var<4>(f[st.idx[q][2]], 2),
+                                              var<4>(f[st.idx[q][3]], 3));
+      const double w = (q & 1 ? 1.0 : -1.0) / (q < 2 ? a.dx : a.dz);
+      div += w * F.v;
+      for (int m = 0; m < 4; ++m)
+        if (F.d[m] != 0.0) atomicAdd(lam_f + st.idx[q][m], ld * w * F.d[m]);
+    }
+    gs += factor * li * (-a.dt * div * a.rdi[c]) / flux_scale;
+    if (a.trel) {   // relax_j depends on the column mean of field j
+      const double lr = -factor * li * a.dt / (a.trel[j] * (double)a.nx);
+      for (int64_t ii = 0; ii < a.nx; ++ii) atomicAdd(lam_f + ii * a.nz + j, lr);
+    }
+  }
+  if (gs != 0.0) atomicAdd(grad_s, gs);
+}
+
 static inline int nb(int64_t n, int t) {
   int64_t b = (n + t - 1) / t;
   return (int)(b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b));
@@ -373,8 +571,9 @@ using namespace lacmo::adj;
 static Args make_args(int64_t n, int64_t C, double* m_w, const double* m_s, const double* xi,
                       const int32_t* cell, double* Th, double* r_v, const double* rho_d,
                       const double* mdi, const double* dTh, const double* drv, double* dml,
-                      double dt, double kappa, double p_ref, double V) {
+                      double dt, double kappa, double p_ref, double V, int no_iter) {
   Args a;
+  a.no_iter = no_iter;
   a.n = n; a.C = C; a.m_w = m_w; a.m_s = m_s; a.xi = xi; a.cell = cell; a.Th = Th; a.r_v = r_v;
   a.rho_d = rho_d; a.mdi = mdi; a.dTh = dTh; a.drv = drv; a.dml = dml; a.dt = dt;
   a.ks = kappa / 0.6;
@@ -385,18 +584,20 @@ static Args make_args(int64_t n, int64_t C, double* m_w, const double* m_s, cons
 extern "C" {
 
 int lacmo_adj_forward(int64_t n, int64_t C, double* m_w, const double* m_s, const double* xi,
-                      const int32_t* cell, double* Th, double* r_v, const double* rho_d,
-                      const double* mdi, const double* dTh, const double* drv, double* dml,
-                      double dt_sub, double kappa, double p_ref, double V, int n_sub,
-                      double* tape_m, double* tape_c, void* stream) {
+                      const int32_t* cell, int64_t cell_stride, double* Th, double* r_v,
+                      const double* rho_d, const double* mdi, const double* dTh,
+                      const double* drv, double* dml, double dt_sub, double kappa, double p_ref,
+                      double V, int n_sub, int no_iter, double* tape_m, double* tape_c,
+                      void* stream) {
   if (n <= 0 || C <= 0 || !m_w || !m_s || !xi || !cell || !Th || !r_v || !rho_d || !mdi || !dml ||
-      n_sub < 0 || !(kappa > 0.0) || !(p_ref > 0.0))
+      n_sub < 0 || cell_stride < 0 || no_iter < 0 || !(kappa > 0.0) || !(p_ref > 0.0))
     return LACMO_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   Args a = make_args(n, C, m_w, m_s, xi, cell, Th, r_v, rho_d, mdi, dTh, drv, dml, dt_sub, kappa,
-                     p_ref, V);
+                     p_ref, V, no_iter);
   if (cudaMemsetAsync(dml, 0, 8 * C, s) != cudaSuccess) return LACMO_ERR_CUDA;
   for (int k = 0; k < n_sub; ++k) {
+    a.cell = cell + (size_t)k * cell_stride;
     k_fwd_sips<<<nb(n, 128), 128, 0, s>>>(a, tape_m ? tape_m + (size_t)k * n : nullptr);
     k_fwd_cells<<<nb(C, 64), 64, 0, s>>>(a, tape_c ? tape_c + (size_t)k * 2 * C : nullptr);
     note_launches(2);
@@ -410,30 +611,75 @@ int lacmo_adj_forward(int64_t n, int64_t C, double* m_w, const double* m_s, cons
 }
 
 int lacmo_adj_backward(int64_t n, int64_t C, const double* m_s, const double* xi,
-                       const int32_t* cell, const double* rho_d, const double* mdi,
-                       const double* dTh, const double* drv, double* dml, double dt_sub,
-                       double kappa, double p_ref, double V, int n_sub, const double* tape_m,
-                       const double* tape_c, double* lam_m, double* lam_Th, double* lam_rv,
-                       double* lam_dml, double* grad_ms, double* grad_kappa, void* stream) {
+                       const int32_t* cell, int64_t cell_stride, const double* rho_d,
+                       const double* mdi, const double* dTh, const double* drv, double* dml,
+                       double dt_sub, double kappa, double p_ref, double V, int n_sub,
+                       int no_iter, const double* tape_m, const double* tape_c, double* lam_m,
+                       double* lam_Th, double* lam_rv, double* lam_dml, double* grad_ms,
+                       double* grad_kappa, double* lam_inc, void* stream) {
   if (n <= 0 || C <= 0 || !m_s || !xi || !cell || !rho_d || !mdi || !dml || n_sub < 0 ||
-      !tape_m || !tape_c || !lam_m || !lam_Th || !lam_rv || !lam_dml || !grad_ms || !grad_kappa ||
-      !(kappa > 0.0))
+      cell_stride < 0 || no_iter < 0 || !tape_m || !tape_c || !lam_m || !lam_Th || !lam_rv ||
+      !lam_dml || !grad_ms || !grad_kappa || !(kappa > 0.0))
     return LACMO_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   Args a = make_args(n, C, nullptr, m_s, xi, cell, nullptr, nullptr, rho_d, mdi, dTh, drv, dml,
-                     dt_sub, kappa, p_ref, V);
+                     dt_sub, kappa, p_ref, V, no_iter);
   if (cudaMemsetAsync(dml, 0, 8 * C, s) != cudaSuccess) return LACMO_ERR_CUDA;
-  double* gks = grad_kappa;
   for (int k = n_sub - 1; k >= 0; --k) {
+    a.cell = cell + (size_t)k * cell_stride;
     const double* mb = tape_m + (size_t)k * n;
     const double* ma = tape_m + (size_t)(k + 1) * n;
     const double* tc = tape_c + (size_t)k * 2 * C;
     k_bwd_sum_dml<<<nb(n, 128), 128, 0, s>>>(a, mb, ma);
-    k_bwd_cells<<<nb(C, 64), 64, 0, s>>>(a, tc, mb, ma, lam_Th, lam_rv, lam_dml);
+    k_bwd_cells<<<nb(C, 64), 64, 0, s>>>(a, tc, mb, ma, lam_Th, lam_rv, lam_dml, lam_inc);
     k_bwd_sips<<<nb(n, 128), 128, 0, s>>>(a, tc, mb, ma, lam_m, lam_dml, lam_Th, lam_rv, grad_ms,
-                                          gks);
+                                          grad_kappa);
     note_launches(3);
   }
+  return cudaGetLastError() == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
+}
+
+static bool inc_args(IncArgs* a, const double* Th, const double* r_v, const double* rdi,
+                     const double* flux, int64_t nx, int64_t nz, double dx, double dz,
+                     double dt_sub, const double* prof_Th, const double* prof_rv,
+                     const double* t_relax) {
+  if (!Th || !r_v || !rdi || !flux || nx <= 0 || nz <= 0 || !(dx > 0.0) || !(dz > 0.0))
+    return false;
+  if (t_relax && (!prof_Th || !prof_rv)) return false;
+  a->f[0] = Th; a->f[1] = r_v; a->rdi = rdi; a->flux = flux; a->trel = t_relax;
+  a->prof[0] = prof_Th; a->prof[1] = prof_rv;
+  a->nx = nx; a->nz = nz; a->dx = dx; a->dz = dz; a->dt = dt_sub;
+  return true;
+}
+
+int lacmo_adj_increments(const double* Th, const double* r_v, const double* rho_dry_inv,
+                         const double* flux, int64_t nx, int64_t nz, double dx, double dz,
+                         double dt_sub, const double* prof_Th, const double* prof_rv,
+                         const double* t_relax, int second, double* inc_Th, double* inc_rv,
+                         void* stream) {
+  IncArgs a;
+  if (!inc_args(&a, Th, r_v, rho_dry_inv, flux, nx, nz, dx, dz, dt_sub, prof_Th, prof_rv,
+                t_relax) || !inc_Th || !inc_rv)
+    return LACMO_ERR_ARG;
+  k_increments<<<nb(2 * nx * nz, 128), 128, 0, (cudaStream_t)stream>>>(a, second ? 1 : 0,
+                                                                       inc_Th, inc_rv);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
+}
+
+int lacmo_adj_increments_vjp(const double* Th, const double* r_v, const double* rho_dry_inv,
+                             const double* flux, int64_t nx, int64_t nz, double dx, double dz,
+                             double dt_sub, const double* prof_Th, const double* prof_rv,
+                             const double* t_relax, double factor, double flux_scale,
+                             const double* lam_inc, double* lam_Th, double* lam_rv,
+                             double* grad_s, void* stream) {
+  IncArgs a;
+  if (!inc_args(&a, Th, r_v, rho_dry_inv, flux, nx, nz, dx, dz, dt_sub, prof_Th, prof_rv,
+                t_relax) || !lam_inc || !lam_Th || !lam_rv || !grad_s || !(flux_scale > 0.0))
+    return LACMO_ERR_ARG;
+  k_increments_vjp<<<nb(2 * nx * nz, 128), 128, 0, (cudaStream_t)stream>>>(
+      a, factor, flux_scale, lam_inc, lam_Th, lam_rv, grad_s);
+  note_launches(1);
   return cudaGetLastError() == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
 }
 

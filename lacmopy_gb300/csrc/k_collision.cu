@@ -711,13 +711,12 @@ __device__ __forceinline__ int2 thin_cell(const CellArgs& a, const CellSmem S, i
 // order (collections and undecided pairs) are processed one at a time.
 constexpr size_t CELL_WARP_BYTES = (size_t)CELL_SMEM * (4 * 4 + 4 + 4) + (CELL_SMEM / 32) * 32;
 
-// THIN: the thinned draws, else per-pair draws; 3 blocks per SM either way
-// (the thinned rounds gain more from the warps than they lose to spills)
-#ifndef LACMO_COL_BLOCKS
-#define LACMO_COL_BLOCKS 3
-#endif
-template <bool THIN>
-__global__ void __launch_bounds__(CELL_WARPS * 32, LACMO_COL_BLOCKS)
+// THIN: the thinned draws, else per-pair draws.  MINB: resident blocks per
+// SM the register budget is set for (the TUNE_COLLISION_BLOCKS knob picks the
+// instance; 3 by default: the thinned rounds gain more from the warps than
+// they lose to spills)
+template <bool THIN, int MINB>
+__global__ void __launch_bounds__(CELL_WARPS * 32, MINB)
     k_collide_cells(const __grid_constant__ CK x) {
   // the member's arguments, once per block (all warps of a block belong to
   // the same member); shared memory keeps them addressable without a copy
@@ -1263,21 +1262,40 @@ static float fp32_bin_margin(double lo, double bl, int64_t nb) {
   return (float)(m < 0.5 ? m : 0.5);
 }
 
-cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d,
-                                 cudaStream_t s) {
+// persistent blocks: as many as are resident at once, split over members
+template <bool THIN, int MINB>
+static cudaError_t launch_cells(const Bt& B, const CK& x, cudaStream_t s) {
+  static std::atomic<int> resident[64];
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  static std::atomic<uint64_t> attr_done{0};   // one bit per device
-  if (dev < 64 && !(attr_done.load() & (1ull << dev))) {
-    e = cudaFuncSetAttribute(k_collide_cells<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)CELL_SMEM_BYTES);
+  int res = dev < 64 ? resident[dev].load() : 0;
+  if (res <= 0) {
+    e = cudaFuncSetAttribute(k_collide_cells<THIN, MINB>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CELL_SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_collide_cells<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)CELL_SMEM_BYTES);
+    int per_sm = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collide_cells<THIN, MINB>,
+                                                      CELL_WARPS * 32, CELL_SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    attr_done.fetch_or(1ull << dev);
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    res = per_sm * sms > 0 ? per_sm * sms : 1;
+    if (dev < 64) resident[dev].store(res);
   }
+  const int64_t C = B.nx * B.nz;
+  int64_t bx = res / B.M;
+  const int64_t need = (C + CELL_WARPS - 1) / CELL_WARPS;
+  if (bx > need) bx = need;
+  if (bx < 1) bx = 1;
+  k_collide_cells<THIN, MINB><<<dim3((unsigned)bx, (unsigned)B.M), CELL_WARPS * 32,
+                                CELL_SMEM_BYTES, s>>>(x);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d,
+                                 cudaStream_t s) {
   if (B.M > 1 && d.draws) return cudaErrorInvalidValue;   // batches draw from Philox
   CellCommon cc;
   cc.dtdv = p.dt_col_over_dV; cc.E = p.E_col_grid; cc.E_const = p.E_col_const;
@@ -1304,33 +1322,16 @@ cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lac
   // thinned draws need the row maxima of a tabulated efficiency
   cc.thin = (p.thin_draws != 0 && d.draws == nullptr && (!p.E_col_grid || cc.erow)) ? 1 : 0;
   CK x{B.ref(), cc};
-  // persistent blocks: as many as are resident at once, split over members
-  static std::atomic<int> resident[2][64];
-  const int th = cc.thin ? 1 : 0;
-  int res = dev < 64 ? resident[th][dev].load() : 0;
-  if (res <= 0) {
-    int per_sm = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, th ? k_collide_cells<true> : k_collide_cells<false>, CELL_WARPS * 32,
-        CELL_SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    res = per_sm * sms > 0 ? per_sm * sms : 1;
-    if (dev < 64) resident[th][dev].store(res);
+  cudaError_t e;
+  const int minb = tune_value(TUNE_COLLISION_BLOCKS);
+  if (cc.thin) {
+    e = minb == 2 ? launch_cells<true, 2>(B, x, s)
+                  : (minb == 4 ? launch_cells<true, 4>(B, x, s) : launch_cells<true, 3>(B, x, s));
+  } else {
+    e = minb == 2 ? launch_cells<false, 2>(B, x, s)
+                  : (minb == 4 ? launch_cells<false, 4>(B, x, s)
+                               : launch_cells<false, 3>(B, x, s));
   }
-  const int64_t C = B.nx * B.nz;
-  int64_t bx = res / B.M;
-  const int64_t need = (C + CELL_WARPS - 1) / CELL_WARPS;
-  if (bx > need) bx = need;
-  if (bx < 1) bx = 1;
-  dim3 grid((unsigned)bx, (unsigned)B.M);
-  if (th)
-    k_collide_cells<true><<<grid, CELL_WARPS * 32, CELL_SMEM_BYTES, s>>>(x);
-  else
-    k_collide_cells<false><<<grid, CELL_WARPS * 32, CELL_SMEM_BYTES, s>>>(x);
-  note_launches(1);
-  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_col_advance<<<dim3(1, B.M), 1, 0, s>>>(B.ref(), d.draws ? 1 : 0); note_launches(1);
   return cudaGetLastError();

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "lacmo_internal.cuh"
+#include "lacmo_physics.cuh"
 
 namespace lacmo {
 
@@ -109,9 +110,91 @@ static int diag_run(DiagArgs d, void* ws, size_t bytes, cudaStream_t s) {
   return cudaGetLastError() == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
 }
 
+// microphysics.py:208-266: radius (condensation path: cbrt), solute mass
+// fraction and density per SIP
+__global__ void k_R_p_w_s_rho_p(int sol, int64_t n, const double* __restrict__ m_w,
+                                const double* __restrict__ m_s, const double* __restrict__ T_p,
+                                double* R_p, double* w_s, double* rho_p) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const double m_p = m_w[k] + m_s[k];
+    const double w = m_s[k] / m_p;
+    const double rho = sol == SOL_AS ? density_water(T_p[k]) * poly_rho_AS(w)
+                                     : density_NaCl_solution(w, T_p[k]);
+    R_p[k] = radius_from_mass(m_p, rho);
+    if (w_s) w_s[k] = w;
+    if (rho_p) rho_p[k] = rho;
+  }
+}
+// microphysics.py:83-100 with one density for every mass
+__global__ void k_radius_from_mass(int64_t n, const double* __restrict__ m, double rho,
+                                   double* R) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    R[k] = radius_from_mass(m[k], rho);
+}
+// numpy.histogram with weights: bins [e_b, e_b+1), the last one closed;
+// values outside [e_0, e_nb] and NaN count nowhere.  The bin comes from a
+// binary search of the ascending edges; the weights add up with FP64
+// atomics (any order).
+__global__ void k_histogram_weighted(const double* __restrict__ x, const double* __restrict__ w,
+                                     int64_t n, const double* __restrict__ e, int64_t nb,
+                                     double* out) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[k];
+    if (!(v >= e[0] && v <= e[nb])) continue;
+    int64_t lo = 0, hi = nb;   // the last edge <= v, among e[0 .. nb - 1]
+    while (hi - lo > 1) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (e[mid] <= v) lo = mid; else hi = mid;
+    }
+    atomicAdd(out + lo, w ? w[k] : 1.0);
+  }
+}
+
+static int diag_blocks(int64_t n) {
+  const int64_t b = (n + 255) / 256;
+  return (int)(b < 152 * 32 ? (b > 0 ? b : 1) : 152 * 32);
+}
+
 }  // namespace lacmo
 
 using namespace lacmo;
+
+extern "C" int lacmo_compute_R_p_w_s_rho_p(int solute, int64_t n, const double* m_w,
+                                           const double* m_s, const double* T_p, double* R_p,
+                                           double* w_s, double* rho_p, void* stream) {
+  if ((solute != 0 && solute != 1) || n < 0 || !m_w || !m_s || !T_p || !R_p)
+    return LACMO_ERR_ARG;
+  if (n == 0) return LACMO_OK;
+  k_R_p_w_s_rho_p<<<diag_blocks(n), 256, 0, (cudaStream_t)stream>>>(solute, n, m_w, m_s, T_p,
+                                                                    R_p, w_s, rho_p);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
+}
+
+extern "C" int lacmo_radius_from_mass(int64_t n, const double* m, double rho, double* R,
+                                      void* stream) {
+  if (n < 0 || !m || !R) return LACMO_ERR_ARG;
+  if (n == 0) return LACMO_OK;
+  k_radius_from_mass<<<diag_blocks(n), 256, 0, (cudaStream_t)stream>>>(n, m, rho, R);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
+}
+
+extern "C" int lacmo_histogram_weighted(const double* x, const double* w, int64_t n,
+                                        const double* edges, int64_t nbins, double* out,
+                                        void* stream) {
+  if (n < 0 || nbins < 1 || !x || !edges || !out) return LACMO_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(out, 0, (size_t)nbins * sizeof(double), s) != cudaSuccess)
+    return LACMO_ERR_CUDA;
+  if (n == 0) return LACMO_OK;
+  k_histogram_weighted<<<diag_blocks(n), 256, 0, s>>>(x, w, n, edges, nbins, out);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
+}
 
 extern "C" int lacmo_update_cell_sum(int kind, const double* m_w, const double* xi,
                                      const int32_t* cell, const uint8_t* mask,

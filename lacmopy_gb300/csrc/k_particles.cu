@@ -17,6 +17,8 @@
 // deterministic and, given identical per-SIP values, equal to the reference's.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "lacmo_internal.cuh"
 #include "lacmo_physics.cuh"
 
@@ -822,11 +824,10 @@ struct PmTiles {
   }
 };
 
-template <bool PHYS>
-#ifndef LACMO_PM_BLOCKS
-#define LACMO_PM_BLOCKS 6   // resident blocks per SM (register budget 80)
-#endif
-__global__ void __launch_bounds__(PM_THREADS, LACMO_PM_BLOCKS) k_particles_mixed(const __grid_constant__ PK x) {
+// MINB: resident blocks per SM the register budget is set for (the
+// TUNE_PARTICLE_BLOCKS knob picks the instance)
+template <bool PHYS, int MINB>
+__global__ void __launch_bounds__(PM_THREADS, MINB) k_particles_mixed(const __grid_constant__ PK x) {
   // the member's arguments, once per block in shared memory: threads read
   // them on use instead of holding some 60 registers of pointers and sizes
   __shared__ PArgs s_a;
@@ -1388,7 +1389,8 @@ cudaError_t launch_bin(const Bt& B, cudaStream_t s) {
   const int64_t C = B.nx * B.nz;
   k_scan<<<dim3(1, B.M), 1024, 0, s>>>(B.ref()); note_launches(1);
   k_scatter<<<grid2(B.n_max, 256, B.M), 256, 0, s>>>(B.ref()); note_launches(1);
-  k_order<<<grid2(C * 32, 256, B.M, 152 * 16), 256, 0, s>>>(B.ref()); note_launches(1);
+  k_order<<<grid2(C * 32, 256, B.M, 152 * tune_value(TUNE_ORDER_CTAS)), 256, 0, s>>>(B.ref());
+  note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_particles(const Bt& B, const lacmo_params_t& p, double dt_sub,
@@ -1405,51 +1407,55 @@ cudaError_t launch_move(const Bt& B, double dt_pos, cudaStream_t s) {
 }
 // Resident-sized grid for the pipelined mixed kernel: each thread walks many
 // SIPs so the one-ahead staging hides the loads of all but the first.
-template <bool PHYS>
-static cudaError_t mixed_grid(const Bt& B, dim3* grid) {
-  static int cached[2][64];
+template <bool PHYS, int MINB>
+static cudaError_t mixed_launch(const Bt& B, const PK& x, cudaStream_t s) {
+  static std::atomic<int> cached[64];
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  int res = dev < 64 ? cached[PHYS][dev] : 0;
+  int res = dev < 64 ? cached[dev].load() : 0;
   if (res <= 0) {
     int per_sm = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_particles_mixed<PHYS>,
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_particles_mixed<PHYS, MINB>,
                                                       PM_THREADS, PM_SMEM);
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     res = per_sm * sms > 0 ? per_sm * sms : 1;
-    if (dev < 64) cached[PHYS][dev] = res;
+    if (dev < 64) cached[dev].store(res);
   }
+  // resident-sized grid: each warp walks many tiles through the staging
+  // pipeline; small states take one block per tile (more blocks in flight
+  // hide the latency better)
   int64_t bx = res / B.M;
   const int64_t need = (B.n_max + PM_THREADS - 1) / PM_THREADS;
-  // small states: below 8 SIPs per thread the staging gains little, and more
-  // blocks in flight hide the latency better
   if (bx * PM_THREADS * 8 > B.n_max) bx = need < 152 * 16 ? need : 152 * 16;
   if (bx > need) bx = need;
   if (bx < 1) bx = 1;
-  *grid = dim3((unsigned)bx, (unsigned)B.M);
-  return cudaSuccess;
+  k_particles_mixed<PHYS, MINB><<<dim3((unsigned)bx, (unsigned)B.M), PM_THREADS, PM_SMEM, s>>>(x);
+  note_launches(1);
+  return cudaGetLastError();
+}
+template <bool PHYS>
+static cudaError_t mixed_launch_tuned(const Bt& B, const PK& x, cudaStream_t s) {
+  switch (tune_value(TUNE_PARTICLE_BLOCKS)) {
+    case 5: return mixed_launch<PHYS, 5>(B, x, s);
+    case 8: return mixed_launch<PHYS, 8>(B, x, s);
+    default: return mixed_launch<PHYS, 6>(B, x, s);
+  }
 }
 cudaError_t launch_particles_mixed(const Bt& B, const lacmo_params_t& p, double dt_sub,
                                    double dt_sub_pos, bool write_Tp, bool hist, cudaStream_t s) {
   PK x{B.ref(), pcall(p, dt_sub, dt_sub_pos, write_Tp, hist)};
-  dim3 grid;
-  cudaError_t e = mixed_grid<true>(B, &grid);
+  cudaError_t e = mixed_launch_tuned<true>(B, x, s);
   if (e != cudaSuccess) return e;
-  k_particles_mixed<true><<<grid, PM_THREADS, PM_SMEM, s>>>(x); note_launches(1);
   k_newton_fallback<<<dim3(64, B.M), 128, 0, s>>>(x); note_launches(1);
   return cudaGetLastError();
 }
 cudaError_t launch_move_mixed(const Bt& B, double dt_pos, cudaStream_t s) {
   lacmo_params_t p = {};
   PK x{B.ref(), pcall(p, 0.0, dt_pos, false, true)};
-  dim3 grid;
-  cudaError_t e = mixed_grid<false>(B, &grid);
-  if (e != cudaSuccess) return e;
-  k_particles_mixed<false><<<grid, PM_THREADS, PM_SMEM, s>>>(x); note_launches(1);
-  return cudaGetLastError();
+  return mixed_launch<false, 6>(B, x, s);
 }
 cudaError_t launch_wind_float(const Bt& B, cudaStream_t s) {
   k_wind_table<<<grid2(B.nx * B.nz, 256, B.M), 256, 0, s>>>(B.ref()); note_launches(1);

@@ -56,6 +56,11 @@ __host__ __device__ inline float4* cell_records(double* aux, int64_t C) {
 constexpr int CELL_REC = 8;   // float4 per cell record
 
 
+// launch-shape knobs of lacmo_tune_* (process-wide; read at launch, so a
+// CUDA graph keeps the shapes it was captured with)
+enum { TUNE_PARTICLE_BLOCKS = 0, TUNE_COLLISION_BLOCKS = 1, TUNE_ORDER_CTAS = 2, TUNE_KNOBS = 3 };
+int tune_value(int knob);
+
 size_t ws_bytes(int64_t n, int64_t nx, int64_t nz);
 bool ws_carve(void* base, size_t bytes, int64_t n, int64_t nx, int64_t nz, Ws* ws);
 // process-wide count of kernels this library has launched (lacmo_kernel_launches)

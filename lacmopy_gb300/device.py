@@ -301,6 +301,31 @@ class DeviceState:
         self._subloop(p.scale_dt_cond - 1, 1 if ncol in (1, 2) else p.scale_dt_cond)
         self._substep(p.dt_sub_half, True)
 
+    def adv_step_tracked(self, record):
+        """One advection step without collisions, sub-step by sub-step
+        (integration.py:1474-1610), calling ``record(k)`` before particle
+        sub-step k = 0 .. 2 scale_dt_cond - 1, while ``self.cell`` holds the
+        cells that sub-step's condensation uses."""
+        p = self.params
+        s = _stream()
+        _lib.check(self.lib.lacmo_adv_step_begin(ctypes.byref(self.sips), ctypes.byref(self.grid),
+                                                 ctypes.byref(p), _ptr(self.ws), self.ws_bytes, s),
+                   "adv_step_begin")
+        k = 0
+        for _ in range(p.scale_dt_cond):
+            record(k)
+            k += 1
+            self._substep(p.dt_sub, False)
+        _lib.check(self.lib.lacmo_adv_step_second_half(
+            ctypes.byref(self.sips), ctypes.byref(self.grid), ctypes.byref(p), _ptr(self.ws),
+            self.ws_bytes, s), "adv_step_second_half")
+        for _ in range(p.scale_dt_cond - 1):
+            record(k)
+            k += 1
+            self._substep(p.dt_sub, False)
+        record(k)
+        self._substep(p.dt_sub_half, True)
+
     def particles_substep(self, dt_sub, dt_sub_pos):
         """integration.py:944 propagate_particles_subloop_step_np."""
         _lib.check(self.lib.lacmo_propagate_particles_subloop_step(
@@ -402,10 +427,11 @@ class BatchState:
     kernel launch covering every member.  Collision draws come from Philox
     keyed by each member's seed, so member m evolves exactly like a
     ``DeviceState(states[m], draws="thinned", seed=seeds[m])`` on its own
-    (``draws="philox"``: per-pair draws)."""
+    (``draws="philox"``: per-pair draws).  ``tune=True`` sets the launch
+    shapes with the autotuner first (lacmopy_gb300.autotune)."""
 
     def __init__(self, states, seeds, device="cuda", precision="mixed", draws="thinned",
-                 thin=None):
+                 thin=None, tune=False):
         if draws not in ("thinned", "philox"):
             raise ValueError(f"batch draws must be 'thinned' or 'philox', got {draws!r}")
         if thin is None:
@@ -413,6 +439,11 @@ class BatchState:
         if len(states) != len(seeds) or not states:
             raise ValueError("one seed per member state is required")
         self.lib = _lib.load()
+        if tune:
+            # launch shapes timed on a throw-away batch of these states (or
+            # taken from the autotuner's cache); see lacmopy_gb300.autotune
+            from . import autotune
+            autotune.tune_batch(states, seeds, precision=precision, draws=draws)
         self.members = [DeviceState(st, device=device, draws="philox", seed=int(sd),
                                     precision=precision, workspace=False, thin=thin)
                         for st, sd in zip(states, seeds)]

@@ -322,8 +322,13 @@ class FrameWriter:
         try:
             return key, pool.get_nowait()
         except queue.Empty:
-            if self.made.get(key, 0) >= self.depth:
-                return key, pool.get()   # every set in flight: wait for one
+            while self.made.get(key, 0) >= self.depth:
+                # every set in flight: wait for the writer to free one
+                try:
+                    return key, pool.get(timeout=1.0)
+                except queue.Empty:
+                    if not self.thread.is_alive():
+                        raise RuntimeError("frame writer thread stopped") from self.error
         self.made[key] = self.made.get(key, 0) + 1
         t = self.torch
         n, nx, nz = key
@@ -347,10 +352,10 @@ class FrameWriter:
         key, buf = self._buffers(ds)
         self.stream.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(self.stream):
-            for key, src in (("gsf", ds.gsf), ("pos", ds.pos), ("vel", ds.vel),
-                             ("cells", cells), ("act", act), ("m_w", ds.m_w), ("m_s", ds.m_s),
-                             ("xi", ds.xi), ("no_cols", ds.no_cols)):
-                buf[key].copy_(src, non_blocking=True)
+            for name, src in (("gsf", ds.gsf), ("pos", ds.pos), ("vel", ds.vel),
+                              ("cells", cells), ("act", act), ("m_w", ds.m_w), ("m_s", ds.m_s),
+                              ("xi", ds.xi), ("no_cols", ds.no_cols)):
+                buf[name].copy_(src, non_blocking=True)
             for x in (cells, act, ds.gsf, ds.pos, ds.vel, ds.m_w, ds.m_s, ds.xi, ds.no_cols):
                 x.record_stream(self.stream)
             done = torch.cuda.Event()
@@ -372,9 +377,10 @@ class FrameWriter:
                                        buf["m_s"].numpy(), buf["xi"].numpy(),
                                        buf["act"].numpy().astype(bool), p)
                 np.save(p + f"no_cols_{_t(t)}.npy", buf["no_cols"].numpy())
-            except Exception as e:   # reported by the next dump() or close()
+            except BaseException as e:   # reported by the next dump() or close()
                 self.error = e
-            self.pools[key].put(buf)
+            finally:
+                self.pools[key].put(buf)   # the buffer set is free again either way
 
     def close(self):
         self.jobs.put(None)

@@ -548,10 +548,118 @@ def gen_kernel_generators(R):
     save("kernel_generators.npz", **out)
 
 
+def gen_evaluation(R):
+    """evaluation.py:1172-1660 on frames the reference's own writers saved
+    (two seeds, two save times, small grids): size spectra around target
+    cells, per-cell moments of every seed and time, box averages."""
+    import datetime
+    import tempfile
+    sys.modules.pop("evaluation", None)
+    import evaluation as ev
+    out = {}
+    times = np.array([0, 10])
+    with tempfile.TemporaryDirectory() as d:
+        paths = []
+        for k in range(2):
+            path = d + f"/seed{k}/"
+            os.makedirs(path)
+            for tn, t in enumerate(times):
+                st = _small_state(90 + 10 * k + tn, Nx=6, Nz=5, spcm=(6, 8))
+                st["active_ids"][::23] = False
+                st["cells"][1, ~st["active_ids"]] = -1
+                R.fh.save_grid_scalar_fields(t, st["grid_scalar_fields"], path,
+                                             datetime.datetime.now())
+                R.fh.dump_particle_data_all(t, st["pos"], st["vel"], st["cells"], st["m_w"],
+                                            st["m_s"], st["xi"], st["active_ids"], path)
+            np.save(path + "grid_save_times.npy", times)
+            np.save(path + "data_saving_paras.npy", (10, 1, 10))
+            paths.append(path)
+            for fn in sorted(os.listdir(path)):
+                out[f"file__seed{k}__{fn}"] = np.frombuffer(open(path + fn, "rb").read(),
+                                                            dtype=np.uint8)
+        mdi = st["grid_scalar_fields"][8]
+        tg = np.array([[2, 4], [1, 3]])
+        spec = ev.generate_size_spectra_R(paths, np.array([0, 1]), mdi, np.array([6, 5]), "AS",
+                                          tg, 3, 3, 12, 8)
+        for nm, a in zip(("f_R_p", "f_R_s", "bins_R_p", "bins_R_s", "save_times", "r_l",
+                          "R_min", "R_max"), spec):
+            out["spec__" + nm] = np.asarray(a)
+        mom, mt = ev.generate_moments_all_seeds(paths, 4, np.array([0, 1]),
+                                                float(st["grid_volume_cell"]),
+                                                np.array([6, 5]), "AS")
+        out["mom__moments"] = mom
+        out["mom__save_times"] = mt
+        out["box__avg"] = ev.avg_moments_over_boxes(mom, 2, np.array([0, 1]), 4,
+                                                    np.array([1, 4]), np.array([1, 3]), 3, 3)
+    out["in__mass_dry_inv"] = mdi
+    out["in__target_cells"] = tg
+    out["in__volume_cell"] = np.float64(st["grid_volume_cell"])
+    save("evaluation.npz", **out)
+
+
+def init_config(path, no_cells=(3, 15), steps=(20.0, 100.0), no_spcm=(4, 6), seed=1001,
+                eta_threshold="fix"):
+    """A small ICMW 2012 case 1 configuration with the reference's values
+    (config.py:64-132) on a narrow column of few cells."""
+    return {
+        "paths": {"simdata": path}, "seed_SIP_gen": seed, "seed_sim": seed + 5000,
+        "reseed": False, "solute_type": "AS",
+        "grid_ranges": [[0.0, no_cells[0] * steps[0]], [0.0, no_cells[1] * steps[1]]],
+        "grid_steps": list(steps), "dy": 1.0, "no_cells": np.array(no_cells),
+        "p_0": 1015E2, "p_ref": 1E5, "r_tot_0": 7.5E-3, "Theta_l": 289.0,
+        "no_spcm": list(no_spcm), "dist": "lognormal",
+        "DNC0": np.array([60.0E6, 40.0E6]), "mu_R": 0.5 * np.array([0.04, 0.15]),
+        "sigma_R": np.array([1.4, 1.6]), "eta": 1E-10, "eta_threshold": eta_threshold,
+        "r_critmin": np.array([1., 3.]) * 1E-3, "m_high_over_m_low": 1.0E8,
+        "S_init_max": 1.04, "dt_init": 0.1, "Newton_iterations": 2, "iter_cnt_limit": 4000}
+
+
+def gen_init(R):
+    """init.py:439-1236 initialize_grid_and_particles_SinSIP on a 3 x 15
+    column (dz = 100 m: the upper levels are cloudy), with the generation
+    configuration of set_config (init.py:43-108)."""
+    import tempfile
+    import init as ref_init
+    out = {}
+    for tag, eta_thr in (("fix", "fix"), ("weak", "weak")):
+        with tempfile.TemporaryDirectory() as d:
+            cfg = init_config(d + "/", eta_threshold=eta_thr)
+            ref_init.set_config(cfg, "generation")
+            grid, pos, cells, vel, m_w, m_s, xi, act = \
+                ref_init.initialize_grid_and_particles_SinSIP(cfg)
+            out[tag + "__dist_par"] = np.array(cfg["dist_par"])
+            out[tag + "__idx_mode_nonzero"] = np.asarray(cfg["idx_mode_nonzero"])
+            out[tag + "__no_modes"] = np.int64(cfg["no_modes"])
+            for nm, a in (("pos", pos), ("cells", cells), ("vel", vel), ("m_w", m_w),
+                          ("m_s", m_s), ("xi", xi), ("active_ids", act)):
+                out[tag + "__" + nm] = np.asarray(a)
+            for nm in ("pressure", "temperature", "potential_temperature",
+                       "mass_density_air_dry", "mixing_ratio_water_vapor",
+                       "mixing_ratio_water_liquid", "saturation", "saturation_pressure",
+                       "mass_dry_inv", "velocity", "mass_flux_air_dry"):
+                out[tag + "__grid_" + nm] = np.asarray(getattr(grid, nm))
+            out[tag + "__modes"] = np.load(cfg["paths"]["grid"] + "modes_0.npy")
+    save("init.npz", **out)
+
+
+def gen_wang2007(R):
+    """The bin-model moments of Wang et al. (2007) the reference compares its
+    box model with (collision/ref_data/{Long_Bott,Hall_Bott}/
+    Wang_2007_{moments,times}.txt, read at run_box_model.py:458-469), as
+    shipped."""
+    out = {}
+    for kt in ("Long_Bott", "Hall_Bott"):
+        d = "collision/ref_data/" + kt + "/"
+        out[kt + "__moments"] = np.loadtxt(d + "Wang_2007_moments.txt")
+        out[kt + "__times"] = np.loadtxt(d + "Wang_2007_times.txt")
+    save("wang2007.npz", **out)
+
+
 GENERATORS = [gen_tables, gen_mass_rate, gen_interp, gen_golovin, gen_ecol_box, gen_cells_2d,
               gen_grid_and_divergence, gen_particle_substep, gen_adv_step, gen_diagnostics,
               gen_kernel_grid_m, gen_box_model_kgrid, gen_file_formats,
-              gen_kernel_generators]
+              gen_kernel_generators, gen_evaluation,
+              gen_init, gen_wang2007]
 
 
 def main(ref_root, only=()):
