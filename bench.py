@@ -425,6 +425,7 @@ def run_ours(args):
             batch.adv_step(1, graph=graph)
         torch.cuda.synchronize()
         spin_s = time.perf_counter() - t0
+        shapes_d = batch.retune() if not args.no_tune else autotune.current()
         cols = sum(int(m.no_cols.sum()) for m in batch.members)
         ms_d, ups_d, _, _ = timed(batch, False)
         cols_d = sum(int(m.no_cols.sum()) for m in batch.members) - cols
@@ -435,9 +436,11 @@ def run_ours(args):
                       f"of the headline ensemble, then {args.warmup} warm-up and "
                       f"{args.steps} timed steps",
             "collisions_per_step": cols_d / (args.warmup + args.steps),
+            "launch_shapes": shapes_d,
             "over_fresh": (ups_d / (ms_d / 1000.0)) / value}
         del batch
         torch.cuda.empty_cache()
+        autotune.apply(shapes)   # the headline's shapes for the modes below
 
     # ---- the FP64 plain path and the mixed single state (75 x 75 x 64) ----
     if single is not None:

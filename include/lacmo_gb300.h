@@ -332,7 +332,8 @@ int lacmo_sinsip_generate(const double* rnd, const int64_t* rnd_off, const int32
  * count), multiplicities = weights * seg_scale[s] (real particles per cell). */
 int lacmo_sinsip_gather(const double* masses, const double* weights, const int32_t* count,
                         const int64_t* off, int64_t n_seg, int64_t lmax_cap,
-                        const double* seg_scale, double* m_out, double* xi_out, void* stream);
+                        const double* seg_scale, double* m_out, double* xi_out, int64_t n_out,
+                        void* stream);
 /* Replaces microphysics.py:686-785 compute_initial_mass_fraction_solute_m_s
  * (AS or NaCl, scipy fminbound / brentq per SIP): the solute mass fraction in
  * equilibrium with S_amb at T_amb, the activation maximum where S_amb is
@@ -343,10 +344,12 @@ int lacmo_init_mass_fraction(int solute, int64_t n, const double* m_s, double S_
 /* One saturation-adjustment iteration of a level (init.py:887-960): the
  * implicit Newton condensation step dt (no_iter evaluations) of every SIP at
  * the level's T and p and its cell's capped S and e_s; the SIPs of cell c are
- * off[c] .. off[c + 1] - 1; m_w is updated; dml_cell / mwxi_cell [cells]
- * receive the cell sums of dm * xi and m_w * xi (1e-18 kg). */
-int lacmo_saturation_adjust_level(int solute, int64_t cells, const int64_t* off, double* m_w,
-                                  const double* m_s, const double* xi, const double* S_cap,
+ * off[c] .. off[c + 1] - 1 (clipped to the n_sips of m_w, m_s, xi); m_w is
+ * updated; dml_cell / mwxi_cell [cells] receive the cell sums of dm * xi and
+ * m_w * xi (1e-18 kg). */
+int lacmo_saturation_adjust_level(int solute, int64_t cells, const int64_t* off, int64_t n_sips,
+                                  double* m_w, const double* m_s, const double* xi,
+                                  const double* S_cap,
                                   const double* e_s, double T, double p, double L_v, double K,
                                   double D_v, double dt, int no_iter, double* dml_cell,
                                   double* mwxi_cell, void* stream);

@@ -121,12 +121,12 @@ PROTOTYPES = {
     "lacmo_histogram_weighted": (ctypes.c_int, [vp, vp, i64, vp, i64, vp, vp]),
     "lacmo_sinsip_generate": (ctypes.c_int, [vp, vp, vp, i64, ctypes.c_int, vp, vp, dbl,
                                              ctypes.c_int, i64, vp, vp, vp, vp]),
-    "lacmo_sinsip_gather": (ctypes.c_int, [vp, vp, vp, vp, i64, i64, vp, vp, vp, vp]),
+    "lacmo_sinsip_gather": (ctypes.c_int, [vp, vp, vp, vp, i64, i64, vp, vp, vp, i64, vp]),
     "lacmo_init_mass_fraction": (ctypes.c_int, [ctypes.c_int, i64, vp, dbl, dbl, dbl, dbl, dbl,
                                                 vp, vp]),
-    "lacmo_saturation_adjust_level": (ctypes.c_int, [ctypes.c_int, i64, vp, vp, vp, vp, vp, vp,
-                                                     dbl, dbl, dbl, dbl, dbl, dbl, ctypes.c_int,
-                                                     vp, vp, vp]),
+    "lacmo_saturation_adjust_level": (ctypes.c_int, [ctypes.c_int, i64, vp, i64, vp, vp, vp, vp,
+                                                     vp, dbl, dbl, dbl, dbl, dbl, dbl,
+                                                     ctypes.c_int, vp, vp, vp]),
     "lacmo_collision_step_cells": (ctypes.c_int, [P(Sips), P(Grid), P(Params), P(Draws), vp, sz,
                                                   vp]),
     "lacmo_collision_pair_count": (ctypes.c_int, [vp, i64, i64, i64, P(i64), vp]),

@@ -28,7 +28,7 @@ sulfate water activity, a_w = 1 + (kappa / 0.6)(a_w_AS - 1); kappa = 0.6 is
 the reference's a_w) and ``flux_scale`` (a common factor of the mass flux,
 i.e. of j_max at init.py:1146-1148; dJ/dj_max = dJ/dflux_scale / j_max).
 ``StepModel.lwp_weights()`` and ``rain_weights()`` give the domain-mean liquid
-water path at the end and the surface rain accumulated over the run (the SIPs
+water path at the end and the mean surface rain flux over the run (the SIPs
 removed at the ground, integration.py:606-630, whose masses froze at removal).
 """
 
@@ -172,6 +172,7 @@ class StepModel(_Base):
     def __init__(self, st, n_adv, device="cuda"):
         self._common(st, device)
         self.n_adv = int(n_adv)
+        self.dt = float(st["dt"])
         self.S = int(st["scale_dt_cond"])
         self.K = 2 * self.S * self.n_adv
         gsf = np.asarray(st["grid_scalar_fields"])
@@ -202,9 +203,11 @@ class StepModel(_Base):
         return torch.where(self.cell_end >= 0, w, torch.zeros_like(w))
 
     def rain_weights(self):
-        """Surface rain accumulated over the run (kg m^-2 per fg of m_w): the
-        SIPs in the domain at the start and removed at the ground by the end."""
-        w = self.xi * 1.0E-18 / (self.nx * self.dx)
+        """Mean surface rain flux over the run (kg m^-2 s^-1 per fg of m_w):
+        the water of the SIPs in the domain at the start and removed at the
+        ground by the end (water_removed, integration.py:617-628), per
+        domain width and run time."""
+        w = self.xi * 1.0E-18 / (self.nx * self.dx * self.n_adv * self.dt)
         removed = (self.cell_start >= 0) & (self.cell_end < 0)
         return torch.where(removed, w, torch.zeros_like(w))
 

@@ -31,7 +31,8 @@ struct SinSIPArgs {
   const int32_t* seg_mode;  // [S]
   const double *mu_m_log, *sigma_m_log, *bin_factor, *m_low;   // [modes]
   const int32_t* l_max;     // [modes]
-  double eta, two_pi_sqrt;
+  double eta;
+  const double* two_pi_sqrt;   // device: mode_par[4 n_modes]
   int weak;                 // weak threshold: a second draw per bin
   int64_t S, lmax_cap;
   double *masses, *weights; // [S][lmax_cap], the kept bins first
@@ -53,7 +54,7 @@ __global__ void k_sinsip(const SinSIPArgs a) {
       const double m_right = m_left * a.bin_factor[k];
       const double width = m_right - m_left;
       const double mu = m_left + r[b] * width;
-      const double w = pdf_lognormal(mu, a.mu_m_log[k], a.sigma_m_log[k], a.two_pi_sqrt) * width;
+      const double w = pdf_lognormal(mu, a.mu_m_log[k], a.sigma_m_log[k], *a.two_pi_sqrt) * width;
       M[b] = mu;
       W[b] = w;
       wmax = (b == 0 || w > wmax) ? w : wmax;
@@ -75,13 +76,16 @@ __global__ void k_sinsip(const SinSIPArgs a) {
   }
 }
 
-// the kept bins of every segment, concatenated (off: exclusive sums of count)
+// the kept bins of every segment, concatenated (off: exclusive sums of
+// count); a segment whose range leaves [0, n_out) is skipped
 __global__ void k_sinsip_gather(const double* masses, const double* weights, const int32_t* count,
                                 const int64_t* off, int64_t S, int64_t lmax_cap,
-                                const double* seg_scale, double* m_out, double* xi_out) {
+                                const double* seg_scale, double* m_out, double* xi_out,
+                                int64_t n_out) {
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < S;
        s += (int64_t)gridDim.x * blockDim.x) {
     const int32_t n = count[s];
+    if (n < 0 || n > lmax_cap || off[s] < 0 || off[s] + n > n_out) continue;
     for (int b = 0; b < n; ++b) {
       m_out[off[s] + b] = masses[s * lmax_cap + b];
       xi_out[off[s] + b] = weights[s * lmax_cap + b] * seg_scale[s];
@@ -199,8 +203,8 @@ __global__ void k_init_mass_fraction(int sol, int64_t n, const double* m_s, doub
 // level at the level's T, p and per-cell S (capped) and e_s; one warp per
 // cell (SIPs of a cell are contiguous: off[c] .. off[c + 1]); writes m_w and
 // the cell sums of dm * xi and m_w * xi
-__global__ void k_sat_adjust(int sol, int64_t cells, const int64_t* off, double* m_w,
-                             const double* m_s, const double* xi, const double* S2,
+__global__ void k_sat_adjust(int sol, int64_t cells, const int64_t* off, int64_t n_sips,
+                             double* m_w, const double* m_s, const double* xi, const double* S2,
                              const double* e_s, double T, double p, double L_v, double K,
                              double D_v, double dt, int no_iter, double* dml_cell,
                              double* mwxi_cell) {
@@ -209,7 +213,10 @@ __global__ void k_sat_adjust(int sol, int64_t cells, const int64_t* off, double*
   if (c >= cells) return;
   const CellAmb amb = make_cell_amb(T, p, S2[c], e_s[c], L_v, K, D_v);
   double sd = 0.0, sm = 0.0;
-  for (int64_t k = off[c] + lane; k < off[c + 1]; k += 32) {
+  // the cell's SIPs, clipped to [0, n_sips)
+  const int64_t k0 = off[c] < 0 ? 0 : off[c];
+  const int64_t k1 = off[c + 1] > n_sips ? n_sips : off[c + 1];
+  for (int64_t k = k0 + lane; k < k1; k += 32) {
     const double mw = m_w[k], ms = m_s[k];
     const double m_p = mw + ms;
     const double w = ms / m_p;
@@ -252,7 +259,7 @@ extern "C" int lacmo_sinsip_generate(const double* rnd, const int64_t* rnd_off,
   a.rnd = rnd; a.rnd_off = rnd_off; a.seg_mode = seg_mode;
   a.mu_m_log = mode_par; a.sigma_m_log = mode_par + n_modes;
   a.bin_factor = mode_par + 2 * n_modes; a.m_low = mode_par + 3 * n_modes;
-  a.l_max = l_max; a.eta = eta; a.two_pi_sqrt = mode_par[4 * n_modes];
+  a.l_max = l_max; a.eta = eta; a.two_pi_sqrt = mode_par + 4 * n_modes;
   a.weak = weak; a.S = n_seg; a.lmax_cap = lmax_cap;
   a.masses = masses; a.weights = weights; a.count = count;
   k_sinsip<<<nblk(n_seg, 128), 128, 0, (cudaStream_t)stream>>>(a);
@@ -263,13 +270,13 @@ extern "C" int lacmo_sinsip_generate(const double* rnd, const int64_t* rnd_off,
 extern "C" int lacmo_sinsip_gather(const double* masses, const double* weights,
                                    const int32_t* count, const int64_t* off, int64_t n_seg,
                                    int64_t lmax_cap, const double* seg_scale, double* m_out,
-                                   double* xi_out, void* stream) {
+                                   double* xi_out, int64_t n_out, void* stream) {
   if (!masses || !weights || !count || !off || n_seg < 0 || lmax_cap < 1 || !seg_scale ||
-      !m_out || !xi_out)
+      !m_out || !xi_out || n_out < 0)
     return LACMO_ERR_ARG;
   if (n_seg == 0) return LACMO_OK;
   k_sinsip_gather<<<nblk(n_seg, 128), 128, 0, (cudaStream_t)stream>>>(
-      masses, weights, count, off, n_seg, lmax_cap, seg_scale, m_out, xi_out);
+      masses, weights, count, off, n_seg, lmax_cap, seg_scale, m_out, xi_out, n_out);
   note_launches(1);
   return cudaGetLastError() == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
 }
@@ -286,18 +293,19 @@ extern "C" int lacmo_init_mass_fraction(int solute, int64_t n, const double* m_s
 }
 
 extern "C" int lacmo_saturation_adjust_level(int solute, int64_t cells, const int64_t* off,
-                                             double* m_w, const double* m_s, const double* xi,
+                                             int64_t n_sips, double* m_w, const double* m_s,
+                                             const double* xi,
                                              const double* S_cap, const double* e_s, double T,
                                              double p, double L_v, double K, double D_v,
                                              double dt, int no_iter, double* dml_cell,
                                              double* mwxi_cell, void* stream) {
-  if ((solute != 0 && solute != 1) || cells < 1 || !off || !m_w || !m_s || !xi || !S_cap ||
-      !e_s || no_iter < 1 || !dml_cell || !mwxi_cell)
+  if ((solute != 0 && solute != 1) || cells < 1 || !off || n_sips < 0 || !m_w || !m_s || !xi ||
+      !S_cap || !e_s || no_iter < 1 || !dml_cell || !mwxi_cell)
     return LACMO_ERR_ARG;
   const int64_t blocks = (cells + 3) / 4;
   k_sat_adjust<<<(unsigned)blocks, 128, 0, (cudaStream_t)stream>>>(
-      solute, cells, off, m_w, m_s, xi, S_cap, e_s, T, p, L_v, K, D_v, dt, no_iter, dml_cell,
-      mwxi_cell);
+      solute, cells, off, n_sips, m_w, m_s, xi, S_cap, e_s, T, p, L_v, K, D_v, dt, no_iter,
+      dml_cell, mwxi_cell);
   note_launches(1);
   return cudaGetLastError() == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
 }

@@ -232,6 +232,23 @@ class DeviceState:
         self._plan_draws = d
         return handle
 
+    def drop_graph(self):
+        """Forget the captured step graph (the next graph step captures a new
+        one, e.g. with launch shapes the autotuner changed since)."""
+        torch.cuda.synchronize()
+        if self._plan_handle is not None:
+            self.lib.lacmo_plan_destroy(self._plan_handle)
+            self._plan_handle = None
+
+    def retune(self):
+        """Time the launch shapes on this batch in its current regime (it
+        advances a few steps), set them and drop the captured graph; see
+        lacmopy_gb300.autotune.tune_live."""
+        from . import autotune
+        choice = autotune.tune_live(self)
+        self.drop_graph()
+        return choice
+
     def graph_kernel_count(self):
         """Kernel nodes in the captured one-step graph (0 if none)."""
         if getattr(self, "_plan_handle", None) is None:
@@ -444,6 +461,7 @@ class BatchState:
             # taken from the autotuner's cache); see lacmopy_gb300.autotune
             from . import autotune
             autotune.tune_batch(states, seeds, precision=precision, draws=draws)
+        self.precision, self.draws = precision, draws
         self.members = [DeviceState(st, device=device, draws="philox", seed=int(sd),
                                     precision=precision, workspace=False, thin=thin)
                         for st, sd in zip(states, seeds)]
@@ -499,6 +517,23 @@ class BatchState:
         cur.wait_stream(side)
         self._plan_handle = handle
         return handle
+
+    def drop_graph(self):
+        """Forget the captured step graph (the next graph step captures a new
+        one, e.g. with launch shapes the autotuner changed since)."""
+        torch.cuda.synchronize()
+        if self._plan_handle is not None:
+            self.lib.lacmo_plan_destroy(self._plan_handle)
+            self._plan_handle = None
+
+    def retune(self):
+        """Time the launch shapes on this batch in its current regime (it
+        advances a few steps), set them and drop the captured graph; see
+        lacmopy_gb300.autotune.tune_live."""
+        from . import autotune
+        choice = autotune.tune_live(self)
+        self.drop_graph()
+        return choice
 
     def graph_kernel_count(self):
         if self._plan_handle is None:

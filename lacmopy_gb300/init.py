@@ -253,10 +253,14 @@ def initialize_grid_and_particles_SinSIP(config, write_files=True):
         seg_scale = np.tile(no_rpcm.astype(np.float64), nx)
         m_s_d = torch.empty(n_lvl, dtype=torch.float64, device=dev)
         xi_d = torch.empty_like(m_s_d)
+        # device copies bound to names: a temporary freed while the call's
+        # arguments are formed would hand its block to the next one
+        off_seg_d = to_device(off[:-1], torch.int64)
+        seg_scale_d = to_device(seg_scale)
         _lib.check(lib.lacmo_sinsip_gather(
             _ptr(gen["masses"][seg0:]), _ptr(gen["weights"][seg0:]), _ptr(gen["count"][seg0:]),
-            _ptr(to_device(off[:-1], torch.int64)), nx * no_modes, gen["cap"],
-            _ptr(to_device(seg_scale)), _ptr(m_s_d), _ptr(xi_d), s), "sinsip_gather")
+            _ptr(off_seg_d), nx * no_modes, gen["cap"], _ptr(seg_scale_d), _ptr(m_s_d),
+            _ptr(xi_d), n_lvl, s), "sinsip_gather")
         no_spc[:, j] = cnt.reshape(nx, no_modes).sum(axis=1)
         cell_off = np.concatenate([[0], np.cumsum(no_spc[:, j])]).astype(np.int64)
         # equilibrium solute mass fraction at the level's mean state
@@ -300,10 +304,11 @@ def initialize_grid_and_particles_SinSIP(config, write_files=True):
             D_v = diffusion_constant(T_avg, p_avg)
             K = thermal_conductivity(T_avg)
             L_v = heat_of_vaporization(T_avg)
-            S2 = np.minimum(S_cells, S_init_max)
+            S2_d = to_device(np.minimum(S_cells, S_init_max))
+            e_s_d = to_device(e_s_cells)
             _lib.check(lib.lacmo_saturation_adjust_level(
-                sol, nx, _ptr(off_d), _ptr(m_w_d), _ptr(m_s_d), _ptr(xi_d), _ptr(to_device(S2)),
-                _ptr(to_device(e_s_cells)), float(T_avg), float(p_avg), float(L_v), float(K),
+                sol, nx, _ptr(off_d), n_lvl, _ptr(m_w_d), _ptr(m_s_d), _ptr(xi_d), _ptr(S2_d),
+                _ptr(e_s_d), float(T_avg), float(p_avg), float(L_v), float(K),
                 float(D_v), dt_init, newton_it, _ptr(dml_c), _ptr(mwxi_c), s),
                 "saturation_adjust_level")
             dml_cells = dml_c.cpu().numpy()

@@ -655,11 +655,23 @@ def gen_wang2007(R):
     save("wang2007.npz", **out)
 
 
+def gen_golovin_moments(R):
+    """golovin.compute_moments_Golovin (golovin.py:48-58) of the box-model
+    setup (config 1's DNC and LWC, b = 1.5 m^3 kg^-1 s^-1) at the report's
+    save times, moments 0..3."""
+    DNC, LWC, b = 2.97E8, 1.0E-3, 1.5
+    t = np.arange(0.0, 3601.0, 600.0)
+    mom = np.array([[R.golovin.compute_moments_Golovin(tt, n, DNC, LWC, b) for tt in t]
+                    for n in range(4)])
+    save("golovin_moments.npz", t=t, moments=mom, DNC=np.float64(DNC), LWC=np.float64(LWC),
+         b=np.float64(b))
+
+
 GENERATORS = [gen_tables, gen_mass_rate, gen_interp, gen_golovin, gen_ecol_box, gen_cells_2d,
               gen_grid_and_divergence, gen_particle_substep, gen_adv_step, gen_diagnostics,
               gen_kernel_grid_m, gen_box_model_kgrid, gen_file_formats,
               gen_kernel_generators, gen_evaluation,
-              gen_init, gen_wang2007]
+              gen_init, gen_wang2007, gen_golovin_moments]
 
 
 def main(ref_root, only=()):

@@ -31,6 +31,11 @@ def test_workload_key_and_cache(tmp_path):
     assert k1 != autotune.workload_key([a, b], "fp64", "thinned", "GPU")
     assert k1 != autotune.workload_key([a, b], "mixed", "philox", "GPU")
     assert k1 != autotune.workload_key([c, c], "mixed", "thinned", "GPU")
+    # a raining ensemble (a drop of 1e8 fg = R ~ 290 um) is a different workload
+    r = dict(a)
+    r["m_w"] = np.asarray(a["m_w"]).copy()
+    r["m_w"][np.flatnonzero(np.asarray(a["active_ids"]))[0]] = 1e8
+    assert k1 != autotune.workload_key([r, b], "mixed", "thinned", "GPU")
     path = str(tmp_path / "shapes.json")
     assert autotune.load_cache(path) == {}
     autotune.save_cache(path, {k1: {"choice": {"particle_blocks_per_sm": 8}}})

@@ -103,7 +103,7 @@ def test_step_model_replays_the_product_run(step_model):
     torch.testing.assert_close(m_w, mw_p, rtol=1e-11, atol=1e-30)
     torch.testing.assert_close(Th, ds.gsf[2].reshape(-1), rtol=1e-13, atol=0)
     torch.testing.assert_close(rv, ds.gsf[4].reshape(-1), rtol=1e-11, atol=0)
-    removed = (model.rain_weights() > 0)
+    removed = model.rain_weights() > 0
     rain = float((m_w * model.xi)[removed].sum())
     rain_p = float(ds.water_removed[0]) - float(np.asarray(st["water_removed"])[0])
     assert removed.any() and abs(rain - rain_p) <= 1e-11 * abs(rain_p)

@@ -1,6 +1,7 @@
-"""Box model against the analytic Golovin solution, and the precision-form
-error statement, at sizes that run in seconds (the full-size runs are
-`python -m lacmopy_gb300.reports golovin|precision`)."""
+"""Box model against the analytic Golovin solution and the Wang et al. (2007)
+bin-model moments, and the precision-form error statements, at sizes that
+run in seconds to a minute (the full-size runs are `python -m
+lacmopy_gb300.reports golovin-ensemble|box-ecol|precision|precision-ensemble`)."""
 import pytest
 
 torch = pytest.importorskip("torch")
@@ -28,13 +29,73 @@ def test_golovin_box_moments_vs_analytic():
 
 
 def test_precision_form_small():
-    """Mixed vs FP64 from the same spun-up state, 30 x 30 cells at 128
-    SIPs/cell: domain liquid water within 1e-5, Theta within 1e-7, r_v within
-    1e-6, water masses within 1e-4 for 99% of the SIPs."""
+    """Mixed vs FP64 from the same spun-up state with the same draws, 30 x 30
+    cells at 128 SIPs/cell, 120 steps after the spin-up: domain liquid water
+    within 1e-5, Theta within 1e-5, r_v within 1e-4, water masses within 1e-3
+    for 99% of the SIPs.  At full size (75 x 75 x 128) the 1e-5 LWP bound
+    holds through 200 steps (9.6e-7) and not at 300 (4.1e-5): from then on
+    flipped collision decisions make the runs different realisations, and
+    the ensemble test below states the precision form."""
     from lacmopy_gb300 import reports
-    r = reports.precision(spcm=(52, 76), nx=30, nz=30, spinup=20, horizons=(20,))["rows"][0]
+    r = reports.precision(spcm=(52, 76), nx=30, nz=30, spinup=20, horizons=(120,))["rows"][0]
     assert r["lwp_rel"] < 1e-5
-    assert r["theta_rel_max"] < 1e-7
-    assert r["r_v_rel_max"] < 1e-6
-    assert r["m_w_rel_p99"] < 1e-4
+    assert r["theta_rel_max"] < 1e-5
+    assert r["r_v_rel_max"] < 1e-4
+    assert r["m_w_rel_p99"] < 1e-3
     assert r["cells_differ_frac"] < 1e-3
+
+
+def test_precision_ensemble_small():
+    """The precision form as ensemble statistics (8 members, 30 x 30 cells,
+    300 steps after a 100-step spin-up): the mixed - FP64 difference of the
+    ensemble means of liquid water, mean Theta, mean r_v and rain flux lies
+    within 4 standard errors of the difference (seed spread)."""
+    from lacmopy_gb300 import reports
+    r = reports.precision_ensemble(members=8, spcm=(52, 76), nx=30, nz=30, spinup=100,
+                                   horizon=300)
+    for key in ("lwp", "theta_mean", "r_v_mean", "rain_flux"):
+        assert abs(r[key]["diff_over_se"]) < 4.0, (key, r[key])
+    assert r["lwp"]["fp64_sd"] > 0.0
+
+
+def test_golovin_ensemble_vs_analytic_moments():
+    """Config 1 over 20 seeds (~5000 SIPs each, 3600 s): the ensemble means of
+    M0 and M2 against golovin.compute_moments_Golovin (golovin.py:48-58)
+    within 4 standard errors of the mean at every save time, M1 conserved."""
+    from lacmopy_gb300 import reports
+    r = reports.golovin_ensemble(seeds=tuple(range(1001, 1041, 2)), kappa=1000, t_end=3600.0,
+                                 dt_save=600.0)
+    assert r["seeds"] == 20
+    assert r["M1_conservation_max_rel"] < 1e-12
+    # t = 0: the sampled exponential distribution, cut at 0.6 um and at
+    # 1e6 times that mass, against the uncut one
+    r0 = r["rows"][0]
+    assert abs(r0["M2_rel"]) < 1e-3 and abs(r0["M3_rel"]) < 2e-3
+    for row in r["rows"][1:]:
+        for n in (0, 2):
+            assert abs(row[f"M{n}_dev_over_se"]) < 4.0, (row["t"], n, row)
+
+
+@pytest.mark.parametrize("kernel", ["Long_Bott", "Hall_Bott"])
+def test_box_ecol_vs_wang2007(kernel):
+    """The box model with the Long or Hall efficiencies and Beard velocities
+    (10 seeds, kappa = 600, ~3000 SIPs) against the bin-model moments of Wang
+    et al. (2007) the reference plots its box model against
+    (run_box_model.py:458-469; fixture tests/golden/wang2007.npz): M1 is
+    conserved; until the onset of rain (t <= 800 s) M0..M3 agree within 2%;
+    afterwards the SIP ensemble follows the bin model within a factor of 4
+    (the bin model forms its first large drops some 200 s earlier, and the
+    moments M2, M3 are carried by a few SIPs)."""
+    import numpy as np
+    from conftest import golden
+    from lacmopy_gb300 import reports
+    w = golden("wang2007.npz")
+    r = reports.box_ecol_ensemble(kernel, seeds=tuple(range(1001, 1021, 2)), kappa=600,
+                                  t_end=3600.0, dt_save=200.0)
+    assert np.array_equal(np.array(r["times"]), w[kernel + "__times"])
+    M = np.array(r["moments_mean"])
+    ratio = M / w[kernel + "__moments"]
+    np.testing.assert_allclose(ratio[1], 1.0, rtol=1e-12)
+    early = np.array(r["times"]) <= 800.0
+    assert np.all(np.abs(ratio[:, early] - 1.0) < 0.02), ratio[:, early]
+    assert np.all((ratio > 0.25) & (ratio < 4.0)), ratio

@@ -244,3 +244,14 @@ def test_box_model_kernel_grid_m_loop(oracle_py):
     assert np.array_equal(np.array(snaps), g["xis_vs_time"])
     assert np.array_equal(no_cols, g["no_cols"])
     assert np.array_equal(m, g["m"])
+
+
+def test_golovin_moments_restatement_vs_reference():
+    """reports.compute_moments_Golovin equals the reference's
+    golovin.compute_moments_Golovin (golovin.py:48-58) on the box setup."""
+    from lacmopy_gb300 import reports
+    d = golden("golovin_moments.npz")
+    for n in range(4):
+        for k, t in enumerate(d["t"]):
+            assert reports.compute_moments_Golovin(t, n, float(d["DNC"]), float(d["LWC"]),
+                                                   float(d["b"])) == d["moments"][n, k]
