@@ -32,6 +32,7 @@ specific_gas_constant_water_vapor = 461.53
 specific_gas_constant_air_dry = 287.06
 specific_heat_capacity_air_dry_NTP = 1004.71
 specific_heat_capacity_water_vapor_20C = 1906
+specific_heat_capacity_water_NTP = 4183.8
 
 # atmosphere.py
 kappa_air_dry = specific_gas_constant_air_dry / specific_heat_capacity_air_dry_NTP

@@ -599,108 +599,131 @@ __device__ __forceinline__ int2 thin_cell(const CellArgs& a, const CellSmem S, i
       }
     }
     const unsigned ev = __ballot_sync(FULL, valid && (indiv || hit));
-    if (!ev) {
-      if (__ballot_sync(FULL, valid) != FULL) break;   // the cell's last segment is done
-      si = __shfl_sync(FULL, i, 31);
-      sb = __shfl_sync(FULL, b, 31);
-      advance_seg(n, B, si, sb, 1);
-      if (sb >= B) break;
-      sj = (sb << 5) > si + 1 ? (sb << 5) : si + 1;
-      ssub = 0;
-      continue;
-    }
-    // the first segment with an event
-    const int L = __ffs(ev) - 1;
-    const int ei = __shfl_sync(FULL, i, L), eb = __shfl_sync(FULL, b, L);
-    const int ej = __shfl_sync(FULL, j, L), eend = __shfl_sync(FULL, jend, L);
-    const int ejf = __shfl_sync(FULL, jfirst, L), ee = __shfl_sync(FULL, e, L);
-    const uint32_t esub = __shfl_sync(FULL, sub, L);
-    const bool eind = __shfl_sync(FULL, (int)indiv, L) != 0;
-    if (!scratch) { init_exact_scratch(a, S, n, lane); scratch = true; }
-    int next_j = eend;
-    if (eind) {
-      // per-pair draws of the rest of the segment (pair ej + lane per lane,
-      // drawn once), screened in parallel; the candidates are processed in
-      // order, and the rest is screened again only after a state change
-      const int q = ej + lane;
-      const bool mine = q < eend;
-      uint64_t k53 = 0;
-      float r_lo = 0.0f, r_hi = 0.0f;
-      if (mine) {
-        k53 = philox_bits53(a.seed, (uint64_t)pair_rank(ei, q, n), pc1);
-        philox_interval(k53, r_lo, r_hi);
-      }
-      unsigned todo = __ballot_sync(FULL, mine);   // pairs not processed yet
-      while (todo) {
-        int sc = 0;
-        if ((todo >> lane) & 1u)
-          sc = screen_pair(a, use_E, S.v[ei], S.sk[ei], S.v[q], S.sk[q], r_lo, r_hi);
-        unsigned cand = __ballot_sync(FULL, sc != 0);
-        bool changed = false;
-        while (cand) {
-          const int t = __ffs(cand) - 1;
-          int col = 0;
-          if (lane == t) {
-            if (sc == 1) {
-              certain_collection(a, S, ei, q, Tc, use_E);
-              c0 += 1;
-              col = 1;
-            } else {
-              const int o = exact_pair(a, S, S.sid[ei], S.sid[q], ei, q, Tc, use_E,
-                                       philox_from_bits(k53));
-              c0 += o == 1;
-              c1 += o == 2;
-              col = o != 0;
-            }
-          }
-          col = __shfl_sync(FULL, col, t);
-          __threadfence_block();
-          __syncwarp();
-          todo &= ~((2u << t) - 1u);   // pairs up to t are done
-          if (col) { changed = true; break; }
-          cand &= cand - 1u;   // no change: the later screens still hold
+    // the round's segments with an event, in order.  An event that changes
+    // nothing (no collection) leaves the state, and so the bounds and hit
+    // draws of the later lanes, as they were: the next event of the round is
+    // processed at once.  A collection (or a hit whose segment has pairs
+    // left, a new part with its own draw) ends the round; the next one
+    // starts after it.
+    unsigned pend = ev;
+    bool restart = false, cell_done = false;
+    while (pend) {
+      const int L = __ffs(pend) - 1;
+      pend &= pend - 1u;
+      const int ei = __shfl_sync(FULL, i, L), eb = __shfl_sync(FULL, b, L);
+      const int ej = __shfl_sync(FULL, j, L), eend = __shfl_sync(FULL, jend, L);
+      const int ejf = __shfl_sync(FULL, jfirst, L), ee = __shfl_sync(FULL, e, L);
+      const uint32_t esub = __shfl_sync(FULL, sub, L);
+      const bool eind = __shfl_sync(FULL, (int)indiv, L) != 0;
+      if (!scratch) { init_exact_scratch(a, S, n, lane); scratch = true; }
+      int next_j = eend;
+      bool changed = false;
+      if (eind) {
+        // per-pair draws of the rest of the segment (pair ej + lane per
+        // lane, drawn once), screened in parallel; the candidates are
+        // processed in order, and the rest is screened again only after a
+        // state change
+        const int q = ej + lane;
+        const bool mine = q < eend;
+        uint64_t k53 = 0;
+        float r_lo = 0.0f, r_hi = 0.0f;
+        if (mine) {
+          k53 = philox_bits53(a.seed, (uint64_t)pair_rank(ei, q, n), pc1);
+          philox_interval(k53, r_lo, r_hi);
         }
-        if (!changed) break;
+        unsigned todo = __ballot_sync(FULL, mine);   // pairs not processed yet
+        while (todo) {
+          int sc = 0;
+          if ((todo >> lane) & 1u)
+            sc = screen_pair(a, use_E, S.v[ei], S.sk[ei], S.v[q], S.sk[q], r_lo, r_hi);
+          unsigned cand = __ballot_sync(FULL, sc != 0);
+          bool col_now = false;
+          while (cand) {
+            const int t = __ffs(cand) - 1;
+            int col = 0;
+            if (lane == t) {
+              if (sc == 1) {
+                certain_collection(a, S, ei, q, Tc, use_E);
+                c0 += 1;
+                col = 1;
+              } else {
+                const int o = exact_pair(a, S, S.sid[ei], S.sid[q], ei, q, Tc, use_E,
+                                         philox_from_bits(k53));
+                c0 += o == 1;
+                c1 += o == 2;
+                col = o != 0;
+              }
+            }
+            col = __shfl_sync(FULL, col, t);
+            __threadfence_block();
+            __syncwarp();
+            todo &= ~((2u << t) - 1u);   // pairs up to t are done
+            if (col) { col_now = true; break; }
+            cand &= cand - 1u;   // no change: the later screens still hold
+          }
+          if (!col_now) break;
+          changed = true;
+        }
+      } else {
+        // the hit: first-hit draws of all lanes, then the pair with r = q u
+        const int m = eend - ej;
+        const uint64_t chunk = (uint64_t)pair_rank(ei, ejf, n);
+        bool succ = false;
+        if (lane < m - 1)
+          succ = lt_bits53(a.seed, chunk, esub, (uint32_t)(1 + lane), pc1) <
+                 __ldg(&LACMO_THIN_PT[ee - LACMO_THIN_E_MIN][m - lane - 1]);
+        const unsigned bal = __ballot_sync(FULL, succ);
+        const int g = bal ? __ffs(bal) - 1 : m - 1;
+        const uint32_t jd = g < m - 1 ? (uint32_t)(g + 2) : (uint32_t)m;
+        int col = 0;
+        if (lane == 0) {
+          const double r = ldexp((double)lt_bits53(a.seed, chunk, esub, jd, pc1) *
+                                     (1.0 / 9007199254740992.0), -ee);
+          // a float interval around r: truncation and the next float up
+          // (below the normal range: [0, 2^-126])
+          const bool normal = r >= 0x1p-126;
+          const float r_lo = normal ? d2f_down_pos(r) : 0.0f;
+          const float r_hi = normal ? __uint_as_float(__float_as_uint(r_lo) + 1u) : 0x1p-126f;
+          const int64_t before = c0 + c1;
+          decide_pair(a, S, use_E, ei, ej + g, r, r_lo, r_hi, Tc, c0, c1);
+          col = c0 + c1 != before;
+        }
+        changed = __shfl_sync(FULL, col, 0) != 0;
+        __threadfence_block();
+        __syncwarp();
+        next_j = ej + g + 1;
       }
-    } else {
-      // the hit: first-hit draws of all lanes, then the pair with r = q u
-      const int m = eend - ej;
-      const uint64_t chunk = (uint64_t)pair_rank(ei, ejf, n);
-      bool succ = false;
-      if (lane < m - 1)
-        succ = lt_bits53(a.seed, chunk, esub, (uint32_t)(1 + lane), pc1) <
-               __ldg(&LACMO_THIN_PT[ee - LACMO_THIN_E_MIN][m - lane - 1]);
-      const unsigned bal = __ballot_sync(FULL, succ);
-      const int g = bal ? __ffs(bal) - 1 : m - 1;
-      const uint32_t jd = g < m - 1 ? (uint32_t)(g + 2) : (uint32_t)m;
-      if (lane == 0) {
-        const double r = ldexp((double)lt_bits53(a.seed, chunk, esub, jd, pc1) *
-                                   (1.0 / 9007199254740992.0), -ee);
-        // a float interval around r: truncation and the next float up
-        // (below the normal range: [0, 2^-126])
-        const bool normal = r >= 0x1p-126;
-        const float r_lo = normal ? d2f_down_pos(r) : 0.0f;
-        const float r_hi = normal ? __uint_as_float(__float_as_uint(r_lo) + 1u) : 0x1p-126f;
-        decide_pair(a, S, use_E, ei, ej + g, r, r_lo, r_hi, Tc, c0, c1);
+      const bool part_left = !eind && next_j < eend;
+      if (!changed && !part_left) continue;   // the round goes on
+      if (changed) {
+        // the statistics of the blocks the event may have changed
+        block_stats(S, n, ei >> 5, lane);
+        if ((ei >> 5) != eb) block_stats(S, n, eb, lane);
+        __syncwarp();
       }
-      __threadfence_block();
-      __syncwarp();
-      next_j = ej + g + 1;
+      si = ei; sb = eb;
+      if (part_left) {
+        sj = next_j;
+        ssub = (int)esub + 1;
+      } else {
+        advance_seg(n, B, si, sb, 1);
+        if (sb >= B) { cell_done = true; break; }
+        sj = (sb << 5) > si + 1 ? (sb << 5) : si + 1;
+        ssub = 0;
+      }
+      restart = true;
+      break;
     }
-    // the statistics of the blocks the event may have changed
-    block_stats(S, n, ei >> 5, lane);
-    if ((ei >> 5) != eb) block_stats(S, n, eb, lane);
-    __syncwarp();
-    si = ei; sb = eb;
-    if (!eind && next_j < eend) {
-      sj = next_j;
-      ssub = (int)esub + 1;
-    } else {
-      advance_seg(n, B, si, sb, 1);
-      if (sb >= B) break;
-      sj = (sb << 5) > si + 1 ? (sb << 5) : si + 1;
-      ssub = 0;
-    }
+    if (cell_done) break;
+    if (restart) continue;
+    // every segment of the round is done
+    if (__ballot_sync(FULL, valid) != FULL) break;   // the cell's last segment is done
+    si = __shfl_sync(FULL, i, 31);
+    sb = __shfl_sync(FULL, b, 31);
+    advance_seg(n, B, si, sb, 1);
+    if (sb >= B) break;
+    sj = (sb << 5) > si + 1 ? (sb << 5) : si + 1;
+    ssub = 0;
   }
   return make_int2((int)c0, (int)c1);
 }

@@ -567,6 +567,16 @@ class BatchState:
     def snapshot(self, m):
         return self.members[m].snapshot()
 
+    def update_grid_r_l(self, m):
+        """grid.py:370 update_grid_r_l_np of member m, with the member's slice
+        of the batch workspace (its current cell binning)."""
+        ws, nb = ctypes.c_void_p(), ctypes.c_size_t()
+        _lib.check(self.lib.lacmo_batch_member_workspace(self.handle, m, ctypes.byref(ws),
+                                                         ctypes.byref(nb)), "member_workspace")
+        mb = self.members[m]
+        _lib.check(self.lib.lacmo_update_grid_r_l(ctypes.byref(mb.sips), ctypes.byref(mb.grid),
+                                                  ws, nb.value, _stream()), "update_grid_r_l")
+
     def __del__(self):
         try:
             if getattr(self, "_plan_handle", None) is not None:

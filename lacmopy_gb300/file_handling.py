@@ -293,10 +293,11 @@ class FrameWriter:
     """Frame dumps of device-resident states that do not stall them.
 
     ``dump(ds, t)`` brings r_l of the device state up to date
-    (grid.py:370-412, on the GPU), then copies the frame's arrays to pinned
-    host buffers on a side stream that waits only for the work queued so far,
-    and returns: the state's own stream keeps running its next steps.  A
-    writer thread waits for each copy and writes the frame's files in the
+    (grid.py:370-412, on the GPU), snapshots the frame's arrays device to
+    device on the state's own stream (so steps queued after ``dump`` cannot
+    change them), copies the snapshot to pinned host buffers on a side
+    stream and returns: the state's own stream keeps running its next steps.
+    A writer thread waits for each copy and writes the frame's files in the
     reference's format (``save_grid_scalar_fields``,
     ``dump_particle_data_all`` and ``no_cols_<t>.npy``, as integration.py:
     2055-2066 writes them).  ``close()`` waits for every frame to be on disk.
@@ -332,16 +333,14 @@ class FrameWriter:
         self.made[key] = self.made.get(key, 0) + 1
         t = self.torch
         n, nx, nz = key
-        pin = dict(pin_memory=True)
-        return key, {"gsf": t.empty((10, nx, nz), dtype=t.float64, **pin),
-                     "pos": t.empty((2, n), dtype=t.float64, **pin),
-                     "vel": t.empty((2, n), dtype=t.float64, **pin),
-                     "cells": t.empty((2, n), dtype=t.int64, **pin),
-                     "act": t.empty(n, dtype=t.uint8, **pin),
-                     "m_w": t.empty(n, dtype=t.float64, **pin),
-                     "m_s": t.empty(n, dtype=t.float64, **pin),
-                     "xi": t.empty(n, dtype=t.float64, **pin),
-                     "no_cols": t.empty(2, dtype=t.int64, **pin)}
+        shapes = {"gsf": ((10, nx, nz), t.float64), "pos": ((2, n), t.float64),
+                  "vel": ((2, n), t.float64), "cells": ((2, n), t.int64),
+                  "act": ((n,), t.uint8), "m_w": ((n,), t.float64), "m_s": ((n,), t.float64),
+                  "xi": ((n,), t.float64), "no_cols": ((2,), t.int64)}
+        # a pinned host set and a device snapshot set per buffer set
+        host = {k: t.empty(sh, dtype=dt, pin_memory=True) for k, (sh, dt) in shapes.items()}
+        dev = {k: t.empty(sh, dtype=dt, device=ds.pos.device) for k, (sh, dt) in shapes.items()}
+        return key, (host, dev)
 
     def dump(self, ds, t):
         if self.error is not None:
@@ -349,25 +348,29 @@ class FrameWriter:
         torch = self.torch
         ds.update_grid_r_l()
         cells, act = ds.cells_and_active()
-        key, buf = self._buffers(ds)
-        self.stream.wait_stream(torch.cuda.current_stream())
+        key, (buf, snap) = self._buffers(ds)
+        cur = torch.cuda.current_stream()
+        for name, src in (("gsf", ds.gsf), ("pos", ds.pos), ("vel", ds.vel), ("cells", cells),
+                          ("act", act), ("m_w", ds.m_w), ("m_s", ds.m_s), ("xi", ds.xi),
+                          ("no_cols", ds.no_cols)):
+            snap[name].copy_(src)   # device to device, on the state's stream
+        taken = torch.cuda.Event()
+        taken.record(cur)
+        self.stream.wait_event(taken)
         with torch.cuda.stream(self.stream):
-            for name, src in (("gsf", ds.gsf), ("pos", ds.pos), ("vel", ds.vel),
-                              ("cells", cells), ("act", act), ("m_w", ds.m_w), ("m_s", ds.m_s),
-                              ("xi", ds.xi), ("no_cols", ds.no_cols)):
-                buf[name].copy_(src, non_blocking=True)
-            for x in (cells, act, ds.gsf, ds.pos, ds.vel, ds.m_w, ds.m_s, ds.xi, ds.no_cols):
-                x.record_stream(self.stream)
+            for name in buf:
+                buf[name].copy_(snap[name], non_blocking=True)
             done = torch.cuda.Event()
             done.record(self.stream)
-        self.jobs.put((t, key, buf, done))
+        self.jobs.put((t, key, (buf, snap), done))
 
     def _run(self):
         while True:
             job = self.jobs.get()
             if job is None:
                 return
-            t, key, buf, done = job
+            t, key, bufs, done = job
+            buf = bufs[0]
             try:
                 done.synchronize()
                 p = self.path
@@ -380,7 +383,7 @@ class FrameWriter:
             except BaseException as e:   # reported by the next dump() or close()
                 self.error = e
             finally:
-                self.pools[key].put(buf)   # the buffer set is free again either way
+                self.pools[key].put(bufs)   # the buffer set is free again either way
 
     def close(self):
         self.jobs.put(None)

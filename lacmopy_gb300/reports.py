@@ -217,13 +217,30 @@ def box_ecol_ensemble(kernel_name="Long_Bott", seeds=tuple(range(1001, 1021, 2))
             "wall_s": time.perf_counter() - t0}
 
 
+def _spin_up(st, steps, seed, draws="philox"):
+    """The reference's spin-up (init.py:137-146: without gravity, collisions
+    and relaxation) of ``steps`` advection steps in FP64, in place on the
+    state dict; the simulation's own settings are kept for what follows."""
+    from . import DeviceState
+    if not steps:
+        return
+    keep = {k: st[k] for k in ("act_collisions", "act_relaxation", "g_set")}
+    st.update(act_collisions=False, act_relaxation=False, g_set=0.0)
+    d = DeviceState(st, draws=draws, seed=seed, precision="fp64")
+    d.adv_step(steps, graph=True)
+    d.export_to(st)
+    del d
+    st.update(keep)
+
+
 def _lwp(s):
     return float((s["m_w"] * s["xi"] * s["active_ids"]).sum())
 
 
 def precision(spcm=(52, 76), nx=75, nz=75, spinup=60, horizons=(10, 60), seed=1001,
               kernel="Long_Bott"):
-    """Spin up in FP64, then advance copies of the spun-up state: FP64 and mixed
+    """Spin up in FP64 (the reference's spin-up: no gravity, collisions or
+    relaxation), then advance copies of the spun-up state: FP64 and mixed
     precision with identical Philox draws, and FP64 with other draws (the
     seed-to-seed spread of the stochastic collisions, the noise floor of any
     comparison once collision outcomes differ).  Errors of the mixed run
@@ -231,11 +248,7 @@ def precision(spcm=(52, 76), nx=75, nz=75, spinup=60, horizons=(10, 60), seed=10
     from . import DeviceState, synthetic
     st = synthetic.make_icmw_state(Nx=nx, Nz=nz, no_spcm=tuple(spcm), seed=seed,
                                    kernel_type=kernel)
-    d = DeviceState(st, draws="philox", seed=seed, precision="fp64")
-    if spinup:
-        d.adv_step(spinup, graph=True)
-    d.export_to(st)
-    del d
+    _spin_up(st, spinup, seed)
     cp = lambda: {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in st.items()}
     a = DeviceState(cp(), draws="philox", seed=seed + 1, precision="fp64")
     b = DeviceState(cp(), draws="philox", seed=seed + 1, precision="mixed")
@@ -292,7 +305,8 @@ def _member_stats(b, m, horizon, wr0):
 def precision_ensemble(members=16, spcm=(52, 76), nx=75, nz=75, spinup=7200, horizon=3600,
                        seed=1001, kernel="Long_Bott"):
     """The precision form as ensemble statistics.  One state is spun up in
-    FP64; ``members`` copies of it then advance ``horizon`` steps with
+    FP64 (the reference's spin-up: no gravity, collisions or relaxation);
+    ``members`` copies of it then advance ``horizon`` steps with
     collision draws keyed by different seeds, once in FP64 and once in mixed
     precision (member k has the same seed in both).  Collision outcomes
     make the members different realisations, so the mixed and FP64 paths are
@@ -305,11 +319,7 @@ def precision_ensemble(members=16, spcm=(52, 76), nx=75, nz=75, spinup=7200, hor
     st = synthetic.make_icmw_state(Nx=nx, Nz=nz, no_spcm=tuple(spcm), seed=seed,
                                    kernel_type=kernel)
     t0 = time.perf_counter()
-    if spinup:
-        d = DeviceState(st, draws="thinned", seed=seed, precision="fp64")
-        d.adv_step(spinup, graph=True)
-        d.export_to(st)
-        del d
+    _spin_up(st, spinup, seed, draws="thinned")
     wr0 = float(st["water_removed"][0])
     seeds = [seed + 100 + k for k in range(members)]
     out = {"members": members, "spinup_steps": spinup, "horizon_steps": horizon,
@@ -321,7 +331,7 @@ def precision_ensemble(members=16, spcm=(52, 76), nx=75, nz=75, spinup=7200, hor
         b = BatchState(states, seeds, precision=prec, draws="thinned")
         b.adv_step(horizon, graph=True)
         for m in range(members):
-            b.members[m].update_grid_r_l()
+            b.update_grid_r_l(m)
         stats[prec] = [_member_stats(b, m, horizon, wr0) for m in range(members)]
         del b
     for key in ("lwp", "theta_mean", "r_v_mean", "rain_flux"):

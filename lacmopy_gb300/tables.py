@@ -235,7 +235,9 @@ def generate_and_save_kernel_grid(R_low, R_high, no_bins_10, mass_density, kerne
 
 def kernel_grid_m_parameters(mass_grid):
     """The binning parameters of the kernel-grid-m box model from a mass grid
-    (logarithmic): (no_kernel_bins, m_kernel_low_log, bin_factor_m_log)."""
+    (logarithmic) in the SIPs' mass unit, fg: the generators' grids are in kg,
+    so pass 1e18 times them, as run_box_model.py:379-389 does;
+    (no_kernel_bins, m_kernel_low_log, bin_factor_m_log)."""
     return len(mass_grid), math.log(mass_grid[0]), math.log(mass_grid[1] / mass_grid[0])
 
 

@@ -102,11 +102,11 @@ def test_kernel_grid_m_box_with_generated_table(oracle_py, tmp_path):
     from lacmopy_gb300 import collision as Cg
     from lacmopy_gb300 import tables
     K, vel, mass, rg = tables.generate_kernel_grid_Long_Bott_np(0.6, 3000.0, 10, 1000.0)
-    nb, m_lo, bf = tables.kernel_grid_m_parameters(mass)
+    nb, m_lo, bf = tables.kernel_grid_m_parameters(1.0E18 * mass)   # kg -> fg
     rng = np.random.default_rng(8)
     n = 300
     xis0 = np.exp(rng.uniform(np.log(1e6), np.log(1e9), n))
-    m0 = np.exp(rng.uniform(np.log(1e1), np.log(1e7), n))
+    m0 = np.exp(rng.uniform(np.log(1e5), np.log(1e10), n))   # fg: R of 3 to 130 um
     seed, dV, dt, t_end, dt_save = 4242, 1.0, 1.0, 4.0, 2.0
     xis, m = xis0.copy(), m0.copy()
     nc = np.zeros(2, np.int64)

@@ -95,7 +95,8 @@ def test_box_ecol_vs_wang2007(kernel):
     assert np.array_equal(np.array(r["times"]), w[kernel + "__times"])
     M = np.array(r["moments_mean"])
     ratio = M / w[kernel + "__moments"]
-    np.testing.assert_allclose(ratio[1], 1.0, rtol=1e-12)
+    # mass conserved (the sampled initial mass is 1.4e-5 below the bin model's)
+    np.testing.assert_allclose(M[1], M[1][0], rtol=1e-12)
     early = np.array(r["times"]) <= 800.0
     assert np.all(np.abs(ratio[:, early] - 1.0) < 0.02), ratio[:, early]
     assert np.all((ratio > 0.25) & (ratio < 4.0)), ratio
