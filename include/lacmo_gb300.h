@@ -45,6 +45,8 @@ extern "C" {
                                            the binning (not collided)           */
 #define LACMO_FLAG_SYNC_TIMEOUT 0x20u   /* a kernel's bounded wait on its own
                                            copies ran out; its work is incomplete */
+#define LACMO_FLAG_ACC_RANGE 0x40u      /* mixed precision: a SIP's dm * xi beyond
+                                           2^58 fg in a cell sum (clamped)      */
 
 #define LACMO_SOLUTE_AS 0
 #define LACMO_SOLUTE_NACL 1

@@ -17,6 +17,8 @@ FLAG_CELL_CLAMPED = 0x2
 FLAG_NONFINITE = 0x4
 FLAG_CELL_TOO_BIG = 0x8
 FLAG_CELL_RANGE = 0x10
+FLAG_SYNC_TIMEOUT = 0x20
+FLAG_ACC_RANGE = 0x40
 NOALLOC_MAX_SIPS = 524288
 NOALLOC_MAX_CELLS = 16384
 BOX_MAX_SIPS = 8192

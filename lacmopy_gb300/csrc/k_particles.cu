@@ -354,7 +354,7 @@ struct PArgs {
   double* fb_mw;
   uint32_t* flags;
   // mixed precision
-  double* acc;                  // [C] per-cell FP64 sums of dm * xi
+  double* acc;                  // [C] per-cell sums of dm * xi, int64 units of 2^-4 fg
   int hist;                     // count SIPs per new cell for a following binning
   unsigned long long* nfb;      // SIPs whose Newton fell back to FP64
   const float4* crec;           // [C][CELL_REC] FP32 cell records (cell_records)
@@ -746,6 +746,37 @@ __device__ __forceinline__ uint64_t l2_evict_first_policy() {
 __device__ __forceinline__ void prefetch_l1(const void* p) {
   asm volatile("prefetch.global.L1 [%0];\n" ::"l"(p));
 }
+// Mixed precision: the per-cell sums of dm * xi (FP32 products) are exact
+// integer sums in units of 2^-4 fg, so their order does not matter and a
+// step gives the same bits run to run and batched or not.  v 2^4 rounded to
+// the nearest integer (halves away from zero) from the FP32 bits, without a
+// conversion instruction; |v| up to 2^58 fg (a cell's per-sub-step total
+// stays below 2^59 / 2^4 fg = 36 kg); beyond, the value is clamped and
+// LACMO_FLAG_ACC_RANGE raised.
+constexpr double ACC_UNIT = 0.0625;   // fg per integer unit
+__device__ __forceinline__ long long fix_of(float v, uint32_t* flags) {
+  const uint32_t b = __float_as_uint(v);
+  const int e = (int)((b >> 23) & 0xffu);
+  if (e == 0) return 0;   // zero or below 2^-126
+  const uint64_t m = (uint64_t)((b & 0x7fffffu) | 0x800000u);
+  const int sh = e - 146;   // v 2^4 = m 2^(e - 150 + 4)
+  uint64_t mag;
+  if (sh >= 35 || e == 0xff) {
+    atomicOr(flags, LACMO_FLAG_ACC_RANGE);
+    mag = 1ull << 58;
+  } else if (sh >= 0) {
+    mag = m << sh;
+  } else if (sh > -26) {
+    mag = (m + (1ull << (-sh - 1))) >> (-sh);
+  } else {
+    mag = 0;
+  }
+  return (b >> 31) ? -(long long)mag : (long long)mag;
+}
+__device__ __forceinline__ void acc_add(double* acc, int64_t c, float v, uint32_t* flags) {
+  atomicAdd((unsigned long long*)(acc + c), (unsigned long long)fix_of(v, flags));
+}
+
 // an mbarrier wait never spins without bound: after this many polls (each
 // try_wait suspends the thread for a while) the kernel gives up and raises
 // LACMO_FLAG_SYNC_TIMEOUT
@@ -936,8 +967,8 @@ __global__ void __launch_bounds__(PM_THREADS, MINB) k_particles_mixed(const __gr
       const bool ok = newton_mixed_f(a.sol, a.dt_subf, a.no_iter, mwf, msf, wsf, R, af.T, rho,
                                      sig, af, d_effl, &d);
       if (ok) {
-        // per-cell FP64 sum of dm * xi (executed by L2)
-        atomicAdd(a.acc + c, f2d_int(d * d2f_int(tl.get(S, PF_XI, t))));
+        // per-cell exact sum of dm * xi (executed by L2)
+        acc_add(a.acc, c, d * d2f_int(tl.get(S, PF_XI, t)), a.flags);
       } else {
         // near the critical radius the Newton repeats in FP64, in full warps
         // in k_newton_fallback: queue the SIP with its mass before the
@@ -1014,7 +1045,7 @@ __global__ void __launch_bounds__(PM_THREADS, MINB) k_particles_mixed(const __gr
                                                        a.sol, a.no_iter, a.nfb},
                                             c, mw0, tl.get(S, PF_MS, t));
         mw = mw0 + dm;
-        atomicAdd(a.acc + c, f2d_int(d2f_int(dm) * d2f_int(xik)));
+        acc_add(a.acc, c, d2f_int(dm) * d2f_int(xik), a.flags);
         a.fb_id[fb_slot] = -1;
       }
       if (PHYS) __stcs(a.m_w + k, mw);
@@ -1079,7 +1110,7 @@ __global__ void __launch_bounds__(128) k_newton_fallback(const __grid_constant__
                                                    a.sol, a.no_iter, a.nfb},
                                         c, mw0, a.m_s[k]);
     a.m_w[k] = mw0 + dm;
-    atomicAdd(a.acc + c, f2d_int(d2f_int(dm) * d2f_int(a.xi[k])));
+    acc_add(a.acc, c, d2f_int(dm) * d2f_int(a.xi[k]), a.flags);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1140,7 +1171,7 @@ __device__ __forceinline__ void grid_cell_update_mixed(double* gsf, double* gmp,
   af[2] = make_float4((float)mu, (float)rho_f, 0.0f, 0.0f);
 }
 
-// mixed precision: the grid sub-step from the per-cell FP64 sums (then zeroed)
+// mixed precision: the grid sub-step from the per-cell exact sums (then zeroed)
 __global__ void k_grid_acc(const __grid_constant__ MRef mr) {
   const Member& mb = mr.get();
   double *acc = mb.w.div, *delta_m_l = mb.g.delta_m_l, *gsf = mb.g.scalar_fields,
@@ -1150,8 +1181,9 @@ __global__ void k_grid_acc(const __grid_constant__ MRef mr) {
   const double p_ref = mb.g.p_ref, p_ref_inv = mb.g.p_ref_inv, V = mb.g.volume_cell;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
        c += (int64_t)gridDim.x * blockDim.x) {
-    const double dml = acc[c] * 1.0E-18;
-    acc[c] = 0.0;
+    long long* acc_i = (long long*)acc;
+    const double dml = (double)acc_i[c] * ACC_UNIT * 1.0E-18;
+    acc_i[c] = 0;
     delta_m_l[c] = dml;
     grid_cell_update_mixed(gsf, gmp, aux, c, C, p_ref, p_ref_inv, dTh[c], drv[c], dml, V);
   }

@@ -303,7 +303,7 @@ def _member_stats(b, m, horizon, wr0):
 
 
 def precision_ensemble(members=16, spcm=(52, 76), nx=75, nz=75, spinup=7200, horizon=3600,
-                       seed=1001, kernel="Long_Bott"):
+                       seed=1001, kernel="Long_Bott", **state_kw):
     """The precision form as ensemble statistics.  One state is spun up in
     FP64 (the reference's spin-up: no gravity, collisions or relaxation);
     ``members`` copies of it then advance ``horizon`` steps with
@@ -317,7 +317,7 @@ def precision_ensemble(members=16, spcm=(52, 76), nx=75, nz=75, spinup=7200, hor
     stays within a few standard errors of the difference."""
     from . import BatchState, DeviceState, synthetic
     st = synthetic.make_icmw_state(Nx=nx, Nz=nz, no_spcm=tuple(spcm), seed=seed,
-                                   kernel_type=kernel)
+                                   kernel_type=kernel, **state_kw)
     t0 = time.perf_counter()
     _spin_up(st, spinup, seed, draws="thinned")
     wr0 = float(st["water_removed"][0])

@@ -105,8 +105,8 @@ def test_kernel_grid_m_box_with_generated_table(oracle_py, tmp_path):
     nb, m_lo, bf = tables.kernel_grid_m_parameters(1.0E18 * mass)   # kg -> fg
     rng = np.random.default_rng(8)
     n = 300
-    xis0 = np.exp(rng.uniform(np.log(1e6), np.log(1e9), n))
-    m0 = np.exp(rng.uniform(np.log(1e5), np.log(1e10), n))   # fg: R of 3 to 130 um
+    xis0 = np.exp(rng.uniform(np.log(1e4), np.log(1e7), n))
+    m0 = np.exp(rng.uniform(np.log(1e5), np.log(1e9), n))   # fg: R of 3 to 60 um
     seed, dV, dt, t_end, dt_save = 4242, 1.0, 1.0, 4.0, 2.0
     xis, m = xis0.copy(), m0.copy()
     nc = np.zeros(2, np.int64)
