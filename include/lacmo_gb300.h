@@ -459,6 +459,17 @@ int lacmo_radius_and_bin(const double* m, const double* rho, int64_t n, double R
                          double bin_factor_R_log, int64_t no_kernel_bins, double* R,
                          int64_t* bin, void* stream);
 
+/* Event log of the all-cells collision steps of single states (not batches),
+ * for the adjoint's replay of collisions as recorded events.  While set,
+ * every such step appends one 32-byte record per collection to events[]:
+ * int32 imin, imax (the SIPs of smaller and larger multiplicity), int32 kind
+ * (0 ordinary collection, 1 equal-multiplicity split, 2 multiple collection),
+ * int32 0, double a, b (kind 1: the multiplicities of imin and imax before;
+ * kind 2: a = p_crit).  *count (device) counts the records, also those past
+ * capacity, which are not written; a cell's records appear in its sequential
+ * order.  events = null switches the log off.  Process-wide. */
+int lacmo_collision_event_log(void* events, int64_t capacity, unsigned long long* count);
+
 /* ---- adjoint of the condensation sub-steps (k_adjoint.cu) ----
  * The differentiated model: the SIPs' cells per sub-step and their
  * multiplicities are recorded events (SIP motion, ground removal and cell
@@ -518,6 +529,18 @@ int lacmo_adj_increments_vjp(const double* Th, const double* r_v, const double* 
                              const double* t_relax, double factor, double flux_scale,
                              const double* lam_inc, double* lam_Th, double* lam_rv,
                              double* grad_s, void* stream);
+/* Collisions as recorded events (records of lacmo_collision_event_log,
+ * grouped: the records of group g are events[off[g] .. off[g + 1] - 1] in
+ * their sequential order, groups independent, e.g. one per cell).
+ * lacmo_adj_collisions_forward replays them on m_w, m_s, xi as the collision
+ * step applies them (collision/all_or_nothing.py:577-633, kind 2 with the
+ * recorded p_crit); lacmo_adj_collisions_backward maps the adjoints of m_w
+ * and m_s after the events to those before (the transposed linear maps, in
+ * reverse order; p_crit and the split's multiplicities held fixed). */
+int lacmo_adj_collisions_forward(const void* events, const int64_t* off, int64_t n_groups,
+                                 double* m_w, double* m_s, double* xi, void* stream);
+int lacmo_adj_collisions_backward(const void* events, const int64_t* off, int64_t n_groups,
+                                  double* lam_w, double* lam_s, void* stream);
 
 #ifdef __cplusplus
 }

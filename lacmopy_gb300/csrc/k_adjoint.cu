@@ -557,6 +557,68 @@ __global__ void k_increments_vjp(IncArgs a, double factor, double flux_scale,
   if (gs != 0.0) atomicAdd(grad_s, gs);
 }
 
+// ---- collisions as recorded events (collision/all_or_nothing.py:577-633) ----
+struct EvRec {
+  int32_t imin, imax, kind, pad;
+  double a, b;
+};
+
+// one thread per group, the group's records in order, in the collision
+// step's own operation order
+__global__ void k_ev_forward(const EvRec* ev, const int64_t* off, int64_t G, double* MW,
+                             double* MS, double* XI) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < G;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t q = off[g]; q < off[g + 1]; ++q) {
+      const EvRec r = ev[q];
+      const int32_t imin = r.imin, imax = r.imax;
+      if (r.kind == 2) {
+        const double p = r.a;
+        const double xi_col = p * XI[imin];
+        MW[imin] = MW[imin] + p * MW[imax];
+        MS[imin] = MS[imin] + p * MS[imax];
+        XI[imax] -= xi_col;
+      } else if (r.kind == 1) {
+        const double xi_min = XI[imin], xi_max = XI[imax];
+        const double xi_ges = xi_min + xi_max;
+        MW[imin] = 2.0 * (xi_min * MW[imin] + xi_max * MW[imax]) / xi_ges;
+        MS[imin] = 2.0 * (xi_min * MS[imin] + xi_max * MS[imax]) / xi_ges;
+        MW[imax] = MW[imin];
+        MS[imax] = MS[imin];
+        XI[imax] = 0.5 * 0.7 * xi_ges;
+        XI[imin] = 0.5 * xi_ges - XI[imax];
+      } else {
+        MW[imin] += MW[imax];
+        MS[imin] += MS[imax];
+        XI[imax] -= XI[imin];
+      }
+    }
+  }
+}
+
+// the transposed maps, records in reverse order
+__global__ void k_ev_backward(const EvRec* ev, const int64_t* off, int64_t G, double* LW,
+                              double* LS) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < G;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t q = off[g + 1] - 1; q >= off[g]; --q) {
+      const EvRec r = ev[q];
+      const int32_t imin = r.imin, imax = r.imax;
+      if (r.kind == 1) {   // both take 2 (xi_min m_min + xi_max m_max) / xi_ges
+        const double xi_ges = r.a + r.b;
+        const double cmin = 2.0 * r.a / xi_ges, cmax = 2.0 * r.b / xi_ges;
+        const double sw = LW[imin] + LW[imax], ss = LS[imin] + LS[imax];
+        LW[imin] = cmin * sw; LW[imax] = cmax * sw;
+        LS[imin] = cmin * ss; LS[imax] = cmax * ss;
+      } else {   // m_min += f m_max, f = p_crit (kind 2) or 1
+        const double f = r.kind == 2 ? r.a : 1.0;
+        LW[imax] += f * LW[imin];
+        LS[imax] += f * LS[imin];
+      }
+    }
+  }
+}
+
 static inline int nb(int64_t n, int t) {
   int64_t b = (n + t - 1) / t;
   return (int)(b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b));
@@ -679,6 +741,28 @@ int lacmo_adj_increments_vjp(const double* Th, const double* r_v, const double* 
     return LACMO_ERR_ARG;
   k_increments_vjp<<<nb(2 * nx * nz, 128), 128, 0, (cudaStream_t)stream>>>(
       a, factor, flux_scale, lam_inc, lam_Th, lam_rv, grad_s);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
+}
+
+int lacmo_adj_collisions_forward(const void* events, const int64_t* off, int64_t n_groups,
+                                 double* m_w, double* m_s, double* xi, void* stream) {
+  if (n_groups < 0 || (n_groups > 0 && (!events || !off || !m_w || !m_s || !xi)))
+    return LACMO_ERR_ARG;
+  if (n_groups == 0) return LACMO_OK;
+  k_ev_forward<<<nb(n_groups, 128), 128, 0, (cudaStream_t)stream>>>(
+      (const EvRec*)events, off, n_groups, m_w, m_s, xi);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
+}
+
+int lacmo_adj_collisions_backward(const void* events, const int64_t* off, int64_t n_groups,
+                                  double* lam_w, double* lam_s, void* stream) {
+  if (n_groups < 0 || (n_groups > 0 && (!events || !off || !lam_w || !lam_s)))
+    return LACMO_ERR_ARG;
+  if (n_groups == 0) return LACMO_OK;
+  k_ev_backward<<<nb(n_groups, 128), 128, 0, (cudaStream_t)stream>>>(
+      (const EvRec*)events, off, n_groups, lam_w, lam_s);
   note_launches(1);
   return cudaGetLastError() == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
 }

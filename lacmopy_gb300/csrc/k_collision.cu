@@ -142,7 +142,18 @@ __device__ __forceinline__ int64_t pair_rank(int64_t i, int64_t j, int64_t n) {
 constexpr int CELL_SMEM = 256;
 constexpr int CELL_WARPS = 8;
 
+// one collection of the sequential order, as a log record for the adjoint's
+// replay (recorded events): kind 0 ordinary, 1 equal-xi split (a, b: xi of
+// imin and imax before), 2 multiple collection (a: p_crit)
+struct EvRec {
+  int32_t imin, imax, kind, pad;
+  double a, b;
+};
+
 struct CellArgs {
+  EvRec* log;                       // event log (single states), or null
+  int64_t log_cap;
+  unsigned long long* log_count;
   double *xi, *m_w, *m_s;
   const double* vel;
   const double* T;
@@ -176,6 +187,9 @@ struct CellArgs {
 
 // the parameters a collision step shares across members
 struct CellCommon {
+  EvRec* log;
+  int64_t log_cap;
+  unsigned long long* log_count;
   double dtdv;
   const double* E;
   double E_const;
@@ -194,6 +208,7 @@ struct CK {
   CellCommon cc;
 };
 __device__ __forceinline__ void make_cellargs(CellArgs& a, const Member& mb, const CellCommon& cc) {
+  a.log = cc.log; a.log_cap = cc.log_cap; a.log_count = cc.log_count;
   a.xi = mb.sp.xi; a.m_w = mb.sp.m_w; a.m_s = mb.sp.m_s; a.vel = mb.sp.vel;
   a.T = mb.g.scalar_fields;
   a.start = mb.w.start; a.perm = mb.w.perm; a.draw_off = mb.w.draw_off;
@@ -323,6 +338,19 @@ __device__ __noinline__ void masses_changed(const CellArgs& a, const CellSmem* S
   S->sk[l] = kb;
 }
 
+// append a collection to the event log; a cell's events come from one warp
+// in its sequential order, one at a time, so their slots increase in that
+// order (slots past the capacity are counted, not written)
+__device__ __noinline__ void log_event(const CellArgs& a, int32_t imin, int32_t imax, int kind,
+                                       double x, double y) {
+  const unsigned long long slot = atomicAdd(a.log_count, 1ull);
+  if (slot < (unsigned long long)a.log_cap) {
+    EvRec r;
+    r.imin = imin; r.imax = imax; r.kind = kind; r.pad = 0; r.a = x; r.b = y;
+    a.log[slot] = r;
+  }
+}
+
 // One ordinary collection (p_crit <= 1 and p_crit > r) of the pair imin/imax
 // (collision/all_or_nothing.py:607-633) on the global arrays; the density of
 // imin must be known.  S (may be null) receives the FP32 copies at local
@@ -337,6 +365,7 @@ __device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* 
   const double m_s_min = MS[imin], m_s_max = MS[imax];
   const double xi_rel_dev = (xi_max - xi_min) / xi_max;
   if (xi_rel_dev < 1.0E-5) {
+    if (a.log) log_event(a, imin, imax, 1, xi_min, xi_max);
     // both radii follow from imin's density (all_or_nothing.py:615-624):
     // computed now, not left stale
     ensure_density(a, imax, Tc);
@@ -358,6 +387,7 @@ __device__ __forceinline__ void collect_once(const CellArgs& a, const CellSmem* 
       S->sk[lmin] = a.gk[imin]; S->sk[lmax] = a.gk[imax];
     }
   } else {
+    if (a.log) log_event(a, imin, imax, 0, 0.0, 0.0);
     MW[imin] += m_w_max;
     MS[imin] += m_s_max;
     XI[imax] -= xi_min;
@@ -388,6 +418,7 @@ __device__ __noinline__ int exact_pair(const CellArgs& a, CellSmem Sm, int32_t i
   const double dv = sqrt(du * du + dw * dw);
   const double p_crit = xi_max * a.dtdv * (LC_PI * Rs * Rs * e * dv * 1.0E-12);
   if (p_crit > 1.0) {
+    if (a.log) log_event(a, imin, imax, 2, p_crit, 0.0);
     const double xi_col = p_crit * xi_min;
     MW[imin] = MW[imin] + p_crit * MW[imax];
     MS[imin] = MS[imin] + p_crit * MS[imax];
@@ -1317,10 +1348,19 @@ static cudaError_t launch_cells(const Bt& B, const CK& x, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// the event log of single-state collision steps (lacmo_collision_event_log)
+static std::atomic<EvRec*> g_log{nullptr};
+static std::atomic<int64_t> g_log_cap{0};
+static std::atomic<unsigned long long*> g_log_count{nullptr};
+
 cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d,
                                  cudaStream_t s) {
   if (B.M > 1 && d.draws) return cudaErrorInvalidValue;   // batches draw from Philox
   CellCommon cc;
+  cc.log = B.M == 1 ? g_log.load() : nullptr;
+  cc.log_cap = g_log_cap.load();
+  cc.log_count = g_log_count.load();
+  if (!cc.log_count) cc.log = nullptr;
   cc.dtdv = p.dt_col_over_dV; cc.E = p.E_col_grid; cc.E_const = p.E_col_const;
   cc.nb = p.no_kernel_bins; cc.lo = p.R_kernel_low_log; cc.bl = p.bin_factor_R_log;
   cc.sol = p.solute; cc.draws = d.draws; cc.n_draws = d.n_draws;
@@ -1402,3 +1442,12 @@ cudaError_t launch_radius_bin(const double* m, const double* rho, int64_t n, dou
 }
 
 }  // namespace lacmo
+
+extern "C" int lacmo_collision_event_log(void* events, int64_t capacity,
+                                         unsigned long long* count) {
+  if (events && (capacity < 0 || !count)) return LACMO_ERR_ARG;
+  lacmo::g_log_count.store(events ? count : nullptr);
+  lacmo::g_log_cap.store(events ? capacity : 0);
+  lacmo::g_log.store((lacmo::EvRec*)events);
+  return LACMO_OK;
+}

@@ -318,28 +318,42 @@ class DeviceState:
         self._subloop(p.scale_dt_cond - 1, 1 if ncol in (1, 2) else p.scale_dt_cond)
         self._substep(p.dt_sub_half, True)
 
-    def adv_step_tracked(self, record):
-        """One advection step without collisions, sub-step by sub-step
-        (integration.py:1474-1610), calling ``record(k)`` before particle
-        sub-step k = 0 .. 2 scale_dt_cond - 1, while ``self.cell`` holds the
-        cells that sub-step's condensation uses."""
+    def adv_step_tracked(self, record, collide=None):
+        """One advection step sub-step by sub-step (integration.py:1474-1610,
+        the collision placement of :1095-1294), calling ``record(k)`` before
+        particle sub-step k = 0 .. 2 scale_dt_cond - 1, while ``self.cell``
+        holds the cells that sub-step's condensation uses, and, for each
+        collision step (when the state collides), ``collide(k, step)`` with k
+        the next sub-step and ``step`` the function that runs it (default:
+        run it)."""
         p = self.params
         s = _stream()
+        col = bool(p.act_collisions)
+        collide = collide or (lambda k, step: step())
+        k = 0
+
+        def subloop(no_cond, no_col):
+            nonlocal k
+            if col and no_col == 1:
+                collide(k, self.collision_step)
+            for _ in range(no_cond):
+                if col and no_col > 1:
+                    collide(k, self.collision_step)
+                record(k)
+                k += 1
+                self._substep(p.dt_sub, False)
+            if col and no_col > no_cond:
+                collide(k, self.collision_step)
+
         _lib.check(self.lib.lacmo_adv_step_begin(ctypes.byref(self.sips), ctypes.byref(self.grid),
                                                  ctypes.byref(p), _ptr(self.ws), self.ws_bytes, s),
                    "adv_step_begin")
-        k = 0
-        for _ in range(p.scale_dt_cond):
-            record(k)
-            k += 1
-            self._substep(p.dt_sub, False)
+        ncol = p.no_col_per_adv
+        subloop(p.scale_dt_cond, 0 if ncol == 1 else (1 if ncol == 2 else p.scale_dt_cond))
         _lib.check(self.lib.lacmo_adv_step_second_half(
             ctypes.byref(self.sips), ctypes.byref(self.grid), ctypes.byref(p), _ptr(self.ws),
             self.ws_bytes, s), "adv_step_second_half")
-        for _ in range(p.scale_dt_cond - 1):
-            record(k)
-            k += 1
-            self._substep(p.dt_sub, False)
+        subloop(p.scale_dt_cond - 1, 1 if ncol in (1, 2) else p.scale_dt_cond)
         record(k)
         self._substep(p.dt_sub_half, True)
 

@@ -93,14 +93,18 @@ def step_model():
 
 
 def test_step_model_replays_the_product_run(step_model):
-    """With the recorded cells the forward model is the product's FP64 step
-    (collisions off): the same masses, Theta, r_v and surface rain."""
+    """With the recorded cells and collisions the forward model is the
+    product's FP64 step: the same masses, multiplicities, Theta, r_v and
+    surface rain."""
     st, model = step_model
-    m_w, Th, rv = model.run()
+    m_w, m_s, xi, Th, rv = model.run(full=True)
     ds = model.product
     mw_p = ds.m_w
     assert model.cells.min() < 0 <= model.cells.max()
+    assert model.n_events > 0   # collisions replayed
     torch.testing.assert_close(m_w, mw_p, rtol=1e-11, atol=1e-30)
+    torch.testing.assert_close(m_s, ds.m_s, rtol=1e-12, atol=0)
+    torch.testing.assert_close(xi, ds.xi, rtol=1e-12, atol=0)
     torch.testing.assert_close(Th, ds.gsf[2].reshape(-1), rtol=1e-13, atol=0)
     torch.testing.assert_close(rv, ds.gsf[4].reshape(-1), rtol=1e-11, atol=0)
     removed = model.rain_weights() > 0
@@ -147,13 +151,16 @@ def test_step_gradients_vs_finite_differences(step_model, target):
 
 def test_step_gradients_vs_torch_fp64_autograd():
     """The hand-written adjoint against autograd through an FP64 PyTorch
-    restatement of the same model (tests/torch_step_model.py) on the CPU."""
+    restatement of the same model (tests/torch_step_model.py) on the CPU,
+    collisions replayed in both."""
     import torch_step_model as ref
     from lacmopy_gb300 import adjoint, synthetic
     st = synthetic.make_icmw_state(Nx=4, Nz=6, no_spcm=(3, 4), seed=5, kernel_type="Long_Bott",
                                    drizzle_fraction=0.3, r_tot=12.5E-3)
+    st["dt_col_over_dV"] = 60.0 / st["grid_volume_cell"]   # collisions within two steps
     n_adv = 2
     model = adjoint.StepModel(st, n_adv)
+    assert model.n_events > 0
     gen = torch.Generator().manual_seed(3)
     w = torch.rand(model.n, generator=gen, dtype=torch.float64)
     m_s = model.m_s0.clone().requires_grad_(True)
@@ -164,7 +171,8 @@ def test_step_gradients_vs_torch_fp64_autograd():
     m_s_r = torch.as_tensor(st["m_s"], dtype=torch.float64).clone().requires_grad_(True)
     kappa_r = torch.tensor(0.6, dtype=torch.float64, requires_grad=True)
     s_r = torch.tensor(1.0, dtype=torch.float64, requires_grad=True)
-    m_w_r = ref.run(st, model.cells.cpu(), m_s_r, kappa_r, s_r, n_adv, 3)
+    m_w_r = ref.run(st, model.cells.cpu(), m_s_r, kappa_r, s_r, n_adv, 3,
+                    events=ref.decode_events(model.events))
     J_r = (w * m_w_r).sum()
     J_r.backward()
     assert abs(float(J) - float(J_r)) <= 1e-12 * abs(float(J_r))

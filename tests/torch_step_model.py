@@ -1,8 +1,10 @@
 """FP64 PyTorch restatement of the differentiated step model, for reference
 gradients by autograd.  Test infrastructure: nothing in the package imports it.
 
-The model is the reference's time step with collisions off and the SIPs'
-cells per sub-step given (recorded from a product run): per advection step
+The model is the reference's time step with the SIPs' cells per sub-step and
+the collisions given (recorded from a product run; a collection adds the
+collected masses, p_crit times them for a multiple collection, or splits an
+equal-multiplicity pair, collision/all_or_nothing.py:577-633): per advection step
 the advective + relaxation increments of Theta and r_v of the two half steps
 (integration.py:1483-1508, 1536-1561) with the upwind divergence of
 integration.py:80-287; per sub-step the condensation of every SIP in a cell
@@ -123,9 +125,54 @@ def relaxation(f, prof, trel, dt):   # integration.py:325-354
     return dt * (prof - f.sum(0) / f.shape[0]) / trel
 
 
-def run(st, cells, m_s, kappa, flux_scale, n_adv, no_iter):
+def decode_events(events):
+    """{sub-step: [(records [r][32] uint8 tensor, offsets, G), ...]} of a
+    StepModel -> {sub-step: [(imin, imax, kind, a, b), ...]} in order."""
+    import numpy as np
+    out = {}
+    for k, groups in events.items():
+        lst = []
+        for rec, _, _ in groups:
+            r = rec.cpu().numpy()
+            ints = r.view(np.int32).reshape(-1, 8)
+            dbl = r.view(np.float64).reshape(-1, 4)
+            lst += [(int(i[0]), int(i[1]), int(i[2]), float(d[2]), float(d[3]))
+                    for i, d in zip(ints, dbl)]
+        out[k] = lst
+    return out
+
+
+def collide(m_w, m_s, xi, evs):
+    """collision/all_or_nothing.py:577-633 with the recorded outcomes."""
+    for imin, imax, kind, a, b in evs:
+        w_min, w_max, s_min, s_max = m_w[imin], m_w[imax], m_s[imin], m_s[imax]
+        xmin, xmax = float(xi[imin]), float(xi[imax])
+        if kind == 2:
+            m_w = m_w.index_put((torch.tensor([imin]),), (w_min + a * w_max).reshape(1))
+            m_s = m_s.index_put((torch.tensor([imin]),), (s_min + a * s_max).reshape(1))
+            xi[imax] = xmax - a * xmin
+        elif kind == 1:
+            ges = xmin + xmax
+            w = 2.0 * (xmin * w_min + xmax * w_max) / ges
+            sm = 2.0 * (xmin * s_min + xmax * s_max) / ges
+            idx = torch.tensor([imin, imax])
+            m_w = m_w.index_put((idx,), torch.stack([w, w]))
+            m_s = m_s.index_put((idx,), torch.stack([sm, sm]))
+            xi[imax] = 0.5 * 0.7 * ges
+            xi[imin] = 0.5 * ges - xi[imax]
+        else:
+            m_w = m_w.index_put((torch.tensor([imin]),), (w_min + w_max).reshape(1))
+            m_s = m_s.index_put((torch.tensor([imin]),), (s_min + s_max).reshape(1))
+            xi[imax] = xmax - xmin
+    return m_w, m_s
+
+
+def run(st, cells, m_s, kappa, flux_scale, n_adv, no_iter, events=None):
     """Final m_w of the model; cells [2 scale_dt_cond n_adv][n] (int, < 0:
-    not condensing); m_s, kappa, flux_scale tensors (autograd)."""
+    not condensing); m_s, kappa, flux_scale tensors (autograd); events
+    {sub-step: [(imin, imax, kind, a, b), ...]} the collisions recorded
+    before that sub-step (decode_events)."""
+    events = events or {}
     nx, nz = (int(v) for v in st["grid_no_cells"])
     C = nx * nz
     t = lambda x: torch.as_tensor(x, dtype=torch.float64)
@@ -133,7 +180,7 @@ def run(st, cells, m_s, kappa, flux_scale, n_adv, no_iter):
     Th, rv = gsf[2].reshape(C).clone(), gsf[4].reshape(C).clone()
     rho_d, mdi, rdi = gsf[3].reshape(C), gsf[8].reshape(C), gsf[9].reshape(C)
     m_w = t(st["m_w"]).clone()
-    xi = t(st["xi"])
+    xi = t(st["xi"]).clone()
     flux = t(st["grid_mass_flux_air_dry"]) * flux_scale
     dx, dz = (float(v) for v in st["grid_steps"])
     dt = float(st["dt_sub"])
@@ -150,7 +197,7 @@ def run(st, cells, m_s, kappa, flux_scale, n_adv, no_iter):
                                dt).repeat(nx)
         return v
 
-    def sub_step(m_w, Th, rv, cell, dTh, drv):
+    def sub_step(m_w, m_s, Th, rv, cell, dTh, drv):
         act = cell >= 0
         ci = cell.clamp_min(0)
         a = ambient(Th, rv, rho_d, p_ref)
@@ -169,9 +216,13 @@ def run(st, cells, m_s, kappa, flux_scale, n_adv, no_iter):
         dTh = inc_first(Th, st["init_profile_Theta"])
         drv = inc_first(rv, st["init_profile_r_v"])
         for k in range(S):
-            m_w, Th, rv = sub_step(m_w, Th, rv, cells[2 * S * adv + k], dTh, drv)
+            kg = 2 * S * adv + k
+            m_w, m_s = collide(m_w, m_s, xi, events.get(kg, ()))
+            m_w, Th, rv = sub_step(m_w, m_s, Th, rv, cells[kg], dTh, drv)
         dTh = 2.0 * inc_first(Th, st["init_profile_Theta"]) - dTh
         drv = 2.0 * inc_first(rv, st["init_profile_r_v"]) - drv
         for k in range(S):
-            m_w, Th, rv = sub_step(m_w, Th, rv, cells[(2 * adv + 1) * S + k], dTh, drv)
+            kg = (2 * adv + 1) * S + k
+            m_w, m_s = collide(m_w, m_s, xi, events.get(kg, ()))
+            m_w, Th, rv = sub_step(m_w, m_s, Th, rv, cells[kg], dTh, drv)
     return m_w
