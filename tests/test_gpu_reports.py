@@ -32,10 +32,10 @@ def test_precision_form_small():
     """Mixed vs FP64 from the same spun-up state with the same draws, 30 x 30
     cells at 128 SIPs/cell, 120 steps after the spin-up: domain liquid water
     within 1e-5, Theta within 1e-5, r_v within 1e-4, water masses within 1e-3
-    for 99% of the SIPs.  At full size (75 x 75 x 128) the 1e-5 LWP bound
-    holds through 200 steps (9.6e-7) and not at 300 (4.1e-5): from then on
-    flipped collision decisions make the runs different realisations, and
-    the ensemble test below states the precision form."""
+    for 99% of the SIPs.  At full size (75 x 75 x 128, 600 s spin-up) the
+    1e-5 LWP bound holds through 300 steps (3.1e-6) and not at 400 (2.8e-5):
+    from then on flipped collision decisions make the runs different
+    realisations, and the ensemble test below states the precision form."""
     from lacmopy_gb300 import reports
     r = reports.precision(spcm=(52, 76), nx=30, nz=30, spinup=20, horizons=(120,))["rows"][0]
     assert r["lwp_rel"] < 1e-5
