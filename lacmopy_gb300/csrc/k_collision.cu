@@ -577,7 +577,7 @@ __device__ __forceinline__ void advance_seg(int n, int B, int& i, int& b, int ad
 __device__ __forceinline__ int2 thin_cell(const CellArgs& a, const CellSmem S, int n, double Tc,
                                        bool use_E, uint64_t pc1, int lane) {
   static_assert(LACMO_THIN_L == 32, "one block of slots per warp");
-  int64_t c0 = 0, c1 = 0;   // this lane's outcome counts
+  int c0 = 0, c1 = 0;   // this lane's outcome counts
   constexpr unsigned FULL = 0xffffffffu;
   const int B = (n + 31) >> 5;
   for (int b = 0; b < B; ++b) block_stats(S, n, b, lane);
@@ -630,6 +630,13 @@ __device__ __forceinline__ int2 thin_cell(const CellArgs& a, const CellSmem S, i
       }
     }
     const unsigned ev = __ballot_sync(FULL, valid && (indiv || hit));
+    const bool all_valid = __ballot_sync(FULL, valid) == FULL;
+    // the lane's segment, packed into three words for the event loop
+    // (n <= 65535 so i, j < 2^16; B <= 2048; e < 128; sub <= 32)
+    const uint32_t pk_ij = (uint32_t)i | ((uint32_t)j << 16);
+    const uint32_t pk_fe = (uint32_t)jfirst | ((uint32_t)jend << 16);
+    const uint32_t pk_b = ((uint32_t)b & 0x7ffu) | ((uint32_t)e << 11) | ((uint32_t)indiv << 18) |
+                          (sub << 19);
     // the round's segments with an event, in order.  An event that changes
     // nothing (no collection) leaves the state, and so the bounds and hit
     // draws of the later lanes, as they were: the next event of the round is
@@ -641,11 +648,13 @@ __device__ __forceinline__ int2 thin_cell(const CellArgs& a, const CellSmem S, i
     while (pend) {
       const int L = __ffs(pend) - 1;
       pend &= pend - 1u;
-      const int ei = __shfl_sync(FULL, i, L), eb = __shfl_sync(FULL, b, L);
-      const int ej = __shfl_sync(FULL, j, L), eend = __shfl_sync(FULL, jend, L);
-      const int ejf = __shfl_sync(FULL, jfirst, L), ee = __shfl_sync(FULL, e, L);
-      const uint32_t esub = __shfl_sync(FULL, sub, L);
-      const bool eind = __shfl_sync(FULL, (int)indiv, L) != 0;
+      const uint32_t qij = __shfl_sync(FULL, pk_ij, L), qfe = __shfl_sync(FULL, pk_fe, L);
+      const uint32_t qb = __shfl_sync(FULL, pk_b, L);
+      const int ei = (int)(qij & 0xffffu), ej = (int)(qij >> 16);
+      const int ejf = (int)(qfe & 0xffffu), eend = (int)(qfe >> 16);
+      const int eb = (int)(qb & 0x7ffu), ee = (int)((qb >> 11) & 0x7fu);
+      const bool eind = ((qb >> 18) & 1u) != 0;
+      const uint32_t esub = qb >> 19;
       if (!scratch) { init_exact_scratch(a, S, n, lane); scratch = true; }
       int next_j = eend;
       bool changed = false;
@@ -715,9 +724,11 @@ __device__ __forceinline__ int2 thin_cell(const CellArgs& a, const CellSmem S, i
           const bool normal = r >= 0x1p-126;
           const float r_lo = normal ? d2f_down_pos(r) : 0.0f;
           const float r_hi = normal ? __uint_as_float(__float_as_uint(r_lo) + 1u) : 0x1p-126f;
-          const int64_t before = c0 + c1;
-          decide_pair(a, S, use_E, ei, ej + g, r, r_lo, r_hi, Tc, c0, c1);
-          col = c0 + c1 != before;
+          int64_t d0 = 0, d1 = 0;
+          decide_pair(a, S, use_E, ei, ej + g, r, r_lo, r_hi, Tc, d0, d1);
+          c0 += (int)d0;
+          c1 += (int)d1;
+          col = (d0 | d1) != 0;
         }
         changed = __shfl_sync(FULL, col, 0) != 0;
         __threadfence_block();
@@ -748,9 +759,9 @@ __device__ __forceinline__ int2 thin_cell(const CellArgs& a, const CellSmem S, i
     if (cell_done) break;
     if (restart) continue;
     // every segment of the round is done
-    if (__ballot_sync(FULL, valid) != FULL) break;   // the cell's last segment is done
-    si = __shfl_sync(FULL, i, 31);
-    sb = __shfl_sync(FULL, b, 31);
+    if (!all_valid) break;   // the cell's last segment is done
+    si = (int)(__shfl_sync(FULL, pk_ij, 31) & 0xffffu);
+    sb = (int)(__shfl_sync(FULL, pk_b, 31) & 0x7ffu);
     advance_seg(n, B, si, sb, 1);
     if (sb >= B) break;
     sj = (sb << 5) > si + 1 ? (sb << 5) : si + 1;

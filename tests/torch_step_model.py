@@ -143,7 +143,11 @@ def decode_events(events):
 
 
 def collide(m_w, m_s, xi, evs):
-    """collision/all_or_nothing.py:577-633 with the recorded outcomes."""
+    """collision/all_or_nothing.py:577-633 with the recorded outcomes;
+    returns the new (m_w, m_s, xi) (xi a new tensor: the old one may be
+    saved for the backward pass)."""
+    if evs:
+        xi = xi.clone()
     for imin, imax, kind, a, b in evs:
         w_min, w_max, s_min, s_max = m_w[imin], m_w[imax], m_s[imin], m_s[imax]
         xmin, xmax = float(xi[imin]), float(xi[imax])
@@ -164,7 +168,7 @@ def collide(m_w, m_s, xi, evs):
             m_w = m_w.index_put((torch.tensor([imin]),), (w_min + w_max).reshape(1))
             m_s = m_s.index_put((torch.tensor([imin]),), (s_min + s_max).reshape(1))
             xi[imax] = xmax - xmin
-    return m_w, m_s
+    return m_w, m_s, xi
 
 
 def run(st, cells, m_s, kappa, flux_scale, n_adv, no_iter, events=None):
@@ -217,12 +221,12 @@ def run(st, cells, m_s, kappa, flux_scale, n_adv, no_iter, events=None):
         drv = inc_first(rv, st["init_profile_r_v"])
         for k in range(S):
             kg = 2 * S * adv + k
-            m_w, m_s = collide(m_w, m_s, xi, events.get(kg, ()))
+            m_w, m_s, xi = collide(m_w, m_s, xi, events.get(kg, ()))
             m_w, Th, rv = sub_step(m_w, m_s, Th, rv, cells[kg], dTh, drv)
         dTh = 2.0 * inc_first(Th, st["init_profile_Theta"]) - dTh
         drv = 2.0 * inc_first(rv, st["init_profile_r_v"]) - drv
         for k in range(S):
             kg = (2 * adv + 1) * S + k
-            m_w, m_s = collide(m_w, m_s, xi, events.get(kg, ()))
+            m_w, m_s, xi = collide(m_w, m_s, xi, events.get(kg, ()))
             m_w, Th, rv = sub_step(m_w, m_s, Th, rv, cells[kg], dTh, drv)
     return m_w
