@@ -224,6 +224,13 @@ int lacmo_batch_create(int M, const lacmo_sips_t* sips, const lacmo_grid_t* grid
 int lacmo_batch_prepare(lacmo_batch* batch, const lacmo_params_t* prm, void* stream);
 /* one advection step of every member (lacmo_integrate_adv_step, Philox draws) */
 int lacmo_batch_adv_step(lacmo_batch* batch, const lacmo_params_t* prm, void* stream);
+/* A mixed-precision batch step does not bin its SIPs after its last sub-step
+ * (the next step bins after its half-step move; the ground removals are
+ * folded into water_removed all the same), so between steps a member's
+ * binning is empty; lacmo_batch_rebin bins every member's SIPs by their
+ * current cells, for entry points that read a member's binning between steps
+ * (lacmo_update_grid_r_l with lacmo_batch_member_workspace). */
+int lacmo_batch_rebin(lacmo_batch* batch, void* stream);
 /* a CUDA graph of n_steps batch advection steps (see lacmo_plan_create) */
 int lacmo_batch_plan_create(lacmo_batch* batch, const lacmo_params_t* prm, int n_steps,
                             void* stream, lacmo_plan** plan);

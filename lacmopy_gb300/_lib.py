@@ -150,6 +150,7 @@ PROTOTYPES = {
     "lacmo_adj_backward": (ctypes.c_int, [i64, i64, vp, vp, vp, i64] + [vp] * 5 + [
         dbl, dbl, dbl, dbl, ctypes.c_int, ctypes.c_int] + [vp] * 10),
     "lacmo_collision_event_log": (ctypes.c_int, [vp, i64, vp]),
+    "lacmo_batch_rebin": (ctypes.c_int, [vp, vp]),
     "lacmo_adj_collisions_forward": (ctypes.c_int, [vp, vp, i64, vp, vp, vp, vp]),
     "lacmo_adj_collisions_backward": (ctypes.c_int, [vp, vp, i64, vp, vp, vp]),
     "lacmo_adj_increments": (ctypes.c_int, [vp] * 4 + [i64, i64, dbl, dbl, dbl] + [vp] * 3 + [

@@ -176,8 +176,13 @@ static int subloop_mixed(const Bt& B, const lacmo_params_t& p, const lacmo_draws
   return LACMO_OK;
 }
 
+// keep_binning: bin the SIPs after the step's last sub-step (single states,
+// whose entry points between steps read the binning); otherwise (mixed
+// batches) only the ground removals are folded: the next step bins after its
+// half-step move anyway, and the batch's between-step entry points rebin
+// first (lacmo_batch_rebin)
 static int adv_step_mixed(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d,
-                          cudaStream_t s) {
+                          cudaStream_t s, bool keep_binning) {
   LCHK(launch_wind_float(B, s));
   LCHK(launch_move_mixed(B, p.dt_sub_half, s));
   LCHK(launch_bin(B, s));
@@ -191,14 +196,15 @@ static int adv_step_mixed(const Bt& B, const lacmo_params_t& p, const lacmo_draw
   if (rc) return rc;
   // last sub-step; the binning afterwards keeps it valid for the entry points
   // that use it between advection steps
-  LCHK(launch_particles_mixed(B, p, p.dt_sub, p.dt_sub_half, true, true, s));
+  LCHK(launch_particles_mixed(B, p, p.dt_sub, p.dt_sub_half, true, keep_binning, s));
   LCHK(launch_grid_acc(B, s));
-  LCHK(launch_bin(B, s));
+  LCHK(keep_binning ? launch_bin(B, s) : launch_fold_removals(B, s));
   return LACMO_OK;
 }
 
-static int adv_step(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d, cudaStream_t s) {
-  if (p.precision == LACMO_PRECISION_MIXED) return adv_step_mixed(B, p, d, s);
+static int adv_step(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d, cudaStream_t s,
+                    bool keep_binning = true) {
+  if (p.precision == LACMO_PRECISION_MIXED) return adv_step_mixed(B, p, d, s, keep_binning);
   // b) x_{n+1/2} (integration.py:1474-1481)
   LCHK(launch_move(B, p.dt_sub_half, s));
   LCHK(launch_bin(B, s));
@@ -215,17 +221,18 @@ static int adv_step(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d
   // last sub-step: positions move by dt_sub/2 (integration.py:1593-1610)
   LCHK(launch_particles(B, p, p.dt_sub, p.dt_sub_half, true, s));
   LCHK(launch_cell_update(B, true, s));
-  LCHK(launch_bin(B, s));
+  LCHK(launch_bin(B, s));   // the FP64 path counts cells in every sub-step
   return LACMO_OK;
 }
 
 // capture n_steps advection steps of B into an executable graph
 static int capture_plan(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d, int n_steps,
-                        cudaStream_t s, cudaGraph_t* graph_out, cudaGraphExec_t* exec_out) {
+                        cudaStream_t s, cudaGraph_t* graph_out, cudaGraphExec_t* exec_out,
+                        bool keep_binning = true) {
   if (s == nullptr) return LACMO_ERR_ARG;  // the legacy default stream cannot be captured
   LCHK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   int rc = LACMO_OK;
-  for (int k = 0; k < n_steps && rc == LACMO_OK; ++k) rc = adv_step(B, p, d, s);
+  for (int k = 0; k < n_steps && rc == LACMO_OK; ++k) rc = adv_step(B, p, d, s, keep_binning);
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamEndCapture(s, &graph);
   if (rc != LACMO_OK || e != cudaSuccess) {
@@ -570,7 +577,15 @@ int lacmo_batch_prepare(lacmo_batch* b, const lacmo_params_t* p, void* stream) {
 int lacmo_batch_adv_step(lacmo_batch* b, const lacmo_params_t* p, void* stream) {
   if (!b || !prm_ok(p)) return LACMO_ERR_ARG;
   const lacmo_draws_t d = {nullptr, 0, 0};
-  return adv_step(b->B, *p, d, (cudaStream_t)stream);
+  return adv_step(b->B, *p, d, (cudaStream_t)stream, false);
+}
+
+int lacmo_batch_rebin(lacmo_batch* b, void* stream) {
+  if (!b) return LACMO_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  LCHK(launch_histogram(b->B, s));
+  LCHK(launch_bin(b->B, s));
+  return LACMO_OK;
 }
 
 int lacmo_batch_plan_create(lacmo_batch* b, const lacmo_params_t* p, int n_steps, void* stream,
@@ -581,7 +596,7 @@ int lacmo_batch_plan_create(lacmo_batch* b, const lacmo_params_t* p, int n_steps
   const lacmo_draws_t d = {nullptr, 0, 0};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  const int rc = capture_plan(b->B, *p, d, n_steps, (cudaStream_t)stream, &graph, &exec);
+  const int rc = capture_plan(b->B, *p, d, n_steps, (cudaStream_t)stream, &graph, &exec, false);
   if (rc != LACMO_OK) return rc;
   *out = new lacmo_plan{graph, exec};
   return LACMO_OK;

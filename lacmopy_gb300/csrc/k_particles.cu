@@ -1417,6 +1417,12 @@ cudaError_t launch_histogram(const Bt& B, cudaStream_t s) {
   k_histogram<<<grid2(B.n_max, 256, B.M), 256, 0, s>>>(B.ref()); note_launches(1);
   return cudaGetLastError();
 }
+// the ground removals folded into water_removed without binning (k_scan over
+// counts left at zero: the binning it writes is empty until the next one)
+cudaError_t launch_fold_removals(const Bt& B, cudaStream_t s) {
+  k_scan<<<dim3(1, B.M), 1024, 0, s>>>(B.ref()); note_launches(1);
+  return cudaGetLastError();
+}
 cudaError_t launch_bin(const Bt& B, cudaStream_t s) {
   const int64_t C = B.nx * B.nz;
   k_scan<<<dim3(1, B.M), 1024, 0, s>>>(B.ref()); note_launches(1);

@@ -141,6 +141,7 @@ cudaError_t launch_cell_aux(const Bt& B, cudaStream_t s);
 cudaError_t launch_set_i64(int64_t* p, int64_t v, cudaStream_t s);
 cudaError_t launch_histogram(const Bt& B, cudaStream_t s);
 cudaError_t launch_bin(const Bt& B, cudaStream_t s);
+cudaError_t launch_fold_removals(const Bt& B, cudaStream_t s);
 cudaError_t launch_particles(const Bt& B, const lacmo_params_t& p, double dt_sub,
                              double dt_sub_pos, bool write_Tp, cudaStream_t s);
 cudaError_t launch_move(const Bt& B, double dt_pos, cudaStream_t s);

@@ -583,7 +583,9 @@ class BatchState:
 
     def update_grid_r_l(self, m):
         """grid.py:370 update_grid_r_l_np of member m, with the member's slice
-        of the batch workspace (its current cell binning)."""
+        of the batch workspace (the members are binned by their current cells
+        first: a batch step does not bin after its last sub-step)."""
+        _lib.check(self.lib.lacmo_batch_rebin(self.handle, _stream()), "batch_rebin")
         ws, nb = ctypes.c_void_p(), ctypes.c_size_t()
         _lib.check(self.lib.lacmo_batch_member_workspace(self.handle, m, ctypes.byref(ws),
                                                          ctypes.byref(nb)), "member_workspace")
