@@ -879,9 +879,17 @@ static void collide_cell_2d(double* xis, double* m_w, double* m_s, double* radii
   }
 }
 
+/* the FP32 radius of a SIP whose masses a collection changed: from the
+   rounded mass sum and the rounded step-start density */
+static float th_radius_f(double m_w, double m_s, double rho) {
+  return th_cbrtf((float)LC_FOUR_PI_OVER_THREE_INV * (float)(m_w + m_s) / (float)rho);
+}
+
 /* One pair (i, j) with draw r (collision/all_or_nothing.py:553-633), as in
-   collide_cell_2d; when xf is given the FP32 copies (xi, R) of the changed
-   SIPs are refreshed the way the GPU refreshes its shared copies. */
+   collide_cell_2d.  When xf is given the FP32 copies (xi, R) of the changed
+   SIPs are refreshed the way the GPU refreshes its shared copies: an
+   equal-multiplicity split rounds the new exact radius, the other
+   collections recompute R in FP32 (th_radius_f). */
 static void process_pair_2d(int64_t i, int64_t j, double r, double* xis, double* m_w,
                             double* m_s, double* radii, const double* v0, const double* v1,
                             const double* rho, double dt_over_dV, const double* E,
@@ -904,7 +912,7 @@ static void process_pair_2d(int64_t i, int64_t j, double r, double* xis, double*
     xis[imax] -= xi_col;
     if (E) kbuf[imin] = kernel_index(radii[imin], lo, bl, nb);
     no_cols[1] += 1;
-    if (xf) { xf[imax] = (float)xis[imax]; Rf[imin] = (float)radii[imin]; }
+    if (xf) { xf[imax] = (float)xis[imax]; Rf[imin] = th_radius_f(m_w[imin], m_s[imin], rho[imin]); }
   } else if (p_crit > r) {
     no_cols[0] += 1;
     double xi_rel_dev = (xi_max - xi_min) / xi_max;
@@ -929,16 +937,17 @@ static void process_pair_2d(int64_t i, int64_t j, double r, double* xis, double*
       radii[imin] = radius_from_mass_col((m_w[imin] + m_s[imin]), rho[imin]);
       xis[imax] -= xi_min;
       if (E) kbuf[imin] = kernel_index(radii[imin], lo, bl, nb);
-      if (xf) { xf[imax] = (float)xis[imax]; Rf[imin] = (float)radii[imin]; }
+      if (xf) { xf[imax] = (float)xis[imax]; Rf[imin] = th_radius_f(m_w[imin], m_s[imin], rho[imin]); }
     }
   }
 }
 
 /* The thinned Philox draws for one cell: the sequential definition the GPU
-   kernel parallelises (segments of row i over blocks of ORC_THIN_L slots).  FP32 copies follow the GPU: xi, u, w
-   rounded from the doubles; R from the FP32 mass and density at the cell
-   temperature Tc; refreshed from the exact values after each change.  erow[k]
-   is the largest FP32 efficiency of row k of the table. */
+   kernel parallelises (segments of row i over blocks of ORC_THIN_L slots).
+   FP32 copies follow the GPU: xi, u, w rounded from the doubles; R from the
+   FP32 mass and density at the cell temperature Tc, refreshed after each
+   change as process_pair_2d says.  erow[k] is the largest FP32 efficiency of
+   row k of the table. */
 static void collide_cell_2d_thin(double* xis, double* m_w, double* m_s, double* radii,
                                  const double* v0, const double* v1, const double* rho, int64_t n,
                                  double dt_over_dV, const double* E, double E_const, int64_t nb,

@@ -247,16 +247,23 @@ def _oversized(st):
     return st
 
 
-@pytest.mark.parametrize("boost,big,const_E", [(1.0, False, False), (40.0, False, False),
-                                               (400.0, False, False), (200.0, True, False),
-                                               (40.0, False, True)])
-def test_thinned_philox_draws_match_oracle(oracle_cr, boost, big, const_E):
+@pytest.mark.parametrize("boost,big,const_E,rain", [(1.0, False, False, 0),
+                                                    (40.0, False, False, 0),
+                                                    (400.0, False, False, 0),
+                                                    (200.0, True, False, 0),
+                                                    (40.0, False, True, 0),
+                                                    (1.0, False, False, 1),
+                                                    (1.0, False, False, 4),
+                                                    (1.0, True, False, 6)])
+def test_thinned_philox_draws_match_oracle(oracle_cr, boost, big, const_E, rain):
     """Thinned Philox draws: GPU == the oracle's sequential thinning bit for
     bit over two consecutive collision steps (the FP32 segment bounds, the
     block statistics, the draws and every decision agree); with boosted
     kernels many segments take per-pair draws, and oversized cells keep their
     block statistics in global memory; a constant efficiency replaces the
-    table's row maxima."""
+    table's row maxima; drops among the droplets give a raining state (many
+    collections, FP32 radii refreshed after each)."""
+    from conftest import with_rain
     from lacmopy_gb300 import DeviceState
     if big:
         st = _oversized(_full_state(21, nx=6, nz=5, spcm=(150, 180), kernel="Hall_Bott",
@@ -264,6 +271,8 @@ def test_thinned_philox_draws_match_oracle(oracle_cr, boost, big, const_E):
     else:
         st = _full_state(13, nx=40, nz=40, kernel="Hall_Bott", drizzle_fraction=0.1,
                          r_tot=12.5E-3)
+    if rain:
+        st = with_rain(st, rain)
     st["dt_col_over_dV"] = st["dt_col_over_dV"] * boost
     if const_E:   # constant collection efficiency: the row maximum is the constant
         st["E_col_grid"] = 0.5

@@ -6,12 +6,16 @@ the conserved water mass and the multiplicity sum agree within sampling error
 import numpy as np
 import pytest
 
+from conftest import with_rain
 
-@pytest.mark.parametrize("boost", [20.0, 400.0])
-def test_thinned_and_per_pair_draws_agree_in_distribution(oracle_nb, boost):
+
+@pytest.mark.parametrize("boost,rain", [(20.0, 0), (400.0, 0), (1.0, 1), (1.0, 3)])
+def test_thinned_and_per_pair_draws_agree_in_distribution(oracle_nb, boost, rain):
     from lacmopy_gb300 import synthetic
     st = synthetic.make_icmw_state(Nx=24, Nz=24, seed=13, kernel_type="Hall_Bott",
                                    drizzle_fraction=0.1, r_tot=12.5E-3)
+    if rain:
+        st = with_rain(st, rain)
     out = {}
     for thin in (False, True):
         rows = []
