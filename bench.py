@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--spcm", type=int, nargs=2, default=[26, 38],
                     help="SIPs per cell per aerosol mode of the single-state modes")
     ap.add_argument("--e2e-members", type=int, default=4)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-single", action="store_true", help="skip the single-state modes")
@@ -483,24 +483,68 @@ def run_ours(args):
                        ("pos", "vel", "rel_pos", "m_w", "m_s", "xi", "T_p", "water_removed",
                         "cells", "grid_scalar_fields", "grid_mat_prop", "delta_m_l",
                         "no_cols")) + n
-        I.integrate_adv_step_np(*[sts[0][k] for k in keys], draws=args.draws, seed=7,
-                                precision="mixed")  # warm-up
+        import threading
+
+        updates = [0] * len(sts)   # SIP updates of the calls, per member
+
+        def calls(m, n_calls, bar=None, errs=None):
+            se = sts[m]
+            try:
+                with torch.cuda.stream(streams[m]):
+                    if bar is not None:
+                        bar.wait()
+                    for _ in range(n_calls):
+                        updates[m] += int(np.count_nonzero(se["active_ids"]))
+                        I.integrate_adv_step_np(*[se[k] for k in keys], draws=args.draws,
+                                                seed=7 + m, precision="mixed")
+                    torch.cuda.current_stream().synchronize()
+            except BaseException as ex:   # re-raised by the main thread
+                if errs is not None:
+                    errs.append(ex)
+                raise
+
+        def threaded(n_calls):
+            bar, errs = threading.Barrier(len(sts) + 1), []
+            ths = [threading.Thread(target=calls, args=(m, n_calls, bar, errs))
+                   for m in range(len(sts))]
+            for th in ths:
+                th.start()
+            bar.wait()
+            t0 = time.perf_counter()
+            for th in ths:
+                th.join()
+            torch.cuda.synchronize()
+            t = time.perf_counter() - t0
+            if errs:
+                raise errs[0]
+            return t
+
+        streams = [torch.cuda.Stream() for _ in sts]
+        threaded(1)   # warm-up: one call per member (device buffers, step graph)
+        # one host thread and CUDA stream per member, calls overlapping
+        updates[:] = [0] * len(sts)
+        te = threaded(args.e2e_steps)
+        ups_e = sum(updates)
+        # the same calls one after another from one thread
+        updates[:] = [0] * len(sts)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ups_e = 0
         for _ in range(args.e2e_steps):
-            for m, se in enumerate(sts):
-                ups_e += int(np.count_nonzero(se["active_ids"]))
-                I.integrate_adv_step_np(*[se[k] for k in keys], draws=args.draws, seed=7 + m,
-                                        precision="mixed")
+            for m in range(len(sts)):
+                calls(m, 1)
         torch.cuda.synchronize()
-        te = time.perf_counter() - t0
+        ts = time.perf_counter() - t0
+        ups_s = sum(updates)
         e2e = {"value": ups_e / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h),
                "api": "lacmopy_gb300.integration.integrate_adv_step_np (reference argument "
-                      "list, precision=\"mixed\") per member, NumPy host state copied in and "
-                      "out every call",
-               "sample": f"{len(sts)} members x {args.e2e_steps} steps of the workload"}
+                      "list, precision=\"mixed\") per member and step, NumPy host state "
+                      "copied in and out every call (into the device buffers and step graph "
+                      "the previous call of the same shape left; one untimed call per member "
+                      "first); one host thread and CUDA stream per member, calls overlapping",
+               "sample": f"{len(sts)} members x {args.e2e_steps} steps of the workload",
+               "sequential": {"value": ups_s / ts, "unit": UNIT,
+                              "api": "the same calls one after another from one thread"}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

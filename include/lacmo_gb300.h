@@ -203,6 +203,43 @@ int lacmo_plan_destroy(lacmo_plan* plan);
 /* Kernel launches one replay of the plan performs (-1 on error). */
 int64_t lacmo_plan_kernel_nodes(const lacmo_plan* plan);
 
+/* One call of integrate_adv_step_np (integration.py:1298-1313) on host
+ * arrays, in place, with the device buffers the caller keeps between calls:
+ * copies the host arrays in (the `in` list), imports the cells (lacmo_cells_
+ * import), clears the workspace, prepares (lacmo_prepare), sets the Philox
+ * collision-step counter to col_step (when >= 0), advances one step (the
+ * captured plan when given, else lacmo_integrate_adv_step), exports the
+ * cells (lacmo_cells_export into cells_out / active_out), copies the `out`
+ * list back to the host, stores the counter after the step in *col_step_out
+ * (when given) and synchronises `stream`.  One cudaMemcpyAsync per entry;
+ * host memory may be pageable.  The sips/grid/params/draws structures name
+ * the device buffers. */
+typedef struct {
+  void* dst;
+  const void* src;
+  int64_t bytes;
+} lacmo_copy_t;
+typedef struct {
+  const lacmo_copy_t* in;   /* host -> device, before the step */
+  int32_t n_in;
+  const lacmo_copy_t* out;  /* device -> host, after it         */
+  int32_t n_out;
+  const lacmo_sips_t* sips;
+  const lacmo_grid_t* grid;
+  const lacmo_params_t* prm;
+  const lacmo_draws_t* draws;
+  void* ws;
+  size_t ws_bytes;
+  const int64_t* cells_in;  /* device [2][n]: the reference's cells      */
+  const uint8_t* active_in; /* device [n]: its active_ids as bytes       */
+  int64_t* cells_out;       /* device [2][n], written by the export      */
+  uint8_t* active_out;      /* device [n]                                */
+  lacmo_plan* plan;         /* a plan of this state (one step), or NULL  */
+  int64_t col_step;         /* collision-step counter to start from; -1: 0 after the clear */
+  int64_t* col_step_out;    /* host: the counter after the step, or NULL */
+} lacmo_dropin_t;
+int lacmo_dropin_adv_step(const lacmo_dropin_t* call, void* stream);
+
 /* Batched ensemble: M independent model states (members) advanced together,
  * each kernel launch covering all members (blockIdx.y = member).  The
  * reference runs one simulation per process (integration.py:1790-2066

@@ -65,6 +65,19 @@ class Draws(ctypes.Structure):
     _fields_ = [("draws", vp), ("n_draws", i64), ("seed", u64)]
 
 
+class Copy(ctypes.Structure):
+    _fields_ = [("dst", vp), ("src", vp), ("bytes", i64)]
+
+
+class Dropin(ctypes.Structure):
+    _fields_ = [("in_", ctypes.POINTER(Copy)), ("n_in", i32), ("out", ctypes.POINTER(Copy)),
+                ("n_out", i32), ("sips", ctypes.POINTER(Sips)), ("grid", ctypes.POINTER(Grid)),
+                ("prm", ctypes.POINTER(Params)), ("draws", ctypes.POINTER(Draws)), ("ws", vp),
+                ("ws_bytes", ctypes.c_size_t), ("cells_in", vp), ("active_in", vp),
+                ("cells_out", vp), ("active_out", vp), ("plan", vp), ("col_step", i64),
+                ("col_step_out", ctypes.POINTER(i64))]
+
+
 P = ctypes.POINTER
 # name -> (restype, argtypes)
 PROTOTYPES = {
@@ -93,6 +106,7 @@ PROTOTYPES = {
     "lacmo_plan_launch": (ctypes.c_int, [vp, vp]),
     "lacmo_plan_destroy": (ctypes.c_int, [vp]),
     "lacmo_plan_kernel_nodes": (i64, [vp]),
+    "lacmo_dropin_adv_step": (ctypes.c_int, [P(Dropin), vp]),
     "lacmo_batch_workspace_bytes": (sz, [ctypes.c_int, P(i64), i64, i64]),
     "lacmo_batch_create": (ctypes.c_int, [ctypes.c_int, P(Sips), P(Grid), P(Params), P(u64), vp,
                                           sz, P(vp)]),

@@ -493,6 +493,50 @@ int lacmo_plan_destroy(lacmo_plan* pl) {
   return LACMO_OK;
 }
 
+int lacmo_dropin_adv_step(const lacmo_dropin_t* c, void* stream) {
+  if (!c || !sips_ok(c->sips) || !grid_ok(c->grid) || !prm_ok(c->prm) || !c->draws ||
+      !c->cells_in || !c->active_in || !c->cells_out || !c->active_out || c->n_in < 0 ||
+      c->n_out < 0 || (c->n_in && !c->in) || (c->n_out && !c->out))
+    return LACMO_ERR_ARG;
+  if (c->draws->draws && c->draws->n_draws < 0) return LACMO_ERR_ARG;
+  const lacmo_sips_t& sp = *c->sips;
+  const lacmo_grid_t& g = *c->grid;
+  Ws w;
+  if (!ws_carve(c->ws, c->ws_bytes, sp.n, g.nx, g.nz, &w)) return LACMO_ERR_WORKSPACE;
+  for (int32_t i = 0; i < c->n_in + c->n_out; ++i) {
+    const lacmo_copy_t& e = i < c->n_in ? c->in[i] : c->out[i - c->n_in];
+    if (e.bytes < 0 || (e.bytes && (!e.dst || !e.src))) return LACMO_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int32_t i = 0; i < c->n_in; ++i)
+    if (c->in[i].bytes)
+      LCHK(cudaMemcpyAsync(c->in[i].dst, c->in[i].src, (size_t)c->in[i].bytes,
+                           cudaMemcpyHostToDevice, s));
+  LCHK(launch_cells_import(c->cells_in, c->active_in, sp.cell, sp.n, g.nx, g.nz, s));
+  LCHK(cudaMemsetAsync(c->ws, 0, ws_bytes(sp.n, g.nx, g.nz), s));
+  const Bt B = single(sp, g, w, c->draws->seed);
+  LCHK(launch_cell_aux(B, s));
+  LCHK(launch_histogram(B, s));
+  LCHK(launch_bin(B, s));
+  if (c->col_step >= 0) LCHK(launch_set_i64(w.col_step, c->col_step, s));
+  if (c->plan) {
+    LCHK(cudaGraphLaunch(c->plan->exec, s));
+  } else {
+    const int rc = adv_step(B, *c->prm, *c->draws, s);
+    if (rc != LACMO_OK) return rc;
+  }
+  LCHK(launch_cells_export(sp.cell, sp.pos, sp.rel_pos, c->cells_out, c->active_out, sp.n, g.nx,
+                           g.nz, g.x_min, g.z_min, g.dx, g.dz, s));
+  if (c->col_step_out)
+    LCHK(cudaMemcpyAsync(c->col_step_out, w.col_step, 8, cudaMemcpyDeviceToHost, s));
+  for (int32_t i = 0; i < c->n_out; ++i)
+    if (c->out[i].bytes)
+      LCHK(cudaMemcpyAsync(c->out[i].dst, c->out[i].src, (size_t)c->out[i].bytes,
+                           cudaMemcpyDeviceToHost, s));
+  LCHK(cudaStreamSynchronize(s));
+  return LACMO_OK;
+}
+
 struct lacmo_batch {
   Bt B;
   std::vector<Member> members;

@@ -27,6 +27,8 @@ from . import _lib
 from .constants import solute_code
 
 F64 = torch.float64
+_NP_OF = {torch.float64: np.dtype(np.float64), torch.int64: np.dtype(np.int64),
+          torch.uint8: np.dtype(np.uint8), torch.int32: np.dtype(np.int32)}
 
 # Philox collision-step counter per seed for the drop-in step functions.  They
 # build a fresh device state on every call; without this the counter would
@@ -70,6 +72,24 @@ def _copy_to_host(dst, t):
         np.copyto(dst, t.cpu().numpy().reshape(np.shape(dst)))
 
 
+def _upload_into(t, a):
+    """The host array ``a`` into the existing device tensor ``t`` (same
+    element type and count) in place; False when ``a`` is not such an array
+    (a tensor, a scalar, another type or size, a non-contiguous view)."""
+    if isinstance(a, torch.Tensor) or np.ndim(a) == 0:
+        return False
+    arr = np.asarray(a)
+    if arr.dtype == np.bool_:
+        arr = arr.view(np.uint8)
+    if arr.size != t.numel() or not arr.flags.c_contiguous or not arr.flags.writeable:
+        return False
+    src = torch.from_numpy(arr)
+    if src.dtype != t.dtype:
+        return False
+    t.view(-1).copy_(src.view(-1), non_blocking=True)
+    return True
+
+
 def to_device(a, dtype=F64, device="cuda"):
     """NumPy array / scalar / tensor -> contiguous CUDA tensor of ``dtype``."""
     if isinstance(a, torch.Tensor):
@@ -89,43 +109,49 @@ class DeviceState:
                  "grid_mass_flux_air_dry")
 
     def __init__(self, st, device="cuda", draws="philox", seed=1001, precision="fp64",
-                 workspace=True, thin=False):
+                 workspace=True, thin=False, reuse=None):
+        """``reuse``: a DeviceState of the same shape (SIP count and grid)
+        that is done with: its device buffers (and, for the same parameters
+        and draw source, its captured step graph) take this state's data
+        instead of new allocations, and it must not be used afterwards."""
         self.lib = _lib.load()
         self.device = device
         g = st["grid_no_cells"]
         self.nx, self.nz = int(g[0]), int(g[1])
         pos = np.asarray(st["pos"]) if not isinstance(st["pos"], torch.Tensor) else st["pos"]
         self.n = int(pos.shape[1])
+        self._plan_handle = None
+        self._reuse = (reuse if reuse is not None and (reuse.n, reuse.nx, reuse.nz, reuse.device)
+                       == (self.n, self.nx, self.nz, device) else None)
         dev = device
-        self.pos = to_device(st["pos"], device=dev)
-        self.vel = to_device(st["vel"], device=dev)
-        self.rel_pos = to_device(st["rel_pos"], device=dev)
-        self.m_w = to_device(st["m_w"], device=dev)
-        self.m_s = to_device(st["m_s"], device=dev)
-        self.xi = to_device(st["xi"], device=dev)
-        self.T_p = to_device(st["T_p"], device=dev)
-        self.water_removed = to_device(st["water_removed"], device=dev)
-        self.no_cols = to_device(st.get("no_cols", np.zeros(2, np.int64)), torch.int64, dev)
-        self.cell = torch.empty(self.n, dtype=torch.int32, device=dev)
-        cells = to_device(st["cells"], torch.int64, dev)
-        act = to_device(np.asarray(st["active_ids"]).astype(np.uint8)
-                        if not isinstance(st["active_ids"], torch.Tensor) else st["active_ids"],
-                        torch.uint8, dev)
+        self.pos = self._dev("pos", st["pos"])
+        self.vel = self._dev("vel", st["vel"])
+        self.rel_pos = self._dev("rel_pos", st["rel_pos"])
+        self.m_w = self._dev("m_w", st["m_w"])
+        self.m_s = self._dev("m_s", st["m_s"])
+        self.xi = self._dev("xi", st["xi"])
+        self.T_p = self._dev("T_p", st["T_p"])
+        self.water_removed = self._dev("water_removed", st["water_removed"])
+        self.no_cols = self._dev("no_cols", st.get("no_cols", np.zeros(2, np.int64)), torch.int64)
+        self.cell = (self._reuse.cell if self._reuse is not None
+                     else torch.empty(self.n, dtype=torch.int32, device=dev))
+        # the reference's cells (int64) and active flags (bool, as bytes)
+        self._cells_in = self._dev("_cells_in", st["cells"], torch.int64)
+        act = st["active_ids"]
+        if not isinstance(act, torch.Tensor):
+            act = np.asarray(act)
+            act = act.view(np.uint8) if act.dtype == np.bool_ else act.astype(np.uint8)
+        self._act_in = self._dev("_act_in", act, torch.uint8)
         s = _stream()
-        _lib.check(self.lib.lacmo_cells_import(_ptr(cells), _ptr(act), _ptr(self.cell), self.n,
-                                               self.nx, self.nz, s), "cells_import")
-        self.gsf = to_device(st["grid_scalar_fields"], device=dev)
-        self.gmp = to_device(st["grid_mat_prop"], device=dev)
-        self.gvel = to_device(st["grid_velocity"], device=dev)
-        self.flux = to_device(st["grid_mass_flux_air_dry"], device=dev)
-        self.delta_m_l = to_device(st["delta_m_l"], device=dev)
-        ranges = np.asarray(st["grid_ranges"], dtype=np.float64)
-        steps = np.asarray(st["grid_steps"], dtype=np.float64)
-        self.grid = _lib.Grid(self.nx, self.nz, self.gsf.data_ptr(), self.gmp.data_ptr(),
-                              self.gvel.data_ptr(), self.flux.data_ptr(),
-                              self.delta_m_l.data_ptr(), ranges[0, 0], ranges[0, 1], ranges[1, 0],
-                              ranges[1, 1], steps[0], steps[1], float(st["grid_volume_cell"]),
-                              float(st["p_ref"]), float(st["p_ref_inv"]))
+        _lib.check(self.lib.lacmo_cells_import(_ptr(self._cells_in), _ptr(self._act_in),
+                                               _ptr(self.cell), self.n, self.nx, self.nz, s),
+                   "cells_import")
+        self.gsf = self._dev("gsf", st["grid_scalar_fields"])
+        self.gmp = self._dev("gmp", st["grid_mat_prop"])
+        self.gvel = self._dev("gvel", st["grid_velocity"])
+        self.flux = self._dev("flux", st["grid_mass_flux_air_dry"])
+        self.delta_m_l = self._dev("delta_m_l", st["delta_m_l"])
+        self.grid = self._make_grid(st)
         self.sips = _lib.Sips(self.n, self.pos.data_ptr(), self.vel.data_ptr(),
                               self.rel_pos.data_ptr(), self.m_w.data_ptr(), self.m_s.data_ptr(),
                               self.xi.data_ptr(), self.T_p.data_ptr(), self.cell.data_ptr(),
@@ -142,36 +168,76 @@ class DeviceState:
         self.draw_buf = None
         if not workspace:   # a batch member: the batch owns the workspace
             self.ws, self.ws_bytes = None, 0
+            self._reuse = None
             return
         self.ws_bytes = int(self.lib.lacmo_workspace_bytes(self.n, self.nx, self.nz))
-        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
+        old = self._reuse
+        self.ws = (old.ws if old is not None and old.ws is not None
+                   and old.ws_bytes == self.ws_bytes else
+                   torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev))
         _lib.check(self.lib.lacmo_workspace_reset(_ptr(self.ws), self.ws_bytes, self.n, self.nx,
                                                   self.nz, s), "workspace_reset")
         if not isinstance(draws, str):
-            self.draw_buf = to_device(draws, device=dev)
+            self.draw_buf = self._dev("draw_buf", draws)
+        if old is not None:
+            # the captured step graph holds the buffers' addresses, the
+            # parameters and the draw source: it carries over when they match
+            h = getattr(old, "_plan_handle", None)
+            if (h is not None and self.draw_buf is None and old.draw_buf is None
+                    and bytes(self.params) == bytes(old.params) and self.seed == old.seed
+                    and bytes(self.grid) == bytes(old.grid)
+                    and bytes(self.sips) == bytes(old.sips) and self.ws is old.ws):
+                self._plan_handle = h
+                self._plan_draws = old._plan_draws
+                old._plan_handle = None
+        self._reuse = None
         self.prepare()
+
+    def _dev(self, name, a, dtype=F64):
+        """``a`` on the device: into the reused state's buffer ``name`` when
+        it fits, else a new tensor (to_device)."""
+        old = getattr(self._reuse, name, None) if getattr(self, "_reuse", None) is not None \
+            else None
+        if isinstance(old, torch.Tensor) and old.dtype == dtype and _upload_into(old, a):
+            return old
+        return to_device(a, dtype, self.device)
 
     # -- parameters -------------------------------------------------------------
     def set_params(self, st):
         dev = self.device
         nz = self.nz
-        prof = lambda k: (to_device(st[k], device=dev) if st.get(k) is not None
-                          else torch.zeros(nz, dtype=F64, device=dev))
-        self.prof_rv = prof("init_profile_r_v")
-        self.prof_th = prof("init_profile_Theta")
-        self.t_relax = prof("relaxation_time_profile")
+        prof = lambda k, name: (self._dev(name, st[k]) if st.get(k) is not None
+                                else torch.zeros(nz, dtype=F64, device=dev))
+        self._no_prof = {"prof_rv": st.get("init_profile_r_v") is None,
+                         "prof_th": st.get("init_profile_Theta") is None,
+                         "t_relax": st.get("relaxation_time_profile") is None}
+        self.prof_rv = prof("init_profile_r_v", "prof_rv")
+        self.prof_th = prof("init_profile_Theta", "prof_th")
+        self.t_relax = prof("relaxation_time_profile", "t_relax")
         E = st["E_col_grid"]
         if isinstance(E, (float, np.floating)) or np.ndim(E) == 0:
             self.E = None
             E_const = float(E)
             nb, lo, bl = 0, 0.0, 1.0
         else:
-            self.E = to_device(E, device=dev)
+            self.E = self._dev("E", E)
+            E_const = 0.0
+            nb, lo, bl = (int(st["no_kernel_bins"]), float(st["R_kernel_low_log"]),
+                          float(st["bin_factor_R_log"]))
+        self.params = self._make_params(st)
+
+    def _make_params(self, st):
+        """The parameter structure of ``st`` over this state's device buffers
+        (profiles and efficiency table as set_params placed them)."""
+        E = st["E_col_grid"]
+        if isinstance(E, (float, np.floating)) or np.ndim(E) == 0:
+            E_const, nb, lo, bl = float(E), 0, 0.0, 1.0
+        else:
             E_const = 0.0
             nb, lo, bl = (int(st["no_kernel_bins"]), float(st["R_kernel_low_log"]),
                           float(st["bin_factor_R_log"]))
         has_relax = st.get("init_profile_r_v") is not None
-        self.params = _lib.Params(
+        return _lib.Params(
             float(st["dt"]), float(st["dt_sub"]), float(st["dt_sub_half"]),
             float(st["dt_col_over_dV"]), float(st["g_set"]), int(st["scale_dt_cond"]),
             int(st["no_col_per_adv"]), int(bool(st["act_collisions"])),
@@ -180,6 +246,106 @@ class DeviceState:
             self.t_relax.data_ptr(), self.E.data_ptr() if self.E is not None else None, E_const,
             nb, lo, bl, _lib.PRECISION_MIXED if getattr(self, "precision", "fp64") == "mixed"
             else _lib.PRECISION_FP64, int(getattr(self, "thin", False)))
+
+    def _make_grid(self, st):
+        ranges = np.asarray(st["grid_ranges"], dtype=np.float64)
+        steps = np.asarray(st["grid_steps"], dtype=np.float64)
+        return _lib.Grid(self.nx, self.nz, self.gsf.data_ptr(), self.gmp.data_ptr(),
+                         self.gvel.data_ptr(), self.flux.data_ptr(), self.delta_m_l.data_ptr(),
+                         ranges[0, 0], ranges[0, 1], ranges[1, 0], ranges[1, 1], steps[0],
+                         steps[1], float(st["grid_volume_cell"]), float(st["p_ref"]),
+                         float(st["p_ref_inv"]))
+
+    # host arrays of integrate_adv_step_np and the device buffers they fill
+    # (copied in) or take (copied out); cells and active flags go through
+    # the import / export kernels
+    _IN = (("pos", "pos"), ("vel", "vel"), ("rel_pos", "rel_pos"), ("m_w", "m_w"),
+           ("m_s", "m_s"), ("xi", "xi"), ("T_p", "T_p"), ("water_removed", "water_removed"),
+           ("no_cols", "no_cols"), ("_cells_in", "cells"), ("_act_in", "active_ids"),
+           ("gsf", "grid_scalar_fields"), ("gmp", "grid_mat_prop"), ("gvel", "grid_velocity"),
+           ("flux", "grid_mass_flux_air_dry"), ("delta_m_l", "delta_m_l"),
+           ("prof_rv", "init_profile_r_v"), ("prof_th", "init_profile_Theta"),
+           ("t_relax", "relaxation_time_profile"), ("E", "E_col_grid"))
+    _OUT = (("pos", "pos"), ("vel", "vel"), ("rel_pos", "rel_pos"), ("m_w", "m_w"),
+            ("m_s", "m_s"), ("xi", "xi"), ("T_p", "T_p"), ("water_removed", "water_removed"),
+            ("gsf", "grid_scalar_fields"), ("gmp", "grid_mat_prop"), ("delta_m_l", "delta_m_l"),
+            ("no_cols", "no_cols"), ("_cells_out", "cells"), ("_act_out", "active_ids"))
+
+    @staticmethod
+    def _host_view(a, t, write):
+        """``a`` as a C-contiguous NumPy array of ``t``'s element type and
+        count (writeable when ``write``), or None."""
+        if not isinstance(a, np.ndarray):
+            return None
+        if a.dtype == np.bool_:
+            a = a.view(np.uint8)
+        if (a.size != t.numel() or not a.flags.c_contiguous or (write and not a.flags.writeable)
+                or a.dtype != _NP_OF[t.dtype]):
+            return None
+        return a
+
+    def dropin_step(self, st, seed, draws, precision, col_step=None):
+        """One integrate_adv_step_np call on the host arrays of ``st`` in one
+        native call (lacmo_dropin_adv_step): the arrays are copied into this
+        state's buffers, the step replays the captured graph, and the results
+        are copied back in place.  Returns False, having done nothing, when
+        the call does not fit this state (shape, array types, parameters,
+        draw source), for the caller to build a new state instead."""
+        thin = draws == "thinned"
+        if (self.ws is None or draws not in ("philox", "thinned") or self.draw_mode != "philox"
+                or self.thin != thin or self.precision != precision or self.seed != int(seed)
+                or self.draw_buf is not None):
+            return False
+        if getattr(self, "_cells_out", None) is None:
+            self._cells_out = torch.empty((2, self.n), dtype=torch.int64, device=self.device)
+            self._act_out = torch.empty(self.n, dtype=torch.uint8, device=self.device)
+        ins, outs, keep = [], [], []
+        for name, key in self._IN:
+            t = getattr(self, name)
+            a = st.get(key)
+            if name in self._no_prof:   # an absent profile stays zeros on the device
+                if self._no_prof[name] != (a is None):
+                    return False
+                if a is None:
+                    continue
+            elif name == "E":           # a constant efficiency lives in the parameters
+                if (t is None) != (np.ndim(a) == 0):
+                    return False
+                if t is None:
+                    continue
+            h = self._host_view(a, t, False)
+            if h is None:
+                return False
+            keep.append(h)
+            ins.append((t.data_ptr(), h.ctypes.data, h.nbytes))
+        for name, key in self._OUT:
+            t = getattr(self, name)
+            a = st.get(key)
+            if a is None:
+                continue
+            h = self._host_view(a, t, True)
+            if h is None:
+                return False
+            keep.append(h)
+            outs.append((h.ctypes.data, t.data_ptr(), h.nbytes))
+        if (bytes(self._make_params(st)) != bytes(self.params)
+                or bytes(self._make_grid(st)) != bytes(self.grid)):
+            return False
+        plan = self._plan()
+        cin = (_lib.Copy * max(1, len(ins)))(*[_lib.Copy(*e) for e in ins])
+        cout = (_lib.Copy * max(1, len(outs)))(*[_lib.Copy(*e) for e in outs])
+        d = self._draws_struct()
+        after = ctypes.c_int64(0)
+        call = _lib.Dropin(cin, len(ins), cout, len(outs), ctypes.pointer(self.sips),
+                           ctypes.pointer(self.grid), ctypes.pointer(self.params),
+                           ctypes.pointer(d), self.ws.data_ptr(), self.ws_bytes,
+                           self._cells_in.data_ptr(), self._act_in.data_ptr(),
+                           self._cells_out.data_ptr(), self._act_out.data_ptr(), plan,
+                           philox_counter(seed) if col_step is None else int(col_step),
+                           ctypes.pointer(after))
+        _lib.check(self.lib.lacmo_dropin_adv_step(ctypes.byref(call), _stream()), "dropin_adv_step")
+        _philox_next[self.seed] = int(after.value)
+        return True
 
     def prepare(self):
         _lib.check(self.lib.lacmo_prepare(ctypes.byref(self.sips), ctypes.byref(self.grid),

@@ -17,10 +17,20 @@ previous call with that seed stopped (``lacmopy_gb300.device.philox_counter``),
 so every call draws fresh uniforms as the reference does.  ``col_step=k``
 pins the counter; ``lacmopy_gb300.device.reset_philox_counters`` restarts it.
 
+``integrate_adv_step_np`` keeps the device buffers of its last call per state
+shape (SIP count and grid) and reuses them, with the captured step graph when
+the parameters and draw source are the same, for the next call with NumPy
+arrays of that shape: the call then copies the arrays in, steps and copies
+them back without allocating.  ``release_resident()`` frees those buffers.
+Calls for different states may come from several host threads, each with its
+own current CUDA stream (``torch.cuda.stream``): they overlap on the GPU.
+
 For repeated stepping keep the state on the device with
 ``lacmopy_gb300.DeviceState`` instead of calling these per step.
 """
 import ctypes
+import threading
+from collections import OrderedDict
 
 import numpy as np
 import torch
@@ -60,14 +70,49 @@ def integrate_adv_step_np(grid_scalar_fields, grid_mat_prop, grid_velocity,
         act_relaxation, init_profile_r_v, init_profile_Theta, relaxation_time_profile,
         no_iter_impl_mass, g_set, E_col_grid, no_kernel_bins, R_kernel_low_log,
         bin_factor_R_log, no_cols)))
-    ds = DeviceState(st, draws=draws, seed=seed, precision=precision)
+    # NumPy arrays only: CUDA tensors passed in are the device state itself
+    host = not any(isinstance(v, torch.Tensor) for v in st.values())
+    key = (np.shape(pos)[1], int(grid_no_cells[0]), int(grid_no_cells[1]))
+    old = None
+    if host:
+        with _resident_lock:
+            old = _resident.pop(key, None)
+        # the state of the last call of this shape: copies in, the graph step
+        # and the copies back in one native call
+        if (old is not None and isinstance(draws, str)
+                and old.dropin_step(st, seed, draws, precision, col_step)):
+            with _resident_lock:
+                _resident[key] = old
+            return
+    ds = DeviceState(st, draws=draws, seed=seed, precision=precision, reuse=old)
     philox = isinstance(draws, str) and draws in ("philox", "thinned")
     if philox:
         ds.continue_philox(col_step)
-    ds.adv_step(1)
+    ds.adv_step(1, graph=philox)
     if philox:
         ds.record_philox()
     ds.export_to(st)
+    if host:
+        with _resident_lock:
+            _resident[key] = ds
+            while len(_resident) > _RESIDENT_MAX:
+                _resident.popitem(last=False)
+
+
+# the device states of the last integrate_adv_step_np calls with NumPy arrays,
+# by (SIP count, nx, nz), oldest first; their buffers serve the next call of
+# the same shape.  Calls from several host threads (each on its own current
+# CUDA stream) run concurrently: a call takes its shape's state out of the
+# table for its duration.
+_resident = OrderedDict()
+_resident_lock = threading.Lock()
+_RESIDENT_MAX = 8
+
+
+def release_resident():
+    """Free the device buffers integrate_adv_step_np keeps between calls."""
+    with _resident_lock:
+        _resident.clear()
 
 
 def propagate_particles_subloop_step_np(grid_scalar_fields, grid_mat_prop, grid_velocity,

@@ -88,3 +88,114 @@ def test_repeated_collision_calls_draw_fresh_uniforms(draws):
     assert outs[0][2].sum() > 0 and outs[1][2].sum() > 0
     assert not np.array_equal(outs[0][0], outs[1][0])
     reset_philox_counters(seed)
+
+
+def test_resident_buffers_and_graph_between_calls():
+    """integrate_adv_step_np keeps its device buffers (and the captured step
+    graph) between calls of the same shape: three calls in mixed precision
+    equal three steps of one resident DeviceState bit for bit; a call with
+    changed parameters captures a new graph and equals a fresh state with
+    those parameters; another shape in between leaves both intact."""
+    from lacmopy_gb300 import DeviceState
+    from lacmopy_gb300 import integration as I
+    from lacmopy_gb300.device import reset_philox_counters
+    seed = 913
+    st = _state(seed=47)
+    key = (st["pos"].shape[1], 20, 18)
+    want_ds = DeviceState(copy.deepcopy(st), draws="thinned", seed=seed, precision="mixed")
+    want_ds.adv_step(3)
+    want = want_ds.snapshot()
+
+    I.release_resident()
+    reset_philox_counters(seed)
+    got = copy.deepcopy(st)
+    other = _state(seed=48)
+    other["pos"] = other["pos"][:, :-5].copy()   # another SIP count
+    for k in ("vel", "rel_pos"):
+        other[k] = other[k][:, :-5].copy()
+    for k in ("m_w", "m_s", "xi", "T_p", "active_ids"):
+        other[k] = other[k][:-5].copy()
+    other["cells"] = other["cells"][:, :-5].copy()
+    plans = []
+    for step in range(3):
+        I.integrate_adv_step_np(*[got[k] for k in I._STATE_KEYS], draws="thinned", seed=seed,
+                                precision="mixed")
+        plans.append(I._resident[key]._plan_handle.value)
+        if step == 0:
+            I.integrate_adv_step_np(*[other[k] for k in I._STATE_KEYS], draws="thinned",
+                                    seed=seed + 1, precision="mixed")
+    assert plans[0] == plans[1] == plans[2]          # one graph, replayed
+    assert want["no_cols"].sum() > 0
+    for k in ("xi", "m_w", "m_s", "pos", "vel", "T_p", "grid_scalar_fields", "no_cols"):
+        assert np.array_equal(got[k], want[k]), k
+    assert np.array_equal(got["cells"], want["cells"])
+
+    # changed parameters: a new graph, the results of a fresh state
+    got2 = copy.deepcopy(got)
+    got2["dt_col_over_dV"] = got2["dt_col_over_dV"] * 2.0
+    fresh = DeviceState(copy.deepcopy(got2), draws="thinned", seed=seed, precision="mixed")
+    fresh.continue_philox(6)
+    fresh.adv_step(1)
+    want2 = fresh.snapshot()
+    reset_philox_counters(seed)
+    I.integrate_adv_step_np(*[got2[k] for k in I._STATE_KEYS], draws="thinned", seed=seed,
+                            precision="mixed", col_step=6)
+    assert I._resident[key]._plan_handle.value != plans[0]
+    for k in ("xi", "m_w", "m_s", "pos", "vel", "no_cols"):
+        assert np.array_equal(got2[k], want2[k]), k
+    I.release_resident()
+    assert not I._resident
+    reset_philox_counters(seed)
+    reset_philox_counters(seed + 1)
+
+
+def test_concurrent_dropin_calls_from_threads():
+    """Two host threads, each on its own CUDA stream, step their own states
+    through integrate_adv_step_np at the same time: each equals its own
+    resident DeviceState bit for bit."""
+    import threading
+    from lacmopy_gb300 import DeviceState
+    from lacmopy_gb300 import integration as I
+    from lacmopy_gb300.device import reset_philox_counters
+    states = [_state(seed=51), _state(seed=52)]
+    states[1]["pos"] = states[1]["pos"][:, :-3].copy()
+    for k in ("vel", "rel_pos"):
+        states[1][k] = states[1][k][:, :-3].copy()
+    for k in ("m_w", "m_s", "xi", "T_p", "active_ids"):
+        states[1][k] = states[1][k][:-3].copy()
+    states[1]["cells"] = states[1]["cells"][:, :-3].copy()
+    seeds = [301, 302]
+    want = []
+    for st, sd in zip(states, seeds):
+        ds = DeviceState(copy.deepcopy(st), draws="thinned", seed=sd, precision="mixed")
+        ds.adv_step(3)
+        want.append(ds.snapshot())
+    for sd in seeds:
+        reset_philox_counters(sd)
+    I.release_resident()
+    got = [copy.deepcopy(st) for st in states]
+    errs = []
+
+    def run(m):
+        try:
+            with torch.cuda.stream(torch.cuda.Stream()):
+                for _ in range(3):
+                    I.integrate_adv_step_np(*[got[m][k] for k in I._STATE_KEYS], draws="thinned",
+                                            seed=seeds[m], precision="mixed")
+        except BaseException as ex:
+            errs.append(ex)
+
+    ths = [threading.Thread(target=run, args=(m,)) for m in range(2)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    torch.cuda.synchronize()
+    assert not errs, errs
+    for m in range(2):
+        assert want[m]["no_cols"].sum() > 0
+        for k in ("xi", "m_w", "m_s", "pos", "vel", "no_cols"):
+            assert np.array_equal(got[m][k], want[m][k]), (m, k)
+    I.release_resident()
+    for sd in seeds:
+        reset_philox_counters(sd)
