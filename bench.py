@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--nz", type=int, default=75)
     ap.add_argument("--spcm", type=int, nargs=2, default=[26, 38],
                     help="SIPs per cell per aerosol mode of the single-state modes")
-    ap.add_argument("--e2e-members", type=int, default=4)
+    ap.add_argument("--e2e-members", type=int, default=8)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")

@@ -1298,14 +1298,34 @@ __global__ void k_table_to_float(const double* __restrict__ E, float* __restrict
        k += (int64_t)gridDim.x * blockDim.x)
     Ef[k] = (float)E[k];
 }
-// largest FP32 efficiency of each row, in column order (the oracle's order)
+// largest FP32 efficiency of each row, one warp per row: the maximum of the
+// row's positive values by a warp reduction; a row with a NaN, or whose
+// largest value is not positive (where the sign of a zero or the place of a
+// NaN decides), is taken in column order by one lane, as the oracle does
 __global__ void k_table_rowmax(const double* __restrict__ E, float* __restrict__ erow, int64_t nb) {
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nb;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    float mx = (float)E[k * nb];
-#pragma unroll 8
-    for (int64_t q = 1; q < nb; ++q) mx = lt_max(mx, (float)E[k * nb + q]);
-    erow[k] = mx;
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t k = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); k < nb;
+       k += warps) {
+    const double* row = E + k * nb;
+    uint32_t mk = 0;
+    bool odd = false;
+    for (int64_t q = lane; q < nb; q += 32) {
+      const float v = (float)__ldg(row + q);
+      odd |= v != v;
+      if (v > 0.0f) mk = max(mk, __float_as_uint(v));   // positive floats order as integers
+    }
+    mk = __reduce_max_sync(0xffffffffu, mk);
+    odd = __any_sync(0xffffffffu, odd) || mk == 0;
+    if (lane == 0) {
+      if (odd) {
+        float mx = (float)row[0];
+        for (int64_t q = 1; q < nb; ++q) mx = lt_max(mx, (float)row[q]);
+        erow[k] = mx;
+      } else {
+        erow[k] = __uint_as_float(mk);
+      }
+    }
   }
 }
 
@@ -1387,8 +1407,8 @@ cudaError_t launch_collide_cells(const Bt& B, const lacmo_params_t& p, const lac
     cc.Ef = Ef;
     if (p.thin_draws) {
       float* erow = Ef + (int64_t)LACMO_MAX_KERNEL_BINS * LACMO_MAX_KERNEL_BINS;
-      k_table_rowmax<<<nblk(p.no_kernel_bins, 128), 128, 0, s>>>(p.E_col_grid, erow,
-                                                                 p.no_kernel_bins);
+      k_table_rowmax<<<nblk(p.no_kernel_bins * 32, 128), 128, 0, s>>>(p.E_col_grid, erow,
+                                                                      p.no_kernel_bins);
       note_launches(1);
       cc.erow = erow;
     }

@@ -353,9 +353,10 @@ def precision_ensemble(members=16, spcm=(52, 76), nx=75, nz=75, spinup=7200, hor
 def adjoint(spcm=(52, 76), nx=75, nz=75, seconds=600, every_steps=60, seed=1001,
             kappa=0.6, fd_h=1e-5):
     """Gradients of the domain-mean liquid water path at the end and of the
-    surface rain over ``seconds`` of the product's time step (collisions off,
-    the SIPs' cells recorded from the product's own run and held fixed) by
-    m_s, kappa and the mass-flux scale (dJ/dj_max = that / j_max),
+    surface rain over ``seconds`` of the product's time step (with the
+    state's collisions; the SIPs' cells and the collisions recorded from the
+    product's own run and held fixed) by m_s, kappa and the mass-flux scale
+    (dJ/dj_max = that / j_max),
     checkpointed every ``every_steps`` advection steps; the forward model
     against the product's run, timing, and central finite differences of the
     kappa and flux-scale derivatives."""
@@ -376,6 +377,7 @@ def adjoint(spcm=(52, 76), nx=75, nz=75, seconds=600, every_steps=60, seed=1001,
     Lx, Lz = (float(a) * float(b) for a, b in zip(st["grid_steps"], st["grid_no_cells"]))
     j_max = 0.6 * math.sqrt(Lx * Lx + Lz * Lz) / math.sqrt(2.0 * 1500.0 * 1500.0)
     out = {"n_sips": model.n, "advection_steps": n_adv, "sub_steps": model.K,
+           "collisions": model.collisions, "collision_events": int(model.n_events),
            "record_s": t_rec, "replay_max_rel_diff_m_w": rel, "j_max": j_max}
     for name, w in (("lwp", model.lwp_weights()), ("rain", model.rain_weights())):
         m_s = model.m_s0.clone().requires_grad_(True)
