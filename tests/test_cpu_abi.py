@@ -61,6 +61,10 @@ def test_workspace_size_and_argument_errors():
     assert lib.lacmo_collision_step_golovin(None, None, 10, 1.0, None, None, 0, 0, None) == -1
     x = ctypes.c_void_p(16)
     assert lib.lacmo_collision_step_golovin(x, x, 9000, 1.0, x, None, 0, 0, None) == -5
+    # the one-call drop-in step: a missing call, or one without its structures
+    assert lib.lacmo_dropin_adv_step(None, None) == -1
+    call = _lib.Dropin()
+    assert lib.lacmo_dropin_adv_step(ctypes.byref(call), None) == -1
 
 
 def test_constants_header_matches_python():
