@@ -103,7 +103,8 @@ typedef struct {
  * drag update in FP32, with the Newton repeated in FP64 for SIPs near the
  * critical radius of activation; state, positions, per-cell condensed-mass
  * sums (into Theta / r_v), multiplicities and the collision step stay FP64;
- * per-cell sums are formed with atomics (any order). */
+ * the per-cell sums of dm * xi are exact integer sums (units of 2^-4 fg), so
+ * their order does not matter and a step is deterministic. */
 #define LACMO_PRECISION_FP64 0
 #define LACMO_PRECISION_MIXED 1
 
@@ -211,9 +212,17 @@ int64_t lacmo_plan_kernel_nodes(const lacmo_plan* plan);
  * captured plan when given, else lacmo_integrate_adv_step), exports the
  * cells (lacmo_cells_export into cells_out / active_out), copies the `out`
  * list back to the host, stores the counter after the step in *col_step_out
- * (when given) and synchronises `stream`.  One cudaMemcpyAsync per entry;
- * host memory may be pageable.  The sips/grid/params/draws structures name
- * the device buffers. */
+ * (when given) and synchronises `stream`.  Host memory may be pageable.
+ * copy_mode: LACMO_COPY_AUTO takes LACMO_COPY_KERNEL where the device reads
+ * and writes pageable host memory directly (cudaDevAttrPageableMemoryAccess:
+ * a Grace host's coherent NVLink-C2C link), else LACMO_COPY_ENGINE;
+ * LACMO_COPY_ENGINE issues one cudaMemcpyAsync per entry; LACMO_COPY_KERNEL
+ * moves every entry of a list in one kernel launch, asynchronously to the
+ * host (LACMO_ERR_ARG where the device cannot).  The sips/grid/params/draws
+ * structures name the device buffers. */
+#define LACMO_COPY_AUTO 0
+#define LACMO_COPY_ENGINE 1
+#define LACMO_COPY_KERNEL 2
 typedef struct {
   void* dst;
   const void* src;
@@ -237,6 +246,7 @@ typedef struct {
   lacmo_plan* plan;         /* a plan of this state (one step), or NULL  */
   int64_t col_step;         /* collision-step counter to start from; -1: 0 after the clear */
   int64_t* col_step_out;    /* host: the counter after the step, or NULL */
+  int32_t copy_mode;        /* LACMO_COPY_*                              */
 } lacmo_dropin_t;
 int lacmo_dropin_adv_step(const lacmo_dropin_t* call, void* stream);
 

@@ -75,7 +75,10 @@ class Dropin(ctypes.Structure):
                 ("prm", ctypes.POINTER(Params)), ("draws", ctypes.POINTER(Draws)), ("ws", vp),
                 ("ws_bytes", ctypes.c_size_t), ("cells_in", vp), ("active_in", vp),
                 ("cells_out", vp), ("active_out", vp), ("plan", vp), ("col_step", i64),
-                ("col_step_out", ctypes.POINTER(i64))]
+                ("col_step_out", ctypes.POINTER(i64)), ("copy_mode", i32)]
+
+
+COPY_AUTO, COPY_ENGINE, COPY_KERNEL = 0, 1, 2
 
 
 P = ctypes.POINTER

@@ -493,6 +493,93 @@ int lacmo_plan_destroy(lacmo_plan* pl) {
   return LACMO_OK;
 }
 
+// Host <-> device copies by the SMs, for devices that access pageable host
+// memory directly: one launch moves every entry of a list (blockIdx.y =
+// entry), 16-byte words where both ends are 16-byte aligned, else 8-byte
+// words where 8-byte aligned, and the remaining bytes one by one.
+constexpr int XFER_MAX = 40;
+struct Xfer {
+  int32_t n;
+  const char* src[XFER_MAX];
+  char* dst[XFER_MAX];
+  int64_t bytes[XFER_MAX];
+};
+__global__ void __launch_bounds__(256) k_xfer(const __grid_constant__ Xfer x) {
+  const int e = blockIdx.y;
+  if (e >= x.n) return;
+  const char* src = x.src[e];
+  char* dst = x.dst[e];
+  const int64_t nb = x.bytes[e];
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const uintptr_t al = (uintptr_t)src | (uintptr_t)dst;
+  int64_t done = 0;
+  if (al % 16 == 0) {
+    const int64_t nv = nb / 16;
+    for (int64_t i = t; i < nv; i += stride) ((int4*)dst)[i] = ((const int4*)src)[i];
+    done = nv * 16;
+  } else if (al % 8 == 0) {
+    const int64_t nv = nb / 8;
+    for (int64_t i = t; i < nv; i += stride) ((long long*)dst)[i] = ((const long long*)src)[i];
+    done = nv * 8;
+  }
+  for (int64_t i = done + t; i < nb; i += stride) dst[i] = src[i];
+}
+
+// the device reads and writes pageable host memory (cached per device)
+static bool pageable_access() {
+  static std::atomic<int> cached[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return false;
+  int v = dev < 64 ? cached[dev].load() : 0;
+  if (v == 0) {
+    int a = 0;
+    if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) a = 0;
+    v = a == 1 ? 1 : -1;
+    if (dev < 64) cached[dev].store(v);
+  }
+  return v == 1;
+}
+
+// the entries of a copy list with bytes > 0, by the SMs (launches of up to
+// XFER_MAX entries) or one cudaMemcpyAsync each
+static cudaError_t copy_list(const lacmo_copy_t* l, int32_t n, bool by_kernel,
+                             cudaMemcpyKind kind, cudaStream_t s) {
+  if (!by_kernel) {
+    for (int32_t i = 0; i < n; ++i)
+      if (l[i].bytes) {
+        const cudaError_t e = cudaMemcpyAsync(l[i].dst, l[i].src, (size_t)l[i].bytes, kind, s);
+        if (e != cudaSuccess) return e;
+      }
+    return cudaSuccess;
+  }
+  Xfer x;
+  x.n = 0;
+  int64_t largest = 0;
+  for (int32_t i = 0; i <= n; ++i) {
+    if (i == n || x.n == XFER_MAX) {
+      if (x.n) {
+        const int64_t blocks = (largest / 16 + 255) / 256;
+        const unsigned gx = (unsigned)(blocks < 1 ? 1 : (blocks > 304 ? 304 : blocks));
+        k_xfer<<<dim3(gx, (unsigned)x.n), 256, 0, s>>>(x);
+        note_launches(1);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+      }
+      x.n = 0;
+      largest = 0;
+      if (i == n) break;
+    }
+    if (!l[i].bytes) continue;
+    x.src[x.n] = (const char*)l[i].src;
+    x.dst[x.n] = (char*)l[i].dst;
+    x.bytes[x.n] = l[i].bytes;
+    largest = l[i].bytes > largest ? l[i].bytes : largest;
+    ++x.n;
+  }
+  return cudaSuccess;
+}
+
 int lacmo_dropin_adv_step(const lacmo_dropin_t* c, void* stream) {
   if (!c || !sips_ok(c->sips) || !grid_ok(c->grid) || !prm_ok(c->prm) || !c->draws ||
       !c->cells_in || !c->active_in || !c->cells_out || !c->active_out || c->n_in < 0 ||
@@ -507,11 +594,13 @@ int lacmo_dropin_adv_step(const lacmo_dropin_t* c, void* stream) {
     const lacmo_copy_t& e = i < c->n_in ? c->in[i] : c->out[i - c->n_in];
     if (e.bytes < 0 || (e.bytes && (!e.dst || !e.src))) return LACMO_ERR_ARG;
   }
+  if (c->copy_mode < LACMO_COPY_AUTO || c->copy_mode > LACMO_COPY_KERNEL) return LACMO_ERR_ARG;
+  const bool direct = pageable_access();
+  if (c->copy_mode == LACMO_COPY_KERNEL && !direct) return LACMO_ERR_ARG;
+  const bool by_kernel = c->copy_mode == LACMO_COPY_KERNEL ||
+                         (c->copy_mode == LACMO_COPY_AUTO && direct);
   cudaStream_t s = (cudaStream_t)stream;
-  for (int32_t i = 0; i < c->n_in; ++i)
-    if (c->in[i].bytes)
-      LCHK(cudaMemcpyAsync(c->in[i].dst, c->in[i].src, (size_t)c->in[i].bytes,
-                           cudaMemcpyHostToDevice, s));
+  LCHK(copy_list(c->in, c->n_in, by_kernel, cudaMemcpyHostToDevice, s));
   LCHK(launch_cells_import(c->cells_in, c->active_in, sp.cell, sp.n, g.nx, g.nz, s));
   LCHK(cudaMemsetAsync(c->ws, 0, ws_bytes(sp.n, g.nx, g.nz), s));
   const Bt B = single(sp, g, w, c->draws->seed);
@@ -529,10 +618,7 @@ int lacmo_dropin_adv_step(const lacmo_dropin_t* c, void* stream) {
                            g.nz, g.x_min, g.z_min, g.dx, g.dz, s));
   if (c->col_step_out)
     LCHK(cudaMemcpyAsync(c->col_step_out, w.col_step, 8, cudaMemcpyDeviceToHost, s));
-  for (int32_t i = 0; i < c->n_out; ++i)
-    if (c->out[i].bytes)
-      LCHK(cudaMemcpyAsync(c->out[i].dst, c->out[i].src, (size_t)c->out[i].bytes,
-                           cudaMemcpyDeviceToHost, s));
+  LCHK(copy_list(c->out, c->n_out, by_kernel, cudaMemcpyDeviceToHost, s));
   LCHK(cudaStreamSynchronize(s));
   return LACMO_OK;
 }

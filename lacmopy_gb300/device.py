@@ -284,13 +284,15 @@ class DeviceState:
             return None
         return a
 
-    def dropin_step(self, st, seed, draws, precision, col_step=None):
+    def dropin_step(self, st, seed, draws, precision, col_step=None, copy_mode=None):
         """One integrate_adv_step_np call on the host arrays of ``st`` in one
         native call (lacmo_dropin_adv_step): the arrays are copied into this
         state's buffers, the step replays the captured graph, and the results
         are copied back in place.  Returns False, having done nothing, when
         the call does not fit this state (shape, array types, parameters,
-        draw source), for the caller to build a new state instead."""
+        draw source), for the caller to build a new state instead.
+        ``copy_mode``: _lib.COPY_AUTO (None), COPY_ENGINE or COPY_KERNEL (the
+        SMs read and write the host pages; where the device can)."""
         thin = draws == "thinned"
         if (self.ws is None or draws not in ("philox", "thinned") or self.draw_mode != "philox"
                 or self.thin != thin or self.precision != precision or self.seed != int(seed)
@@ -342,7 +344,8 @@ class DeviceState:
                            self._cells_in.data_ptr(), self._act_in.data_ptr(),
                            self._cells_out.data_ptr(), self._act_out.data_ptr(), plan,
                            philox_counter(seed) if col_step is None else int(col_step),
-                           ctypes.pointer(after))
+                           ctypes.pointer(after),
+                           _lib.COPY_AUTO if copy_mode is None else int(copy_mode))
         _lib.check(self.lib.lacmo_dropin_adv_step(ctypes.byref(call), _stream()), "dropin_adv_step")
         _philox_next[self.seed] = int(after.value)
         return True

@@ -199,3 +199,41 @@ def test_concurrent_dropin_calls_from_threads():
     I.release_resident()
     for sd in seeds:
         reset_philox_counters(sd)
+
+
+@pytest.mark.parametrize("mode", ["engine", "kernel"])
+def test_dropin_copy_paths(mode):
+    """The one-call drop-in step with its host copies by the copy engines
+    (one cudaMemcpyAsync per array) and by the SMs reading and writing the
+    host pages directly: both equal two steps of a resident DeviceState bit
+    for bit."""
+    from lacmopy_gb300 import DeviceState, _lib
+    from lacmopy_gb300 import integration as I
+    from lacmopy_gb300.device import reset_philox_counters
+    seed = 401
+    st = _state(seed=55)
+    key = (st["pos"].shape[1], 20, 18)
+    want_ds = DeviceState(copy.deepcopy(st), draws="thinned", seed=seed, precision="mixed")
+    want_ds.adv_step(2)
+    want = want_ds.snapshot()
+    reset_philox_counters(seed)
+    I.release_resident()
+    got = copy.deepcopy(st)
+    I.integrate_adv_step_np(*[got[k] for k in I._STATE_KEYS], draws="thinned", seed=seed,
+                            precision="mixed")
+    ds = I._resident[key]
+    code = _lib.COPY_ENGINE if mode == "engine" else _lib.COPY_KERNEL
+    try:
+        ok = ds.dropin_step(dict(zip(I._STATE_KEYS, [got[k] for k in I._STATE_KEYS])), seed,
+                            "thinned", "mixed", copy_mode=code)
+    except _lib.LacmoError:
+        if mode == "kernel":
+            pytest.skip("the device does not access pageable host memory")
+        raise
+    assert ok
+    assert want["no_cols"].sum() > 0
+    for k in ("xi", "m_w", "m_s", "pos", "vel", "rel_pos", "T_p", "grid_scalar_fields",
+              "no_cols", "cells", "active_ids"):
+        assert np.array_equal(got[k], want[k]), k
+    I.release_resident()
+    reset_philox_counters(seed)
