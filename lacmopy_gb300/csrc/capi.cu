@@ -580,6 +580,32 @@ static cudaError_t copy_list(const lacmo_copy_t* l, int32_t n, bool by_kernel,
   return cudaSuccess;
 }
 
+// the stream work of lacmo_dropin_adv_step, without the final synchronisation
+static int dropin_sequence(const lacmo_dropin_t& c, const Ws& w, bool by_kernel, cudaStream_t s) {
+  const lacmo_sips_t& sp = *c.sips;
+  const lacmo_grid_t& g = *c.grid;
+  LCHK(copy_list(c.in, c.n_in, by_kernel, cudaMemcpyHostToDevice, s));
+  LCHK(launch_cells_import(c.cells_in, c.active_in, sp.cell, sp.n, g.nx, g.nz, s));
+  LCHK(cudaMemsetAsync(c.ws, 0, ws_bytes(sp.n, g.nx, g.nz), s));
+  const Bt B = single(sp, g, w, c.draws->seed);
+  LCHK(launch_cell_aux(B, s));
+  LCHK(launch_histogram(B, s));
+  LCHK(launch_bin(B, s));
+  if (c.col_step >= 0) LCHK(launch_set_i64(w.col_step, c.col_step, s));
+  if (c.plan) {
+    LCHK(cudaGraphLaunch(c.plan->exec, s));
+  } else {
+    const int rc = adv_step(B, *c.prm, *c.draws, s);
+    if (rc != LACMO_OK) return rc;
+  }
+  LCHK(launch_cells_export(sp.cell, sp.pos, sp.rel_pos, c.cells_out, c.active_out, sp.n, g.nx,
+                           g.nz, g.x_min, g.z_min, g.dx, g.dz, s));
+  if (c.col_step_out)
+    LCHK(cudaMemcpyAsync(c.col_step_out, w.col_step, 8, cudaMemcpyDeviceToHost, s));
+  LCHK(copy_list(c.out, c.n_out, by_kernel, cudaMemcpyDeviceToHost, s));
+  return LACMO_OK;
+}
+
 int lacmo_dropin_adv_step(const lacmo_dropin_t* c, void* stream) {
   if (!c || !sips_ok(c->sips) || !grid_ok(c->grid) || !prm_ok(c->prm) || !c->draws ||
       !c->cells_in || !c->active_in || !c->cells_out || !c->active_out || c->n_in < 0 ||
@@ -600,27 +626,12 @@ int lacmo_dropin_adv_step(const lacmo_dropin_t* c, void* stream) {
   const bool by_kernel = c->copy_mode == LACMO_COPY_KERNEL ||
                          (c->copy_mode == LACMO_COPY_AUTO && direct);
   cudaStream_t s = (cudaStream_t)stream;
-  LCHK(copy_list(c->in, c->n_in, by_kernel, cudaMemcpyHostToDevice, s));
-  LCHK(launch_cells_import(c->cells_in, c->active_in, sp.cell, sp.n, g.nx, g.nz, s));
-  LCHK(cudaMemsetAsync(c->ws, 0, ws_bytes(sp.n, g.nx, g.nz), s));
-  const Bt B = single(sp, g, w, c->draws->seed);
-  LCHK(launch_cell_aux(B, s));
-  LCHK(launch_histogram(B, s));
-  LCHK(launch_bin(B, s));
-  if (c->col_step >= 0) LCHK(launch_set_i64(w.col_step, c->col_step, s));
-  if (c->plan) {
-    LCHK(cudaGraphLaunch(c->plan->exec, s));
-  } else {
-    const int rc = adv_step(B, *c->prm, *c->draws, s);
-    if (rc != LACMO_OK) return rc;
-  }
-  LCHK(launch_cells_export(sp.cell, sp.pos, sp.rel_pos, c->cells_out, c->active_out, sp.n, g.nx,
-                           g.nz, g.x_min, g.z_min, g.dx, g.dz, s));
-  if (c->col_step_out)
-    LCHK(cudaMemcpyAsync(c->col_step_out, w.col_step, 8, cudaMemcpyDeviceToHost, s));
-  LCHK(copy_list(c->out, c->n_out, by_kernel, cudaMemcpyDeviceToHost, s));
-  LCHK(cudaStreamSynchronize(s));
-  return LACMO_OK;
+  const int rc = dropin_sequence(*c, w, by_kernel, s);
+  // copies into the caller's host arrays may be in flight when a step of the
+  // sequence failed: none outlives the call
+  const cudaError_t e = cudaStreamSynchronize(s);
+  if (rc != LACMO_OK) return rc;
+  return e == cudaSuccess ? LACMO_OK : LACMO_ERR_CUDA;
 }
 
 struct lacmo_batch {
