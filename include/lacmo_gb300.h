@@ -104,7 +104,9 @@ typedef struct {
  * critical radius of activation; state, positions, per-cell condensed-mass
  * sums (into Theta / r_v), multiplicities and the collision step stay FP64;
  * the per-cell sums of dm * xi are exact integer sums (units of 2^-4 fg), so
- * their order does not matter and a step is deterministic. */
+ * their order does not matter and the state after a step is the same run to
+ * run; only water_removed adds the SIPs reaching the ground with FP64
+ * atomics (any order). */
 #define LACMO_PRECISION_FP64 0
 #define LACMO_PRECISION_MIXED 1
 
@@ -272,9 +274,8 @@ int lacmo_batch_prepare(lacmo_batch* batch, const lacmo_params_t* prm, void* str
 /* one advection step of every member (lacmo_integrate_adv_step, Philox draws) */
 int lacmo_batch_adv_step(lacmo_batch* batch, const lacmo_params_t* prm, void* stream);
 /* A mixed-precision batch step does not bin its SIPs after its last sub-step
- * (the next step bins after its half-step move; the ground removals are
- * folded into water_removed all the same), so between steps a member's
- * binning is empty; lacmo_batch_rebin bins every member's SIPs by their
+ * (the next step bins after its half-step move; water_removed is complete
+ * all the same), so between steps a member's binning is empty; lacmo_batch_rebin bins every member's SIPs by their
  * current cells, for entry points that read a member's binning between steps
  * (lacmo_update_grid_r_l with lacmo_batch_member_workspace). */
 int lacmo_batch_rebin(lacmo_batch* batch, void* stream);

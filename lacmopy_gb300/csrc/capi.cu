@@ -178,9 +178,9 @@ static int subloop_mixed(const Bt& B, const lacmo_params_t& p, const lacmo_draws
 
 // keep_binning: bin the SIPs after the step's last sub-step (single states,
 // whose entry points between steps read the binning); otherwise (mixed
-// batches) only the ground removals are folded: the next step bins after its
-// half-step move anyway, and the batch's between-step entry points rebin
-// first (lacmo_batch_rebin)
+// batches) the binning is left empty (launch_fold_removals: the scan over
+// zero counts): the next step bins after its half-step move anyway, and the
+// batch's between-step entry points rebin first (lacmo_batch_rebin)
 static int adv_step_mixed(const Bt& B, const lacmo_params_t& p, const lacmo_draws_t& d,
                           cudaStream_t s, bool keep_binning) {
   LCHK(launch_wind_float(B, s));

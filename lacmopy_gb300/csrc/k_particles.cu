@@ -635,10 +635,12 @@ __global__ void __launch_bounds__(32) k_cell_update(const __grid_constant__ MRef
 //  * comparisons of non-negative doubles compare their bit patterns;
 //  * the new cell index comes from the FP32 position with a certified margin
 //    (1e-4 of a cell) around cell edges, inside which FP64 decides;
-//  * the per-cell sums of dm * xi are FP64 atomics, which L2 executes.
+//  * the per-cell sums of dm * xi are exact integer sums (acc_add), which L2
+//    executes, independent of their order.
 // The Newton condensation and the drag update run in FP32 (lacmo_physics.cuh)
-// with the FP64 Newton for SIPs near the critical radius.  Per-cell sums and
-// water_removed are formed in arbitrary order.
+// with the FP64 Newton for SIPs near the critical radius.  water_removed takes
+// the SIPs reaching the ground with FP64 atomics, in arbitrary order (the
+// removal list of the FP64 path holds the FP64 Newton queue here).
 // Rare FP64 paths stay out of line (__noinline__) so that the common path
 // issues no FP64 instruction, not even predicated off.
 // removed SIP: only the relative position keeps its per-call division
